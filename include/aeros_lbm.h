@@ -1,0 +1,239 @@
+/*
+ * aeros_lbm.h — C ABI of the GB300 lattice-Boltzmann solver step.
+ *
+ * Plain C, plain pointers and sizes. Every entry point returns an int status
+ * (AEROS_OK == 0, negative on failure) and records a message that
+ * aeros_consume_error() hands back and clears — the same record/consume
+ * convention as the reference CUDA layer (aeros/src/cuda_api.h:53-56,
+ * aeros/src/kernel.cu:57-82). No exceptions cross this boundary.
+ *
+ * Lattice: D3Q19 (fluid) and D3Q7 (temperature), velocity sets, weights and
+ * opposite tables identical to aeros/src/lbm.cpp:92-109 and
+ * aeros/src/thermal_lbm.cpp:31-40. Cell index = (z*ny + y)*nx + x.
+ *
+ * Reference functions each entry point replaces are cited beside it.
+ */
+#ifndef AEROS_LBM_H
+#define AEROS_LBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define AEROS_OK               0
+#define AEROS_ERR_INVALID     -1   /* bad argument (null pointer, size, mode) */
+#define AEROS_ERR_CUDA        -2   /* CUDA runtime error (message has the call) */
+#define AEROS_ERR_ALLOC       -3   /* device or host allocation failed */
+#define AEROS_ERR_UNSUPPORTED -4   /* mode combination not implemented */
+#define AEROS_ERR_STATE       -5   /* call not valid in the handle's state */
+#define AEROS_ERR_TIMEOUT     -6   /* a bounded device wait gave up */
+
+/* ---- enums --------------------------------------------------------------- */
+enum { AEROS_CELL_FLUID = 0, AEROS_CELL_SOLID = 1, AEROS_CELL_GROUND = 2 };
+
+/* Population storage. FP32 is the drop-in form (bitwise the reference's
+ * arithmetic); FP16/BF16 store shifted deviations f_i - w_i and compute in
+ * FP32. */
+enum { AEROS_STORE_FP32 = 0, AEROS_STORE_FP16 = 1, AEROS_STORE_BF16 = 2 };
+
+/* Lateral (non-flow-axis, non-periodic) faces. COPY is the reference's rule
+ * (an out-of-domain source copies the cell's own post-collision population,
+ * aeros/src/lbm.cpp:1392-1394). FREESLIP is a specular-reflection wall that
+ * the reference does not have. */
+enum { AEROS_LATERAL_COPY = 0, AEROS_LATERAL_FREESLIP = 1 };
+
+/* Outlet face. REFERENCE = convective outlet when convective_outlet != 0
+ * (aeros/src/lbm.cpp:1465-1544), otherwise copy-own. ZEROGRAD copies the
+ * post-streaming unknowns of the plane upstream (not in the reference). */
+enum { AEROS_OUTLET_REFERENCE = 0, AEROS_OUTLET_ZEROGRAD = 1 };
+
+/* ---- parameters ------------------------------------------------------------
+ * Lattice-unit parameters after the host has resolved world units; mirrors
+ * LBMParams (aeros/src/lbm.h:11-75) plus the inlet velocity that
+ * computeInletVelocityLB derives from flowAzimuth/flowElevation/U0
+ * (aeros/src/lbm.cpp:186-199). */
+typedef struct aeros_lbm_params {
+    int32_t nx, ny, nz;          /* grid, each >= 4                                */
+    float   tau;                 /* BGK tau / TRT s+ = 1/tau (clamped as the reference) */
+    float   smagorinsky_c;       /* Cs (reference clamps to [0, 0.3])              */
+    int32_t use_les;             /* useTurbulence: two-pass |S| + Van Driest       */
+    int32_t use_trt;             /* useTRT                                          */
+    int32_t periodic_x;          /* periodicX (disables inlet/outlet)               */
+    int32_t periodic_z;          /* periodicZ                                       */
+    int32_t convective_outlet;   /* useConvectiveOutlet                             */
+    int32_t flow_axis;           /* 0,1,2 : axis of the inlet/outlet planes         */
+    int32_t flow_sign;           /* +1 : inlet at coordinate 0, -1 : at N-1          */
+    float   u_in[3];             /* inlet lattice velocity (equilibrium at rho = 1)  */
+    float   u_init[3];           /* initial uniform velocity of fluid cells          */
+    float   body_force[3];       /* Guo body force, lattice units                    */
+    float   vel_scale;           /* flowSpeed / |u_in| (TKE in m^2/s^2)              */
+    float   convergence_threshold; /* lbmParams.convergenceThreshold                  */
+    int32_t storage;             /* AEROS_STORE_*                                    */
+    int32_t lateral_bc;          /* AEROS_LATERAL_*                                  */
+    int32_t outlet_bc;           /* AEROS_OUTLET_*                                   */
+    int32_t reserved[8];         /* zero                                             */
+} aeros_lbm_params;
+
+/* Mirrors ThermalParams (aeros/src/thermal_lbm.h:33-41); nu_lb is the solver
+ * viscosity handed to thermalInit (aeros/src/lbm.cpp:876-885). */
+typedef struct aeros_thermal_params {
+    int32_t enabled;
+    float   rayleigh;
+    float   prandtl;
+    int32_t fixed_wall_temps;    /* hot wall y = 0, cold wall y = ny-1 */
+    float   hot_temp;
+    float   cold_temp;
+    float   perturbation;        /* cos*sin seed amplitude (fraction of dT) */
+    float   nu_lb;
+    int32_t reserved[4];
+} aeros_thermal_params;
+
+/* Per-step diagnostics of the last executed step, as the reference exposes
+ * them through globals (aeros/src/lbm.h:78-125, aeros/src/lbm.cpp:1554-1580). */
+typedef struct aeros_lbm_stats {
+    int64_t step;                /* lbmCurrentStep                               */
+    float   avg_rho;             /* lbmAvgRho (fluid mean, FP64 sum)             */
+    float   avg_kinetic;         /* lbmAvgKineticEnergy                          */
+    float   avg_tke;             /* lbmTKE                                       */
+    float   max_velocity_lb;     /* lbmMaxVelocityLB                             */
+    float   convergence;         /* lbmConvergence = |dKE|                       */
+    int32_t converged;           /* lbmConverged                                 */
+    int32_t diverged;            /* last call tripped the divergence guard and   */
+                                 /* re-equilibrated (lbm.cpp:1313-1319,1574-1600) */
+    int32_t pad0;
+    int64_t negative_pops;       /* lbmNegativePops                              */
+    int64_t bad_pops;            /* lbmBadPops                                   */
+    int64_t rho_out_of_range;    /* lbmRhoOutOfRange                             */
+    int64_t rho_non_finite;      /* lbmRhoNonFinite                              */
+    int64_t u_limited;           /* lbmULimited                                  */
+    int64_t nan_count;           /* nanCount of the last step                    */
+    double  sum_rho;             /* raw FP64 sums of the last step               */
+    double  sum_kinetic;
+    double  sum_tke;
+    float   nusselt;             /* thermalNusselt (FP64 row sum)                */
+    float   mean_t;              /* thermalMeanT                                 */
+    int32_t fluid_cells;
+    int32_t pad1;
+} aeros_lbm_stats;
+
+typedef struct aeros_lbm aeros_lbm;   /* opaque solver handle (one domain) */
+
+/* ---- errors --------------------------------------------------------------- */
+/* Replaces cudaConsumeError (aeros/src/cuda_api.h:56): returns the last error
+ * code (0 = none), copies its message into buf, clears it. Thread-local. */
+int aeros_consume_error(char* buf, int buf_size);
+
+/* ---- lifecycle ------------------------------------------------------------- */
+/* Replaces initLBM (aeros/src/lbm.cpp:405-886) once the host has resolved the
+ * domain: mask (nx*ny*nz bytes, AEROS_CELL_*), wall-distance chamfer
+ * (lbm.cpp:647-675), fluid count (:677-680), equilibrium at u_init
+ * (:686-739). Allocates all device memory. */
+int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* mask,
+                     aeros_lbm** out);
+/* Replaces shutdownLBM (aeros/src/lbm.cpp:894-904) + cudaReleaseAll. */
+int aeros_lbm_destroy(aeros_lbm* h);
+
+/* Stream the handle launches on (a cudaStream_t; NULL = legacy default). */
+int aeros_lbm_set_stream(aeros_lbm* h, void* cuda_stream);
+int aeros_lbm_synchronize(aeros_lbm* h);
+
+/* Replaces thermalInit (aeros/src/thermal_lbm.cpp:84-140): alpha, tau_T, g,
+ * H from the mask, conduction profile + cos*sin seed. */
+int aeros_lbm_thermal_init(aeros_lbm* h, const aeros_thermal_params* tp);
+
+/* ---- stepping --------------------------------------------------------------- */
+/* Replaces stepLBMCPU(steps) (aeros/src/lbm.cpp:907-1709) minus the readback
+ * prep: LES pre-pass, collision, stream + BCs, thermal step, per-step stats,
+ * divergence guard + re-equilibration. Enqueued on the handle's stream; the
+ * call waits for the final stats (one device->host read per call). */
+int aeros_lbm_step(aeros_lbm* h, int nsteps);
+/* Same, without the final wait; stats are read by aeros_lbm_get_stats. */
+int aeros_lbm_step_async(aeros_lbm* h, int nsteps);
+int aeros_lbm_get_stats(aeros_lbm* h, aeros_lbm_stats* out);
+
+/* ---- state I/O (host buffers, nx*ny*nz elements each unless stated) ------- */
+/* Field readback (lbmRho, lbmUx/Uy/Uz, lbmStrainMag, lbmTKEField; lbm.h:132-152).
+ * Any pointer may be NULL. */
+int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float* uy,
+                          float* uz, float* strain, float* tke);
+/* Device pointers of the same fields (valid until the next step call).
+ * Any out-pointer may be NULL. */
+int aeros_lbm_device_fields(aeros_lbm* h, const float** rho, const float** ux,
+                            const float** uy, const float** uz);
+/* Pre-collision populations, layout [19][nx*ny*nz] (the reference's f after
+ * stepLBMCPU, lbm.cpp:89,1546). Converted to FP32 for shifted storage. */
+int aeros_lbm_read_populations(aeros_lbm* h, float* f);
+/* Overwrite pre-collision populations (checkpoint restore / fault injection). */
+int aeros_lbm_write_populations(aeros_lbm* h, const float* f);
+/* Equilibrium re-initialisation from per-cell rho and u (fluid cells; rho may
+ * be NULL = 1). |u| limited to 0.3 as initLBM does (lbm.cpp:725-730). */
+int aeros_lbm_set_equilibrium(aeros_lbm* h, const float* rho, const float* ux,
+                              const float* uy, const float* uz);
+int aeros_lbm_read_mask(aeros_lbm* h, uint8_t* mask, uint8_t* wall_dist);
+
+/* ---- thermal ---------------------------------------------------------------- */
+/* Replaces thermalUpload (aeros/src/thermal_lbm.cpp:187-197). */
+int aeros_lbm_thermal_upload(aeros_lbm* h, const float* T);
+/* thermalT and thermalBuoyancyY (thermal_lbm.h:46-49). Either may be NULL. */
+int aeros_lbm_thermal_read(aeros_lbm* h, float* T, float* buoyancy);
+
+/* ---- forces ------------------------------------------------------------------ */
+/* Replaces lbmControlVolumeForce (aeros/src/lbm.cpp:2183-2232): box centred on
+ * the domain centre, half sizes as fractions of N, FP64 accumulation. */
+int aeros_lbm_cv_force(aeros_lbm* h, float half_x, float half_y, float half_z,
+                       double out[3]);
+/* Same momentum balance on an explicit box [x0,x1]x[y0,y1]x[z0,z1] (cells,
+ * inclusive; not in the reference, which only centres the box). */
+int aeros_lbm_cv_force_box(aeros_lbm* h, const int32_t box[6], double out[3]);
+/* Replaces lbmProjectedAreaCells (aeros/src/lbm.cpp:2236-2256). */
+int aeros_lbm_projected_area(aeros_lbm* h, int axis, double* area);
+
+/* ---- voxelizer ------------------------------------------------------------------ */
+typedef struct aeros_voxel_grid {
+    int32_t nx, ny, nz;
+    float   min[3];              /* lower corner                      */
+    float   cell[3];             /* cell size; centre = min + (i+0.5)*cell */
+} aeros_voxel_grid;
+
+/* Solid mask of a closed triangle mesh at the grid's cell centres: BVH
+ * (median split, leaf 4, aeros/src/mesh_bvh.h:219-266) + three-ray parity vote
+ * with FP64 Moller-Trumbore (mesh_bvh.h:62-96,116-185) — the mask loop of
+ * buildVoxelGrid (aeros/src/voxel_grid.cpp:337-351). tris: ntri*9 floats.
+ * mask_out: nx*ny*nz bytes, 1 = inside. Degenerate / non-finite triangles are
+ * dropped as voxel_grid.cpp:313-325 does. */
+int aeros_voxelize(const float* tris, int64_t ntri, const aeros_voxel_grid* grid,
+                   uint8_t* mask_out);
+/* Same with a device-resident output mask (nx*ny*nz bytes). */
+int aeros_voxelize_device(const float* tris, int64_t ntri,
+                          const aeros_voxel_grid* grid, uint8_t* d_mask_out);
+
+/* Grid plan (aeros/src/voxel_grid.cpp:172-215): dimensions for a bounding box
+ * and resolution against a byte budget (0 = unlimited). */
+typedef struct aeros_voxel_plan_t {
+    int32_t nx, ny, nz;
+    int32_t fits;
+    int64_t cells;
+    uint64_t bytes;
+    int32_t requested_res;
+    int32_t suggested_res;
+} aeros_voxel_plan_t;
+int aeros_voxel_plan(const float size[3], int res, uint64_t budget_bytes,
+                     aeros_voxel_plan_t* out);
+
+/* ---- timing helper for benches ------------------------------------------------ */
+/* Milliseconds of the step kernels enqueued by the last aeros_lbm_step*/
+/* call, measured with CUDA events on the handle's stream. */
+int aeros_lbm_last_step_ms(aeros_lbm* h, float* ms);
+/* Number of kernels the last aeros_lbm_step* call launched. */
+int aeros_lbm_last_launch_count(aeros_lbm* h, int64_t* n);
+/* Bytes of device memory the handle holds. */
+int aeros_lbm_device_bytes(aeros_lbm* h, uint64_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AEROS_LBM_H */

@@ -1,0 +1,330 @@
+"""ctypes bindings of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Loaded by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` — as the checker, never as the thing measured on the product
+path. Two builds of the same C restatement: ``precision="f32"`` (bitwise the
+reference's float arithmetic) and ``precision="f64"`` (the FP64 run).
+``RefHarness`` drives the reference's own sources (built in place by
+``make ref``; only where the reference tree exists).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "aeros-engine_gb300"))
+from aeros_gb300.capi import LbmParams, LbmStats, ThermalParams, VoxelGrid, VoxelPlan  # noqa: E402
+
+_FP = C.POINTER(C.c_float)
+_U8P = C.POINTER(C.c_uint8)
+_DP = C.POINTER(C.c_double)
+
+
+def build(quiet: bool = True) -> None:
+    """Compiles the oracle libraries (and the reference harness when the
+    reference tree is present)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"], stdout=out)
+    if os.path.isdir("/root/reference/aeros/src"):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref"], stdout=out)
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(_FP)
+
+
+def u8ptr(a: np.ndarray):
+    return a.ctypes.data_as(_U8P)
+
+
+_libs: dict[str, C.CDLL] = {}
+
+
+def oracle_lib(precision: str = "f32") -> C.CDLL:
+    if precision not in _libs:
+        path = os.path.join(HERE, f"liboracle_{precision}.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.ao_lbm_create.restype = C.c_void_p
+        L.ao_lbm_create.argtypes = [C.POINTER(LbmParams), _U8P]
+        L.ao_lbm_destroy.argtypes = [C.c_void_p]
+        L.ao_thermal_init.argtypes = [C.c_void_p, C.POINTER(ThermalParams)]
+        L.ao_thermal_upload.argtypes = [C.c_void_p, _FP]
+        L.ao_lbm_step.argtypes = [C.c_void_p, C.c_int]
+        L.ao_lbm_get_stats.argtypes = [C.c_void_p, C.POINTER(LbmStats)]
+        L.ao_lbm_get_fields.argtypes = [C.c_void_p] + [_FP] * 6
+        L.ao_lbm_get_fields_f64.argtypes = [C.c_void_p] + [_DP] * 4
+        L.ao_lbm_get_populations.argtypes = [C.c_void_p, _FP]
+        L.ao_lbm_set_populations.argtypes = [C.c_void_p, _FP]
+        L.ao_lbm_set_equilibrium.argtypes = [C.c_void_p, _FP, _FP, _FP, _FP]
+        L.ao_lbm_get_wall_dist.argtypes = [C.c_void_p, _U8P]
+        L.ao_thermal_get.argtypes = [C.c_void_p, _FP, _FP]
+        L.ao_lbm_cv_force.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, _DP]
+        L.ao_lbm_cv_force_box.argtypes = [C.c_void_p, C.POINTER(C.c_int32), _DP]
+        L.ao_lbm_projected_area.restype = C.c_double
+        L.ao_lbm_projected_area.argtypes = [C.c_void_p, C.c_int]
+        L.ao_equilibrium_moments.argtypes = [C.c_float] * 4 + [_FP] * 4
+        L.ao_voxelize_brute.argtypes = [_FP, C.c_int64, C.POINTER(VoxelGrid), _U8P]
+        L.ao_count_hits_brute.argtypes = [_FP, C.c_int64, _FP, C.c_int]
+        L.ao_voxel_plan.argtypes = [_FP, C.c_int, C.c_uint64, C.POINTER(VoxelPlan)]
+        L.ao_set_threads.argtypes = [C.c_int]
+        _libs[precision] = L
+    return _libs[precision]
+
+
+def set_threads(n: int, precision: str = "f32") -> int:
+    return oracle_lib(precision).ao_set_threads(int(n))
+
+
+class OracleLBM:
+    """One domain of the C restatement."""
+
+    def __init__(self, params: LbmParams, mask: np.ndarray, precision: str = "f32"):
+        self.L = oracle_lib(precision)
+        self.precision = precision
+        self.shape = (params.nz, params.ny, params.nx)
+        self.n = params.nx * params.ny * params.nz
+        self.mask = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+        assert self.mask.size == self.n
+        self.h = self.L.ao_lbm_create(C.byref(params), u8ptr(self.mask))
+        if not self.h:
+            raise RuntimeError("oracle create failed")
+
+    def close(self):
+        if self.h:
+            self.L.ao_lbm_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def thermal_init(self, tp: ThermalParams) -> None:
+        if self.L.ao_thermal_init(self.h, C.byref(tp)) != 0:
+            raise RuntimeError("oracle thermal init failed")
+
+    def thermal_upload(self, T: np.ndarray) -> None:
+        t = np.ascontiguousarray(T, dtype=np.float32).reshape(-1)
+        self.L.ao_thermal_upload(self.h, fptr(t))
+
+    def step(self, n: int) -> None:
+        self.L.ao_lbm_step(self.h, int(n))
+
+    def stats(self) -> dict:
+        s = LbmStats()
+        self.L.ao_lbm_get_stats(self.h, C.byref(s))
+        return s.as_dict()
+
+    def fields(self) -> dict:
+        out = {k: np.empty(self.n, np.float32) for k in ("rho", "ux", "uy", "uz", "strain", "tke")}
+        self.L.ao_lbm_get_fields(self.h, *(fptr(out[k]) for k in ("rho", "ux", "uy", "uz", "strain", "tke")))
+        return out
+
+    def fields_f64(self) -> dict:
+        out = {k: np.empty(self.n, np.float64) for k in ("rho", "ux", "uy", "uz")}
+        self.L.ao_lbm_get_fields_f64(self.h, *(out[k].ctypes.data_as(_DP) for k in ("rho", "ux", "uy", "uz")))
+        return out
+
+    def populations(self) -> np.ndarray:
+        f = np.empty((19, self.n), np.float32)
+        self.L.ao_lbm_get_populations(self.h, fptr(f))
+        return f
+
+    def set_populations(self, f: np.ndarray) -> None:
+        a = np.ascontiguousarray(f, dtype=np.float32)
+        self.L.ao_lbm_set_populations(self.h, fptr(a))
+
+    def set_equilibrium(self, rho, ux, uy, uz) -> None:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (rho, ux, uy, uz)]
+        self.L.ao_lbm_set_equilibrium(self.h, *(None if a is None else fptr(a) for a in arrs))
+
+    def wall_dist(self) -> np.ndarray:
+        w = np.empty(self.n, np.uint8)
+        self.L.ao_lbm_get_wall_dist(self.h, u8ptr(w))
+        return w
+
+    def thermal(self) -> tuple[np.ndarray, np.ndarray]:
+        T = np.empty(self.n, np.float32)
+        b = np.empty(self.n, np.float32)
+        self.L.ao_thermal_get(self.h, fptr(T), fptr(b))
+        return T, b
+
+    def cv_force(self, hx=0.3, hy=0.3, hz=0.3) -> np.ndarray:
+        out = np.zeros(3, np.float64)
+        self.L.ao_lbm_cv_force(self.h, hx, hy, hz, out.ctypes.data_as(_DP))
+        return out
+
+    def cv_force_box(self, box) -> np.ndarray:
+        b = (C.c_int32 * 6)(*[int(v) for v in box])
+        out = np.zeros(3, np.float64)
+        self.L.ao_lbm_cv_force_box(self.h, b, out.ctypes.data_as(_DP))
+        return out
+
+    def projected_area(self, axis: int) -> float:
+        return float(self.L.ao_lbm_projected_area(self.h, int(axis)))
+
+
+def equilibrium_moments(rho, ux, uy, uz):
+    L = oracle_lib("f32")
+    out = np.zeros(4, np.float32)
+    ptrs = [C.cast(out.ctypes.data + 4 * i, _FP) for i in range(4)]
+    ok = L.ao_equilibrium_moments(rho, ux, uy, uz, *ptrs)
+    return bool(ok), tuple(float(v) for v in out)
+
+
+def voxelize_brute(tris: np.ndarray, grid: VoxelGrid) -> np.ndarray:
+    L = oracle_lib("f32")
+    t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+    m = np.zeros(grid.nx * grid.ny * grid.nz, np.uint8)
+    rc = L.ao_voxelize_brute(fptr(t), t.size // 9, C.byref(grid), u8ptr(m))
+    if rc != 0:
+        raise RuntimeError("oracle voxelize failed")
+    return m
+
+
+def count_hits_brute(tris: np.ndarray, origin, axis: int) -> int:
+    L = oracle_lib("f32")
+    t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+    o = np.asarray(origin, np.float32)
+    return L.ao_count_hits_brute(fptr(t), t.size // 9, fptr(o), int(axis))
+
+
+def voxel_plan(size, res: int, budget: int = 0) -> VoxelPlan:
+    L = oracle_lib("f32")
+    s = np.asarray(size, np.float32)
+    p = VoxelPlan()
+    L.ao_voxel_plan(fptr(s), int(res), int(budget), C.byref(p))
+    return p
+
+
+class RefHarness:
+    """The reference's own solver sources (oracle/_ref/libaeros_ref.so)."""
+
+    PATH = os.path.join(HERE, "_ref", "libaeros_ref.so")
+
+    @classmethod
+    def available(cls) -> bool:
+        return os.path.exists(cls.PATH)
+
+    def __init__(self):
+        L = C.CDLL(self.PATH)
+        L.ref_lbm_setup.argtypes = [C.c_int, C.c_int, C.c_int, _U8P, C.c_int, C.c_float, C.c_float, C.c_float,
+                                    C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _FP,
+                                    C.c_float, _FP]
+        L.ref_thermal_setup.argtypes = [C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float]
+        L.ref_thermal_upload.argtypes = [_FP]
+        L.ref_thermal_get.argtypes = [_FP, _FP, _FP, _FP]
+        L.ref_lbm_set_uniform.argtypes = [C.c_float] * 3
+        L.ref_lbm_step.argtypes = [C.c_int]
+        L.ref_lbm_get_fields.argtypes = [_FP] * 6
+        L.ref_lbm_get_populations.argtypes = [_FP]
+        L.ref_lbm_set_populations.argtypes = [_FP]
+        L.ref_lbm_get_wall_dist.argtypes = [_U8P]
+        L.ref_lbm_stats.argtypes = [_FP, C.POINTER(C.c_longlong)]
+        L.ref_lbm_cv_force.argtypes = [C.c_float] * 3 + [_FP]
+        L.ref_lbm_projected_area.restype = C.c_float
+        L.ref_lbm_projected_area.argtypes = [C.c_int]
+        L.ref_equilibrium_moments.argtypes = [C.c_float] * 4 + [_FP]
+        L.ref_voxelize.argtypes = [_FP, C.c_longlong, C.c_int, C.c_int, C.c_int, _FP, _FP, _U8P]
+        L.ref_count_hits.argtypes = [_FP, C.c_longlong, _FP, C.c_int]
+        L.ref_voxel_plan.argtypes = [_FP, C.c_int, C.c_ulonglong, C.POINTER(C.c_int)]
+        self.L = L
+        self.n = 0
+
+    def setup(self, nx, ny, nz, solid, *, ground_rows=0, tau=0.6, u0=0.08, smag=0.12, les=False, trt=False,
+              periodic_x=False, periodic_z=False, convective=False, flow_axis=0, flow_sign=1,
+              body_force=(0.0, 0.0, 0.0), flow_speed=1.0):
+        s = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+        bf = np.asarray(body_force, np.float32)
+        uin = np.zeros(3, np.float32)
+        rc = self.L.ref_lbm_setup(nx, ny, nz, u8ptr(s), int(ground_rows), tau, u0, smag, int(les), int(trt),
+                                  int(periodic_x), int(periodic_z), int(convective), int(flow_axis),
+                                  int(flow_sign), fptr(bf), flow_speed, fptr(uin))
+        if rc != 0:
+            raise RuntimeError(f"reference setup failed: {rc}")
+        self.n = nx * ny * nz
+        return uin
+
+    def thermal_setup(self, rayleigh, prandtl, fixed, hot, cold, perturbation):
+        if self.L.ref_thermal_setup(rayleigh, prandtl, int(fixed), hot, cold, perturbation) != 0:
+            raise RuntimeError("reference thermal setup failed")
+
+    def thermal_upload(self, T):
+        t = np.ascontiguousarray(T, dtype=np.float32).reshape(-1)
+        self.L.ref_thermal_upload(fptr(t))
+
+    def thermal(self):
+        T = np.empty(self.n, np.float32)
+        b = np.empty(self.n, np.float32)
+        nu = np.zeros(1, np.float32)
+        mt = np.zeros(1, np.float32)
+        self.L.ref_thermal_get(fptr(T), fptr(b), fptr(nu), fptr(mt))
+        return T, b, float(nu[0]), float(mt[0])
+
+    def set_uniform(self, ux, uy, uz):
+        self.L.ref_lbm_set_uniform(ux, uy, uz)
+
+    def step(self, n):
+        self.L.ref_lbm_step(int(n))
+
+    def fields(self) -> dict:
+        out = {k: np.empty(self.n, np.float32) for k in ("rho", "ux", "uy", "uz", "strain", "tke")}
+        self.L.ref_lbm_get_fields(*(fptr(out[k]) for k in ("rho", "ux", "uy", "uz", "strain", "tke")))
+        return out
+
+    def populations(self):
+        f = np.empty((19, self.n), np.float32)
+        self.L.ref_lbm_get_populations(fptr(f))
+        return f
+
+    def set_populations(self, f):
+        a = np.ascontiguousarray(f, dtype=np.float32)
+        self.L.ref_lbm_set_populations(fptr(a))
+
+    def wall_dist(self):
+        w = np.empty(self.n, np.uint8)
+        self.L.ref_lbm_get_wall_dist(u8ptr(w))
+        return w
+
+    def stats(self) -> dict:
+        fs = np.zeros(6, np.float32)
+        is_ = (C.c_longlong * 6)()
+        self.L.ref_lbm_stats(fptr(fs), is_)
+        keys_f = ("avg_rho", "avg_kinetic", "max_velocity_lb", "avg_tke", "convergence", "converged")
+        keys_i = ("step", "negative_pops", "bad_pops", "rho_out_of_range", "rho_non_finite", "u_limited")
+        d = {k: float(v) for k, v in zip(keys_f, fs)}
+        d.update({k: int(v) for k, v in zip(keys_i, is_)})
+        return d
+
+    def cv_force(self, hx=0.3, hy=0.3, hz=0.3):
+        out = np.zeros(3, np.float32)
+        self.L.ref_lbm_cv_force(hx, hy, hz, fptr(out))
+        return out
+
+    def projected_area(self, axis):
+        return float(self.L.ref_lbm_projected_area(int(axis)))
+
+    def equilibrium_moments(self, rho, ux, uy, uz):
+        out = np.zeros(4, np.float32)
+        ok = self.L.ref_equilibrium_moments(rho, ux, uy, uz, fptr(out))
+        return bool(ok), tuple(float(v) for v in out)
+
+    def voxelize(self, tris, nx, ny, nz, mn, cs):
+        t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+        m = np.zeros(nx * ny * nz, np.uint8)
+        self.L.ref_voxelize(fptr(t), t.size // 9, nx, ny, nz, fptr(np.asarray(mn, np.float32)),
+                            fptr(np.asarray(cs, np.float32)), u8ptr(m))
+        return m
+
+    def count_hits(self, tris, origin, axis):
+        t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+        return self.L.ref_count_hits(fptr(t), t.size // 9, fptr(np.asarray(origin, np.float32)), int(axis))
+
+    def voxel_plan(self, size, res, budget):
+        out = (C.c_int * 6)()
+        self.L.ref_voxel_plan(fptr(np.asarray(size, np.float32)), int(res), int(budget), out)
+        return tuple(out)

@@ -1,0 +1,230 @@
+// ref_harness.cpp — drives the reference's OWN solver sources (TEST
+// INFRASTRUCTURE ONLY). oracle/Makefile compiles this translation unit
+// together with the reference sources where they lie (never copied into this
+// repository) into oracle/_ref/libaeros_ref.so; tests/golden/make_golden.py
+// uses it to pin the C restatement (lbm_oracle.c) and to write the golden
+// fixtures under tests/golden/.
+//
+// The solver's state (f, fNext, lbmWallDist, the thermal populations) is
+// file-static in the reference, so the two solver files are included into
+// this unit, the way the reference's own headless tests link them with stubs
+// for GL/GLFW/CUDA (aeros/tests/physics_ref_headless.cpp:40-45).
+#include "lbm.cpp"
+#include "thermal_lbm.cpp"
+
+#include <cstdint>
+#include <cstring>
+
+#include "mesh_bvh.h"
+
+extern "C" double glfwGetTime(void) { static double t = 0.0; return (t += 1.0 / 60.0); }
+extern "C" void setVoxelData(const int*, const float*, int, int, int, float, float, float, float, float, float) {}
+extern "C" int cudaConsumeError(char* buf, int sz) { if (buf && sz > 0) buf[0] = 0; return 0; }
+void updateVertexColors() {}
+void computeLiftDrag() {}
+void drawModel() {}
+
+extern "C" {
+
+// Grid of one cell per world unit starting at 0, domain padding 0: the solver
+// grid equals the mask grid (dimensions >= 8, lbm.cpp:505). Ground: rows
+// y <= ground_rows-1 (lbm.cpp:624-643). Flow direction from axis/sign via the
+// reference's own azimuth/elevation path. u0 = |inlet| (the reference forces
+// 0.08 when u0 < 1e-6, lbm.cpp:196). Returns 0 on success and writes the
+// inlet velocity the reference derived.
+int ref_lbm_setup(int nx, int ny, int nz, const uint8_t* solid, int ground_rows,
+                  float tau, float u0, float smag, int les, int trt,
+                  int periodic_x, int periodic_z, int convective, int flow_axis, int flow_sign,
+                  const float* body_force, float flow_speed, float* u_in_out) {
+    g_voxNx = nx; g_voxNy = ny; g_voxNz = nz;
+    g_voxMinX = 0.0f; g_voxMinY = 0.0f; g_voxMinZ = 0.0f;
+    g_voxMaxX = (float)nx; g_voxMaxY = (float)ny; g_voxMaxZ = (float)nz;
+    g_voxelData.assign((size_t)nx * ny * nz, 0);
+    g_distanceField.assign((size_t)nx * ny * nz, 0.0f);
+    for (size_t i = 0; i < (size_t)nx * ny * nz; ++i) g_voxelData[i] = solid[i] ? 1 : 0;
+    minBB = glm::vec3(0.0f); maxBB = glm::vec3((float)nx, (float)ny, (float)nz);
+    center = 0.5f * maxBB; maxDim = (float)std::max(nx, std::max(ny, nz));
+    voxelResolution = nx;
+    flowSpeed = flow_speed;
+    flowAzimuth = 0.0f; flowElevation = 0.0f;
+    if (flow_axis == 0 && flow_sign < 0) flowAzimuth = 180.0f;
+    if (flow_axis == 2) flowAzimuth = flow_sign > 0 ? 90.0f : -90.0f;
+    if (flow_axis == 1) flowElevation = flow_sign > 0 ? 90.0f : -90.0f;
+    altitude = 0.0f; timeScale = 1.0f; aeroMachEffects = false; aeroGroundEffect = false;
+    lbmParams.enabled = true;
+    lbmParams.useGPU = false;
+    lbmParams.U0 = u0;
+    lbmParams.stepsPerFrame = 1;
+    lbmParams.tau = tau;
+    lbmParams.smagorinskyC = smag;
+    lbmParams.useTurbulence = les != 0;
+    lbmParams.useTRT = trt != 0;
+    lbmParams.useGround = ground_rows > 0;
+    lbmParams.groundHeight = ground_rows > 0 ? (float)ground_rows - 0.5f : 0.0f;
+    lbmParams.inletTurbulence = 0.0f;
+    lbmParams.domainPadding = 0.0f;
+    lbmParams.autoViscosity = false;
+    lbmParams.useConvectiveOutlet = convective != 0;
+    lbmParams.periodicX = periodic_x != 0;
+    lbmParams.periodicZ = periodic_z != 0;
+    lbmParams.bodyForceX = body_force[0];
+    lbmParams.bodyForceY = body_force[1];
+    lbmParams.bodyForceZ = body_force[2];
+    lbmParams.convergenceThreshold = 1e-5f;
+    thermalParams.enabled = false;   // thermal is attached by ref_thermal_setup
+    shutdownLBM();
+    initLBM();
+    if (!lbmInitialized) return -1;
+    if (lbmNx != nx || lbmNy != ny || lbmNz != nz) return -2;
+    float ux, uy, uz;
+    computeInletVelocityLB(ux, uy, uz);
+    u_in_out[0] = ux; u_in_out[1] = uy; u_in_out[2] = uz;
+    return 0;
+}
+
+// Thermal module on the current grid (thermalInit through initLBM's call
+// site, lbm.cpp:876-885).
+int ref_thermal_setup(float rayleigh, float prandtl, int fixed, float hot, float cold, float perturbation) {
+    thermalParams.enabled = true;
+    thermalParams.rayleigh = rayleigh;
+    thermalParams.prandtl = prandtl;
+    thermalParams.fixedWallTemps = fixed != 0;
+    thermalParams.hotTemp = hot;
+    thermalParams.coldTemp = cold;
+    thermalParams.perturbation = perturbation;
+    std::vector<char> m(lbmIsSolid.begin(), lbmIsSolid.end());
+    for (size_t i = 0; i < m.size(); ++i) if (lbmIsGround[i]) m[i] = 1;
+    return thermalInit(lbmNx, lbmNy, lbmNz, m, lbmParams.viscosity) ? 0 : -1;
+}
+
+void ref_thermal_disable() { thermalParams.enabled = false; thermalShutdown(); }
+
+int ref_thermal_upload(const float* T) {
+    std::vector<float> v(T, T + (size_t)lbmNx * lbmNy * lbmNz);
+    return thermalUpload(v) ? 0 : -1;
+}
+
+void ref_thermal_get(float* T, float* buoy, float* nusselt, float* mean_t) {
+    const size_t n = (size_t)lbmNx * lbmNy * lbmNz;
+    if (T) std::memcpy(T, thermalT.data(), n * sizeof(float));
+    if (buoy) std::memcpy(buoy, thermalBuoyancyY.data(), n * sizeof(float));
+    if (nusselt) *nusselt = thermalNusselt;
+    if (mean_t) *mean_t = thermalMeanT;
+}
+
+// Overwrite the initial populations with the equilibrium at u_init for fluid
+// cells (the reference cannot start from rest: lbm.cpp:196).
+void ref_lbm_set_uniform(float ux, float uy, float uz) {
+    const int total = lbmNx * lbmNy * lbmNz;
+    float usqr = ux * ux + uy * uy + uz * uz;
+    for (int c = 0; c < total; ++c) {
+        if (lbmIsSolid[c] || lbmIsGround[c]) continue;
+        for (int q = 0; q < Q; ++q) f[(size_t)c * Q + q] = computeEquilibriumFast(q, 1.0f, ux, uy, uz, usqr);
+    }
+}
+
+// One call per step: stepLBMCPU(n) with n > 1 keeps the raw population
+// pointers taken before its first swap (lbm.cpp:937-938 vs :1546), so only
+// single-step calls advance the lattice correctly; every reference test and
+// the reference bench call it with 1.
+void ref_lbm_step(int n) { for (int i = 0; i < n; ++i) stepLBMCPU(1); }
+
+void ref_lbm_get_fields(float* rho, float* ux, float* uy, float* uz, float* strain, float* tke) {
+    const size_t n = (size_t)lbmNx * lbmNy * lbmNz;
+    if (rho) std::memcpy(rho, lbmRho.data(), n * 4);
+    if (ux) std::memcpy(ux, lbmUx.data(), n * 4);
+    if (uy) std::memcpy(uy, lbmUy.data(), n * 4);
+    if (uz) std::memcpy(uz, lbmUz.data(), n * 4);
+    if (strain) std::memcpy(strain, lbmStrainMag.data(), n * 4);
+    if (tke) std::memcpy(tke, lbmTKEField.data(), n * 4);
+}
+
+// Pre-collision populations, written SoA [19][cells].
+void ref_lbm_get_populations(float* out) {
+    const size_t n = (size_t)lbmNx * lbmNy * lbmNz;
+    for (size_t c = 0; c < n; ++c)
+        for (int q = 0; q < Q; ++q) out[(size_t)q * n + c] = f[c * Q + q];
+}
+
+void ref_lbm_set_populations(const float* in) {
+    const size_t n = (size_t)lbmNx * lbmNy * lbmNz;
+    for (size_t c = 0; c < n; ++c)
+        for (int q = 0; q < Q; ++q) f[c * Q + q] = in[(size_t)q * n + c];
+}
+
+void ref_lbm_get_wall_dist(uint8_t* out) {
+    std::memcpy(out, lbmWallDist.data(), lbmWallDist.size());
+}
+
+// Scalars of the last step: avgRho, KE, maxU, TKE, convergence, converged,
+// step, negPops, badPops, rhoOut, rhoNonFin, uLim.
+void ref_lbm_stats(float* fs, long long* is) {
+    fs[0] = lbmAvgRho; fs[1] = lbmAvgKineticEnergy; fs[2] = lbmMaxVelocityLB; fs[3] = lbmTKE;
+    fs[4] = lbmConvergence; fs[5] = lbmConverged ? 1.0f : 0.0f;
+    is[0] = lbmCurrentStep; is[1] = lbmNegativePops; is[2] = lbmBadPops; is[3] = lbmRhoOutOfRange;
+    is[4] = lbmRhoNonFinite; is[5] = lbmULimited;
+}
+
+void ref_lbm_cv_force(float hx, float hy, float hz, float* out) {
+    glm::vec3 F = lbmControlVolumeForce(hx, hy, hz);
+    out[0] = F.x; out[1] = F.y; out[2] = F.z;
+}
+
+float ref_lbm_projected_area(int axis) { return lbmProjectedAreaCells(axis); }
+
+int ref_equilibrium_moments(float rho, float ux, float uy, float uz, float* out4) {
+    return lbmEquilibriumMoments(rho, ux, uy, uz, &out4[0], &out4[1], &out4[2], &out4[3]) ? 1 : 0;
+}
+
+// The voxelizer's mask loop (voxel_grid.cpp:313-351) at explicit cell centres.
+int ref_voxelize(const float* tris, long long ntri, int nx, int ny, int nz,
+                 const float* mn, const float* cs, uint8_t* mask) {
+    std::vector<meshbvh::Triangle> tv;
+    tv.reserve((size_t)ntri);
+    for (long long i = 0; i < ntri; ++i) {
+        const float* v = tris + 9 * i;
+        const glm::vec3 a(v[0], v[1], v[2]), b(v[3], v[4], v[5]), c(v[6], v[7], v[8]);
+        if (!std::isfinite(a.x) || !std::isfinite(a.y) || !std::isfinite(a.z) ||
+            !std::isfinite(b.x) || !std::isfinite(b.y) || !std::isfinite(b.z) ||
+            !std::isfinite(c.x) || !std::isfinite(c.y) || !std::isfinite(c.z)) continue;
+        meshbvh::Triangle t = meshbvh::makeTriangle(a, b, c);
+        if (meshbvh::isDegenerate(t)) continue;
+        tv.push_back(t);
+    }
+    meshbvh::BVH bvh;
+    if (!tv.empty()) bvh.build(tv);
+    const glm::vec3 cell(cs[0], cs[1], cs[2]);
+    std::memset(mask, 0, (size_t)nx * ny * nz);
+    if (tv.empty()) return 0;
+#pragma omp parallel for collapse(3) schedule(dynamic, 4)
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                const glm::vec3 p(mn[0] + (i + 0.5f) * cs[0], mn[1] + (j + 0.5f) * cs[1], mn[2] + (k + 0.5f) * cs[2]);
+                if (bvh.inside(p, cell)) mask[((size_t)k * ny + j) * nx + i] = 1;
+            }
+    return (int)bvh.nodeCount();
+}
+
+int ref_count_hits(const float* tris, long long ntri, const float* o, int axis) {
+    std::vector<meshbvh::Triangle> tv;
+    for (long long i = 0; i < ntri; ++i) {
+        const float* v = tris + 9 * i;
+        meshbvh::Triangle t = meshbvh::makeTriangle(glm::vec3(v[0], v[1], v[2]), glm::vec3(v[3], v[4], v[5]),
+                                                    glm::vec3(v[6], v[7], v[8]));
+        if (meshbvh::isDegenerate(t)) continue;
+        tv.push_back(t);
+    }
+    meshbvh::BVH bvh;
+    bvh.build(tv);
+    glm::vec3 d(axis == 0 ? 1.0f : 0.0f, axis == 1 ? 1.0f : 0.0f, axis == 2 ? 1.0f : 0.0f);
+    return bvh.countIntersections(glm::vec3(o[0], o[1], o[2]), d);
+}
+
+void ref_voxel_plan(const float* size, int res, unsigned long long budget, int* out6) {
+    VoxelPlan p = voxelPlan(glm::vec3(size[0], size[1], size[2]), res, budget);
+    out6[0] = p.nx; out6[1] = p.ny; out6[2] = p.nz; out6[3] = p.fits ? 1 : 0;
+    out6[4] = p.suggestedRes; out6[5] = (int)p.cells;
+}
+
+}  // extern "C"
