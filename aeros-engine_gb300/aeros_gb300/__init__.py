@@ -1,0 +1,8 @@
+"""GB300 lattice-Boltzmann solver step (host side over the C ABI).
+
+``capi``: ctypes mirror of include/aeros_lbm.h; ``solver``: one device domain;
+``geometry``: seeded meshes and solver configurations; ``batch`` / ``serve``:
+many domains stepped together and the continuous-batching request loop.
+"""
+from . import capi, geometry, solver  # noqa: F401
+from .solver import Solver, voxel_grid, voxelize  # noqa: F401

@@ -1,0 +1,179 @@
+"""Python handle over the C ABI: one solver domain on the GPU.
+
+Mirrors the reference solver's operations (aeros/src/lbm.h:156-202,
+aeros/src/thermal_lbm.h:62-72) on an explicit grid: create (initLBM), step
+(stepLBMCPU), field / population readback, control-volume force, projected
+area, thermal init / upload / readback. Every call goes through
+libaeros_gb300.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import LbmParams, LbmStats, ThermalParams, VoxelGrid, check, lib
+
+_FP = C.POINTER(C.c_float)
+_U8P = C.POINTER(C.c_uint8)
+_DP = C.POINTER(C.c_double)
+
+
+def _f(a: np.ndarray):
+    return a.ctypes.data_as(_FP)
+
+
+class Solver:
+    """One lattice domain (D3Q19 + optional D3Q7) resident on the device."""
+
+    def __init__(self, params: LbmParams, mask: np.ndarray, stream: int | None = None):
+        self.params = params
+        self.n = params.nx * params.ny * params.nz
+        self.shape = (params.nz, params.ny, params.nx)
+        m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+        if m.size != self.n:
+            raise ValueError(f"mask has {m.size} cells, grid has {self.n}")
+        h = C.c_void_p()
+        check(lib().aeros_lbm_create(C.byref(params), m.ctypes.data_as(_U8P), C.byref(h)), "aeros_lbm_create")
+        self.h = h
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().aeros_lbm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream: int) -> None:
+        check(lib().aeros_lbm_set_stream(self.h, C.c_void_p(stream)), "set_stream")
+
+    def synchronize(self) -> None:
+        check(lib().aeros_lbm_synchronize(self.h), "synchronize")
+
+    # ---- stepping --------------------------------------------------------
+    def step(self, n: int = 1) -> None:
+        check(lib().aeros_lbm_step(self.h, int(n)), "aeros_lbm_step")
+
+    def step_async(self, n: int = 1) -> None:
+        check(lib().aeros_lbm_step_async(self.h, int(n)), "aeros_lbm_step_async")
+
+    def stats(self) -> dict:
+        s = LbmStats()
+        check(lib().aeros_lbm_get_stats(self.h, C.byref(s)), "get_stats")
+        return s.as_dict()
+
+    def last_step_ms(self) -> float:
+        v = C.c_float()
+        check(lib().aeros_lbm_last_step_ms(self.h, C.byref(v)), "last_step_ms")
+        return float(v.value)
+
+    def last_launch_count(self) -> int:
+        v = C.c_int64()
+        check(lib().aeros_lbm_last_launch_count(self.h, C.byref(v)), "last_launch_count")
+        return int(v.value)
+
+    def device_bytes(self) -> int:
+        v = C.c_uint64()
+        check(lib().aeros_lbm_device_bytes(self.h, C.byref(v)), "device_bytes")
+        return int(v.value)
+
+    # ---- state I/O -------------------------------------------------------
+    def fields(self) -> dict:
+        out = {k: np.empty(self.n, np.float32) for k in ("rho", "ux", "uy", "uz", "strain", "tke")}
+        check(lib().aeros_lbm_read_fields(self.h, *(_f(out[k]) for k in ("rho", "ux", "uy", "uz", "strain", "tke"))),
+              "read_fields")
+        return out
+
+    def device_fields(self) -> dict:
+        ptrs = [C.c_void_p() for _ in range(4)]
+        check(lib().aeros_lbm_device_fields(self.h, *(C.byref(p) for p in ptrs)), "device_fields")
+        return dict(zip(("rho", "ux", "uy", "uz"), (p.value for p in ptrs)))
+
+    def populations(self) -> np.ndarray:
+        f = np.empty((19, self.n), np.float32)
+        check(lib().aeros_lbm_read_populations(self.h, _f(f)), "read_populations")
+        return f
+
+    def write_populations(self, f: np.ndarray) -> None:
+        a = np.ascontiguousarray(f, dtype=np.float32)
+        if a.size != 19 * self.n:
+            raise ValueError("populations must be [19][cells]")
+        check(lib().aeros_lbm_write_populations(self.h, _f(a)), "write_populations")
+
+    def set_equilibrium(self, rho, ux, uy, uz) -> None:
+        arr = [None if a is None else np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (rho, ux, uy, uz)]
+        check(lib().aeros_lbm_set_equilibrium(self.h, *(None if a is None else _f(a) for a in arr)), "set_equilibrium")
+
+    def mask(self) -> tuple[np.ndarray, np.ndarray]:
+        m = np.empty(self.n, np.uint8)
+        w = np.empty(self.n, np.uint8)
+        check(lib().aeros_lbm_read_mask(self.h, m.ctypes.data_as(_U8P), w.ctypes.data_as(_U8P)), "read_mask")
+        return m, w
+
+    # ---- thermal ---------------------------------------------------------
+    def thermal_init(self, tp: ThermalParams) -> None:
+        check(lib().aeros_lbm_thermal_init(self.h, C.byref(tp)), "thermal_init")
+
+    def thermal_upload(self, T: np.ndarray) -> None:
+        t = np.ascontiguousarray(T, dtype=np.float32).reshape(-1)
+        check(lib().aeros_lbm_thermal_upload(self.h, _f(t)), "thermal_upload")
+
+    def thermal(self) -> tuple[np.ndarray, np.ndarray]:
+        T = np.empty(self.n, np.float32)
+        b = np.empty(self.n, np.float32)
+        check(lib().aeros_lbm_thermal_read(self.h, _f(T), _f(b)), "thermal_read")
+        return T, b
+
+    # ---- forces ----------------------------------------------------------
+    def cv_force(self, hx: float = 0.3, hy: float = 0.3, hz: float = 0.3) -> np.ndarray:
+        out = np.zeros(3, np.float64)
+        check(lib().aeros_lbm_cv_force(self.h, hx, hy, hz, out.ctypes.data_as(_DP)), "cv_force")
+        return out
+
+    def cv_force_box(self, box) -> np.ndarray:
+        b = (C.c_int32 * 6)(*[int(v) for v in box])
+        out = np.zeros(3, np.float64)
+        check(lib().aeros_lbm_cv_force_box(self.h, b, out.ctypes.data_as(_DP)), "cv_force_box")
+        return out
+
+    def projected_area(self, axis: int) -> float:
+        v = C.c_double()
+        check(lib().aeros_lbm_projected_area(self.h, int(axis), C.byref(v)), "projected_area")
+        return float(v.value)
+
+
+def voxel_grid(n, mn, cell) -> VoxelGrid:
+    g = VoxelGrid()
+    g.nx, g.ny, g.nz = (int(v) for v in n)
+    for i in range(3):
+        g.min[i] = float(mn[i])
+        g.cell[i] = float(cell[i])
+    return g
+
+
+def voxelize(tris: np.ndarray, grid: VoxelGrid) -> np.ndarray:
+    """Solid mask (1 = inside) at the grid's cell centres, computed on the GPU."""
+    t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+    m = np.zeros(grid.nx * grid.ny * grid.nz, np.uint8)
+    check(lib().aeros_voxelize(_f(t), t.size // 9, C.byref(grid), m.ctypes.data_as(_U8P)), "voxelize")
+    return m
+
+
+def voxel_plan(size, res: int, budget: int = 0) -> capi.VoxelPlan:
+    s = np.asarray(size, np.float32)
+    p = capi.VoxelPlan()
+    check(lib().aeros_voxel_plan(_f(s), int(res), int(budget), C.byref(p)), "voxel_plan")
+    return p

@@ -1,0 +1,76 @@
+"""In-tree build of libaeros_gb300.so for sm_103a (no cmake, parallel nvcc).
+
+Translation units and their floating-point contraction:
+  lbm_fp32.cu  --fmad=false  drop-in form, rounds every operation as the reference
+  lbm_half.cu  --fmad=true   FP16/BF16 shifted storage
+  forces.cu    --fmad=false  per-cell momentum-flux terms as the reference
+  voxel.cu     --fmad=false  bit-exact inside test
+  capi.cu      --fmad=false  host code with -ffp-contract=off
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "lib")
+BUILD_DIR = os.path.join(HERE, "_build")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-warn-spills"]
+UNITS = {
+    "lbm_fp32.cu": ["--fmad=false"],
+    "lbm_half.cu": ["--fmad=true"],
+    "forces.cu": ["--fmad=false"],
+    "voxel.cu": ["--fmad=false"],
+    "capi.cu": ["--fmad=false"],
+}
+HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh"]
+
+
+def nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return "nvcc"
+
+
+def _stale(obj: str, src: str) -> bool:
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    deps = [src] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(os.path.dirname(HERE), "include", "aeros_lbm.h")]
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _compile(unit: str, flags: list[str], verbose: bool) -> str:
+    src = os.path.join(CSRC, unit)
+    obj = os.path.join(BUILD_DIR, unit.replace(".cu", ".o"))
+    if _stale(obj, src):
+        cmd = [nvcc(), *ARCH, *COMMON, *flags, "-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {unit}:\n{r.stdout}\n{r.stderr}")
+        if verbose and r.stderr.strip():
+            print(r.stderr, file=sys.stderr)
+    return obj
+
+
+def build(verbose: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    os.makedirs(OUT_DIR, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
+    lib = os.path.join(OUT_DIR, "libaeros_gb300.so")
+    if not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", lib]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

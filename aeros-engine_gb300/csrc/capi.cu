@@ -1,0 +1,1051 @@
+// capi.cu — the C ABI (include/aeros_lbm.h): solver handles, device memory,
+// launches, and the record/consume error convention of the reference CUDA
+// layer (aeros/src/kernel.cu:57-82).
+//
+// Host arithmetic that must match the reference bit for bit (inlet
+// equilibrium, thermal parameters, conduction seed) is compiled with
+// -ffp-contract=off.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/aeros_lbm.h"
+#include "forces.cuh"
+#include "lbm_aux.cuh"
+
+using namespace aeros;
+
+// ---------------------------------------------------------------------------
+// error record (thread-local), consumed by aeros_consume_error
+// ---------------------------------------------------------------------------
+static thread_local int g_err_code = 0;
+static thread_local char g_err_msg[1024] = {0};
+
+static int set_error(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+static int set_error(int code, const char* fmt, ...) {
+    g_err_code = code;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err_msg, sizeof(g_err_msg), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                                    \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return set_error(AEROS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" int aeros_consume_error(char* buf, int buf_size) {
+    if (g_err_code == 0) {
+        if (buf && buf_size > 0) buf[0] = 0;
+        return 0;
+    }
+    if (buf && buf_size > 0) snprintf(buf, (size_t)buf_size, "%s", g_err_msg);
+    const int c = g_err_code;
+    g_err_code = 0;
+    g_err_msg[0] = 0;
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+struct aeros_lbm {
+    aeros_lbm_params p{};
+    int nx = 0, ny = 0, nz = 0, ncell = 0;
+    long long qstride = 0;
+    const Launchers* L = nullptr;
+    size_t esize = 4;
+    // device memory
+    void* f = nullptr;
+    uint32_t* desc = nullptr;
+    int* shell = nullptr;
+    float* u[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    float *rho = nullptr, *strain = nullptr, *tke = nullptr;
+    float* out[2] = {nullptr, nullptr};
+    int out_plane = 0;
+    void* g = nullptr;
+    float* T = nullptr;
+    float* T_buoy = nullptr;
+    Partial* partials = nullptr;
+    int max_grid = 0;
+    Control* ctl = nullptr;
+    Control* ctl_host = nullptr;   // pinned
+    double* force_partials = nullptr;
+    double* force_out = nullptr;
+    unsigned int* force_counter = nullptr;
+    unsigned long long* area_count = nullptr;
+    uint64_t dev_bytes = 0;
+    // host geometry
+    std::vector<uint8_t> mask, wall;
+    int n_interior = 0, n_shell = 0, fluid_cells = 1;
+    int outlet_mode = 0;
+    float feq_in[19] = {0};
+    float conv = 0.08f;
+    // layout state of the AA pattern
+    bool next_odd = false;        // next step gathers from neighbours
+    bool overrides_next = false;  // next gather applies inlet/outlet overrides
+    int out_par = 1;              // side buffer written by the next step
+    int ubuf = 0;                 // u[ubuf] holds the latest velocity
+    int grid[2][2] = {{0, 0}, {0, 0}};
+    // thermal
+    bool th_on = false;
+    aeros_thermal_params tp{};
+    int ylo = 0, yhi = 0;
+    float H = 1, tau_t = 0.7f, alpha = 0, glb = 0;
+    int th_buoy_mode = 1;
+    bool th_stepped = false;
+    // stats
+    aeros_lbm_stats stats{};
+    bool stats_dirty = false;
+    long long kexec_before = 0;
+    bool last_diverged = false;
+    // timing
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    long long last_launches = 0;
+    int sm_count = 0;
+};
+
+template <class T>
+static int dalloc(aeros_lbm* h, T** p, size_t bytes) {
+    cudaError_t e = cudaMalloc((void**)p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_error(AEROS_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    h->dev_bytes += bytes;
+    return AEROS_OK;
+}
+
+static void free_handle(aeros_lbm* h) {
+    if (!h) return;
+    cudaFree(h->f);
+    cudaFree(h->desc);
+    cudaFree(h->shell);
+    for (auto& b : h->u)
+        for (auto& c : b) cudaFree(c);
+    cudaFree(h->rho);
+    cudaFree(h->strain);
+    cudaFree(h->tke);
+    cudaFree(h->out[0]);
+    cudaFree(h->out[1]);
+    cudaFree(h->g);
+    cudaFree(h->T);
+    cudaFree(h->T_buoy);
+    cudaFree(h->partials);
+    cudaFree(h->ctl);
+    cudaFree(h->force_partials);
+    cudaFree(h->force_out);
+    cudaFree(h->force_counter);
+    cudaFree(h->area_count);
+    if (h->ctl_host) cudaFreeHost(h->ctl_host);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    delete h;
+}
+
+static inline int cidx(const aeros_lbm* h, int x, int y, int z) { return (z * h->ny + y) * h->nx + x; }
+
+// Per-cell descriptor: links, wall distance (chamfer, lbm.cpp:647-675), LES
+// eligibility (lbm.cpp:994-1011), inlet/outlet planes, outlet side buffer slot.
+static void build_descriptor(aeros_lbm* h, std::vector<uint32_t>& desc, std::vector<int>& shell) {
+    const int nx = h->nx, ny = h->ny, nz = h->nz, n = h->ncell;
+    const auto& m = h->mask;
+    auto& wd = h->wall;
+    wd.assign(n, 255);
+    for (int c = 0; c < n; ++c)
+        if (m[c]) wd[c] = 0;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y) {
+            const int row = (z * ny + y) * nx;
+            for (int x = 0; x < nx; ++x) {
+                int v = wd[row + x];
+                if (v == 0) continue;
+                if (x > 0 && wd[row + x - 1] + 1 < v) v = wd[row + x - 1] + 1;
+                if (y > 0 && wd[row - nx + x] + 1 < v) v = wd[row - nx + x] + 1;
+                if (z > 0 && wd[row - nx * ny + x] + 1 < v) v = wd[row - nx * ny + x] + 1;
+                wd[row + x] = (uint8_t)v;
+            }
+        }
+    for (int z = nz - 1; z >= 0; --z)
+        for (int y = ny - 1; y >= 0; --y) {
+            const int row = (z * ny + y) * nx;
+            for (int x = nx - 1; x >= 0; --x) {
+                int v = wd[row + x];
+                if (v == 0) continue;
+                if (x < nx - 1 && wd[row + x + 1] + 1 < v) v = wd[row + x + 1] + 1;
+                if (y < ny - 1 && wd[row + nx + x] + 1 < v) v = wd[row + nx + x] + 1;
+                if (z < nz - 1 && wd[row + nx * ny + x] + 1 < v) v = wd[row + nx * ny + x] + 1;
+                wd[row + x] = (uint8_t)v;
+            }
+        }
+    const int ax = h->p.flow_axis, sg = h->p.flow_sign;
+    const int na = ax == 0 ? nx : (ax == 1 ? ny : nz);
+    const int oc = sg > 0 ? na - 1 : 0, ic = sg > 0 ? na - 2 : 1, ic2 = sg > 0 ? na - 3 : 2;
+    const int ip = sg > 0 ? 0 : na - 1;
+    desc.assign(n, 0);
+    shell.clear();
+    h->fluid_cells = 0;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const int c = cidx(h, x, y, z);
+                uint32_t d = 0;
+                const bool wall = m[c] != AEROS_CELL_FLUID;
+                if (wall) d |= D_WALL;
+                else ++h->fluid_cells;
+                if (m[c] == AEROS_CELL_GROUND) d |= D_GROUND;
+                const bool on_shell = x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
+                if (on_shell) {
+                    d |= D_SHELL;
+                    shell.push_back(c);
+                }
+                for (int q = 1; q < Q19; ++q) {
+                    const int sx = x - cx19(q), sy = y - cy19(q), sz = z - cz19(q);
+                    const bool in = sx >= 0 && sx < nx && sy >= 0 && sy < ny && sz >= 0 && sz < nz;
+                    if (!in || m[cidx(h, sx, sy, sz)] != AEROS_CELL_FLUID) d |= 1u << q;
+                }
+                d |= (uint32_t)std::min<int>(wd[c], 6) << D_WD_SHIFT;
+                const int pos[3] = {x, y, z};
+                const bool inl = pos[ax] == ip, outl = pos[ax] == oc;
+                if (inl) d |= D_INLET;
+                if (outl) d |= D_OUTLET;
+                if (!wall && !inl && !outl && !on_shell) {
+                    const int nbs[6] = {c - 1, c + 1, c - nx, c + nx, c - nx * ny, c + nx * ny};
+                    bool ok = true;
+                    for (int k = 0; k < 6; ++k)
+                        if (m[nbs[k]] == AEROS_CELL_SOLID) ok = false;
+                    if (ok) d |= D_LES;
+                }
+                if (h->outlet_mode && !wall) {
+                    int slot = 0;
+                    if (pos[ax] == oc) slot = 1;
+                    else if (pos[ax] == ic) slot = 2;
+                    else if (pos[ax] == ic2) slot = 3;
+                    d |= (uint32_t)slot << D_OUT_SHIFT;
+                }
+                desc[c] = d;
+            }
+    if (h->fluid_cells < 1) h->fluid_cells = 1;
+    h->n_shell = (int)shell.size();
+    h->n_interior = (nx - 2) * (ny - 2) * (nz - 2);
+}
+
+static void fill_args(const aeros_lbm* h, FillArgs& fa, const float u[3]) {
+    fa.f = h->f;
+    fa.desc = h->desc;
+    fa.qstride = h->qstride;
+    fa.ncell = h->ncell;
+    const float ux = u[0], uy = u[1], uz = u[2];
+    float usqr = ux * ux + uy * uy + uz * uz;
+    float vx = ux, vy = uy, vz = uz;
+    if (usqr > 0.09f) {   // init limiter, lbm.cpp:725-730
+        const float s = sqrtf(0.09f / usqr);
+        vx *= s; vy *= s; vz *= s;
+        usqr = vx * vx + vy * vy + vz * vz;
+    }
+    for (int q = 0; q < Q19; ++q) {
+        fa.fluid[q] = eq_checked(q, 1.0f, vx, vy, vz, usqr);
+        fa.wall[q] = eq_checked(q, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+static int check_params(const aeros_lbm_params* p) {
+    if (!p) return set_error(AEROS_ERR_INVALID, "params is NULL");
+    if (p->nx < 4 || p->ny < 4 || p->nz < 4)
+        return set_error(AEROS_ERR_INVALID, "grid %dx%dx%d: every dimension must be >= 4", p->nx, p->ny, p->nz);
+    const long long n = (long long)p->nx * p->ny * p->nz;
+    if (n > (1ll << 30)) return set_error(AEROS_ERR_INVALID, "grid of %lld cells exceeds 2^30", n);
+    if (p->storage < AEROS_STORE_FP32 || p->storage > AEROS_STORE_BF16)
+        return set_error(AEROS_ERR_INVALID, "unknown storage %d", p->storage);
+    if (p->flow_axis < 0 || p->flow_axis > 2 || (p->flow_sign != 1 && p->flow_sign != -1))
+        return set_error(AEROS_ERR_INVALID, "flow axis %d / sign %d", p->flow_axis, p->flow_sign);
+    if (p->lateral_bc != AEROS_LATERAL_COPY && p->lateral_bc != AEROS_LATERAL_FREESLIP)
+        return set_error(AEROS_ERR_INVALID, "unknown lateral_bc %d", p->lateral_bc);
+    if (p->outlet_bc != AEROS_OUTLET_REFERENCE && p->outlet_bc != AEROS_OUTLET_ZEROGRAD)
+        return set_error(AEROS_ERR_INVALID, "unknown outlet_bc %d", p->outlet_bc);
+    if (p->lateral_bc == AEROS_LATERAL_FREESLIP && !p->periodic_x && p->flow_axis != 0 &&
+        p->outlet_bc == AEROS_OUTLET_REFERENCE && !p->convective_outlet)
+        return set_error(AEROS_ERR_UNSUPPORTED, "free-slip lateral walls need an overriding outlet");
+    if (p->lateral_bc == AEROS_LATERAL_FREESLIP && !p->periodic_x && p->outlet_bc == AEROS_OUTLET_REFERENCE &&
+        !p->convective_outlet)
+        return set_error(AEROS_ERR_UNSUPPORTED, "free-slip lateral walls need a convective or zero-gradient outlet");
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* mask, aeros_lbm** out) {
+    if (!out) return set_error(AEROS_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (int rc = check_params(params)) return rc;
+    if (!mask) return set_error(AEROS_ERR_INVALID, "mask is NULL");
+    aeros_lbm* h = new (std::nothrow) aeros_lbm();
+    if (!h) return set_error(AEROS_ERR_ALLOC, "host allocation failed");
+    h->p = *params;
+    h->nx = params->nx; h->ny = params->ny; h->nz = params->nz;
+    h->ncell = h->nx * h->ny * h->nz;
+    h->qstride = ((long long)h->ncell + 63) / 64 * 64;
+    h->L = params->storage == AEROS_STORE_FP32 ? &launchers_fp32()
+         : params->storage == AEROS_STORE_FP16 ? &launchers_fp16() : &launchers_bf16();
+    h->esize = params->storage == AEROS_STORE_FP32 ? 4 : 2;
+    h->outlet_mode = params->periodic_x ? 0
+                   : (params->outlet_bc == AEROS_OUTLET_ZEROGRAD ? 2 : (params->convective_outlet ? 1 : 0));
+    h->mask.assign(mask, mask + h->ncell);
+    for (auto& v : h->mask)
+        if (v > AEROS_CELL_GROUND) v = AEROS_CELL_SOLID;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
+
+    std::vector<uint32_t> desc;
+    std::vector<int> shell;
+    build_descriptor(h, desc, shell);
+    int rc = AEROS_OK;
+    const size_t n = (size_t)h->ncell;
+#define ALLOC(ptr, bytes)                        \
+    if ((rc = dalloc(h, &(ptr), (bytes))) != 0) { \
+        free_handle(h);                          \
+        return rc;                               \
+    }
+    ALLOC(h->f, (size_t)h->qstride * Q19 * h->esize);
+    ALLOC(h->desc, n * 4);
+    ALLOC(h->shell, (size_t)std::max(1, h->n_shell) * 4);
+    for (auto& b : h->u)
+        for (auto& c : b) ALLOC(c, n * 4);
+    ALLOC(h->rho, n * 4);
+    ALLOC(h->strain, n * 4);
+    ALLOC(h->tke, n * 4);
+    const int ax = params->flow_axis;
+    h->out_plane = ax == 0 ? h->ny * h->nz : (ax == 1 ? h->nx * h->nz : h->nx * h->ny);
+    if (h->outlet_mode) {
+        ALLOC(h->out[0], (size_t)3 * Q19 * h->out_plane * 4);
+        ALLOC(h->out[1], (size_t)3 * Q19 * h->out_plane * 4);
+    }
+    h->max_grid = std::max(1, h->sm_count) * 8;
+    ALLOC(h->partials, (size_t)h->max_grid * sizeof(Partial));
+    ALLOC(h->ctl, sizeof(Control));
+    ALLOC(h->force_partials, (size_t)h->max_grid * 3 * sizeof(double));
+    ALLOC(h->force_out, 4 * sizeof(double));
+    ALLOC(h->force_counter, sizeof(unsigned int));
+    ALLOC(h->area_count, sizeof(unsigned long long));
+#undef ALLOC
+    if (cudaMallocHost((void**)&h->ctl_host, sizeof(Control)) != cudaSuccess) {
+        free_handle(h);
+        return set_error(AEROS_ERR_ALLOC, "pinned control block allocation failed");
+    }
+    auto fail = [&](cudaError_t e, const char* what) {
+        free_handle(h);
+        return set_error(AEROS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return fail(e, "cudaEventCreate");
+    if ((e = cudaMemcpy(h->desc, desc.data(), n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "desc upload");
+    if (h->n_shell && (e = cudaMemcpy(h->shell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e, "shell upload");
+    for (auto& b : h->u)
+        for (auto& c : b)
+            if ((e = cudaMemset(c, 0, n * 4)) != cudaSuccess) return fail(e, "u memset");
+    if ((e = cudaMemset(h->strain, 0, n * 4)) != cudaSuccess) return fail(e, "memset");
+    if ((e = cudaMemset(h->force_counter, 0, 4)) != cudaSuccess) return fail(e, "memset");
+    if ((e = cudaMemset(h->tke, 0, n * 4)) != cudaSuccess) return fail(e, "memset");
+    {
+        std::vector<float> ones(n, 1.0f);
+        if ((e = cudaMemcpy(h->rho, ones.data(), n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "rho init");
+    }
+    Control c0;
+    memset(&c0, 0, sizeof(c0));
+    c0.avg_rho = 1.0f;
+    if ((e = cudaMemcpy(h->ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "ctl init");
+    *h->ctl_host = c0;
+
+    // inlet equilibrium in storage form (lbm.cpp:1414-1429) and convective
+    // coefficient (lbm.cpp:1468-1470)
+    const float ui0 = params->u_in[0], ui1 = params->u_in[1], ui2 = params->u_in[2];
+    const float usq = ui0 * ui0 + ui1 * ui1 + ui2 * ui2;
+    const bool shifted = params->storage != AEROS_STORE_FP32;
+    for (int q = 0; q < Q19; ++q) {
+        const float v = eq_checked(q, 1.0f, ui0, ui1, ui2, usq);
+        h->feq_in[q] = shifted ? v - w19(q) : v;
+    }
+    float U0mag = sqrtf(usq);
+    if (!std::isfinite(U0mag) || U0mag < 1e-6f) U0mag = 0.08f;
+    float conv = U0mag * 0.8f;
+    if (conv > 0.5f) conv = 0.5f;
+    if (conv < 0.01f) conv = 0.08f;
+    h->conv = conv;
+
+    FillArgs fa;
+    fill_args(h, fa, params->u_init);
+    if ((e = h->L->fill_uniform(fa, nullptr)) != cudaSuccess) return fail(e, "fill");
+    if (h->outlet_mode) {
+        // side buffer entries of wall cells hold what the reference reads
+        // from a wall cell's populations on that step parity: the initial
+        // equilibrium on odd steps, zero on even steps
+        for (int par = 0; par < 2; ++par) {
+            std::vector<float> ob((size_t)3 * Q19 * h->out_plane);
+            for (int pl = 0; pl < 3; ++pl)
+                for (int q = 0; q < Q19; ++q) {
+                    const float plain = par == 1 ? fa.wall[q] : 0.0f;
+                    for (int k = 0; k < h->out_plane; ++k)
+                        ob[((size_t)pl * Q19 + q) * h->out_plane + k] = shifted ? plain - w19(q) : plain;
+                }
+            if ((e = cudaMemcpy(h->out[par], ob.data(), ob.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+                return fail(e, "outlet buffer init");
+        }
+    }
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "init");
+    for (int o = 0; o < 2; ++o)
+        for (int t = 0; t < 2; ++t) h->grid[o][t] = std::min(h->max_grid, std::max(1, h->sm_count) * h->L->occupancy(o, t));
+    h->stats.avg_rho = 1.0f;
+    h->stats.fluid_cells = h->fluid_cells;
+    *out = h;
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_destroy(aeros_lbm* h) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    cudaStreamSynchronize(h->stream);
+    free_handle(h);
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_set_stream(aeros_lbm* h, void* s) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    h->stream = (cudaStream_t)s;
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_synchronize(aeros_lbm* h) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return AEROS_OK;
+}
+
+static void base_args(const aeros_lbm* h, StepArgs& A) {
+    memset(&A, 0, sizeof(A));
+    A.nx = h->nx; A.ny = h->ny; A.nz = h->nz; A.nxny = h->nx * h->ny; A.ncell = h->ncell;
+    A.qstride = h->qstride;
+    A.n_interior = h->n_interior;
+    A.ntiles_interior = (h->n_interior + STEP_BLOCK - 1) / STEP_BLOCK;
+    A.n_shell = h->n_shell;
+    A.ntiles = A.ntiles_interior + (h->n_shell + STEP_BLOCK - 1) / STEP_BLOCK;
+    A.div_ix = FastDiv((uint32_t)(h->nx - 2));
+    A.div_iy = FastDiv((uint32_t)(h->ny - 2));
+    A.div_x = FastDiv((uint32_t)h->nx);
+    A.div_y = FastDiv((uint32_t)h->ny);
+    A.f = h->f; A.desc = h->desc; A.shell = h->shell;
+    A.rho = h->rho; A.strain = h->strain; A.tke = h->tke;
+    A.out_plane = h->out_plane;
+    A.g = h->g; A.T = h->T; A.T_buoy = h->T_buoy;
+    A.partials = h->partials; A.ctl = h->ctl;
+    const aeros_lbm_params& p = h->p;
+    float tau0 = p.tau;   // lbm.cpp:918-920
+    if (!std::isfinite(tau0) || tau0 < 0.51f) tau0 = 0.55f;
+    if (tau0 > 1.5f) tau0 = 1.5f;
+    A.tau0 = tau0;
+    float Cs = p.smagorinsky_c;   // lbm.cpp:1130-1133
+    if (!std::isfinite(Cs) || Cs < 0.0f) Cs = 0.12f;
+    if (Cs > 0.3f) Cs = 0.3f;
+    A.Cs = Cs;
+    A.velScale2 = p.vel_scale * p.vel_scale;
+    A.Fx = p.body_force[0]; A.Fy = p.body_force[1]; A.Fz = p.body_force[2];
+    for (int i = 0; i < 3; ++i) A.uin[i] = p.u_in[i];
+    for (int q = 0; q < Q19; ++q) A.feq_in[q] = h->feq_in[q];
+    A.conv = h->conv;
+    A.flow_axis = p.flow_axis; A.flow_sign = p.flow_sign;
+    A.periodic_x = p.periodic_x; A.periodic_z = p.periodic_z;
+    A.use_trt = p.use_trt; A.use_les = p.use_les;
+    A.freeslip = p.lateral_bc == AEROS_LATERAL_FREESLIP;
+    A.outlet_mode = h->outlet_mode;
+    A.total_div10 = h->ncell / 10;
+    A.fluid_cells = h->fluid_cells;
+    A.conv_threshold = p.convergence_threshold;
+    A.th_on = h->th_on;
+    if (h->th_on) {
+        A.th_fixed = h->tp.fixed_wall_temps;
+        A.th_ylo = h->ylo;
+        A.th_invtau = 1.0f / h->tau_t;
+        A.th_hot = h->tp.hot_temp;
+        A.th_cold = h->tp.cold_temp;
+        A.th_tref = 0.5f * (h->tp.hot_temp + h->tp.cold_temp);
+        A.th_glb = h->glb;
+        A.th_H = h->H;
+        A.th_buoy_mode = h->th_buoy_mode;
+        A.th_rows_n = (double)((long)h->nx * (long)h->nz * (long)(h->yhi - h->ylo + 1));
+    }
+}
+
+// Brings both lattices into the layout an even step gathers from with no
+// pending overrides (after init, reset, or materialize + write-back).
+static int normalize_layout(aeros_lbm* h);
+
+static int launch_materialize(aeros_lbm* h, float* d_f, float* d_g) {
+    StepArgs A;
+    base_args(h, A);
+    A.mat_f = d_f;
+    A.mat_g = d_g;
+    A.apply_overrides = h->overrides_next;
+    A.out_r = h->out[h->out_par ^ 1];
+    A.out_w = h->out[h->out_par];
+    A.up[0] = A.up[1] = A.up[2] = h->u[h->ubuf][0];
+    const int grid = h->grid[h->next_odd][h->th_on];
+    CUDA_TRY(h->L->step(A, h->next_odd, h->th_on, true, grid, h->stream));
+    return AEROS_OK;
+}
+
+static int normalize_layout(aeros_lbm* h) {
+    if (!h->next_odd && !h->overrides_next) return AEROS_OK;
+    float *df = nullptr, *dg = nullptr;
+    const size_t n = (size_t)h->ncell;
+    if (cudaMalloc((void**)&df, n * Q19 * 4) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "normalize buffer");
+    if (h->th_on && cudaMalloc((void**)&dg, n * Q7 * 4) != cudaSuccess) {
+        cudaFree(df);
+        return set_error(AEROS_ERR_ALLOC, "normalize buffer");
+    }
+    int rc = launch_materialize(h, df, dg);
+    if (rc == AEROS_OK) {
+        cudaError_t e = h->L->write_pre(h->f, h->desc, h->qstride, h->ncell, df, Q19, 0.0f, h->stream);
+        if (e == cudaSuccess && h->th_on)
+            e = h->L->write_pre(h->g, h->desc, h->qstride, h->ncell, dg, Q7,
+                                0.5f * (h->tp.hot_temp + h->tp.cold_temp), h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = set_error(AEROS_ERR_CUDA, "normalize: %s", cudaGetErrorString(e));
+    }
+    cudaFree(df);
+    cudaFree(dg);
+    if (rc == AEROS_OK) {
+        h->next_odd = false;
+        h->overrides_next = false;
+    }
+    return rc;
+}
+
+static int enqueue_steps(aeros_lbm* h, int nsteps) {
+    if (nsteps < 0) return set_error(AEROS_ERR_INVALID, "nsteps %d < 0", nsteps);
+    h->last_launches = 0;
+    h->kexec_before = h->ctl_host->kexec;
+    CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    StepArgs A;
+    base_args(h, A);
+    for (int i = 0; i < nsteps; ++i) {
+        A.apply_overrides = h->overrides_next;
+        A.out_w = h->out[h->out_par];
+        A.out_r = h->out[h->out_par ^ 1];
+        for (int k = 0; k < 3; ++k) {
+            A.up[k] = h->u[h->ubuf][k];
+            A.uc[k] = h->u[h->ubuf ^ 1][k];
+        }
+        A.write_obs = (i == nsteps - 1);
+        A.write_u = h->p.use_les || A.write_obs;
+        A.th_buoy_mode = h->th_buoy_mode;
+        const int grid = h->grid[h->next_odd][h->th_on];
+        CUDA_TRY(h->L->step(A, h->next_odd, h->th_on, false, grid, h->stream));
+        h->last_launches++;
+        h->next_odd = !h->next_odd;
+        h->overrides_next = true;
+        h->out_par ^= 1;
+        h->ubuf ^= 1;
+        if (h->th_on) {
+            h->th_buoy_mode = 0;
+            h->th_stepped = true;
+        }
+    }
+    CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(Control), cudaMemcpyDeviceToHost, h->stream));
+    h->stats_dirty = true;
+    h->last_diverged = false;
+    return AEROS_OK;
+}
+
+// Reads the control block of the last enqueued batch; on a tripped
+// divergence guard re-equilibrates (lbm.cpp:1583-1600).
+static int finish_batch(aeros_lbm* h) {
+    if (!h->stats_dirty) return AEROS_OK;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->stats_dirty = false;
+    Control& c = *h->ctl_host;
+    aeros_lbm_stats& s = h->stats;
+    if (c.halt) {
+        const long long executed = c.kexec - h->kexec_before;
+        const long long launched = h->last_launches;
+        // undo the host-side layout bookkeeping of launches that returned early
+        const long long skipped = launched - executed;
+        if (skipped & 1) {
+            h->ubuf ^= 1;
+            h->out_par ^= 1;
+        }
+        FillArgs fa;
+        fill_args(h, fa, h->p.u_in);
+        for (int q = 0; q < Q19; ++q) fa.fluid[q] = eq_checked(q, 1.0f, h->p.u_in[0], h->p.u_in[1], h->p.u_in[2],
+                                                                h->p.u_in[0] * h->p.u_in[0] + h->p.u_in[1] * h->p.u_in[1] +
+                                                                    h->p.u_in[2] * h->p.u_in[2]);
+        const float* uin = h->p.u_in;
+        CUDA_TRY(h->L->reset(h->f, h->desc, h->qstride, h->ncell, fa, h->rho, h->u[h->ubuf][0], h->u[h->ubuf][1],
+                             h->u[h->ubuf][2], uin, h->stream));
+        h->next_odd = false;
+        h->overrides_next = false;
+        const float usqr = uin[0] * uin[0] + uin[1] * uin[1] + uin[2] * uin[2];
+        c.avg_rho = 1.0f;
+        c.avg_ke = usqr;
+        c.halt = 0;
+        c.halt_kind = 0;
+        // clear the device flag; keep the statistics the guard left
+        Control dc = c;
+        dc.blocks_done = 0;
+        CUDA_TRY(cudaMemcpyAsync(h->ctl, &dc, sizeof(Control), cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        h->last_diverged = true;
+    }
+    s.step = c.steps;
+    s.avg_rho = c.avg_rho;
+    s.avg_kinetic = c.avg_ke;
+    s.avg_tke = c.avg_tke;
+    s.max_velocity_lb = c.max_u;
+    s.convergence = c.convergence;
+    s.converged = c.converged;
+    s.diverged = h->last_diverged ? 1 : 0;
+    s.negative_pops = c.neg;
+    s.bad_pops = c.bad;
+    s.rho_out_of_range = c.rout;
+    s.rho_non_finite = c.rnf;
+    s.u_limited = c.ulim;
+    s.nan_count = c.nan;
+    s.sum_rho = c.sum_rho;
+    s.sum_kinetic = c.sum_ke;
+    s.sum_tke = c.sum_tke;
+    s.nusselt = c.nusselt;
+    s.mean_t = c.mean_t;
+    s.fluid_cells = h->fluid_cells;
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_step_async(aeros_lbm* h, int nsteps) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    if (int rc = finish_batch(h)) return rc;
+    return enqueue_steps(h, nsteps);
+}
+
+extern "C" int aeros_lbm_step(aeros_lbm* h, int nsteps) {
+    if (int rc = aeros_lbm_step_async(h, nsteps)) return rc;
+    return finish_batch(h);
+}
+
+extern "C" int aeros_lbm_get_stats(aeros_lbm* h, aeros_lbm_stats* out) {
+    if (!h || !out) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (int rc = finish_batch(h)) return rc;
+    *out = h->stats;
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_last_step_ms(aeros_lbm* h, float* ms) {
+    if (!h || !ms) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    CUDA_TRY(cudaEventSynchronize(h->ev1));
+    CUDA_TRY(cudaEventElapsedTime(ms, h->ev0, h->ev1));
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_last_launch_count(aeros_lbm* h, int64_t* n) {
+    if (!h || !n) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    *n = h->last_launches;
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_device_bytes(aeros_lbm* h, uint64_t* b) {
+    if (!h || !b) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    *b = h->dev_bytes;
+    return AEROS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// state I/O
+// ---------------------------------------------------------------------------
+extern "C" int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float* uy, float* uz, float* strain,
+                                     float* tke) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    if (int rc = finish_batch(h)) return rc;
+    const size_t b = (size_t)h->ncell * 4;
+    if (rho) CUDA_TRY(cudaMemcpyAsync(rho, h->rho, b, cudaMemcpyDeviceToHost, h->stream));
+    if (ux) CUDA_TRY(cudaMemcpyAsync(ux, h->u[h->ubuf][0], b, cudaMemcpyDeviceToHost, h->stream));
+    if (uy) CUDA_TRY(cudaMemcpyAsync(uy, h->u[h->ubuf][1], b, cudaMemcpyDeviceToHost, h->stream));
+    if (uz) CUDA_TRY(cudaMemcpyAsync(uz, h->u[h->ubuf][2], b, cudaMemcpyDeviceToHost, h->stream));
+    if (strain) CUDA_TRY(cudaMemcpyAsync(strain, h->strain, b, cudaMemcpyDeviceToHost, h->stream));
+    if (tke) CUDA_TRY(cudaMemcpyAsync(tke, h->tke, b, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_device_fields(aeros_lbm* h, const float** rho, const float** ux, const float** uy,
+                                       const float** uz) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    if (int rc = finish_batch(h)) return rc;
+    if (rho) *rho = h->rho;
+    if (ux) *ux = h->u[h->ubuf][0];
+    if (uy) *uy = h->u[h->ubuf][1];
+    if (uz) *uz = h->u[h->ubuf][2];
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_read_populations(aeros_lbm* h, float* f) {
+    if (!h || !f) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (int rc = finish_batch(h)) return rc;
+    float* df = nullptr;
+    const size_t n = (size_t)h->ncell;
+    if (cudaMalloc((void**)&df, n * Q19 * 4) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "readback buffer");
+    float* dg = nullptr;
+    if (h->th_on && cudaMalloc((void**)&dg, n * Q7 * 4) != cudaSuccess) {
+        cudaFree(df);
+        return set_error(AEROS_ERR_ALLOC, "readback buffer");
+    }
+    int rc = launch_materialize(h, df, dg);
+    if (rc == AEROS_OK) {
+        cudaError_t e = cudaMemcpyAsync(f, df, n * Q19 * 4, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = set_error(AEROS_ERR_CUDA, "readback: %s", cudaGetErrorString(e));
+    }
+    cudaFree(df);
+    cudaFree(dg);
+    if (rc) return rc;
+    // wall cells: initial equilibrium (never touched by the solver)
+    for (size_t c = 0; c < n; ++c)
+        if (h->mask[c])
+            for (int q = 0; q < Q19; ++q) f[(size_t)q * n + c] = w19(q);
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_write_populations(aeros_lbm* h, const float* f) {
+    if (!h || !f) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (int rc = finish_batch(h)) return rc;
+    if (int rc = normalize_layout(h)) return rc;
+    float* df = nullptr;
+    const size_t n = (size_t)h->ncell;
+    if (cudaMalloc((void**)&df, n * Q19 * 4) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "upload buffer");
+    cudaError_t e = cudaMemcpyAsync(df, f, n * Q19 * 4, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = h->L->write_pre(h->f, h->desc, h->qstride, h->ncell, df, Q19, 0.0f, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(df);
+    if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "write populations: %s", cudaGetErrorString(e));
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_set_equilibrium(aeros_lbm* h, const float* rho, const float* ux, const float* uy,
+                                         const float* uz) {
+    if (!h || !ux || !uy || !uz) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (int rc = finish_batch(h)) return rc;
+    if (int rc = normalize_layout(h)) return rc;
+    const size_t n = (size_t)h->ncell;
+    float* d = nullptr;
+    if (cudaMalloc((void**)&d, n * 4 * 4) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "upload buffer");
+    cudaError_t e = cudaSuccess;
+    if (rho) e = cudaMemcpyAsync(d, rho, n * 4, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d + n, ux, n * 4, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d + 2 * n, uy, n * 4, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d + 3 * n, uz, n * 4, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = h->L->set_equilibrium(h->f, h->desc, h->qstride, h->ncell, rho ? d : nullptr, d + n, d + 2 * n, d + 3 * n,
+                                  h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "set equilibrium: %s", cudaGetErrorString(e));
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_read_mask(aeros_lbm* h, uint8_t* mask, uint8_t* wall_dist) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    if (mask) memcpy(mask, h->mask.data(), h->mask.size());
+    if (wall_dist) memcpy(wall_dist, h->wall.data(), h->wall.size());
+    return AEROS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// thermal (host side mirrors thermal_lbm.cpp:84-197)
+// ---------------------------------------------------------------------------
+static bool th_wall_temp(const aeros_lbm* h, int y, float* Tw) {
+    if (!h->tp.fixed_wall_temps) return false;
+    if (y <= 0) { *Tw = h->tp.hot_temp; return true; }
+    if (y >= h->ny - 1) { *Tw = h->tp.cold_temp; return true; }
+    return false;
+}
+
+static int upload_T(aeros_lbm* h, const std::vector<float>& T) {
+    CUDA_TRY(cudaMemcpyAsync(h->T, T.data(), T.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h->L->thermal_fill(h->g, h->qstride, h->ncell, h->T, 0.5f * (h->tp.hot_temp + h->tp.cold_temp), h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_thermal_init(aeros_lbm* h, const aeros_thermal_params* tp) {
+    if (!h || !tp) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (int rc = finish_batch(h)) return rc;
+    if (!tp->enabled) {
+        h->th_on = false;
+        return AEROS_OK;
+    }
+    if (int rc = normalize_layout(h)) return rc;
+    h->tp = *tp;
+    float nu = tp->nu_lb;
+    if (!std::isfinite(nu) || nu <= 0.0f) nu = 0.05f;
+    h->ylo = -1;
+    h->yhi = -1;
+    for (int y = 0; y < h->ny; ++y) {
+        bool fluid = false;
+        for (int z = 0; z < h->nz && !fluid; ++z)
+            for (int x = 0; x < h->nx && !fluid; ++x)
+                if (!h->mask[cidx(h, x, y, z)]) fluid = true;
+        if (fluid) {
+            if (h->ylo < 0) h->ylo = y;
+            h->yhi = y;
+        }
+    }
+    if (h->ylo < 0 || h->yhi <= h->ylo) return set_error(AEROS_ERR_INVALID, "thermal: fewer than two fluid rows");
+    h->H = (float)(h->yhi - h->ylo + 1);
+    const float pr = std::max(0.05f, tp->prandtl);
+    h->alpha = nu / pr;
+    h->tau_t = 0.5f + h->alpha / 0.25f;
+    if (!std::isfinite(h->tau_t) || h->tau_t < 0.505f) h->tau_t = 0.505f;
+    if (h->tau_t > 1.5f) {
+        h->tau_t = 1.5f;
+        h->alpha = 0.25f * (h->tau_t - 0.5f);
+    }
+    const float dT = tp->hot_temp - tp->cold_temp;
+    h->glb = tp->rayleigh * nu * h->alpha / (std::max(1e-6f, std::fabs(dT)) * h->H * h->H * h->H);
+    const size_t n = (size_t)h->ncell;
+    if (!h->g) {
+        int rc;
+        if ((rc = dalloc(h, &h->g, (size_t)h->qstride * Q7 * h->esize))) return rc;
+        if ((rc = dalloc(h, &h->T, n * 4))) return rc;
+        if ((rc = dalloc(h, &h->T_buoy, n * 4))) return rc;
+    }
+    // thermalResetField, thermal_lbm.cpp:154-185
+    std::vector<float> T(n);
+    const float Th = tp->hot_temp, Tc = tp->cold_temp;
+    const float amp = tp->perturbation * (Th - Tc);
+    for (int z = 0; z < h->nz; ++z)
+        for (int y = 0; y < h->ny; ++y)
+            for (int x = 0; x < h->nx; ++x) {
+                const int c = cidx(h, x, y, z);
+                float t;
+                if (h->mask[c]) {
+                    float Tw;
+                    t = th_wall_temp(h, y, &Tw) ? Tw : 0.5f * (Th + Tc);
+                } else {
+                    const float s = (float)(y - h->ylo) / std::max(1.0f, h->H - 1.0f);
+                    t = Th + (Tc - Th) * s;
+                    const float px = 6.2831853f * (float)x / (float)h->nx;
+                    const float py = 3.1415926f * s;
+                    t += amp * std::cos(px) * std::sin(py);
+                }
+                T[c] = t;
+            }
+    h->th_on = true;
+    h->th_buoy_mode = 1;   // buoyancy field starts at zero (thermal_lbm.cpp:132)
+    h->th_stepped = false;
+    Control c = *h->ctl_host;
+    c.nusselt = 0.0f;
+    c.th_valid = 0;
+    {
+        double sum = 0.0;
+        for (int z = 0; z < h->nz; ++z)
+            for (int y = h->ylo; y <= h->yhi; ++y)
+                for (int x = 0; x < h->nx; ++x)
+                    if (!h->mask[cidx(h, x, y, z)]) sum += T[cidx(h, x, y, z)];
+        const long nn = (long)h->nx * h->nz * (h->yhi - h->ylo + 1);
+        c.mean_t = nn > 0 ? (float)(sum / (double)nn) : 0.5f;
+    }
+    *h->ctl_host = c;
+    CUDA_TRY(cudaMemcpy(h->ctl, &c, sizeof(c), cudaMemcpyHostToDevice));
+    h->stats.mean_t = c.mean_t;
+    h->stats.nusselt = 0.0f;
+    return upload_T(h, T);
+}
+
+extern "C" int aeros_lbm_thermal_upload(aeros_lbm* h, const float* T) {
+    if (!h || !T) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (!h->th_on) return set_error(AEROS_ERR_STATE, "thermal lattice not initialised");
+    if (int rc = finish_batch(h)) return rc;
+    if (int rc = normalize_layout(h)) return rc;
+    const size_t n = (size_t)h->ncell;
+    if (h->th_stepped) {
+        // the buoyancy field keeps the last step's values until the next
+        // thermal step (thermalUpload does not touch it)
+        CUDA_TRY(cudaMemcpyAsync(h->T_buoy, h->T, n * 4, cudaMemcpyDeviceToDevice, h->stream));
+        h->th_buoy_mode = 2;
+    }
+    std::vector<float> t(T, T + n);
+    double sum = 0.0;
+    for (int z = 0; z < h->nz; ++z)
+        for (int y = h->ylo; y <= h->yhi; ++y)
+            for (int x = 0; x < h->nx; ++x)
+                if (!h->mask[cidx(h, x, y, z)]) sum += t[cidx(h, x, y, z)];
+    const long nn = (long)h->nx * h->nz * (h->yhi - h->ylo + 1);
+    h->stats.mean_t = nn > 0 ? (float)(sum / (double)nn) : 0.5f;
+    h->ctl_host->mean_t = h->stats.mean_t;
+    CUDA_TRY(cudaMemcpy(&h->ctl->mean_t, &h->stats.mean_t, sizeof(float), cudaMemcpyHostToDevice));
+    return upload_T(h, t);
+}
+
+extern "C" int aeros_lbm_thermal_read(aeros_lbm* h, float* T, float* buoyancy) {
+    if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    if (!h->th_on) return set_error(AEROS_ERR_STATE, "thermal lattice not initialised");
+    if (int rc = finish_batch(h)) return rc;
+    const size_t n = (size_t)h->ncell;
+    std::vector<float> t(n);
+    CUDA_TRY(cudaMemcpy(t.data(), h->T, n * 4, cudaMemcpyDeviceToHost));
+    if (T) memcpy(T, t.data(), n * 4);
+    if (buoyancy) {
+        std::vector<float> tb;
+        if (h->th_buoy_mode == 2) {
+            tb.resize(n);
+            CUDA_TRY(cudaMemcpy(tb.data(), h->T_buoy, n * 4, cudaMemcpyDeviceToHost));
+        }
+        const float tref = 0.5f * (h->tp.hot_temp + h->tp.cold_temp);
+        for (size_t c = 0; c < n; ++c) {
+            if (h->mask[c] || h->th_buoy_mode == 1) buoyancy[c] = 0.0f;
+            else buoyancy[c] = h->glb * ((h->th_buoy_mode == 2 ? tb[c] : t[c]) - tref);
+        }
+    }
+    return AEROS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// forces
+// ---------------------------------------------------------------------------
+extern "C" int aeros_lbm_cv_force_box(aeros_lbm* h, const int32_t box[6], double out[3]) {
+    if (!h || !box || !out) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (int rc = finish_batch(h)) return rc;
+    if (box[0] < 0 || box[1] >= h->nx || box[0] > box[1] || box[2] < 0 || box[3] >= h->ny || box[2] > box[3] ||
+        box[4] < 0 || box[5] >= h->nz || box[4] > box[5])
+        return set_error(AEROS_ERR_INVALID, "box [%d,%d]x[%d,%d]x[%d,%d] outside the grid", box[0], box[1], box[2],
+                         box[3], box[4], box[5]);
+    ForceArgs a;
+    a.nx = h->nx; a.ny = h->ny; a.nz = h->nz;
+    a.desc = h->desc;
+    a.rho = h->rho;
+    a.ux = h->u[h->ubuf][0]; a.uy = h->u[h->ubuf][1]; a.uz = h->u[h->ubuf][2];
+    for (int k = 0; k < 6; ++k) a.box[k] = box[k];
+    a.partials = h->force_partials;
+    a.out = h->force_out;
+    a.counter = h->force_counter;
+    CUDA_TRY(launch_cv_force(a, cv_force_blocks(a.box, h->max_grid), h->stream));
+    double sums[3];
+    CUDA_TRY(cudaMemcpyAsync(sums, h->force_out, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    // force on the body = minus the momentum flux through the box (lbm.cpp:2231)
+    out[0] = -sums[0]; out[1] = -sums[1]; out[2] = -sums[2];
+    return AEROS_OK;
+}
+
+extern "C" int aeros_lbm_cv_force(aeros_lbm* h, float half_x, float half_y, float half_z, double out[3]) {
+    if (!h || !out) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    // box centred on the domain centre, lbm.cpp:2188-2197
+    auto clamp_side = [](int v, int n) { return v < 1 ? 1 : (v > n - 2 ? n - 2 : v); };
+    const int cx = (int)(h->nx * 0.5f), cy = (int)(h->ny * 0.5f), cz = (int)(h->nz * 0.5f);
+    const int hx = std::max(2, (int)(h->nx * half_x));
+    const int hy = std::max(2, (int)(h->ny * half_y));
+    const int hz = std::max(2, (int)(h->nz * half_z));
+    const int32_t box[6] = {clamp_side(cx - hx, h->nx), clamp_side(cx + hx, h->nx), clamp_side(cy - hy, h->ny),
+                            clamp_side(cy + hy, h->ny), clamp_side(cz - hz, h->nz), clamp_side(cz + hz, h->nz)};
+    return aeros_lbm_cv_force_box(h, box, out);
+}
+
+extern "C" int aeros_lbm_projected_area(aeros_lbm* h, int axis, double* area) {
+    if (!h || !area) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (axis < 0 || axis > 2) return set_error(AEROS_ERR_INVALID, "axis %d", axis);
+    if (int rc = finish_batch(h)) return rc;
+    CUDA_TRY(launch_projected_area(h->nx, h->ny, h->nz, h->desc, axis, h->area_count, h->stream));
+    unsigned long long cnt = 0;
+    CUDA_TRY(cudaMemcpyAsync(&cnt, h->area_count, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    *area = (double)cnt;
+    return AEROS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// voxelizer
+// ---------------------------------------------------------------------------
+namespace aeros {
+int voxelize_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask, cudaStream_t s,
+                  char* err, size_t errn);
+}
+
+static int check_grid(const float* tris, int64_t ntri, const aeros_voxel_grid* g) {
+    if (!g) return set_error(AEROS_ERR_INVALID, "grid is NULL");
+    if (ntri < 0 || (ntri > 0 && !tris)) return set_error(AEROS_ERR_INVALID, "triangles");
+    if (ntri > (1ll << 31) / 9) return set_error(AEROS_ERR_INVALID, "%lld triangles exceed the limit", (long long)ntri);
+    if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || (long long)g->nx * g->ny * g->nz > (1ll << 31))
+        return set_error(AEROS_ERR_INVALID, "grid %dx%dx%d", g->nx, g->ny, g->nz);
+    return AEROS_OK;
+}
+
+extern "C" int aeros_voxelize_device(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask) {
+    if (int rc = check_grid(tris, ntri, g)) return rc;
+    if (!d_mask) return set_error(AEROS_ERR_INVALID, "mask is NULL");
+    char err[512] = {0};
+    const int rc = voxelize_impl(tris, ntri, g, d_mask, nullptr, err, sizeof(err));
+    if (rc) return set_error(rc, "%s", err);
+    return AEROS_OK;
+}
+
+extern "C" int aeros_voxelize(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* mask_out) {
+    if (int rc = check_grid(tris, ntri, g)) return rc;
+    if (!mask_out) return set_error(AEROS_ERR_INVALID, "mask is NULL");
+    const size_t total = (size_t)g->nx * g->ny * g->nz;
+    uint8_t* d = nullptr;
+    if (cudaMalloc((void**)&d, total) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "mask buffer");
+    char err[512] = {0};
+    int rc = voxelize_impl(tris, ntri, g, d, nullptr, err, sizeof(err));
+    if (rc == AEROS_OK) {
+        cudaError_t e = cudaMemcpy(mask_out, d, total, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) snprintf(err, sizeof(err), "mask copy: %s", cudaGetErrorString(e)), rc = AEROS_ERR_CUDA;
+    }
+    cudaFree(d);
+    if (rc) return set_error(rc, "%s", err);
+    return AEROS_OK;
+}
+
+// voxelPlan, aeros/src/voxel_grid.cpp:172-215 (224 bytes per cell, res 8..512)
+extern "C" int aeros_voxel_plan(const float size[3], int res, uint64_t budget, aeros_voxel_plan_t* p) {
+    if (!size || !p) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    memset(p, 0, sizeof(*p));
+    p->requested_res = res;
+    const int r = res < 8 ? 8 : (res > 512 ? 512 : res);
+    float sx = size[0], sy = size[1], sz = size[2];
+    if (!(sx > 1e-6f) || !std::isfinite(sx)) sx = 1.0f;
+    if (!(sy > 1e-6f) || !std::isfinite(sy)) sy = 1.0f;
+    if (!(sz > 1e-6f) || !std::isfinite(sz)) sz = 1.0f;
+    const float m = std::max(sx, std::max(sy, sz));
+    auto dims = [&](int rr, int& nx, int& ny, int& nz) {
+        nx = rr;
+        ny = (int)std::floor(rr * sy / m);
+        if (ny < 4) ny = 4;
+        nz = (int)std::floor(rr * sz / m);
+        if (nz < 4) nz = 4;
+    };
+    int nx, ny, nz;
+    dims(r, nx, ny, nz);
+    p->nx = nx; p->ny = ny; p->nz = nz;
+    p->cells = (int64_t)nx * ny * nz;
+    p->bytes = (uint64_t)p->cells * 224ull;
+    p->fits = (budget == 0) || (p->bytes <= budget);
+    if (!p->fits && budget > 0) {
+        const double scale = std::cbrt((double)budget / (double)p->bytes) * 0.95;
+        int cand = (int)(r * scale);
+        for (int guard = 0; guard < 64 && cand >= 8; ++guard, --cand) {
+            int a, b, c;
+            dims(cand, a, b, c);
+            if ((uint64_t)a * b * c * 224ull <= budget) { p->suggested_res = cand; break; }
+        }
+        if (p->suggested_res < 8) p->suggested_res = 0;
+    }
+    return AEROS_OK;
+}

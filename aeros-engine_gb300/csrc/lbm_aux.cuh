@@ -1,0 +1,188 @@
+// lbm_aux.cuh — initialisation, state I/O and divergence-reset kernels, and
+// the per-storage launcher table the C ABI dispatches through.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lbm_step.cuh"
+
+namespace aeros {
+
+// computeEquilibriumFast, aeros/src/lbm.cpp:146-184 (same expression trees).
+__host__ __device__ __forceinline__ float eq_checked(int q, float rho, float ux, float uy, float uz, float usqr) {
+    if (!isfinite(rho)) rho = 1.0f;
+    if (usqr > 0.09f) {
+        const float scale = sqrtf(0.09f / usqr);
+        ux *= scale; uy *= scale; uz *= scale;
+        usqr = ux * ux + uy * uy + uz * uz;
+    }
+    float cu = (float)cx19(q) * ux + (float)cy19(q) * uy + (float)cz19(q) * uz;
+    if (!isfinite(cu)) cu = 0.0f;
+    float feq = w19(q) * rho * (1.0f + cu * 3.0f + cu * cu * 4.5f - usqr * 1.5f);
+    if (!isfinite(feq)) feq = w19(q) * rho;
+    return feq;
+}
+
+struct FillArgs {
+    void* f;
+    const uint32_t* desc;
+    long long qstride;
+    int ncell;
+    float fluid[19];   // plain values
+    float wall[19];
+};
+
+// Uniform equilibrium (initLBM, aeros/src/lbm.cpp:686-739) in pre-collision layout.
+template <class S>
+__global__ void k_fill_uniform(const FillArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncell) return;
+    const bool wall = (a.desc[c] & D_WALL) != 0;
+    typename S::T* f = reinterpret_cast<typename S::T*>(a.f);
+#pragma unroll
+    for (int q = 0; q < Q19; ++q) {
+        const float v = wall ? a.wall[q] : a.fluid[q];
+        S::store(f + (long long)q * a.qstride + c, S::shifted ? v - w19(q) : v);
+    }
+}
+
+// Equilibrium from per-cell rho/u with the init limiter (lbm.cpp:720-737).
+template <class S>
+__global__ void k_set_equilibrium(void* fp, const uint32_t* desc, long long qstride, int ncell, const float* rho,
+                                  const float* ux, const float* uy, const float* uz) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell || (desc[c] & D_WALL)) return;
+    const float r = rho ? rho[c] : 1.0f;
+    float vx = ux[c], vy = uy[c], vz = uz[c];
+    float usqr = vx * vx + vy * vy + vz * vz;
+    if (usqr > 0.09f) {
+        const float scale = sqrtf(0.09f / usqr);
+        vx *= scale; vy *= scale; vz *= scale;
+        usqr = vx * vx + vy * vy + vz * vz;
+    }
+    typename S::T* f = reinterpret_cast<typename S::T*>(fp);
+#pragma unroll
+    for (int q = 0; q < Q19; ++q) {
+        const float v = eq_checked(q, r, vx, vy, vz, usqr);
+        S::store(f + (long long)q * qstride + c, S::shifted ? v - w19(q) : v);
+    }
+}
+
+// Pre-collision populations [19][ncell] (plain values) into the slots the
+// next even step gathers from. Wall cells are left untouched.
+template <class S>
+__global__ void k_write_pre(void* fp, const uint32_t* desc, long long qstride, int ncell, const float* src, int nq,
+                            float shift_ref) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell || (desc[c] & D_WALL)) return;
+    typename S::T* f = reinterpret_cast<typename S::T*>(fp);
+    for (int q = 0; q < nq; ++q) {
+        const float w = nq == Q19 ? w19(q) : w7(q) * shift_ref;
+        const float v = src[(long long)q * ncell + c];
+        S::store(f + (long long)q * qstride + c, S::shifted ? v - w : v);
+    }
+}
+
+// Re-equilibration after divergence (aeros/src/lbm.cpp:1583-1600): fluid cells
+// get f = feq(1, u_in), rho = 1, u = u_in.
+template <class S>
+__global__ void k_reset(void* fp, const uint32_t* desc, long long qstride, int ncell, FillArgs fa, float* rho, float* ux,
+                        float* uy, float* uz, float uin0, float uin1, float uin2) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell || (desc[c] & D_WALL)) return;
+    typename S::T* f = reinterpret_cast<typename S::T*>(fp);
+#pragma unroll
+    for (int q = 0; q < Q19; ++q) S::store(f + (long long)q * qstride + c, S::shifted ? fa.fluid[q] - w19(q) : fa.fluid[q]);
+    rho[c] = 1.0f;
+    ux[c] = uin0; uy[c] = uin1; uz[c] = uin2;
+}
+
+// D3Q7 populations at rest equilibrium from T (thermal_lbm.cpp:179-183,191-194).
+template <class S>
+__global__ void k_thermal_fill(void* gp, long long qstride, int ncell, const float* T, float tref) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    typename S::T* g = reinterpret_cast<typename S::T*>(gp);
+    const float t = T[c];
+#pragma unroll
+    for (int i = 0; i < Q7; ++i) {
+        const float v = w7(i) * t * (1.0f + 4.0f * 0.0f);
+        S::store(g + (long long)i * qstride + c, S::shifted ? v - w7(i) * tref : v);
+    }
+}
+
+// Launcher table, one instance per storage format (the translation unit of
+// each format is compiled with its own floating-point contraction setting).
+struct Launchers {
+    cudaError_t (*step)(const StepArgs& A, bool odd, bool thermal, bool mat, int grid, cudaStream_t s);
+    int (*occupancy)(bool odd, bool thermal);
+    cudaError_t (*fill_uniform)(const FillArgs& a, cudaStream_t s);
+    cudaError_t (*set_equilibrium)(void* f, const uint32_t* desc, long long qstride, int ncell, const float* rho,
+                                   const float* ux, const float* uy, const float* uz, cudaStream_t s);
+    cudaError_t (*write_pre)(void* f, const uint32_t* desc, long long qstride, int ncell, const float* src, int nq,
+                             float shift_ref, cudaStream_t s);
+    cudaError_t (*reset)(void* f, const uint32_t* desc, long long qstride, int ncell, const FillArgs& fa, float* rho,
+                         float* ux, float* uy, float* uz, const float* uin, cudaStream_t s);
+    cudaError_t (*thermal_fill)(void* g, long long qstride, int ncell, const float* T, float tref, cudaStream_t s);
+};
+
+const Launchers& launchers_fp32();
+const Launchers& launchers_fp16();
+const Launchers& launchers_bf16();
+
+#define AEROS_DEFINE_LAUNCHERS(NAME, STORE)                                                                           \
+    namespace NAME##_detail {                                                                                         \
+    template <bool O, bool T, bool M>                                                                                 \
+    cudaError_t launch_one(const StepArgs& A, int grid, cudaStream_t s) {                                            \
+        k_lbm_step<STORE, O, T, M><<<grid, STEP_BLOCK, 0, s>>>(A);                                                    \
+        return cudaGetLastError();                                                                                    \
+    }                                                                                                                 \
+    cudaError_t step_(const StepArgs& A, bool odd, bool thermal, bool mat, int grid, cudaStream_t s) {               \
+        if (mat) {                                                                                                    \
+            if (odd) return thermal ? launch_one<true, true, true>(A, grid, s) : launch_one<true, false, true>(A, grid, s); \
+            return thermal ? launch_one<false, true, true>(A, grid, s) : launch_one<false, false, true>(A, grid, s);  \
+        }                                                                                                             \
+        if (odd) return thermal ? launch_one<true, true, false>(A, grid, s) : launch_one<true, false, false>(A, grid, s); \
+        return thermal ? launch_one<false, true, false>(A, grid, s) : launch_one<false, false, false>(A, grid, s);    \
+    }                                                                                                                 \
+    template <bool O, bool T>                                                                                         \
+    int occ_one() {                                                                                                   \
+        int n = 0;                                                                                                    \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_step<STORE, O, T, false>, STEP_BLOCK, 0);             \
+        return n > 0 ? n : 1;                                                                                         \
+    }                                                                                                                 \
+    int occupancy_(bool odd, bool thermal) {                                                                          \
+        return odd ? (thermal ? occ_one<true, true>() : occ_one<true, false>())                                       \
+                   : (thermal ? occ_one<false, true>() : occ_one<false, false>());                                    \
+    }                                                                                                                 \
+    cudaError_t fill_(const FillArgs& a, cudaStream_t s) {                                                            \
+        k_fill_uniform<STORE><<<(a.ncell + 255) / 256, 256, 0, s>>>(a);                                               \
+        return cudaGetLastError();                                                                                    \
+    }                                                                                                                 \
+    cudaError_t seteq_(void* f, const uint32_t* desc, long long qs, int n, const float* rho, const float* ux,        \
+                       const float* uy, const float* uz, cudaStream_t s) {                                            \
+        k_set_equilibrium<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, rho, ux, uy, uz);                    \
+        return cudaGetLastError();                                                                                    \
+    }                                                                                                                 \
+    cudaError_t writepre_(void* f, const uint32_t* desc, long long qs, int n, const float* src, int nq, float sr,     \
+                          cudaStream_t s) {                                                                           \
+        k_write_pre<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, src, nq, sr);                              \
+        return cudaGetLastError();                                                                                    \
+    }                                                                                                                 \
+    cudaError_t reset_(void* f, const uint32_t* desc, long long qs, int n, const FillArgs& fa, float* rho, float* ux, \
+                       float* uy, float* uz, const float* uin, cudaStream_t s) {                                      \
+        k_reset<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, fa, rho, ux, uy, uz, uin[0], uin[1], uin[2]); \
+        return cudaGetLastError();                                                                                    \
+    }                                                                                                                 \
+    cudaError_t thfill_(void* g, long long qs, int n, const float* T, float tref, cudaStream_t s) {                   \
+        k_thermal_fill<STORE><<<(n + 255) / 256, 256, 0, s>>>(g, qs, n, T, tref);                                     \
+        return cudaGetLastError();                                                                                    \
+    }                                                                                                                 \
+    }                                                                                                                 \
+    const Launchers& NAME() {                                                                                         \
+        using namespace NAME##_detail;                                                                                \
+        static const Launchers L = {step_, occupancy_, fill_, seteq_, writepre_, reset_, thfill_};                    \
+        return L;                                                                                                     \
+    }
+
+}  // namespace aeros

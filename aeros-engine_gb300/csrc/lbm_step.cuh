@@ -1,0 +1,723 @@
+// lbm_step.cuh — the fused D3Q19 (+D3Q7) solver step on GB300.
+//
+// One launch = one lattice step (aeros/src/lbm.cpp:957-1580): previous-step
+// |S| (LES), collision, stream with the reference's boundary rules, thermal
+// step (aeros/src/thermal_lbm.cpp:199-355), per-step statistics.
+//
+// Layout: structure of arrays, population q of cell c at f[q*qstride + c].
+// Streaming is the in-place AA pattern (one population array):
+//   even step: gather f_q from slot (c, q); scatter post_q to slot (c, opp q)
+//   odd step : gather f_q from slot (c - c_q, opp q); scatter post_q to
+//              slot (c + c_q, q)
+// so every slot is read and written by exactly one thread per step. Boundary
+// links are redirected to slots nobody else owns (bounce-back, copy-own,
+// free-slip); rules that read other cells' post-collision values of the same
+// step (convective / zero-gradient outlet) go through a parity-double-buffered
+// side buffer of the three outlet planes.
+//
+// Threads: one cell each, over a tile list (interior tiles first, then the
+// boundary shell from an explicit cell list); the grid is persistent (SMs x
+// resident blocks) and strides over tiles. Per-block partial sums land in
+// `partials`; the last block to finish reduces them in a fixed order
+// (deterministic) and applies the divergence guard.
+#pragma once
+
+#include "lattice.cuh"
+
+namespace aeros {
+
+constexpr int STEP_BLOCK = 256;
+
+struct Partial {            // 80 bytes, one per block
+    double rho, ke, tke, nu, tsum;
+    float maxu;
+    int nan, neg, bad, rout, rnf, ulim, nun;
+    int pad[2];
+};
+
+struct Control {
+    unsigned int blocks_done;
+    int halt;               // divergence guard tripped: later steps return at once
+    int halt_kind;          // 1: NaN count before streaming, 2: mean density
+    int th_valid;           // Nusselt updated at least once
+    long long steps;        // counted steps (lbmCurrentStep)
+    long long kexec;        // step bodies executed
+    float prev_kinetic;
+    int converged;
+    double sum_rho, sum_ke, sum_tke;
+    float avg_rho, avg_ke, avg_tke, max_u, convergence;
+    float nusselt, mean_t;
+    int pad;
+    long long nan, neg, bad, rout, rnf, ulim;
+};
+
+struct StepArgs {
+    int nx, ny, nz, nxny, ncell;
+    long long qstride;
+    int n_interior, ntiles_interior, n_shell, ntiles;
+    FastDiv div_ix, div_iy;     // interior decode: (nx-2), (ny-2)
+    FastDiv div_x, div_y;       // shell decode: nx, ny
+    void* f;
+    const uint32_t* desc;
+    const int* shell;
+    const float* up[3];
+    float* uc[3];
+    float *rho, *strain, *tke;
+    float* out_w;
+    const float* out_r;
+    int out_plane;
+    void* g;
+    float* T;
+    Partial* partials;
+    Control* ctl;
+    float* mat_f;
+    float* mat_g;
+    float tau0, Cs, velScale2;
+    float Fx, Fy, Fz;
+    float uin[3];
+    float feq_in[19];           // inlet equilibrium in storage form
+    float conv;
+    int flow_axis, flow_sign;
+    int periodic_x, periodic_z;
+    int use_trt, use_les;
+    int freeslip, outlet_mode;  // outlet_mode: 0 none, 1 convective, 2 zero-gradient
+    int apply_overrides, write_obs, write_u;
+    int total_div10, fluid_cells;
+    float conv_threshold;
+    int th_on, th_fixed, th_ylo;
+    float th_invtau, th_hot, th_cold, th_tref, th_glb, th_H;
+    int th_buoy_mode;           // 0: from the previous step's T, 1: zero (fresh
+                                // field, thermal_lbm.cpp:132), 2: from T_buoy
+    const float* T_buoy;
+    double th_rows_n;           // Nx*Nz*(yhi-ylo+1), thermal_lbm.cpp:76
+};
+
+// Van Driest factor table, aeros/src/lbm.cpp:112-120
+__device__ __forceinline__ float van_driest(int d) {
+    return d == 1 ? 0.3934693403f : d == 2 ? 0.6321205588f : d == 3 ? 0.7768698399f
+         : d == 4 ? 0.8646647168f : d == 5 ? 0.9179150014f : 0.0f;
+}
+
+struct Acc {
+    double rho, ke, tke, nu, tsum;
+    float maxu;
+    int nan, neg, bad, rout, rnf, ulim, nun;
+    __device__ void zero() {
+        rho = ke = tke = nu = tsum = 0.0;
+        maxu = 0.0f;
+        nan = neg = bad = rout = rnf = ulim = nun = 0;
+    }
+};
+
+template <class S>
+__device__ __forceinline__ typename S::T* fplane(const StepArgs& A, int q) {
+    return reinterpret_cast<typename S::T*>(A.f) + (long long)q * A.qstride;
+}
+template <class S>
+__device__ __forceinline__ typename S::T* gplane(const StepArgs& A, int q) {
+    return reinterpret_cast<typename S::T*>(A.g) + (long long)q * A.qstride;
+}
+
+__device__ __forceinline__ int nb19(const StepArgs& A, int q) {
+    return cx19(q) + cy19(q) * A.nx + cz19(q) * A.nxny;
+}
+
+__device__ __forceinline__ bool is_wall(const StepArgs& A, int c) { return (A.desc[c] & D_WALL) != 0; }
+
+// ---- boundary-shell link resolution (reference rules, lbm.cpp:1376-1406) ----
+enum LinkKind { L_REGULAR = 0, L_BOUNCE = 1, L_COPYOWN = 2, L_FREESLIP = 3 };
+struct Link {
+    int idx, slot, kind;
+};
+
+// Where pre-collision population q of cell (x,y,z) comes from.
+__device__ __forceinline__ Link resolve_src(const StepArgs& A, int x, int y, int z, int cell, int q) {
+    int s0 = x - cx19(q), s1 = y - cy19(q), s2 = z - cz19(q);
+    if (A.periodic_x) { s0 = s0 < 0 ? s0 + A.nx : (s0 >= A.nx ? s0 - A.nx : s0); }
+    if (A.periodic_z) { s2 = s2 < 0 ? s2 + A.nz : (s2 >= A.nz ? s2 - A.nz : s2); }
+    const int o0 = (s0 < 0 || s0 >= A.nx), o1 = (s1 < 0 || s1 >= A.ny), o2 = (s2 < 0 || s2 >= A.nz);
+    const int outm = o0 | (o1 << 1) | (o2 << 2);
+    if (!outm) {
+        const int sc = (s2 * A.ny + s1) * A.nx + s0;
+        if (is_wall(A, sc)) return {cell, q, L_BOUNCE};
+        return {sc, opp19(q), L_REGULAR};
+    }
+    if (A.freeslip && !((outm >> A.flow_axis) & 1)) {
+        const int r0 = o0 ? x : s0, r1 = o1 ? y : s1, r2 = o2 ? z : s2;
+        const int rq = dir19_of(o0 ? -cx19(q) : cx19(q), o1 ? -cy19(q) : cy19(q), o2 ? -cz19(q) : cz19(q));
+        const int rc = (r2 * A.ny + r1) * A.nx + r0;
+        if (is_wall(A, rc)) return {cell, q, L_BOUNCE};
+        return {rc, opp19(rq), L_FREESLIP};
+    }
+    return {cell, q, L_COPYOWN};
+}
+
+// ---- collision of one fluid cell, plain form ---------------------------------
+// Same expression trees as aeros/src/lbm.cpp:1061-1299 (compiled without
+// contraction, this is bitwise the reference's float arithmetic).
+struct CellResult {
+    float rho, ux, uy, uz, usqr, strain, tke;
+};
+
+__device__ __forceinline__ float eq19(int q, float rho, float cu, float usqr) {
+    return w19(q) * rho * (1.0f + cu * 3.0f + cu * cu * 4.5f - usqr * 1.5f);
+}
+__device__ __forceinline__ float cu19(int q, float ux, float uy, float uz) {
+    // (cx*ux + cy*uy) + cz*uz with the zero terms dropped (exact)
+    float a = 0.0f;
+    bool first = true;
+    if (cx19(q) != 0) { a = cx19(q) > 0 ? ux : -ux; first = false; }
+    if (cy19(q) != 0) { a = first ? (cy19(q) > 0 ? uy : -uy) : (cy19(q) > 0 ? a + uy : a - uy); first = false; }
+    if (cz19(q) != 0) { a = first ? (cz19(q) > 0 ? uz : -uz) : (cz19(q) > 0 ? a + uz : a - uz); }
+    return a;
+}
+__device__ __forceinline__ float src19(int q, float ueX, float ueY, float ueZ, float Fx, float Fy, float Fz) {
+    const float cx = (float)cx19(q), cy = (float)cy19(q), cz = (float)cz19(q);
+    const float cu = cu19(q, ueX, ueY, ueZ);
+    return 3.0f * w19(q) * ((cx - ueX + 3.0f * cu * cx) * Fx + (cy - ueY + 3.0f * cu * cy) * Fy + (cz - ueZ + 3.0f * cu * cz) * Fz);
+}
+
+// f: pre-collision populations in -> post-collision out (the plain values f_i,
+// or the deviations f_i - w_i when SHIFTED).
+template <bool SHIFTED>
+__device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint32_t d, bool isInlet, bool isOutlet,
+                                          float strainPre, float buoy, CellResult& o, Acc& acc) {
+    float rho = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+#pragma unroll
+    for (int q = 0; q < Q19; ++q) {
+        // shifted form: range checks on w + h, moments from the deviation h
+        float m = f[q];
+        const float fi = SHIFTED ? m + w19(q) : m;
+        if (!isfinite(fi)) { m = SHIFTED ? 0.0f : w19(q); acc.nan++; acc.bad++; }
+        else if (fi < -1.0f || fi > 10.0f) { m = SHIFTED ? 0.0f : w19(q); acc.bad++; }
+        rho += m;
+        if (cx19(q) != 0) ux = cx19(q) > 0 ? ux + m : ux - m;
+        if (cy19(q) != 0) uy = cy19(q) > 0 ? uy + m : uy - m;
+        if (cz19(q) != 0) uz = cz19(q) > 0 ? uz + m : uz - m;
+    }
+    if (SHIFTED) rho = 1.0f + rho;
+    if (!isfinite(rho)) { acc.rnf++; acc.nan++; rho = 1.0f; }
+    else if (rho < 0.5f || rho > 1.5f) { acc.rout++; acc.nan++; rho = 1.0f; }
+    const float invRho = 1.0f / rho;
+    ux *= invRho; uy *= invRho; uz *= invRho;
+    if (!isfinite(ux)) { ux = 0.0f; uy = 0.0f; uz = 0.0f; acc.nan++; }
+    const float usqrTmp = ux * ux + uy * uy + uz * uz;
+    if (usqrTmp > 0.09f) {
+        const float sc = sqrtf(0.09f / usqrTmp);
+        ux *= sc; uy *= sc; uz *= sc;
+    }
+    if (isInlet && !A.periodic_x) { rho = 1.0f; ux = A.uin[0]; uy = A.uin[1]; uz = A.uin[2]; }
+
+    const float tau0 = A.tau0;
+    float tauEff = tau0;
+    float strainMag = 0.0f;
+    if (A.use_les && !isInlet && !isOutlet) {
+        strainMag = strainPre;
+        if (isfinite(strainMag) && strainMag < 10.0f && strainMag > 1e-6f) {
+            float cs = A.Cs;
+            const int wd = (int)((d >> D_WD_SHIFT) & 7u);
+            if (wd <= 5) cs *= van_driest(wd);
+            const float nu_t = cs * cs * strainMag;
+            tauEff = tau0 + nu_t / (1.0f / 3.0f);
+            if (tauEff > 1.5f) tauEff = 1.5f;
+            if (tauEff < 0.51f) tauEff = 0.51f;
+        }
+    }
+    float usqr = ux * ux + uy * uy + uz * uz;
+    if (usqr > 0.09f) {
+        acc.ulim++;
+        const float sc = sqrtf(0.09f / usqr);
+        ux *= sc; uy *= sc; uz *= sc;
+        usqr = ux * ux + uy * uy + uz * uz;
+    }
+    const float invTau = 1.0f / tauEff;
+    const float Fx = A.Fx, Fz = A.Fz;
+    const float Fy = A.th_on ? A.Fy + buoy : A.Fy;
+    const bool hasForce = (Fx != 0.0f || Fy != 0.0f || Fz != 0.0f);
+    float ueX = ux, ueY = uy, ueZ = uz, ueSqr = usqr;
+    if (hasForce) {
+        const float half = 0.5f / rho;
+        ueX += Fx * half; ueY += Fy * half; ueZ += Fz * half;
+        ueSqr = ueX * ueX + ueY * ueY + ueZ * ueZ;
+    }
+    float sMinus = invTau;
+    if (A.use_trt) {
+        const float m = invTau - 0.5f;
+        const float denom = (fabsf(m) > 1e-6f) ? (0.1875f / m + 0.5f) : 1.0f;
+        sMinus = 1.0f / fmaxf(0.05f, denom);
+    }
+    const float kP = 1.0f - 0.5f * invTau;
+    const float kM = 1.0f - 0.5f * sMinus;
+    // shifted form: relax deviations; feq - w = w*(rho-1) + w*rho*(...)
+    const float drho = rho - 1.0f;
+    // rest population (pair q == opp q)
+    {
+        const float feq = SHIFTED ? w19(0) * drho + w19(0) * rho * (0.0f - ueSqr * 1.5f) : eq19(0, rho, 0.0f, ueSqr);
+        float fi = f[0];
+        if (!isfinite(fi)) fi = feq;
+        const float srcI = hasForce ? src19(0, ueX, ueY, ueZ, Fx, Fy, Fz) : 0.0f;
+        float fNew = fi - (fi - feq) * invTau + kP * srcI;
+        if (!isfinite(fNew)) fNew = feq;
+        if ((SHIFTED ? fNew + w19(0) : fNew) < 0.0f) acc.neg++;
+        f[0] = fNew;
+    }
+#pragma unroll
+    for (int qi = 1; qi < Q19; qi += 2) {
+        const int qo = qi + 1;
+        const float cu = cu19(qi, ueX, ueY, ueZ);
+        float feq, feqO;
+        if (SHIFTED) {
+            const float wr = w19(qi) * rho;
+            feq = w19(qi) * drho + wr * (cu * 3.0f + cu * cu * 4.5f - ueSqr * 1.5f);
+            feqO = w19(qo) * drho + wr * (-cu * 3.0f + cu * cu * 4.5f - ueSqr * 1.5f);
+        } else {
+            feq = eq19(qi, rho, cu, ueSqr);
+            feqO = eq19(qo, rho, -cu, ueSqr);
+        }
+        float fi = f[qi];
+        if (!isfinite(fi)) fi = feq;
+        float fo = f[qo];
+        if (!isfinite(fo)) fo = feqO;
+        float srcI = 0.0f, srcO = 0.0f;
+        if (hasForce) {
+            srcI = src19(qi, ueX, ueY, ueZ, Fx, Fy, Fz);
+            srcO = src19(qo, ueX, ueY, ueZ, Fx, Fy, Fz);
+        }
+        const float srcP = 0.5f * (srcI + srcO);
+        const float srcM = 0.5f * (srcI - srcO);
+        const float fp = 0.5f * (fi + fo), fm = 0.5f * (fi - fo);
+        const float ep = 0.5f * (feq + feqO), em = 0.5f * (feq - feqO);
+        const float fpN = fp - invTau * (fp - ep);
+        const float fmN = fm - sMinus * (fm - em);
+        float newI = fpN + fmN + kP * srcP + kM * srcM;
+        float newO = fpN - fmN + kP * srcP - kM * srcM;
+        if (!isfinite(newI)) newI = feq;
+        if (!isfinite(newO)) newO = feqO;
+        if ((SHIFTED ? newI + w19(qi) : newI) < 0.0f) acc.neg++;
+        if ((SHIFTED ? newO + w19(qo) : newO) < 0.0f) acc.neg++;
+        f[qi] = newI;
+        f[qo] = newO;
+    }
+    o.rho = rho;
+    if (hasForce) {
+        const float halfInvRho = 0.5f / rho;
+        o.ux = ux + Fx * halfInvRho;
+        o.uy = uy + Fy * halfInvRho;
+        o.uz = uz + Fz * halfInvRho;
+    } else {
+        o.ux = ux; o.uy = uy; o.uz = uz;
+    }
+    o.strain = strainMag;
+    const float tkeLb = (A.Cs * strainMag) * (A.Cs * strainMag);
+    float tke = tkeLb * A.velScale2;
+    if (!isfinite(tke) || tke < 0.0f) tke = 0.0f;
+    if (tke > 1.0e6f) tke = 1.0e6f;
+    o.tke = tke;
+    o.usqr = usqr;
+    const float velMag = sqrtf(usqr);
+    if (velMag > acc.maxu) acc.maxu = velMag;
+    acc.rho += (double)rho;
+    acc.ke += (double)usqr;
+    acc.tke += (double)tke;
+}
+
+// Two-pass |S| from previous-step velocity (aeros/src/lbm.cpp:1012-1031).
+__device__ __forceinline__ float strain_prev(const StepArgs& A, int c) {
+    const float* ux = A.up[0];
+    const float* uy = A.up[1];
+    const float* uz = A.up[2];
+    const int xm = c - 1, xp = c + 1, ym = c - A.nx, yp = c + A.nx, zm = c - A.nxny, zp = c + A.nxny;
+    const float dux_dx = (ux[xp] - ux[xm]) * 0.5f;
+    const float duy_dy = (uy[yp] - uy[ym]) * 0.5f;
+    const float duz_dz = (uz[zp] - uz[zm]) * 0.5f;
+    const float dux_dy = (ux[yp] - ux[ym]) * 0.5f;
+    const float dux_dz = (ux[zp] - ux[zm]) * 0.5f;
+    const float duy_dx = (uy[xp] - uy[xm]) * 0.5f;
+    const float duy_dz = (uy[zp] - uy[zm]) * 0.5f;
+    const float duz_dx = (uz[xp] - uz[xm]) * 0.5f;
+    const float duz_dy = (uz[yp] - uz[ym]) * 0.5f;
+    const float Sxx = dux_dx, Syy = duy_dy, Szz = duz_dz;
+    const float Sxy = 0.5f * (dux_dy + duy_dx);
+    const float Sxz = 0.5f * (dux_dz + duz_dx);
+    const float Syz = 0.5f * (duy_dz + duz_dy);
+    const float S2 = Sxx * Sxx + Syy * Syy + Szz * Szz + 2.0f * (Sxy * Sxy + Sxz * Sxz + Syz * Syz);
+    return sqrtf(2.0f * S2);
+}
+
+__device__ __forceinline__ int plane_index(const StepArgs& A, int x, int y, int z) {
+    return A.flow_axis == 0 ? y + A.ny * z : (A.flow_axis == 1 ? x + A.nx * z : x + A.nx * y);
+}
+
+// ---- thermal lattice (D3Q7), fused into the same thread -------------------------
+// Dirichlet wall temperature seen from source row sy (thermal_lbm.cpp:60-65,283-286).
+__device__ __forceinline__ bool th_dirichlet(const StepArgs& A, int sy, float& Tw) {
+    if (!A.th_fixed) return false;
+    if (sy <= 0) { Tw = A.th_hot; return true; }
+    if (sy >= A.ny - 1) { Tw = A.th_cold; return true; }
+    return false;
+}
+
+// Thermal link of population i at (x,y,z): X/Z always periodic, Y-out and
+// solid sources bounce (anti-bounce-back at fixed-temperature walls).
+struct TLink {
+    int idx;       // source cell (regular) or own cell
+    int bounce;    // 0 regular, 1 bounce, 2 Dirichlet
+    float Tw;
+};
+__device__ __forceinline__ TLink th_resolve(const StepArgs& A, int x, int y, int z, int cell, int i, bool interior,
+                                            uint32_t d) {
+    if (interior) {
+        if (!((d >> i) & 1u)) return {cell - nb19(A, i), 0, 0.0f};
+        float Tw = 0.0f;
+        const bool dir = th_dirichlet(A, y - cy19(i), Tw) && (y - cy19(i) <= 0 || y - cy19(i) >= A.ny - 1);
+        return {cell, dir ? 2 : 1, Tw};
+    }
+    int sx = x - cx19(i), sy = y - cy19(i), sz = z - cz19(i);
+    if (sx < 0) sx = A.nx - 1; else if (sx >= A.nx) sx = 0;
+    if (sz < 0) sz = A.nz - 1; else if (sz >= A.nz) sz = 0;
+    float Tw = 0.0f;
+    if (sy < 0 || sy >= A.ny) {
+        const bool dir = th_dirichlet(A, sy < 0 ? 0 : A.ny - 1, Tw);
+        return {cell, dir ? 2 : 1, Tw};
+    }
+    const int sc = (sz * A.ny + sy) * A.nx + sx;
+    if (is_wall(A, sc)) {
+        const bool dir = th_dirichlet(A, sy, Tw) && (sy <= 0 || sy >= A.ny - 1);
+        return {cell, dir ? 2 : 1, Tw};
+    }
+    return {sc, 0, 0.0f};
+}
+
+// ---- the step ------------------------------------------------------------------
+// MAT: materialize (write the gathered pre-collision populations, no step).
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x, int y, int z, bool interior,
+                                             Acc& acc) {
+    const uint32_t d = A.desc[cell];
+    if (d & D_WALL) return;
+    constexpr bool SH = S::shifted;
+
+    // previous-step strain first: keeps the velocity stencil out of the
+    // register peak of the collision
+    float strainPre = 0.0f;
+    if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, cell);
+    float buoy = 0.0f;
+    if (!MAT && THERMAL && A.th_buoy_mode != 1)
+        buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
+
+    // ---- gather ----
+    float f[Q19];
+    if (!ODD) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
+    } else if (interior) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) {
+            const bool special = (d >> q) & 1u;
+            const int src = special ? cell : cell - nb19(A, q);
+            f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) {
+            const Link L = resolve_src(A, x, y, z, cell, q);
+            f[q] = S::load_rw(fplane<S>(A, L.slot) + L.idx);
+        }
+    }
+    const bool isInlet = (d & D_INLET) != 0, isOutlet = (d & D_OUTLET) != 0;
+    if (A.apply_overrides && !A.periodic_x) {
+        if (isInlet) {
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) f[q] = A.feq_in[q];
+        } else if (isOutlet && A.outlet_mode) {
+            const int P = A.out_plane;
+            const int pi = plane_index(A, x, y, z);
+            if (A.outlet_mode == 1) {
+                // convective outlet, aeros/src/lbm.cpp:1465-1496
+#pragma unroll
+                for (int q = 0; q < Q19; ++q) {
+                    const float fOut = A.out_r[(0 * Q19 + q) * P + pi];
+                    const float fIn = A.out_r[(1 * Q19 + q) * P + pi];
+                    const float fIn2 = A.out_r[(2 * Q19 + q) * P + pi];
+                    const float df = fIn - fOut;
+                    const float df2 = fIn - fIn2;
+                    f[q] = fOut + A.conv * df + 0.15f * A.conv * df2;
+                }
+            } else {
+                // zero-gradient: unknowns take the outlet plane's post value
+                // pulled by the plane upstream (tangential shift)
+                const int pos[3] = {x, y, z};
+                const int n3[3] = {A.nx, A.ny, A.nz};
+                const int per[3] = {A.periodic_x, 0, A.periodic_z};
+#pragma unroll
+                for (int q = 0; q < Q19; ++q) {
+                    if (ca19(q, A.flow_axis) * A.flow_sign >= 0) continue;
+                    int t[3] = {x - cx19(q), y - cy19(q), z - cz19(q)};
+                    t[A.flow_axis] = pos[A.flow_axis];
+                    for (int a = 0; a < 3; ++a) {
+                        if (a == A.flow_axis) continue;
+                        if (t[a] < 0 || t[a] >= n3[a]) t[a] = per[a] ? (t[a] + n3[a]) % n3[a] : pos[a];
+                    }
+                    const int tc = (t[2] * A.ny + t[1]) * A.nx + t[0];
+                    const int tpi = is_wall(A, tc) ? pi : plane_index(A, t[0], t[1], t[2]);
+                    f[q] = A.out_r[(0 * Q19 + q) * P + tpi];
+                }
+            }
+        }
+    }
+    if (MAT) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) A.mat_f[(long long)q * A.ncell + cell] = SH ? f[q] + w19(q) : f[q];
+    }
+
+    // ---- collide ----
+    CellResult r;
+    if (!MAT) {
+        collide19<SH>(f, A, d, isInlet, isOutlet, strainPre, buoy, r, acc);
+
+        // outlet side buffer: post values of the three outlet planes
+        const uint32_t os = (d >> D_OUT_SHIFT) & 3u;
+        if (os) {
+            const int P = A.out_plane;
+            const int pi = plane_index(A, x, y, z);
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) A.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
+        }
+
+        // ---- scatter ----
+        if (!ODD) {
+            if (interior) {
+#pragma unroll
+                for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < Q19; ++j) {
+                    const Link L = resolve_src(A, x, y, z, cell, opp19(j));
+                    S::store(fplane<S>(A, opp19(j)) + cell, L.kind == L_COPYOWN ? f[opp19(j)] : f[j]);
+                }
+            }
+        } else if (interior) {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) {
+                const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
+                if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+                else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) {
+                const Link L = resolve_src(A, x, y, z, cell, opp19(j));
+                if (L.kind == L_REGULAR || L.kind == L_FREESLIP) S::store(fplane<S>(A, L.slot) + L.idx, f[j]);
+                else if (L.kind == L_BOUNCE) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+                else S::store(fplane<S>(A, opp19(j)) + cell, f[opp19(j)]);
+            }
+        }
+        if (A.write_u) { A.uc[0][cell] = r.ux; A.uc[1][cell] = r.uy; A.uc[2][cell] = r.uz; }
+        if (A.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
+    }
+
+    // ---- thermal sub-step (D3Q7), aeros/src/thermal_lbm.cpp:199-336 ----
+    if (THERMAL) {
+        const float wshift = SH ? A.th_tref : 0.0f;   // stored value = g - w*Tref
+        float g[Q7];
+        if (!ODD) {
+#pragma unroll
+            for (int i = 0; i < Q7; ++i) g[i] = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;
+        } else {
+#pragma unroll
+            for (int i = 0; i < Q7; ++i) {
+                const TLink L = th_resolve(A, x, y, z, cell, i, interior, d);
+                if (L.bounce == 0) {
+                    g[i] = S::load_rw(gplane<S>(A, opp19(i)) + L.idx) + w7(i) * wshift;
+                } else {
+                    const float v = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;   // post_{opp i}
+                    g[i] = L.bounce == 2 ? (-v + 2.0f * w7(i) * L.Tw) : v;
+                }
+            }
+        }
+        if (MAT) {
+#pragma unroll
+            for (int i = 0; i < Q7; ++i) A.mat_g[(long long)i * A.ncell + cell] = g[i];
+            return;
+        }
+        float T = 0.0f;
+#pragma unroll
+        for (int i = 0; i < Q7; ++i) T += g[i];
+        if (!isfinite(T)) T = A.th_tref;
+        {
+            const float lo = A.th_cold - 1.0f, hi = A.th_hot + 1.0f;
+            const float m = (lo < T) ? T : lo;
+            T = (m < hi) ? m : hi;
+        }
+        const float v[3] = {r.ux, r.uy, r.uz};
+#pragma unroll
+        for (int i = 0; i < Q7; ++i) {
+            const float cu = i == 0 ? 0.0f : ((i & 1) ? v[(i - 1) >> 1] : -v[(i - 1) >> 1]);
+            const float eq = w7(i) * T * (1.0f + 4.0f * cu);
+            g[i] = g[i] - (g[i] - eq) * A.th_invtau;
+        }
+        A.T[cell] = T;
+        acc.tsum += (double)T;
+        if (y == A.th_ylo) { acc.nu += (double)(A.th_hot - T) / 0.5; acc.nun++; }
+        // scatter
+        if (!ODD) {
+#pragma unroll
+            for (int j = 0; j < Q7; ++j) S::store(gplane<S>(A, opp19(j)) + cell, g[j] - w7(j) * wshift);
+        } else {
+#pragma unroll
+            for (int j = 0; j < Q7; ++j) {
+                const TLink L = th_resolve(A, x, y, z, cell, opp19(j), interior, d);
+                if (L.bounce == 0) {
+                    S::store(gplane<S>(A, j) + L.idx, g[j] - w7(j) * wshift);
+                } else {
+                    // becomes pre-collision population opp j of this cell
+                    const float val = L.bounce == 2 ? (-g[j] + 2.0f * w7(j) * L.Tw) : g[j];
+                    S::store(gplane<S>(A, opp19(j)) + cell, val - w7(j) * wshift);
+                }
+            }
+        }
+    } else if (MAT) {
+        return;
+    }
+}
+
+// Block reduction of the accumulators into one partial; fixed shape, so the
+// result does not depend on scheduling.
+template <int BLOCK>
+__device__ __forceinline__ void block_reduce_store(Acc& a, Partial* out) {
+    __shared__ double sd[5][BLOCK / 32];
+    __shared__ float sf[BLOCK / 32];
+    __shared__ int si[7][BLOCK / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a.rho += __shfl_down_sync(0xffffffffu, a.rho, o);
+        a.ke += __shfl_down_sync(0xffffffffu, a.ke, o);
+        a.tke += __shfl_down_sync(0xffffffffu, a.tke, o);
+        a.nu += __shfl_down_sync(0xffffffffu, a.nu, o);
+        a.tsum += __shfl_down_sync(0xffffffffu, a.tsum, o);
+        a.maxu = fmaxf(a.maxu, __shfl_down_sync(0xffffffffu, a.maxu, o));
+        a.nan += __shfl_down_sync(0xffffffffu, a.nan, o);
+        a.neg += __shfl_down_sync(0xffffffffu, a.neg, o);
+        a.bad += __shfl_down_sync(0xffffffffu, a.bad, o);
+        a.rout += __shfl_down_sync(0xffffffffu, a.rout, o);
+        a.rnf += __shfl_down_sync(0xffffffffu, a.rnf, o);
+        a.ulim += __shfl_down_sync(0xffffffffu, a.ulim, o);
+        a.nun += __shfl_down_sync(0xffffffffu, a.nun, o);
+    }
+    if (lane == 0) {
+        sd[0][wid] = a.rho; sd[1][wid] = a.ke; sd[2][wid] = a.tke; sd[3][wid] = a.nu; sd[4][wid] = a.tsum;
+        sf[wid] = a.maxu;
+        si[0][wid] = a.nan; si[1][wid] = a.neg; si[2][wid] = a.bad; si[3][wid] = a.rout;
+        si[4][wid] = a.rnf; si[5][wid] = a.ulim; si[6][wid] = a.nun;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Partial p;
+        p.rho = p.ke = p.tke = p.nu = p.tsum = 0.0;
+        p.maxu = 0.0f;
+        p.nan = p.neg = p.bad = p.rout = p.rnf = p.ulim = p.nun = 0;
+        for (int w = 0; w < BLOCK / 32; ++w) {
+            p.rho += sd[0][w]; p.ke += sd[1][w]; p.tke += sd[2][w]; p.nu += sd[3][w]; p.tsum += sd[4][w];
+            p.maxu = fmaxf(p.maxu, sf[w]);
+            p.nan += si[0][w]; p.neg += si[1][w]; p.bad += si[2][w]; p.rout += si[3][w];
+            p.rnf += si[4][w]; p.ulim += si[5][w]; p.nun += si[6][w];
+        }
+        *out = p;
+    }
+}
+
+// Last block: sums the partials in block order and updates the control block
+// (aeros/src/lbm.cpp:1313-1319 and 1554-1580).
+template <int BLOCK>
+__device__ void finish_step(const StepArgs& A) {
+    __shared__ bool last;
+    __threadfence();
+    if (threadIdx.x == 0) last = (atomicAdd(&A.ctl->blocks_done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    Acc a;
+    a.zero();
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += BLOCK) {
+        const volatile Partial* p = A.partials + b;
+        a.rho += p->rho; a.ke += p->ke; a.tke += p->tke; a.nu += p->nu; a.tsum += p->tsum;
+        a.maxu = fmaxf(a.maxu, p->maxu);
+        a.nan += p->nan; a.neg += p->neg; a.bad += p->bad; a.rout += p->rout;
+        a.rnf += p->rnf; a.ulim += p->ulim; a.nun += p->nun;
+    }
+    __syncthreads();
+    __shared__ Partial tot;
+    block_reduce_store<BLOCK>(a, &tot);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    Control* c = A.ctl;
+    c->blocks_done = 0;
+    c->kexec += 1;
+    c->nan = tot.nan;
+    if (tot.nan > A.total_div10) {   // diverged before streaming: step not counted
+        c->halt = 1;
+        c->halt_kind = 1;
+        return;
+    }
+    c->steps += 1;
+    c->sum_rho = tot.rho; c->sum_ke = tot.ke; c->sum_tke = tot.tke;
+    const float avg_rho = (float)(tot.rho / A.fluid_cells);
+    const float avg_ke = (float)(tot.ke / A.fluid_cells);
+    c->avg_rho = avg_rho;
+    c->avg_ke = avg_ke;
+    c->avg_tke = (float)(tot.tke / A.fluid_cells);
+    c->max_u = tot.maxu;
+    c->neg = tot.neg; c->bad = tot.bad; c->rout = tot.rout; c->rnf = tot.rnf; c->ulim = tot.ulim;
+    c->convergence = fabsf(avg_ke - c->prev_kinetic);
+    c->prev_kinetic = avg_ke;
+    c->converged = c->convergence < A.conv_threshold;
+    if (A.th_on) {
+        if (tot.nun > 0) {
+            float dT = fabsf(A.th_hot - A.th_cold);
+            if (dT < 1e-6f) dT = 1e-6f;
+            c->nusselt = (float)(tot.nu / (double)tot.nun) * A.th_H / dT;
+            c->th_valid = 1;
+        }
+        c->mean_t = A.th_rows_n > 0.0 ? (float)(tot.tsum / A.th_rows_n) : 0.5f;
+    }
+    if (!isfinite(avg_rho) || avg_rho > 1.2f || avg_rho < 0.8f) {
+        c->halt = 1;
+        c->halt_kind = 2;
+    }
+}
+
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__global__ void __launch_bounds__(STEP_BLOCK) k_lbm_step(const StepArgs A) {
+    if (!MAT && A.ctl->halt) return;   // uniform: every thread reads the same flag
+    Acc acc;
+    acc.zero();
+    for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+        const int li = tile * STEP_BLOCK + (int)threadIdx.x;
+        if (tile < A.ntiles_interior) {
+            if (li < A.n_interior) {
+                const uint32_t r = A.div_ix.div((uint32_t)li);
+                const int x = li - (int)r * (A.nx - 2) + 1;
+                const uint32_t zq = A.div_iy.div(r);
+                const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
+                const int z = (int)zq + 1;
+                process_cell<S, ODD, THERMAL, MAT>(A, (z * A.ny + y) * A.nx + x, x, y, z, true, acc);
+            }
+        } else {
+            const int si = li - A.ntiles_interior * STEP_BLOCK;
+            if (si < A.n_shell) {
+                const int cell = A.shell[si];
+                const uint32_t r = A.div_x.div((uint32_t)cell);
+                const int x = cell - (int)r * A.nx;
+                const uint32_t z = A.div_y.div(r);
+                const int y = (int)(r - z * (uint32_t)A.ny);
+                process_cell<S, ODD, THERMAL, MAT>(A, cell, x, y, (int)z, false, acc);
+            }
+        }
+    }
+    if (MAT) return;
+    block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
+    finish_step<STEP_BLOCK>(A);
+}
+
+}  // namespace aeros

@@ -1,0 +1,290 @@
+"""Benchmark of the GB300 LBM solver step (one JSON line on rank 0).
+
+Workload: the Re = 100 sphere, 240 x 120 x 115 = 3.31 M cells, D3Q19 TRT +
+Smagorinsky (two-pass |S|), icosphere level 6 (81,920 triangles) voxelized on
+the GPU, inlet u = 0.05, zero-gradient outlet, free-slip lateral walls;
+populations stored as FP16 shifted deviations (the headline form) with the
+plain FP32 form measured beside it. A step is one lattice update of the whole
+domain. The working set (populations + two velocity fields + descriptors)
+exceeds the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU implementation of the same step (the C
+restatement of the reference solver, OpenMP over all host cores; the
+reference's own build cannot run on this host) on the same grid.
+Under torchrun (N > 1) each rank runs an independent replica on its GPU
+(the workload does not shard); value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "aeros-engine_gb300"))
+
+# algorithmic bytes per cell update of the step kernel (read + write):
+#   populations 2 x 19 x bytes, previous velocity 12, new velocity 12, descriptor 4
+BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 12 + 12 + 4, "fp16": 2 * 19 * 2 + 12 + 12 + 4, "bf16": 2 * 19 * 2 + 12 + 12 + 4}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.samples = []
+        self.stop = threading.Event()
+        self.t = None
+
+    def _run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([v.strip() for v in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self.stop.set()
+        if self.t:
+            self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def sphere_case(storage, mask=None):
+    from aeros_gb300 import geometry
+    return geometry.sphere_config(storage=storage, mask=mask)
+
+
+def time_steps(solver, steps, warmup):
+    """Device time of `steps` lattice steps (CUDA events around the launches on
+    the solver's stream), after `warmup` untimed steps."""
+    solver.step(warmup)
+    solver.synchronize()
+    solver.step_async(steps)
+    ms = solver.last_step_ms()
+    launches = solver.last_launch_count()
+    st = solver.stats()
+    return ms, launches, st
+
+
+def run_gb300(args):
+    import ctypes
+
+    from aeros_gb300 import capi, solver
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    capi.lib()
+    nx, ny, nz = (240, 120, 115)
+    cells = nx * ny * nz
+    # geometry: the icosphere voxelized on the GPU (BVH path)
+    t0 = time.time()
+    p16, mask, tris = sphere_case("fp16")
+    vox_s = time.time() - t0
+    results = {}
+    peak, peak_kind = measured_peak()
+    with ClockSampler(local) as clk:
+        for storage in ("fp32", "fp16"):
+            p, _, _ = sphere_case(storage, mask=mask)
+            s = solver.Solver(p, mask)
+            ms, launches, st = time_steps(s, args.steps, args.warmup)
+            mlups = cells * args.steps / (ms * 1e-3) / 1e6
+            gbs = BYTES_PER_CELL[storage] * cells * args.steps / (ms * 1e-3) / 1e9
+            results[storage] = dict(ms_per_step=ms / args.steps, mlups=mlups, achieved_gbs=gbs, launches=launches,
+                                    avg_rho=st["avg_rho"], max_u=st["max_velocity_lb"], bytes=s.device_bytes())
+            s.close()
+        # end to end through the C ABI with host buffers: create from the host
+        # mask (H2D), per step one aeros_lbm_step(1) + the control-volume drag
+        # read back (D2H), fields read back to host at the end, destroy.
+        pin = {}
+        e2e_steps = args.steps
+        t1 = time.perf_counter()
+        p, _, _ = sphere_case("fp16", mask=mask)
+        s = solver.Solver(p, mask)
+        forces = []
+        for _ in range(e2e_steps):
+            s.step(1)
+            forces.append(s.cv_force(0.3, 0.3, 0.3))
+        pin = s.fields()
+        s.close()
+        e2e_s = time.perf_counter() - t1
+    e2e_mlups = cells * e2e_steps / e2e_s / 1e6
+    h2d = mask.size  # mask bytes uploaded at create
+    d2h = 24 * e2e_steps + 4 * cells * 6 + 160 * e2e_steps
+    head = results["fp16"]
+    value = head["mlups"]
+    e2e_value = e2e_mlups
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([value, e2e_value, head["ms_per_step"]], dtype=torch.float64, device="cuda")
+        vals = [torch.zeros_like(t) for _ in range(world)]
+        dist.all_gather(vals, t)
+        value = sum(float(v[0]) for v in vals)
+        e2e_value = sum(float(v[1]) for v in vals)
+        ms_step = max(float(v[2]) for v in vals)
+    else:
+        ms_step = head["ms_per_step"]
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(mask, args.cpu_steps)
+    if rank == 0:
+        frac = head["achieved_gbs"] / peak
+        line = {
+            "metric": "MLUPS (D3Q19 TRT+Smagorinsky sphere, FP16-shifted storage)",
+            "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_step, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp16-storage/fp32-math", "data": "synthetic",
+            "config": {"workload": "sphere Re=100, 240x120x115 (3.31 M cells), icosphere L6 voxelized on GPU, "
+                                   "TRT+Smagorinsky, zero-gradient outlet, free-slip lateral walls",
+                       "storage": "fp16 shifted (f - w)", "l2": "working set > 129 MB L2, no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": round(head["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(frac, 4), "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_cell": BYTES_PER_CELL["fp16"]},
+            "fp32_plain": {"mlups": round(results["fp32"]["mlups"], 1),
+                           "ms_per_step": round(results["fp32"]["ms_per_step"], 4),
+                           "achieved_gbs": round(results["fp32"]["achieved_gbs"], 1),
+                           "frac": round(results["fp32"]["achieved_gbs"] / peak, 4),
+                           "bytes_per_cell": BYTES_PER_CELL["fp32"]},
+            "fp16_over_fp32": round(results["fp16"]["mlups"] / results["fp32"]["mlups"], 3),
+            "e2e": {"value": round(e2e_value, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // max(1, e2e_steps)),
+                    "d2h_bytes_per_step": int(d2h // max(1, e2e_steps)),
+                    "what": "create from host mask + per step aeros_lbm_step(1) and CV-force readback + final fields"},
+            "gpu_launches": int(head["launches"]),
+            "clocks": clk.summary(),
+            "voxelize_s": round(vox_s, 3),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline(mask, steps):
+    """The oracle (C restatement of the reference solver, OpenMP) on the same
+    grid, `steps` lattice steps (a bounded sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    p, _, _ = sphere_case("fp32", mask=mask)
+    o = oracle.OracleLBM(p, mask)
+    o.step(1)
+    t = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t
+    cells = p.nx * p.ny * p.nz
+    return {"value": round(cells * steps / dt / 1e6, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"{steps} lattice steps of the full 240x120x115 sphere grid (FP32, OpenMP {cores} threads)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    from aeros_gb300 import geometry
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    nx, ny, nz = geometry.SPHERE_GRID
+    # the reference's CPU path voxelizes on the host: brute-force inside test
+    tris = geometry.icosphere(6, geometry.SPHERE_RADIUS, geometry.SPHERE_CENTER)
+    from aeros_gb300.solver import voxel_grid
+    g = voxel_grid((nx, ny, nz), (0, 0, 0), (1, 1, 1))
+    mpath = os.path.join(ROOT, "tests", "golden", "masks.npz")
+    mask = np.unpackbits(np.load(mpath)["sphere_config_mask"])[: nx * ny * nz].astype(np.uint8)
+    del tris, g
+    p, _, _ = geometry.sphere_config(storage="fp32", mask=mask)
+    o = oracle.OracleLBM(p, mask)
+    o.step(args.warmup)
+    t = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t
+    cells = nx * ny * nz
+    v = cells * args.steps / dt / 1e6
+    line = {"impl": "reference", "metric": "MLUPS (D3Q19 TRT+Smagorinsky sphere, FP16-shifted storage)",
+            "value": round(v, 2), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000 * dt / args.steps, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": "sphere Re=100, 240x120x115 (3.31 M cells), TRT+Smagorinsky, zero-gradient outlet, "
+                                   "free-slip lateral walls", "parallelism": f"OpenMP {cores} threads"},
+            "cpu_baseline": {"value": round(v, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} full-grid lattice steps per timed run"},
+            "e2e": {"value": round(v, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=30)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -232,6 +232,9 @@ class RefHarness:
         L.ref_voxelize.argtypes = [_FP, C.c_longlong, C.c_int, C.c_int, C.c_int, _FP, _FP, _U8P]
         L.ref_count_hits.argtypes = [_FP, C.c_longlong, _FP, C.c_int]
         L.ref_voxel_plan.argtypes = [_FP, C.c_int, C.c_ulonglong, C.POINTER(C.c_int)]
+        L.ref_validation_setup.argtypes = [C.c_int, C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float,
+                                           C.POINTER(C.c_int), _FP, _FP]
+        L.ref_get_mask.argtypes = [_U8P]
         self.L = L
         self.n = 0
 
@@ -323,6 +326,22 @@ class RefHarness:
     def count_hits(self, tris, origin, axis):
         t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
         return self.L.ref_count_hits(fptr(t), t.size // 9, fptr(np.asarray(origin, np.float32)), int(axis))
+
+    def validation_setup(self, shape, res, radius, diameter_cells, re_lat, pad, u0):
+        dims = (C.c_int * 3)()
+        tau = np.zeros(1, np.float32)
+        uin = np.zeros(3, np.float32)
+        rc = self.L.ref_validation_setup(int(shape), int(res), radius, int(diameter_cells), re_lat, pad, u0, dims,
+                                         fptr(tau), fptr(uin))
+        if rc != 0:
+            raise RuntimeError("reference validation setup failed")
+        self.n = dims[0] * dims[1] * dims[2]
+        return tuple(dims), float(tau[0]), uin
+
+    def mask(self):
+        m = np.empty(self.n, np.uint8)
+        self.L.ref_get_mask(u8ptr(m))
+        return m
 
     def voxel_plan(self, size, res, budget):
         out = (C.c_int * 6)()

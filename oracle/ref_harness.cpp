@@ -227,4 +227,65 @@ void ref_voxel_plan(const float* size, int res, unsigned long long budget, int* 
     out6[4] = p.suggestedRes; out6[5] = (int)p.cells;
 }
 
+// The validation case set-up of aeros/tests/validation_headless.cpp:57-81 and
+// :99-129 (sphere / cylinder voxel mask on a [-3,3]^3 box of res^3 cells,
+// padded domain, BGK, convective outlet), restated here to export the solver
+// grid the reference builds from it. Writes nx, ny, nz, the tau the solver
+// uses and the inlet velocity.
+int ref_validation_setup(int shape, int res, float radius, int diameter_cells, float re_lat, float pad,
+                         float u0, int* dims, float* tau_out, float* uin_out) {
+    flowSpeed = 20.0f; flowAzimuth = 0.0f; flowElevation = 0.0f;
+    altitude = 0.0f; timeScale = 1.0f; aeroMachEffects = false; aeroGroundEffect = false;
+    lbmParams = LBMParams();
+    lbmParams.enabled = true;
+    lbmParams.useGPU = false;
+    lbmParams.U0 = u0;
+    lbmParams.stepsPerFrame = 1;
+    lbmParams.useTurbulence = false;
+    lbmParams.useGround = false;
+    lbmParams.inletTurbulence = 0.0f;
+    lbmParams.domainPadding = pad;
+    lbmParams.autoViscosity = false;
+    voxelResolution = res;
+    float tau = 0.5f + 3.0f * u0 * (float)diameter_cells / re_lat;
+    tau = std::max(0.505f, std::min(tau, 1.4f));
+    lbmParams.tau = tau;
+    g_voxNx = g_voxNy = g_voxNz = res;
+    g_voxMinX = g_voxMinY = g_voxMinZ = -3.0f;
+    g_voxMaxX = g_voxMaxY = g_voxMaxZ = 3.0f;
+    const float cs = 6.0f / (float)res;
+    g_voxelData.assign((size_t)res * res * res, 0);
+    g_distanceField.assign((size_t)res * res * res, 0.0f);
+    for (int z = 0; z < res; ++z)
+        for (int y = 0; y < res; ++y)
+            for (int x = 0; x < res; ++x) {
+                const float px = g_voxMinX + (x + 0.5f) * cs;
+                const float py = g_voxMinY + (y + 0.5f) * cs;
+                const float pz = g_voxMinZ + (z + 0.5f) * cs;
+                const float d = shape == 0 ? std::sqrt(px * px + py * py + pz * pz) - radius
+                                           : std::sqrt(py * py + pz * pz) - radius;
+                const size_t i = (size_t)(z * res + y) * res + x;
+                g_voxelData[i] = (d <= 0.0f) ? 1 : 0;
+                g_distanceField[i] = d / cs;
+            }
+    minBB = glm::vec3(-radius); maxBB = glm::vec3(radius);
+    center = glm::vec3(0.0f); maxDim = 2.0f * radius;
+    thermalParams.enabled = false;
+    shutdownLBM();
+    initLBM();
+    if (!lbmInitialized) return -1;
+    dims[0] = lbmNx; dims[1] = lbmNy; dims[2] = lbmNz;
+    *tau_out = lbmParams.tau;
+    float ux, uy, uz;
+    computeInletVelocityLB(ux, uy, uz);
+    uin_out[0] = ux; uin_out[1] = uy; uin_out[2] = uz;
+    return 0;
+}
+
+// Solver mask: 0 fluid, 1 solid, 2 ground.
+void ref_get_mask(uint8_t* out) {
+    const size_t n = lbmIsSolid.size();
+    for (size_t i = 0; i < n; ++i) out[i] = lbmIsSolid[i] ? 1 : (lbmIsGround[i] ? 2 : 0);
+}
+
 }  // extern "C"

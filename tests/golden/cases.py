@@ -1,0 +1,139 @@
+"""Parity cases shared by the golden-fixture generator and the tests.
+
+Each case is a small grid the reference finishes in well under a second per
+hundred steps; ``make_golden.py`` runs it through the reference's own solver
+(oracle/_ref) and records SHA-256 digests of every output field, and the
+tests rerun it through the oracle (CPU) and the CUDA library (GPU).
+Geometry is built in code as the reference's headless tests do.
+"""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+
+from aeros_gb300 import capi
+
+
+def sphere_mask(nx, ny, nz, cx, cy, cz, r) -> np.ndarray:
+    z, y, x = np.mgrid[0:nz, 0:ny, 0:nx]
+    return (((x + 0.5 - cx) ** 2 + (y + 0.5 - cy) ** 2 + (z + 0.5 - cz) ** 2) <= r * r).astype(np.uint8)
+
+
+def channel(nx, ny, nz) -> np.ndarray:
+    m = np.zeros((nz, ny, nx), np.uint8)
+    m[:, 0, :] = 1
+    m[:, ny - 1, :] = 1
+    return m
+
+
+# name -> dict(grid, solid, ground_rows, u_init, steps, harness kwargs, thermal)
+CASES = {
+    "channel_bgk": dict(grid=(16, 34, 8), solid=lambda: channel(16, 34, 8), u_init=(0.0, 0.0, 0.0), steps=600,
+                        kw=dict(tau=0.65, u0=0.0, periodic_x=True, periodic_z=True, body_force=(7.8e-6, 0.0, 0.0))),
+    "channel_trt": dict(grid=(16, 34, 8), solid=lambda: channel(16, 34, 8), u_init=(0.0, 0.0, 0.0), steps=600,
+                        kw=dict(tau=0.65, u0=0.0, trt=True, periodic_x=True, periodic_z=True,
+                                body_force=(7.8e-6, 0.0, 0.0))),
+    "channel_force3": dict(grid=(16, 16, 12), solid=lambda: channel(16, 16, 12), u_init=(0.0, 0.0, 0.0), steps=200,
+                           kw=dict(tau=0.7, u0=0.0, trt=True, les=True, smag=0.15, periodic_x=True, periodic_z=True,
+                                   body_force=(1e-5, 2e-6, -3e-6), flow_speed=5.0)),
+    "sphere_bgk_conv": dict(grid=(40, 24, 24), solid=lambda: sphere_mask(40, 24, 24, 12, 12, 12, 4), steps=150,
+                            kw=dict(tau=0.56, u0=0.08, convective=True, flow_speed=20.0)),
+    "sphere_trt_les_conv": dict(grid=(40, 24, 24), solid=lambda: sphere_mask(40, 24, 24, 12, 12, 12, 4), steps=150,
+                                kw=dict(tau=0.536, u0=0.05, les=True, trt=True, smag=0.1, convective=True,
+                                        flow_speed=20.0)),
+    "sphere_les_ground_copy": dict(grid=(40, 24, 24), solid=lambda: sphere_mask(40, 24, 24, 12, 12, 12, 4),
+                                   ground_rows=2, steps=100,
+                                   kw=dict(tau=0.56, u0=0.08, les=True, flow_speed=10.0)),
+    "sphere_minus_x": dict(grid=(40, 24, 24), solid=lambda: sphere_mask(40, 24, 24, 26, 12, 12, 4), steps=80,
+                           kw=dict(tau=0.56, u0=0.08, les=True, trt=True, convective=True, flow_axis=0, flow_sign=-1)),
+    "sphere_plus_y": dict(grid=(24, 40, 24), solid=lambda: sphere_mask(24, 40, 24, 12, 12, 12, 4), steps=80,
+                          kw=dict(tau=0.56, u0=0.08, les=True, convective=True, flow_axis=1, flow_sign=1)),
+    "sphere_minus_z_perx": dict(grid=(24, 24, 40), solid=lambda: sphere_mask(24, 24, 40, 12, 12, 20, 4), steps=80,
+                                kw=dict(tau=0.56, u0=0.08, les=True, convective=True, flow_axis=2, flow_sign=-1)),
+    "rb_small": dict(grid=(32, 18, 8), solid=lambda: channel(32, 18, 8), u_init=(0.0, 0.0, 0.0), steps=400,
+                     kw=dict(tau=0.65, u0=0.0, periodic_x=True, periodic_z=True),
+                     thermal=dict(rayleigh=2500.0, prandtl=1.0, fixed=True, hot=1.0, cold=0.0, perturbation=0.02)),
+    "rb_pm": dict(grid=(32, 18, 8), solid=lambda: channel(32, 18, 8), u_init=(0.0, 0.0, 0.0), steps=200,
+                  kw=dict(tau=0.6, u0=0.0, periodic_x=True, periodic_z=True),
+                  thermal=dict(rayleigh=5000.0, prandtl=0.71, fixed=True, hot=0.5, cold=-0.5, perturbation=0.05)),
+    "thermal_body": dict(grid=(24, 18, 16), solid=lambda: np.maximum(channel(24, 18, 16),
+                                                                     sphere_mask(24, 18, 16, 12, 9, 8, 3)),
+                         u_init=(0.0, 0.0, 0.0), steps=150,
+                         kw=dict(tau=0.6, u0=0.0, periodic_x=True, periodic_z=False),
+                         thermal=dict(rayleigh=20000.0, prandtl=1.0, fixed=True, hot=1.0, cold=0.0,
+                                      perturbation=0.02)),
+}
+
+
+def thermal_diffusion_T(nx, ny, nz) -> np.ndarray:
+    T = np.zeros((nz, ny, nx), np.float32)
+    T[:] = (0.5 + 0.5 * np.cos(2 * np.pi / nx * np.arange(nx))).astype(np.float32)
+    return T
+
+
+CASES["thermal_diffusion"] = dict(grid=(32, 16, 8), solid=lambda: np.zeros((8, 16, 32), np.uint8), steps=200,
+                                  kw=dict(tau=0.65, u0=0.0, periodic_x=True, periodic_z=True),
+                                  thermal=dict(rayleigh=0.0, prandtl=1.0, fixed=False, hot=1.0, cold=0.0,
+                                               perturbation=0.0),
+                                  upload=lambda: thermal_diffusion_T(32, 16, 8))
+
+
+def solver_mask(case) -> np.ndarray:
+    nx, ny, nz = case["grid"]
+    m = case["solid"]().astype(np.uint8).reshape(nz, ny, nx).copy()
+    g = case.get("ground_rows", 0)
+    if g:
+        ground = np.zeros_like(m)
+        ground[:, :g, :] = 1
+        m = np.where((m == 0) & (ground == 1), capi.AEROS_CELL_GROUND, m).astype(np.uint8)
+    return m
+
+
+def params_for(case, u_in, storage="fp32"):
+    """LbmParams equal to the reference's set-up of the case; u_in is the inlet
+    velocity the reference derived (recorded in the golden file)."""
+    kw = case["kw"]
+    nx, ny, nz = case["grid"]
+    u_in = np.asarray(u_in, np.float32)
+    mag = np.float32(np.sqrt(np.float32(u_in[0] * u_in[0] + u_in[1] * u_in[1] + u_in[2] * u_in[2])))
+    if not np.isfinite(mag) or mag < 1e-6:
+        mag = np.float32(0.08)
+    vs = np.float32(np.float32(kw.get("flow_speed", 1.0)) / mag)
+    if not np.isfinite(vs) or vs > 1000.0:
+        vs = np.float32(20.0)
+    if vs < 0.01:
+        vs = np.float32(0.01)
+    return capi.make_params(nx, ny, nz, tau=kw.get("tau", 0.6), smagorinsky_c=kw.get("smag", 0.12),
+                            les=kw.get("les", False), trt=kw.get("trt", False),
+                            periodic_x=kw.get("periodic_x", False), periodic_z=kw.get("periodic_z", False),
+                            convective_outlet=kw.get("convective", False), flow_axis=kw.get("flow_axis", 0),
+                            flow_sign=kw.get("flow_sign", 1), u_in=u_in,
+                            u_init=case.get("u_init", u_in), body_force=kw.get("body_force", (0.0, 0.0, 0.0)),
+                            vel_scale=float(vs), storage=storage)
+
+
+def thermal_params_for(case, tau):
+    t = case["thermal"]
+    nu = np.float32((np.float32(tau) - np.float32(0.5)) * np.float32(1.0 / 3.0))
+    return capi.make_thermal(rayleigh=t["rayleigh"], prandtl=t["prandtl"], fixed_wall_temps=t["fixed"], hot=t["hot"],
+                             cold=t["cold"], perturbation=t["perturbation"], nu_lb=float(nu))
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def outputs_digest(fields: dict, f: np.ndarray | None, mask: np.ndarray, T=None, buoy=None) -> dict:
+    d = {k: digest(np.asarray(fields[k], np.float32) + np.float32(0.0)) for k in ("rho", "ux", "uy", "uz", "strain", "tke")}
+    if f is not None:
+        fl = mask.reshape(-1) == 0
+        d["f"] = digest(np.ascontiguousarray(f[:, fl]) + np.float32(0.0))
+    if T is not None:
+        d["T"] = digest(np.asarray(T, np.float32) + np.float32(0.0))
+        d["buoy"] = digest(np.asarray(buoy, np.float32) + np.float32(0.0))
+    return d
+
+
+EQ_MOMENT_CASES = [(1.0, 0.0, 0.0, 0.0), (1.0, 0.05, 0.0, 0.0), (0.7, 0.04, -0.03, 0.02), (1.35, -0.02, 0.05, 0.01),
+                   (0.55, 0.1, 0.1, 0.0), (1.6, 0.0, 0.0, -0.08), (1.1, 0.28, 0.0, 0.0)]

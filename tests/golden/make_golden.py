@@ -1,0 +1,172 @@
+"""Generates tests/golden/golden.json and the mask fixtures from the
+reference's OWN solver sources (oracle/_ref/libaeros_ref.so, built in place by
+``make -C oracle ref``). Run where the reference tree exists:
+
+    python tests/golden/make_golden.py
+
+Every fixture is small: SHA-256 digests of float32 fields, scalars, and
+bit-packed masks. The reference is stepped one call per step (see
+oracle/ref_harness.cpp on why).
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "aeros-engine_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, HERE)
+
+import oracle as O  # noqa: E402
+from cases import CASES, EQ_MOMENT_CASES, outputs_digest, solver_mask  # noqa: E402
+
+from aeros_gb300 import geometry  # noqa: E402
+
+
+def run_case(R, name, case):
+    nx, ny, nz = case["grid"]
+    solid = case["solid"]().astype(np.uint8).reshape(-1)
+    kw = dict(case["kw"])
+    u_in = R.setup(nx, ny, nz, solid, ground_rows=case.get("ground_rows", 0), **kw)
+    if "u_init" in case:
+        R.set_uniform(*case["u_init"])
+    th = case.get("thermal")
+    if th:
+        R.thermal_setup(th["rayleigh"], th["prandtl"], th["fixed"], th["hot"], th["cold"], th["perturbation"])
+        if "upload" in case:
+            R.thermal_upload(case["upload"]())
+    R.step(case["steps"])
+    fields = R.fields()
+    f = R.populations()
+    mask = solver_mask(case)
+    T = buoy = None
+    out = {"u_in": [float(v) for v in u_in]}
+    if th:
+        T, buoy, nu, mt = R.thermal()
+        out["nusselt"] = nu
+        out["mean_t"] = mt
+    out["digest"] = outputs_digest(fields, f, mask, T, buoy)
+    out["stats"] = R.stats()
+    out["cv_force"] = [float(v) for v in R.cv_force(0.3, 0.3, 0.3)]
+    out["area"] = [R.projected_area(a) for a in range(3)]
+    out["wall_digest"] = __import__("cases").digest(R.wall_dist())
+    out["checksum"] = {k: float(np.sum(fields[k], dtype=np.float64)) for k in ("rho", "ux", "uy", "uz")}
+    print(f"  {name}: {case['steps']} steps, rho sum {out['checksum']['rho']:.9f}")
+    return out
+
+
+def channel_profile(R, ny, tau, force, steps, trt=False, nx=8, nz=8):
+    """physics_ref_headless.cpp:65-166: profile averaged over x at z = nz/2."""
+    solid = geometry.channel_mask(nx, ny, nz).reshape(-1)
+    R.setup(nx, ny, nz, solid, tau=tau, u0=0.0, trt=trt, periodic_x=True, periodic_z=True,
+            body_force=(force, 0.0, 0.0))
+    R.set_uniform(0.0, 0.0, 0.0) if False else None   # reference starts at U0 -> 0.08 (lbm.cpp:196)
+    R.step(steps)
+    fl = R.fields()
+    ux = fl["ux"].reshape(nz, ny, nx)
+    prof = ux[nz // 2, 1:ny - 1, :].astype(np.float64).mean(axis=1)
+    exact = geometry.poiseuille_exact(ny, tau, force)
+    l2 = float(np.sqrt(np.sum((prof - exact) ** 2) / np.sum(exact ** 2)))
+    mask = solid.reshape(nz, ny, nx)
+    rho = fl["rho"].reshape(nz, ny, nx)
+    drift = float(abs(rho[mask == 0].astype(np.float64).mean() - 1.0))
+    yc = 0.5 * (ny - 1)
+    s = np.arange(1, ny - 1) - yc
+    uc = float(prof[np.abs(s) <= 0.75].max())
+    return dict(l2=l2, u_center=uc, flux=float(prof.sum()), flux_exact=float(exact.sum()), mass_drift=drift,
+                digest=outputs_digest(fl, None, mask), profile=[float(v) for v in prof])
+
+
+def validation_sphere(R, res=48, d_cells=20, pad=0.15, warm=500, meas=50):
+    """validation_headless.cpp:99-183 and :206-251: Cd of the Re = 100 sphere."""
+    radius = 3.0 * d_cells / res
+    dims, tau, u_in = R.validation_setup(0, res, radius, d_cells, 100.0, pad, 0.08)
+    mask = R.mask()
+    R.step(warm)
+    area = R.projected_area(0)
+    q = 0.5 * 0.08 * 0.08 * area
+    cds = []
+    for _ in range(meas):
+        R.step(1)
+        F = R.cv_force(0.3, 0.3, 0.3)
+        cds.append(np.float32(F[0]) / np.float32(q))
+    cd = float(np.mean(np.array(cds, np.float64)))
+    fl = R.fields()
+    return dict(dims=list(dims), tau=tau, u_in=[float(v) for v in u_in], area=area, cd=cd,
+                cd_trace=[float(v) for v in cds], warm=warm, meas=meas,
+                digest=outputs_digest(fl, R.populations(), mask.reshape(-1))), mask
+
+
+def main():
+    O.build()
+    R = O.RefHarness()
+    out = {"cases": {}, "note": "generated from the reference sources by make_golden.py"}
+    t0 = time.time()
+    for name, case in CASES.items():
+        out["cases"][name] = run_case(R, name, case)
+    print("physref channels ...")
+    out["physref"] = {
+        "bgk_40k": channel_profile(R, 34, 0.65, 7.8e-6, 40000),
+        "trt_40k": channel_profile(R, 34, 0.65, 7.8e-6, 40000, trt=True),
+        "h8_4k": channel_profile(R, 10, 0.65, 7.8e-6 * 16.0, 4000),
+        "h16_15k": channel_profile(R, 18, 0.65, 7.8e-6 * 4.0, 15000),
+    }
+    for k, v in out["physref"].items():
+        print(f"  {k}: L2 {100 * v['l2']:.3f} %, u_c {v['u_center']:.6f}")
+    # the Poiseuille configuration (64 x 32 x 32, tau 0.8, F 1e-6, u0 = 0, 4000 steps)
+    print("poiseuille config ...")
+    nx, ny, nz = 64, 32, 32
+    solid = geometry.channel_mask(nx, ny, nz).reshape(-1)
+    u_in = R.setup(nx, ny, nz, solid, tau=0.8, u0=0.0, periodic_x=True, periodic_z=True, body_force=(1e-6, 0, 0))
+    R.set_uniform(0.0, 0.0, 0.0)
+    R.step(4000)
+    fl = R.fields()
+    ux = fl["ux"].reshape(nz, ny, nx)
+    prof = ux[:, 1:ny - 1, :].astype(np.float64).mean(axis=(0, 2))
+    exact = geometry.poiseuille_exact(ny, 0.8, 1e-6)
+    out["poiseuille_config"] = dict(u_in=[float(v) for v in u_in], steps=4000,
+                                    l2=float(np.sqrt(np.sum((prof - exact) ** 2) / np.sum(exact ** 2))),
+                                    digest=outputs_digest(fl, R.populations(), solid.reshape(nz, ny, nx)),
+                                    stats=R.stats())
+    print(f"  L2 vs exact {100 * out['poiseuille_config']['l2']:.4f} %")
+    print("validation sphere ...")
+    val, vmask = validation_sphere(R)
+    out["validation_sphere"] = val
+    print(f"  Cd {val['cd']:.4f} area {val['area']} dims {val['dims']} tau {val['tau']}")
+    masks = {"validation_sphere_mask": np.packbits(vmask)}
+    print("voxelizer ...")
+    nx, ny, nz = geometry.SPHERE_GRID
+    tris = geometry.icosphere(6, geometry.SPHERE_RADIUS, geometry.SPHERE_CENTER)
+    t1 = time.time()
+    sm = R.voxelize(tris, nx, ny, nz, (0, 0, 0), (1, 1, 1))
+    print(f"  sphere config mask: {int(sm.sum())} solid cells in {time.time() - t1:.1f} s")
+    masks["sphere_config_mask"] = np.packbits(sm)
+    out["voxel"] = {"sphere_config": dict(solid=int(sm.sum()), ntri=int(tris.shape[0]),
+                                          digest=__import__("cases").digest(sm))}
+    vox_cases = {
+        "uv_sphere_40": (geometry.uv_sphere(0.35, 32, 48), 40, (-0.5, -0.5, -0.5), 1.0 / 40),
+        "torus_48": (geometry.torus(0.3, 0.11, 64, 32), 48, (-0.45, -0.2, -0.45), 0.9 / 48),
+        "box_32": (geometry.box((0.3, 0.2, 0.25)), 32, (-0.4, -0.4, -0.4), 0.8 / 32),
+        "plate_64": (geometry.box((0.3, 0.003, 0.2)), 64, (-0.4, -0.4, -0.4), 0.8 / 64),
+    }
+    for k, (tv, n, mn, cs) in vox_cases.items():
+        m = R.voxelize(tv, n, n, n, mn, (np.float32(cs),) * 3)
+        out["voxel"][k] = dict(solid=int(m.sum()), digest=__import__("cases").digest(m), n=n, min=list(mn), cell=cs)
+        print(f"  {k}: {int(m.sum())} solid")
+    out["eq_moments"] = [list(R.equilibrium_moments(*c)[1]) for c in EQ_MOMENT_CASES]
+    out["voxel_plan"] = {"1x0.5x0.25@64/8G": list(R.voxel_plan([1, 0.5, 0.25], 64, 8 << 30)),
+                         "1@512/512M": list(R.voxel_plan([1, 1, 1], 512, 512 << 20))}
+    with open(os.path.join(HERE, "golden.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+    np.savez_compressed(os.path.join(HERE, "masks.npz"), **masks)
+    print(f"done in {time.time() - t0:.0f} s")
+
+
+if __name__ == "__main__":
+    main()
