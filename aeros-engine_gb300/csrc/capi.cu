@@ -70,6 +70,9 @@ struct aeros_lbm {
     void* f = nullptr;
     uint32_t* desc = nullptr;
     int* shell = nullptr;
+    unsigned long long* shell_kind = nullptr;
+    std::vector<int> shell_host;
+    std::vector<unsigned long long> shell_kind_host;
     float* u[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     float *rho = nullptr, *strain = nullptr, *tke = nullptr;
     float* out[2] = {nullptr, nullptr};
@@ -133,6 +136,7 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->f);
     cudaFree(h->desc);
     cudaFree(h->shell);
+    cudaFree(h->shell_kind);
     for (auto& b : h->u)
         for (auto& c : b) cudaFree(c);
     cudaFree(h->rho);
@@ -242,6 +246,51 @@ static void build_descriptor(aeros_lbm* h, std::vector<uint32_t>& desc, std::vec
     h->n_interior = (nx - 2) * (ny - 2) * (nz - 2);
 }
 
+// Link kind of pre-collision population q at a shell cell: the host twin of
+// resolve_src (lbm_step.cuh), evaluated once per shell cell.
+static int host_link_kind(const aeros_lbm* h, int x, int y, int z, int q) {
+    const int n[3] = {h->nx, h->ny, h->nz};
+    int sv[3] = {x - cx19(q), y - cy19(q), z - cz19(q)};
+    const int per[3] = {h->p.periodic_x, 0, h->p.periodic_z};
+    int outm = 0;
+    for (int a = 0; a < 3; ++a) {
+        if (per[a]) sv[a] = sv[a] < 0 ? sv[a] + n[a] : (sv[a] >= n[a] ? sv[a] - n[a] : sv[a]);
+        if (sv[a] < 0 || sv[a] >= n[a]) outm |= 1 << a;
+    }
+    if (!outm) return h->mask[cidx(h, sv[0], sv[1], sv[2])] ? L_BOUNCE : L_REGULAR;
+    if (h->p.lateral_bc == AEROS_LATERAL_FREESLIP && !((outm >> h->p.flow_axis) & 1)) {
+        const int pos[3] = {x, y, z};
+        int r[3];
+        for (int a = 0; a < 3; ++a) r[a] = ((outm >> a) & 1) ? pos[a] : sv[a];
+        return h->mask[cidx(h, r[0], r[1], r[2])] ? L_BOUNCE : L_FREESLIP;
+    }
+    return L_COPYOWN;
+}
+
+// Thermal link kind (0 regular, 1 bounce, 2 Dirichlet), host twin of th_resolve.
+static int host_th_kind(const aeros_lbm* h, int x, int y, int z, int i) {
+    int sx = x - cx19(i), sy = y - cy19(i), sz = z - cz19(i);
+    if (sx < 0) sx = h->nx - 1; else if (sx >= h->nx) sx = 0;
+    if (sz < 0) sz = h->nz - 1; else if (sz >= h->nz) sz = 0;
+    const bool fixed = h->tp.fixed_wall_temps != 0;
+    if (sy < 0 || sy >= h->ny) return fixed ? 2 : 1;
+    if (h->mask[cidx(h, sx, sy, sz)]) return (fixed && (sy <= 0 || sy >= h->ny - 1)) ? 2 : 1;
+    return 0;
+}
+
+static void build_shell_kinds(aeros_lbm* h) {
+    h->shell_kind_host.assign(h->shell_host.size(), 0ull);
+    for (size_t k = 0; k < h->shell_host.size(); ++k) {
+        const int c = h->shell_host[k];
+        const int x = c % h->nx, r = c / h->nx, y = r % h->ny, z = r / h->ny;
+        unsigned long long v = 0;
+        for (int q = 0; q < Q19; ++q) v |= (unsigned long long)host_link_kind(h, x, y, z, q) << (2 * q);
+        if (h->th_on)
+            for (int i = 0; i < Q7; ++i) v |= (unsigned long long)host_th_kind(h, x, y, z, i) << (40 + 2 * i);
+        h->shell_kind_host[k] = v;
+    }
+}
+
 static void fill_args(const aeros_lbm* h, FillArgs& fa, const float u[3]) {
     fa.f = h->f;
     fa.desc = h->desc;
@@ -320,6 +369,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     ALLOC(h->f, (size_t)h->qstride * Q19 * h->esize);
     ALLOC(h->desc, n * 4);
     ALLOC(h->shell, (size_t)std::max(1, h->n_shell) * 4);
+    ALLOC(h->shell_kind, (size_t)std::max(1, h->n_shell) * 8);
     for (auto& b : h->u)
         for (auto& c : b) ALLOC(c, n * 4);
     ALLOC(h->rho, n * 4);
@@ -353,6 +403,11 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     if ((e = cudaMemcpy(h->desc, desc.data(), n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "desc upload");
     if (h->n_shell && (e = cudaMemcpy(h->shell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(e, "shell upload");
+    h->shell_host = shell;
+    build_shell_kinds(h);
+    if (h->n_shell && (e = cudaMemcpy(h->shell_kind, h->shell_kind_host.data(), h->shell_kind_host.size() * 8,
+                                      cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e, "shell kinds upload");
     for (auto& b : h->u)
         for (auto& c : b)
             if ((e = cudaMemset(c, 0, n * 4)) != cudaSuccess) return fail(e, "u memset");
@@ -444,7 +499,7 @@ static void base_args(const aeros_lbm* h, StepArgs& A) {
     A.div_iy = FastDiv((uint32_t)(h->ny - 2));
     A.div_x = FastDiv((uint32_t)h->nx);
     A.div_y = FastDiv((uint32_t)h->ny);
-    A.f = h->f; A.desc = h->desc; A.shell = h->shell;
+    A.f = h->f; A.desc = h->desc; A.shell = h->shell; A.shell_kind = h->shell_kind;
     A.rho = h->rho; A.strain = h->strain; A.tke = h->tke;
     A.out_plane = h->out_plane;
     A.g = h->g; A.T = h->T; A.T_buoy = h->T_buoy;
@@ -779,7 +834,9 @@ static bool th_wall_temp(const aeros_lbm* h, int y, float* Tw) {
 
 static int upload_T(aeros_lbm* h, const std::vector<float>& T) {
     CUDA_TRY(cudaMemcpyAsync(h->T, T.data(), T.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(h->L->thermal_fill(h->g, h->qstride, h->ncell, h->T, 0.5f * (h->tp.hot_temp + h->tp.cold_temp), h->stream));
+    StepArgs A;
+    base_args(h, A);
+    CUDA_TRY(h->L->thermal_fill(A, 0.5f * (h->tp.hot_temp + h->tp.cold_temp), h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return AEROS_OK;
 }
@@ -848,6 +905,10 @@ extern "C" int aeros_lbm_thermal_init(aeros_lbm* h, const aeros_thermal_params* 
                 T[c] = t;
             }
     h->th_on = true;
+    build_shell_kinds(h);
+    if (h->n_shell)
+        CUDA_TRY(cudaMemcpy(h->shell_kind, h->shell_kind_host.data(), h->shell_kind_host.size() * 8,
+                            cudaMemcpyHostToDevice));
     h->th_buoy_mode = 1;   // buoyancy field starts at zero (thermal_lbm.cpp:132)
     h->th_stepped = false;
     Control c = *h->ctl_host;

@@ -97,17 +97,30 @@ __global__ void k_reset(void* fp, const uint32_t* desc, long long qstride, int n
     ux[c] = uin0; uy[c] = uin1; uz[c] = uin2;
 }
 
-// D3Q7 populations at rest equilibrium from T (thermal_lbm.cpp:179-183,191-194).
+// D3Q7 populations from a temperature field. The reference's thermal step
+// streams before it collides (thermal_lbm.cpp:199-336), so its freshly set
+// populations g = geq(T, u = 0) (thermal_lbm.cpp:179-183, 191-194) are a
+// post-collision state: they are streamed here once, with the step's own
+// boundary rules, into the slots the next (even) step gathers from.
 template <class S>
-__global__ void k_thermal_fill(void* gp, long long qstride, int ncell, const float* T, float tref) {
+__global__ void k_thermal_prestream(const StepArgs A, float tref) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    typename S::T* g = reinterpret_cast<typename S::T*>(gp);
-    const float t = T[c];
+    if (c >= A.ncell) return;
+    const uint32_t d = A.desc[c];
+    if (d & D_WALL) return;
+    const int x = c % A.nx, r = c / A.nx, y = r % A.ny, z = r / A.ny;
+    typename S::T* g = reinterpret_cast<typename S::T*>(A.g);
 #pragma unroll
     for (int i = 0; i < Q7; ++i) {
-        const float v = w7(i) * t * (1.0f + 4.0f * 0.0f);
-        S::store(g + (long long)i * qstride + c, S::shifted ? v - w7(i) * tref : v);
+        const TLink L = th_resolve(A, x, y, z, c, i, false, d);
+        float v;
+        if (L.bounce == 0) {
+            v = w7(i) * A.T[L.idx] * (1.0f + 4.0f * 0.0f);
+        } else {
+            const float go = w7(opp19(i)) * A.T[c] * (1.0f + 4.0f * 0.0f);
+            v = L.bounce == 2 ? (-go + 2.0f * w7(i) * L.Tw) : go;
+        }
+        S::store(g + (long long)i * A.qstride + c, S::shifted ? v - w7(i) * tref : v);
     }
 }
 
@@ -123,7 +136,7 @@ struct Launchers {
                              float shift_ref, cudaStream_t s);
     cudaError_t (*reset)(void* f, const uint32_t* desc, long long qstride, int ncell, const FillArgs& fa, float* rho,
                          float* ux, float* uy, float* uz, const float* uin, cudaStream_t s);
-    cudaError_t (*thermal_fill)(void* g, long long qstride, int ncell, const float* T, float tref, cudaStream_t s);
+    cudaError_t (*thermal_fill)(const StepArgs& A, float tref, cudaStream_t s);
 };
 
 const Launchers& launchers_fp32();
@@ -174,8 +187,8 @@ const Launchers& launchers_bf16();
         k_reset<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, fa, rho, ux, uy, uz, uin[0], uin[1], uin[2]); \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    cudaError_t thfill_(void* g, long long qs, int n, const float* T, float tref, cudaStream_t s) {                   \
-        k_thermal_fill<STORE><<<(n + 255) / 256, 256, 0, s>>>(g, qs, n, T, tref);                                     \
+    cudaError_t thfill_(const StepArgs& A, float tref, cudaStream_t s) {                                              \
+        k_thermal_prestream<STORE><<<(A.ncell + 255) / 256, 256, 0, s>>>(A, tref);                                    \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
     }                                                                                                                 \

@@ -37,6 +37,7 @@ struct Partial {            // 80 bytes, one per block
 
 struct Control {
     unsigned int blocks_done;
+    unsigned int tile_next;     // dynamic tile scheduler, reset by the finisher
     int halt;               // divergence guard tripped: later steps return at once
     int halt_kind;          // 1: NaN count before streaming, 2: mean density
     int th_valid;           // Nusselt updated at least once
@@ -60,6 +61,8 @@ struct StepArgs {
     void* f;
     const uint32_t* desc;
     const int* shell;
+    const unsigned long long* shell_kind;   // 2 bits per D3Q19 direction (LinkKind),
+                                            // 2 bits per D3Q7 direction from bit 40
     const float* up[3];
     float* uc[3];
     float *rho, *strain, *tke;
@@ -150,6 +153,20 @@ __device__ __forceinline__ Link resolve_src(const StepArgs& A, int x, int y, int
         return {rc, opp19(rq), L_FREESLIP};
     }
     return {cell, q, L_COPYOWN};
+}
+
+// Same resolution with the link kind precomputed on the host: only index
+// arithmetic on the device (no loads of neighbour descriptors).
+__device__ __forceinline__ Link resolve_kind(const StepArgs& A, int x, int y, int z, int cell, int q, int kind) {
+    if (kind == L_BOUNCE || kind == L_COPYOWN) return {cell, q, kind};
+    int s0 = x - cx19(q), s1 = y - cy19(q), s2 = z - cz19(q);
+    if (A.periodic_x) { s0 = s0 < 0 ? s0 + A.nx : (s0 >= A.nx ? s0 - A.nx : s0); }
+    if (A.periodic_z) { s2 = s2 < 0 ? s2 + A.nz : (s2 >= A.nz ? s2 - A.nz : s2); }
+    if (kind == L_REGULAR) return {(s2 * A.ny + s1) * A.nx + s0, opp19(q), L_REGULAR};
+    const bool o0 = (s0 < 0 || s0 >= A.nx), o1 = (s1 < 0 || s1 >= A.ny), o2 = (s2 < 0 || s2 >= A.nz);
+    const int r0 = o0 ? x : s0, r1 = o1 ? y : s1, r2 = o2 ? z : s2;
+    const int rq = dir19_of(o0 ? -cx19(q) : cx19(q), o1 ? -cy19(q) : cy19(q), o2 ? -cz19(q) : cz19(q));
+    return {(r2 * A.ny + r1) * A.nx + r0, opp19(rq), L_FREESLIP};
 }
 
 // ---- collision of one fluid cell, plain form ---------------------------------
@@ -365,7 +382,17 @@ struct TLink {
     float Tw;
 };
 __device__ __forceinline__ TLink th_resolve(const StepArgs& A, int x, int y, int z, int cell, int i, bool interior,
-                                            uint32_t d) {
+                                            uint32_t d, int kind = -1) {
+    if (kind >= 0) {   // shell cell with the kind precomputed: 0 regular, 1 bounce, 2 Dirichlet
+        if (kind == 0) {
+            int sx = x - cx19(i), sz = z - cz19(i);
+            if (sx < 0) sx = A.nx - 1; else if (sx >= A.nx) sx = 0;
+            if (sz < 0) sz = A.nz - 1; else if (sz >= A.nz) sz = 0;
+            return {(sz * A.ny + (y - cy19(i))) * A.nx + sx, 0, 0.0f};
+        }
+        const int sy = y - cy19(i);
+        return {cell, kind, kind == 2 ? (sy <= 0 ? A.th_hot : A.th_cold) : 0.0f};
+    }
     if (interior) {
         if (!((d >> i) & 1u)) return {cell - nb19(A, i), 0, 0.0f};
         float Tw = 0.0f;
@@ -392,7 +419,7 @@ __device__ __forceinline__ TLink th_resolve(const StepArgs& A, int x, int y, int
 // MAT: materialize (write the gathered pre-collision populations, no step).
 template <class S, bool ODD, bool THERMAL, bool MAT>
 __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x, int y, int z, bool interior,
-                                             Acc& acc) {
+                                             unsigned long long skind, Acc& acc) {
     const uint32_t d = A.desc[cell];
     if (d & D_WALL) return;
     constexpr bool SH = S::shifted;
@@ -420,7 +447,7 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
     } else {
 #pragma unroll
         for (int q = 0; q < Q19; ++q) {
-            const Link L = resolve_src(A, x, y, z, cell, q);
+            const Link L = resolve_kind(A, x, y, z, cell, q, (int)((skind >> (2 * q)) & 3ull));
             f[q] = S::load_rw(fplane<S>(A, L.slot) + L.idx);
         }
     }
@@ -492,8 +519,8 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
             } else {
 #pragma unroll
                 for (int j = 0; j < Q19; ++j) {
-                    const Link L = resolve_src(A, x, y, z, cell, opp19(j));
-                    S::store(fplane<S>(A, opp19(j)) + cell, L.kind == L_COPYOWN ? f[opp19(j)] : f[j]);
+                    const bool copyown = ((skind >> (2 * opp19(j))) & 3ull) == L_COPYOWN;
+                    S::store(fplane<S>(A, opp19(j)) + cell, copyown ? f[opp19(j)] : f[j]);
                 }
             }
         } else if (interior) {
@@ -506,7 +533,7 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
         } else {
 #pragma unroll
             for (int j = 0; j < Q19; ++j) {
-                const Link L = resolve_src(A, x, y, z, cell, opp19(j));
+                const Link L = resolve_kind(A, x, y, z, cell, opp19(j), (int)((skind >> (2 * opp19(j))) & 3ull));
                 if (L.kind == L_REGULAR || L.kind == L_FREESLIP) S::store(fplane<S>(A, L.slot) + L.idx, f[j]);
                 else if (L.kind == L_BOUNCE) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
                 else S::store(fplane<S>(A, opp19(j)) + cell, f[opp19(j)]);
@@ -526,7 +553,8 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
         } else {
 #pragma unroll
             for (int i = 0; i < Q7; ++i) {
-                const TLink L = th_resolve(A, x, y, z, cell, i, interior, d);
+                const TLink L = th_resolve(A, x, y, z, cell, i, interior, d,
+                                           interior ? -1 : (int)((skind >> (40 + 2 * i)) & 3ull));
                 if (L.bounce == 0) {
                     g[i] = S::load_rw(gplane<S>(A, opp19(i)) + L.idx) + w7(i) * wshift;
                 } else {
@@ -566,7 +594,8 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
         } else {
 #pragma unroll
             for (int j = 0; j < Q7; ++j) {
-                const TLink L = th_resolve(A, x, y, z, cell, opp19(j), interior, d);
+                const TLink L = th_resolve(A, x, y, z, cell, opp19(j), interior, d,
+                                           interior ? -1 : (int)((skind >> (40 + 2 * opp19(j))) & 3ull));
                 if (L.bounce == 0) {
                     S::store(gplane<S>(A, j) + L.idx, g[j] - w7(j) * wshift);
                 } else {
@@ -653,6 +682,7 @@ __device__ void finish_step(const StepArgs& A) {
     if (threadIdx.x != 0) return;
     Control* c = A.ctl;
     c->blocks_done = 0;
+    c->tile_next = 0;
     c->kexec += 1;
     c->nan = tot.nan;
     if (tot.nan > A.total_div10) {   // diverged before streaming: step not counted
@@ -688,34 +718,50 @@ __device__ void finish_step(const StepArgs& A) {
 }
 
 template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& acc) {
+    const int ntiles_shell = A.ntiles - A.ntiles_interior;
+    if (tile < ntiles_shell) {   // boundary shell first: the costly tiles are spread early
+        const int si = tile * STEP_BLOCK + (int)threadIdx.x;
+        if (si < A.n_shell) {
+            const int cell = A.shell[si];
+            const uint32_t r = A.div_x.div((uint32_t)cell);
+            const int x = cell - (int)r * A.nx;
+            const uint32_t z = A.div_y.div(r);
+            const int y = (int)(r - z * (uint32_t)A.ny);
+            process_cell<S, ODD, THERMAL, MAT>(A, cell, x, y, (int)z, false, A.shell_kind[si], acc);
+        }
+    } else {
+        const int li = (tile - ntiles_shell) * STEP_BLOCK + (int)threadIdx.x;
+        if (li < A.n_interior) {
+            const uint32_t r = A.div_ix.div((uint32_t)li);
+            const int x = li - (int)r * (A.nx - 2) + 1;
+            const uint32_t zq = A.div_iy.div(r);
+            const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
+            const int z = (int)zq + 1;
+            process_cell<S, ODD, THERMAL, MAT>(A, (z * A.ny + y) * A.nx + x, x, y, z, true, 0ull, acc);
+        }
+    }
+}
+
+template <class S, bool ODD, bool THERMAL, bool MAT>
 __global__ void __launch_bounds__(STEP_BLOCK) k_lbm_step(const StepArgs A) {
     if (!MAT && A.ctl->halt) return;   // uniform: every thread reads the same flag
     Acc acc;
     acc.zero();
-    for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
-        const int li = tile * STEP_BLOCK + (int)threadIdx.x;
-        if (tile < A.ntiles_interior) {
-            if (li < A.n_interior) {
-                const uint32_t r = A.div_ix.div((uint32_t)li);
-                const int x = li - (int)r * (A.nx - 2) + 1;
-                const uint32_t zq = A.div_iy.div(r);
-                const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
-                const int z = (int)zq + 1;
-                process_cell<S, ODD, THERMAL, MAT>(A, (z * A.ny + y) * A.nx + x, x, y, z, true, acc);
-            }
-        } else {
-            const int si = li - A.ntiles_interior * STEP_BLOCK;
-            if (si < A.n_shell) {
-                const int cell = A.shell[si];
-                const uint32_t r = A.div_x.div((uint32_t)cell);
-                const int x = cell - (int)r * A.nx;
-                const uint32_t z = A.div_y.div(r);
-                const int y = (int)(r - z * (uint32_t)A.ny);
-                process_cell<S, ODD, THERMAL, MAT>(A, cell, x, y, (int)z, false, acc);
-            }
-        }
+    if (MAT) {
+        for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) process_tile<S, ODD, THERMAL, MAT>(A, tile, acc);
+        return;
     }
-    if (MAT) return;
+    // dynamic tile scheduling: shell tiles cost more than interior tiles
+    __shared__ int s_tile;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ctl->tile_next, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        __syncthreads();
+        if (tile >= A.ntiles) break;
+        process_tile<S, ODD, THERMAL, MAT>(A, tile, acc);
+    }
     block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
     finish_step<STEP_BLOCK>(A);
 }

@@ -131,7 +131,7 @@ def run_gb300(args):
     results = {}
     peak, peak_kind = measured_peak()
     with ClockSampler(local) as clk:
-        for storage in ("fp32", "fp16"):
+        for storage in (("fp32", "fp16") if args.only == "both" else (args.only,)):
             p, _, _ = sphere_case(storage, mask=mask)
             s = solver.Solver(p, mask)
             ms, launches, st = time_steps(s, args.steps, args.warmup)
@@ -143,18 +143,26 @@ def run_gb300(args):
         # end to end through the C ABI with host buffers: create from the host
         # mask (H2D), per step one aeros_lbm_step(1) + the control-volume drag
         # read back (D2H), fields read back to host at the end, destroy.
-        pin = {}
-        e2e_steps = args.steps
+        if args.only != "both" or args.no_e2e:
+            return_early = True
+        else:
+            return_early = False
+        e2e_steps = args.steps if not return_early else 0
         t1 = time.perf_counter()
         p, _, _ = sphere_case("fp16", mask=mask)
         s = solver.Solver(p, mask)
         forces = []
-        for _ in range(e2e_steps):
+        for _ in range(e2e_steps if not return_early else 0):
             s.step(1)
             forces.append(s.cv_force(0.3, 0.3, 0.3))
-        pin = s.fields()
+        if not return_early:
+            s.fields()
         s.close()
         e2e_s = time.perf_counter() - t1
+    if return_early:
+        print(json.dumps({k: {kk: round(vv, 4) if isinstance(vv, float) else vv for kk, vv in v.items()}
+                          for k, v in results.items()}), flush=True)
+        return
     e2e_mlups = cells * e2e_steps / e2e_s / 1e6
     h2d = mask.size  # mask bytes uploaded at create
     d2h = 24 * e2e_steps + 4 * cells * 6 + 160 * e2e_steps
@@ -277,6 +285,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=30)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", default="both", choices=["both", "fp32", "fp16", "bf16"],
+                    help="time one storage form only (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
