@@ -495,6 +495,10 @@ static void base_args(const aeros_lbm* h, StepArgs& A) {
     A.ntiles_interior = (h->n_interior + STEP_BLOCK - 1) / STEP_BLOCK;
     A.n_shell = h->n_shell;
     A.ntiles = A.ntiles_interior + (h->n_shell + STEP_BLOCK - 1) / STEP_BLOCK;
+    {
+        const int nsh = A.ntiles - A.ntiles_interior;
+        A.shell_stride = nsh > 0 ? std::max(1, A.ntiles / nsh) : 1;
+    }
     A.div_ix = FastDiv((uint32_t)(h->nx - 2));
     A.div_iy = FastDiv((uint32_t)(h->ny - 2));
     A.div_x = FastDiv((uint32_t)h->nx);
@@ -524,6 +528,12 @@ static void base_args(const aeros_lbm* h, StepArgs& A) {
     A.freeslip = p.lateral_bc == AEROS_LATERAL_FREESLIP;
     A.outlet_mode = h->outlet_mode;
     A.total_div10 = h->ncell / 10;
+    {
+        // bounded forces keep every intermediate of a clean cell finite
+        float fmax = std::max(std::fabs(p.body_force[0]), std::max(std::fabs(p.body_force[1]), std::fabs(p.body_force[2])));
+        if (h->th_on) fmax += std::fabs(h->glb) * (std::fabs(h->tp.hot_temp - h->tp.cold_temp) + 2.0f);
+        A.fast_ok = std::isfinite(fmax) && fmax <= 1.0f;
+    }
     A.fluid_cells = h->fluid_cells;
     A.conv_threshold = p.convergence_threshold;
     A.th_on = h->th_on;

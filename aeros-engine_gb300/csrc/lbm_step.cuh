@@ -27,6 +27,10 @@
 namespace aeros {
 
 constexpr int STEP_BLOCK = 256;
+#ifndef AEROS_STEP_MIN_BLOCKS
+#define AEROS_STEP_MIN_BLOCKS 3
+#endif
+constexpr int STEP_MIN_BLOCKS = AEROS_STEP_MIN_BLOCKS;   // resident blocks per SM the register budget targets
 
 struct Partial {            // 80 bytes, one per block
     double rho, ke, tke, nu, tsum;
@@ -56,6 +60,7 @@ struct StepArgs {
     int nx, ny, nz, nxny, ncell;
     long long qstride;
     int n_interior, ntiles_interior, n_shell, ntiles;
+    int shell_stride;           // tile sequence position stride of shell tiles
     FastDiv div_ix, div_iy;     // interior decode: (nx-2), (ny-2)
     FastDiv div_x, div_y;       // shell decode: nx, ny
     void* f;
@@ -85,6 +90,7 @@ struct StepArgs {
     int use_trt, use_les;
     int freeslip, outlet_mode;  // outlet_mode: 0 none, 1 convective, 2 zero-gradient
     int apply_overrides, write_obs, write_u;
+    int fast_ok;                // forces bounded: clean states need no non-finite checks
     int total_div10, fluid_cells;
     float conv_threshold;
     int th_on, th_fixed, th_ylo;
@@ -101,14 +107,20 @@ __device__ __forceinline__ float van_driest(int d) {
          : d == 4 ? 0.8646647168f : d == 5 ? 0.9179150014f : 0.0f;
 }
 
+// Per-thread accumulators. A thread sums its own cells (a fixed set: tiles
+// are assigned statically) in FP32 — the density as the deviation rho - 1 —
+// and the block and global sums are FP64 in a fixed order, so the statistics
+// are deterministic.
 struct Acc {
-    double rho, ke, tke, nu, tsum;
-    float maxu;
-    int nan, neg, bad, rout, rnf, ulim, nun;
+    float drho, ke, tke, tsum;
+    double nu;     // Nusselt row sum (few cells per thread), FP64 as the reference
+    float maxu2;   // max |u|^2; the reference's max |u| is its square root
+    int nan, neg, bad, rout, rnf, ulim, nun, cells;
     __device__ void zero() {
-        rho = ke = tke = nu = tsum = 0.0;
-        maxu = 0.0f;
-        nan = neg = bad = rout = rnf = ulim = nun = 0;
+        drho = ke = tke = tsum = 0.0f;
+        nu = 0.0;
+        maxu2 = 0.0f;
+        nan = neg = bad = rout = rnf = ulim = nun = cells = 0;
     }
 };
 
@@ -194,28 +206,113 @@ __device__ __forceinline__ float src19(int q, float ueX, float ueY, float ueZ, f
     return 3.0f * w19(q) * ((cx - ueX + 3.0f * cu * cx) * Fx + (cy - ueY + 3.0f * cu * cy) * Fy + (cz - ueZ + 3.0f * cu * cz) * Fz);
 }
 
+// BGK / TRT relaxation with the Guo source (aeros/src/lbm.cpp:1204-1264).
+// CHECKS: the reference's non-finite replacements; without them the code is
+// the same arithmetic for states where they cannot trigger (finite, in-range
+// populations and bounded forces: every intermediate is finite). FORCE: with
+// the source terms; without a force they add exact zeros and are dropped.
+template <bool SHIFTED, bool CHECKS, bool FORCE>
+__device__ __forceinline__ void relax19(float f[Q19], float rho, float drho, float ueX, float ueY, float ueZ,
+                                        float ueSqr, float invTau, float sMinus, float Fx, float Fy, float Fz) {
+    const float kP = 1.0f - 0.5f * invTau;
+    const float kM = 1.0f - 0.5f * sMinus;
+    {
+        const float feq = SHIFTED ? w19(0) * drho + w19(0) * rho * (0.0f - ueSqr * 1.5f) : eq19(0, rho, 0.0f, ueSqr);
+        float fi = f[0];
+        if (CHECKS && !isfinite(fi)) fi = feq;
+        float fNew = fi - (fi - feq) * invTau;
+        if (FORCE) fNew = fNew + kP * src19(0, ueX, ueY, ueZ, Fx, Fy, Fz);
+        if (CHECKS && !isfinite(fNew)) fNew = feq;
+        f[0] = fNew;
+    }
+#pragma unroll
+    for (int qi = 1; qi < Q19; qi += 2) {
+        const int qo = qi + 1;
+        const float cu = cu19(qi, ueX, ueY, ueZ);
+        float feq, feqO;
+        if (SHIFTED) {
+            const float wr = w19(qi) * rho;
+            feq = w19(qi) * drho + wr * (cu * 3.0f + cu * cu * 4.5f - ueSqr * 1.5f);
+            feqO = w19(qo) * drho + wr * (-cu * 3.0f + cu * cu * 4.5f - ueSqr * 1.5f);
+        } else {
+            feq = eq19(qi, rho, cu, ueSqr);
+            feqO = eq19(qo, rho, -cu, ueSqr);
+        }
+        float fi = f[qi];
+        float fo = f[qo];
+        if (CHECKS) {
+            if (!isfinite(fi)) fi = feq;
+            if (!isfinite(fo)) fo = feqO;
+        }
+        const float fp = 0.5f * (fi + fo), fm = 0.5f * (fi - fo);
+        const float ep = 0.5f * (feq + feqO), em = 0.5f * (feq - feqO);
+        const float fpN = fp - invTau * (fp - ep);
+        const float fmN = fm - sMinus * (fm - em);
+        float newI, newO;
+        if (FORCE) {
+            const float srcI = src19(qi, ueX, ueY, ueZ, Fx, Fy, Fz);
+            const float srcO = src19(qo, ueX, ueY, ueZ, Fx, Fy, Fz);
+            const float srcP = 0.5f * (srcI + srcO);
+            const float srcM = 0.5f * (srcI - srcO);
+            newI = fpN + fmN + kP * srcP + kM * srcM;
+            newO = fpN - fmN + kP * srcP - kM * srcM;
+        } else {
+            newI = fpN + fmN;
+            newO = fpN - fmN;
+        }
+        if (CHECKS) {
+            if (!isfinite(newI)) newI = feq;
+            if (!isfinite(newO)) newO = feqO;
+        }
+        f[qi] = newI;
+        f[qo] = newO;
+    }
+}
+
 // f: pre-collision populations in -> post-collision out (the plain values f_i,
-// or the deviations f_i - w_i when SHIFTED).
+// or the deviations f_i - w_i when SHIFTED). Moments, guards, limiter, inlet
+// override, LES tau, Guo force and TRT rate: aeros/src/lbm.cpp:1061-1299, same
+// expression trees (compiled without contraction the plain form is bitwise
+// the reference's float arithmetic).
 template <bool SHIFTED>
 __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint32_t d, bool isInlet, bool isOutlet,
                                           float strainPre, float buoy, CellResult& o, Acc& acc) {
+    // moments and the range of the populations in one pass
     float rho = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+    float fmn = f[0], fmx = f[0];
 #pragma unroll
     for (int q = 0; q < Q19; ++q) {
-        // shifted form: range checks on w + h, moments from the deviation h
-        float m = f[q];
-        const float fi = SHIFTED ? m + w19(q) : m;
-        if (!isfinite(fi)) { m = SHIFTED ? 0.0f : w19(q); acc.nan++; acc.bad++; }
-        else if (fi < -1.0f || fi > 10.0f) { m = SHIFTED ? 0.0f : w19(q); acc.bad++; }
+        const float m = f[q];
         rho += m;
         if (cx19(q) != 0) ux = cx19(q) > 0 ? ux + m : ux - m;
         if (cy19(q) != 0) uy = cy19(q) > 0 ? uy + m : uy - m;
         if (cz19(q) != 0) uz = cz19(q) > 0 ? uz + m : uz - m;
+        fmn = fminf(fmn, m);
+        fmx = fmaxf(fmx, m);
+    }
+    // A NaN makes the sum non-finite; an infinity or any value outside
+    // [-1, 10] shows in the range. Only then can the reference's per-population
+    // replacement (lbm.cpp:1061-1074) change anything; it is replayed exactly.
+    // Shifted form: bounds on h = f - w that imply f in [-1, 10].
+    const bool clean = isfinite(rho) && fmn >= -1.0f && fmx <= (SHIFTED ? 9.6f : 10.0f);
+    if (!clean) {
+        rho = 0.0f; ux = 0.0f; uy = 0.0f; uz = 0.0f;
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) {
+            float m = f[q];
+            const float fi = SHIFTED ? m + w19(q) : m;
+            if (!isfinite(fi)) { m = SHIFTED ? 0.0f : w19(q); acc.nan++; acc.bad++; }
+            else if (fi < -1.0f || fi > 10.0f) { m = SHIFTED ? 0.0f : w19(q); acc.bad++; }
+            rho += m;
+            if (cx19(q) != 0) ux = cx19(q) > 0 ? ux + m : ux - m;
+            if (cy19(q) != 0) uy = cy19(q) > 0 ? uy + m : uy - m;
+            if (cz19(q) != 0) uz = cz19(q) > 0 ? uz + m : uz - m;
+        }
     }
     if (SHIFTED) rho = 1.0f + rho;
     if (!isfinite(rho)) { acc.rnf++; acc.nan++; rho = 1.0f; }
     else if (rho < 0.5f || rho > 1.5f) { acc.rout++; acc.nan++; rho = 1.0f; }
-    const float invRho = 1.0f / rho;
+    const float invRho = __frcp_rn(rho);   // correctly rounded: equals 1.0f / rho
     ux *= invRho; uy *= invRho; uz *= invRho;
     if (!isfinite(ux)) { ux = 0.0f; uy = 0.0f; uz = 0.0f; acc.nan++; }
     const float usqrTmp = ux * ux + uy * uy + uz * uz;
@@ -247,77 +344,47 @@ __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint3
         ux *= sc; uy *= sc; uz *= sc;
         usqr = ux * ux + uy * uy + uz * uz;
     }
-    const float invTau = 1.0f / tauEff;
+    const float invTau = __frcp_rn(tauEff);
     const float Fx = A.Fx, Fz = A.Fz;
     const float Fy = A.th_on ? A.Fy + buoy : A.Fy;
     const bool hasForce = (Fx != 0.0f || Fy != 0.0f || Fz != 0.0f);
     float ueX = ux, ueY = uy, ueZ = uz, ueSqr = usqr;
+    float halfInvRho = 0.0f;
     if (hasForce) {
-        const float half = 0.5f / rho;
-        ueX += Fx * half; ueY += Fy * half; ueZ += Fz * half;
+        halfInvRho = __frcp_rn(rho) * 0.5f;   // equals 0.5f / rho (power-of-two scaling)
+        ueX += Fx * halfInvRho; ueY += Fy * halfInvRho; ueZ += Fz * halfInvRho;
         ueSqr = ueX * ueX + ueY * ueY + ueZ * ueZ;
     }
     float sMinus = invTau;
     if (A.use_trt) {
         const float m = invTau - 0.5f;
         const float denom = (fabsf(m) > 1e-6f) ? (0.1875f / m + 0.5f) : 1.0f;
-        sMinus = 1.0f / fmaxf(0.05f, denom);
+        sMinus = __frcp_rn(fmaxf(0.05f, denom));
     }
-    const float kP = 1.0f - 0.5f * invTau;
-    const float kM = 1.0f - 0.5f * sMinus;
-    // shifted form: relax deviations; feq - w = w*(rho-1) + w*rho*(...)
     const float drho = rho - 1.0f;
-    // rest population (pair q == opp q)
-    {
-        const float feq = SHIFTED ? w19(0) * drho + w19(0) * rho * (0.0f - ueSqr * 1.5f) : eq19(0, rho, 0.0f, ueSqr);
-        float fi = f[0];
-        if (!isfinite(fi)) fi = feq;
-        const float srcI = hasForce ? src19(0, ueX, ueY, ueZ, Fx, Fy, Fz) : 0.0f;
-        float fNew = fi - (fi - feq) * invTau + kP * srcI;
-        if (!isfinite(fNew)) fNew = feq;
-        if ((SHIFTED ? fNew + w19(0) : fNew) < 0.0f) acc.neg++;
-        f[0] = fNew;
+    if (clean && A.fast_ok) {
+        if (hasForce) relax19<SHIFTED, false, true>(f, rho, drho, ueX, ueY, ueZ, ueSqr, invTau, sMinus, Fx, Fy, Fz);
+        else relax19<SHIFTED, false, false>(f, rho, drho, ueX, ueY, ueZ, ueSqr, invTau, sMinus, Fx, Fy, Fz);
+    } else {
+        if (hasForce) relax19<SHIFTED, true, true>(f, rho, drho, ueX, ueY, ueZ, ueSqr, invTau, sMinus, Fx, Fy, Fz);
+        else relax19<SHIFTED, true, false>(f, rho, drho, ueX, ueY, ueZ, ueSqr, invTau, sMinus, Fx, Fy, Fz);
     }
+    // negative post-collision populations (lbmNegativePops): one minimum per
+    // weight class, exact count only when one is negative
+    {
+        float m0 = f[0], m1 = f[1], m2 = f[7];
 #pragma unroll
-    for (int qi = 1; qi < Q19; qi += 2) {
-        const int qo = qi + 1;
-        const float cu = cu19(qi, ueX, ueY, ueZ);
-        float feq, feqO;
-        if (SHIFTED) {
-            const float wr = w19(qi) * rho;
-            feq = w19(qi) * drho + wr * (cu * 3.0f + cu * cu * 4.5f - ueSqr * 1.5f);
-            feqO = w19(qo) * drho + wr * (-cu * 3.0f + cu * cu * 4.5f - ueSqr * 1.5f);
-        } else {
-            feq = eq19(qi, rho, cu, ueSqr);
-            feqO = eq19(qo, rho, -cu, ueSqr);
+        for (int q = 2; q <= 6; ++q) m1 = fminf(m1, f[q]);
+#pragma unroll
+        for (int q = 8; q < Q19; ++q) m2 = fminf(m2, f[q]);
+        const bool anyneg = SHIFTED ? (m0 < -w19(0) || m1 < -w19(1) || m2 < -w19(7)) : (fminf(m0, fminf(m1, m2)) < 0.0f);
+        if (anyneg || !clean) {
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) acc.neg += ((SHIFTED ? f[q] + w19(q) : f[q]) < 0.0f) ? 1 : 0;
         }
-        float fi = f[qi];
-        if (!isfinite(fi)) fi = feq;
-        float fo = f[qo];
-        if (!isfinite(fo)) fo = feqO;
-        float srcI = 0.0f, srcO = 0.0f;
-        if (hasForce) {
-            srcI = src19(qi, ueX, ueY, ueZ, Fx, Fy, Fz);
-            srcO = src19(qo, ueX, ueY, ueZ, Fx, Fy, Fz);
-        }
-        const float srcP = 0.5f * (srcI + srcO);
-        const float srcM = 0.5f * (srcI - srcO);
-        const float fp = 0.5f * (fi + fo), fm = 0.5f * (fi - fo);
-        const float ep = 0.5f * (feq + feqO), em = 0.5f * (feq - feqO);
-        const float fpN = fp - invTau * (fp - ep);
-        const float fmN = fm - sMinus * (fm - em);
-        float newI = fpN + fmN + kP * srcP + kM * srcM;
-        float newO = fpN - fmN + kP * srcP - kM * srcM;
-        if (!isfinite(newI)) newI = feq;
-        if (!isfinite(newO)) newO = feqO;
-        if ((SHIFTED ? newI + w19(qi) : newI) < 0.0f) acc.neg++;
-        if ((SHIFTED ? newO + w19(qo) : newO) < 0.0f) acc.neg++;
-        f[qi] = newI;
-        f[qo] = newO;
     }
     o.rho = rho;
     if (hasForce) {
-        const float halfInvRho = 0.5f / rho;
         o.ux = ux + Fx * halfInvRho;
         o.uy = uy + Fy * halfInvRho;
         o.uz = uz + Fz * halfInvRho;
@@ -331,11 +398,11 @@ __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint3
     if (tke > 1.0e6f) tke = 1.0e6f;
     o.tke = tke;
     o.usqr = usqr;
-    const float velMag = sqrtf(usqr);
-    if (velMag > acc.maxu) acc.maxu = velMag;
-    acc.rho += (double)rho;
-    acc.ke += (double)usqr;
-    acc.tke += (double)tke;
+    acc.maxu2 = fmaxf(acc.maxu2, usqr);
+    acc.drho += drho;
+    acc.ke += usqr;
+    acc.tke += tke;
+    acc.cells++;
 }
 
 // Two-pass |S| from previous-step velocity (aeros/src/lbm.cpp:1012-1031).
@@ -438,11 +505,16 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
 #pragma unroll
         for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
     } else if (interior) {
+        if ((d & D_LINKS) == 0) {   // no wall next to the cell: plain pull
 #pragma unroll
-        for (int q = 0; q < Q19; ++q) {
-            const bool special = (d >> q) & 1u;
-            const int src = special ? cell : cell - nb19(A, q);
-            f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
+            for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) {
+                const bool special = (d >> q) & 1u;
+                const int src = special ? cell : cell - nb19(A, q);
+                f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
+            }
         }
     } else {
 #pragma unroll
@@ -452,7 +524,7 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
         }
     }
     const bool isInlet = (d & D_INLET) != 0, isOutlet = (d & D_OUTLET) != 0;
-    if (A.apply_overrides && !A.periodic_x) {
+    if (!interior && A.apply_overrides && !A.periodic_x) {
         if (isInlet) {
 #pragma unroll
             for (int q = 0; q < Q19; ++q) f[q] = A.feq_in[q];
@@ -524,11 +596,16 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
                 }
             }
         } else if (interior) {
+            if ((d & D_LINKS) == 0) {
 #pragma unroll
-            for (int j = 0; j < Q19; ++j) {
-                const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
-                if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
-                else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+                for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < Q19; ++j) {
+                    const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
+                    if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+                    else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+                }
             }
         } else {
 #pragma unroll
@@ -585,7 +662,7 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
             g[i] = g[i] - (g[i] - eq) * A.th_invtau;
         }
         A.T[cell] = T;
-        acc.tsum += (double)T;
+        acc.tsum += T;
         if (y == A.th_ylo) { acc.nu += (double)(A.th_hot - T) / 0.5; acc.nun++; }
         // scatter
         if (!ODD) {
@@ -610,35 +687,37 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
     }
 }
 
-// Block reduction of the accumulators into one partial; fixed shape, so the
-// result does not depend on scheduling.
+// Block reduction of the per-thread accumulators into one partial (FP64),
+// fixed shape: the result does not depend on warp scheduling.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
 template <int BLOCK>
-__device__ __forceinline__ void block_reduce_store(Acc& a, Partial* out) {
+__device__ __forceinline__ void block_reduce_store(const Acc& a, Partial* out) {
     __shared__ double sd[5][BLOCK / 32];
     __shared__ float sf[BLOCK / 32];
-    __shared__ int si[7][BLOCK / 32];
+    __shared__ int si[8][BLOCK / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const double d0 = warp_sum((double)a.drho), d1 = warp_sum((double)a.ke), d2 = warp_sum((double)a.tke);
+    const double d3 = warp_sum(a.nu), d4 = warp_sum((double)a.tsum);
+    float mx = a.maxu2;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a.rho += __shfl_down_sync(0xffffffffu, a.rho, o);
-        a.ke += __shfl_down_sync(0xffffffffu, a.ke, o);
-        a.tke += __shfl_down_sync(0xffffffffu, a.tke, o);
-        a.nu += __shfl_down_sync(0xffffffffu, a.nu, o);
-        a.tsum += __shfl_down_sync(0xffffffffu, a.tsum, o);
-        a.maxu = fmaxf(a.maxu, __shfl_down_sync(0xffffffffu, a.maxu, o));
-        a.nan += __shfl_down_sync(0xffffffffu, a.nan, o);
-        a.neg += __shfl_down_sync(0xffffffffu, a.neg, o);
-        a.bad += __shfl_down_sync(0xffffffffu, a.bad, o);
-        a.rout += __shfl_down_sync(0xffffffffu, a.rout, o);
-        a.rnf += __shfl_down_sync(0xffffffffu, a.rnf, o);
-        a.ulim += __shfl_down_sync(0xffffffffu, a.ulim, o);
-        a.nun += __shfl_down_sync(0xffffffffu, a.nun, o);
-    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    const int i0 = warp_sum(a.nan), i1 = warp_sum(a.neg), i2 = warp_sum(a.bad), i3 = warp_sum(a.rout);
+    const int i4 = warp_sum(a.rnf), i5 = warp_sum(a.ulim), i6 = warp_sum(a.nun), i7 = warp_sum(a.cells);
     if (lane == 0) {
-        sd[0][wid] = a.rho; sd[1][wid] = a.ke; sd[2][wid] = a.tke; sd[3][wid] = a.nu; sd[4][wid] = a.tsum;
-        sf[wid] = a.maxu;
-        si[0][wid] = a.nan; si[1][wid] = a.neg; si[2][wid] = a.bad; si[3][wid] = a.rout;
-        si[4][wid] = a.rnf; si[5][wid] = a.ulim; si[6][wid] = a.nun;
+        sd[0][wid] = d0; sd[1][wid] = d1; sd[2][wid] = d2; sd[3][wid] = d3; sd[4][wid] = d4;
+        sf[wid] = mx;
+        si[0][wid] = i0; si[1][wid] = i1; si[2][wid] = i2; si[3][wid] = i3;
+        si[4][wid] = i4; si[5][wid] = i5; si[6][wid] = i6; si[7][wid] = i7;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -646,11 +725,12 @@ __device__ __forceinline__ void block_reduce_store(Acc& a, Partial* out) {
         p.rho = p.ke = p.tke = p.nu = p.tsum = 0.0;
         p.maxu = 0.0f;
         p.nan = p.neg = p.bad = p.rout = p.rnf = p.ulim = p.nun = 0;
+        p.pad[0] = 0;
         for (int w = 0; w < BLOCK / 32; ++w) {
             p.rho += sd[0][w]; p.ke += sd[1][w]; p.tke += sd[2][w]; p.nu += sd[3][w]; p.tsum += sd[4][w];
             p.maxu = fmaxf(p.maxu, sf[w]);
             p.nan += si[0][w]; p.neg += si[1][w]; p.bad += si[2][w]; p.rout += si[3][w];
-            p.rnf += si[4][w]; p.ulim += si[5][w]; p.nun += si[6][w];
+            p.rnf += si[4][w]; p.ulim += si[5][w]; p.nun += si[6][w]; p.pad[0] += si[7][w];
         }
         *out = p;
     }
@@ -666,62 +746,85 @@ __device__ void finish_step(const StepArgs& A) {
     __syncthreads();
     if (!last) return;
     __threadfence();
-    Acc a;
-    a.zero();
+    double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    float m = 0.0f;
+    long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int b = threadIdx.x; b < (int)gridDim.x; b += BLOCK) {
         const volatile Partial* p = A.partials + b;
-        a.rho += p->rho; a.ke += p->ke; a.tke += p->tke; a.nu += p->nu; a.tsum += p->tsum;
-        a.maxu = fmaxf(a.maxu, p->maxu);
-        a.nan += p->nan; a.neg += p->neg; a.bad += p->bad; a.rout += p->rout;
-        a.rnf += p->rnf; a.ulim += p->ulim; a.nun += p->nun;
+        t[0] += p->rho; t[1] += p->ke; t[2] += p->tke; t[3] += p->nu; t[4] += p->tsum;
+        m = fmaxf(m, p->maxu);
+        c[0] += p->nan; c[1] += p->neg; c[2] += p->bad; c[3] += p->rout;
+        c[4] += p->rnf; c[5] += p->ulim; c[6] += p->nun; c[7] += p->pad[0];
     }
-    __syncthreads();
-    __shared__ Partial tot;
-    block_reduce_store<BLOCK>(a, &tot);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int k = 0; k < 5; ++k) t[k] += __shfl_down_sync(0xffffffffu, t[k], o);
+        m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+        for (int k = 0; k < 8; ++k) c[k] += __shfl_down_sync(0xffffffffu, c[k], o);
+    }
+    __shared__ double s_d[5][BLOCK / 32];
+    __shared__ float s_m[BLOCK / 32];
+    __shared__ long long s_i[8][BLOCK / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int k = 0; k < 5; ++k) s_d[k][wid] = t[k];
+        s_m[wid] = m;
+        for (int k = 0; k < 8; ++k) s_i[k][wid] = c[k];
+    }
     __syncthreads();
     if (threadIdx.x != 0) return;
-    Control* c = A.ctl;
-    c->blocks_done = 0;
-    c->tile_next = 0;
-    c->kexec += 1;
-    c->nan = tot.nan;
-    if (tot.nan > A.total_div10) {   // diverged before streaming: step not counted
-        c->halt = 1;
-        c->halt_kind = 1;
+    for (int j = 1; j < BLOCK / 32; ++j) {
+        for (int k = 0; k < 5; ++k) t[k] += s_d[k][j];
+        m = fmaxf(m, s_m[j]);
+        for (int k = 0; k < 8; ++k) c[k] += s_i[k][j];
+    }
+    Control* ctl = A.ctl;
+    ctl->blocks_done = 0;
+    ctl->tile_next = 0;
+    ctl->kexec += 1;
+    ctl->nan = c[0];
+    if (c[0] > A.total_div10) {   // diverged before streaming: step not counted
+        ctl->halt = 1;
+        ctl->halt_kind = 1;
         return;
     }
-    c->steps += 1;
-    c->sum_rho = tot.rho; c->sum_ke = tot.ke; c->sum_tke = tot.tke;
-    const float avg_rho = (float)(tot.rho / A.fluid_cells);
-    const float avg_ke = (float)(tot.ke / A.fluid_cells);
-    c->avg_rho = avg_rho;
-    c->avg_ke = avg_ke;
-    c->avg_tke = (float)(tot.tke / A.fluid_cells);
-    c->max_u = tot.maxu;
-    c->neg = tot.neg; c->bad = tot.bad; c->rout = tot.rout; c->rnf = tot.rnf; c->ulim = tot.ulim;
-    c->convergence = fabsf(avg_ke - c->prev_kinetic);
-    c->prev_kinetic = avg_ke;
-    c->converged = c->convergence < A.conv_threshold;
+    ctl->steps += 1;
+    const double sum_rho = (double)c[7] + t[0];   // cells + sum of (rho - 1)
+    ctl->sum_rho = sum_rho; ctl->sum_ke = t[1]; ctl->sum_tke = t[2];
+    const float avg_rho = (float)(sum_rho / A.fluid_cells);
+    const float avg_ke = (float)(t[1] / A.fluid_cells);
+    ctl->avg_rho = avg_rho;
+    ctl->avg_ke = avg_ke;
+    ctl->avg_tke = (float)(t[2] / A.fluid_cells);
+    ctl->max_u = sqrtf(m);
+    ctl->neg = c[1]; ctl->bad = c[2]; ctl->rout = c[3]; ctl->rnf = c[4]; ctl->ulim = c[5];
+    ctl->convergence = fabsf(avg_ke - ctl->prev_kinetic);
+    ctl->prev_kinetic = avg_ke;
+    ctl->converged = ctl->convergence < A.conv_threshold;
     if (A.th_on) {
-        if (tot.nun > 0) {
+        if (c[6] > 0) {
             float dT = fabsf(A.th_hot - A.th_cold);
             if (dT < 1e-6f) dT = 1e-6f;
-            c->nusselt = (float)(tot.nu / (double)tot.nun) * A.th_H / dT;
-            c->th_valid = 1;
+            ctl->nusselt = (float)(t[3] / (double)c[6]) * A.th_H / dT;
+            ctl->th_valid = 1;
         }
-        c->mean_t = A.th_rows_n > 0.0 ? (float)(tot.tsum / A.th_rows_n) : 0.5f;
+        ctl->mean_t = A.th_rows_n > 0.0 ? (float)(t[4] / A.th_rows_n) : 0.5f;
     }
     if (!isfinite(avg_rho) || avg_rho > 1.2f || avg_rho < 0.8f) {
-        c->halt = 1;
-        c->halt_kind = 2;
+        ctl->halt = 1;
+        ctl->halt_kind = 2;
     }
 }
 
 template <class S, bool ODD, bool THERMAL, bool MAT>
 __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& acc) {
-    const int ntiles_shell = A.ntiles - A.ntiles_interior;
-    if (tile < ntiles_shell) {   // boundary shell first: the costly tiles are spread early
-        const int si = tile * STEP_BLOCK + (int)threadIdx.x;
+    // Shell tiles (costlier: per-link index arithmetic) are spread evenly
+    // through the tile sequence: tile t is shell tile t / k when t % k == 0.
+    const int nsh = A.ntiles - A.ntiles_interior;
+    const int k = A.shell_stride;
+    const bool is_shell = nsh > 0 && (tile % k) == 0 && tile / k < nsh;
+    if (is_shell) {
+        const int si = (tile / k) * STEP_BLOCK + (int)threadIdx.x;
         if (si < A.n_shell) {
             const int cell = A.shell[si];
             const uint32_t r = A.div_x.div((uint32_t)cell);
@@ -731,7 +834,8 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& a
             process_cell<S, ODD, THERMAL, MAT>(A, cell, x, y, (int)z, false, A.shell_kind[si], acc);
         }
     } else {
-        const int li = (tile - ntiles_shell) * STEP_BLOCK + (int)threadIdx.x;
+        const int before = min(nsh, tile / k + 1);   // shell tiles in [0, tile]
+        const int li = (tile - before) * STEP_BLOCK + (int)threadIdx.x;
         if (li < A.n_interior) {
             const uint32_t r = A.div_ix.div((uint32_t)li);
             const int x = li - (int)r * (A.nx - 2) + 1;
@@ -743,25 +847,15 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& a
     }
 }
 
+// One lattice step. Tiles of STEP_BLOCK cells are assigned round-robin to a
+// persistent grid (a fixed assignment, so the statistics are deterministic).
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__global__ void __launch_bounds__(STEP_BLOCK) k_lbm_step(const StepArgs A) {
+__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_step(const StepArgs A) {
     if (!MAT && A.ctl->halt) return;   // uniform: every thread reads the same flag
     Acc acc;
     acc.zero();
-    if (MAT) {
-        for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) process_tile<S, ODD, THERMAL, MAT>(A, tile, acc);
-        return;
-    }
-    // dynamic tile scheduling: shell tiles cost more than interior tiles
-    __shared__ int s_tile;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ctl->tile_next, 1u);
-        __syncthreads();
-        const int tile = s_tile;
-        __syncthreads();
-        if (tile >= A.ntiles) break;
-        process_tile<S, ODD, THERMAL, MAT>(A, tile, acc);
-    }
+    for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) process_tile<S, ODD, THERMAL, MAT>(A, tile, acc);
+    if (MAT) return;
     block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
     finish_step<STEP_BLOCK>(A);
 }
