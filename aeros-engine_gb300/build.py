@@ -28,8 +28,9 @@ UNITS = {
     "forces.cu": ["--fmad=false"],
     "voxel.cu": ["--fmad=false"],
     "capi.cu": ["--fmad=false"],
+    "setup.cu": [],
 }
-HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh"]
+HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh", "setup.cuh"]
 
 
 def nvcc() -> str:

@@ -19,6 +19,7 @@
 #include "../../include/aeros_lbm.h"
 #include "forces.cuh"
 #include "lbm_aux.cuh"
+#include "setup.cuh"
 
 using namespace aeros;
 
@@ -161,9 +162,9 @@ static void free_handle(aeros_lbm* h) {
 
 static inline int cidx(const aeros_lbm* h, int x, int y, int z) { return (z * h->ny + y) * h->nx + x; }
 
-// Per-cell descriptor: links, wall distance (chamfer, lbm.cpp:647-675), LES
-// eligibility (lbm.cpp:994-1011), inlet/outlet planes, outlet side buffer slot.
-static void build_descriptor(aeros_lbm* h, std::vector<uint32_t>& desc, std::vector<int>& shell) {
+// Full-range wall distance (the reference's two-pass chamfer, lbm.cpp:647-675),
+// built on the host only when a caller reads it back.
+static void host_wall_distance(aeros_lbm* h) {
     const int nx = h->nx, ny = h->ny, nz = h->nz, n = h->ncell;
     const auto& m = h->mask;
     auto& wd = h->wall;
@@ -194,54 +195,27 @@ static void build_descriptor(aeros_lbm* h, std::vector<uint32_t>& desc, std::vec
                 wd[row + x] = (uint8_t)v;
             }
         }
-    const int ax = h->p.flow_axis, sg = h->p.flow_sign;
-    const int na = ax == 0 ? nx : (ax == 1 ? ny : nz);
-    const int oc = sg > 0 ? na - 1 : 0, ic = sg > 0 ? na - 2 : 1, ic2 = sg > 0 ? na - 3 : 2;
-    const int ip = sg > 0 ? 0 : na - 1;
-    desc.assign(n, 0);
+}
+
+// Shell cells (any coordinate on the domain boundary) in increasing cell
+// order, fluid-cell count (sFluidCells, lbm.cpp:677-680).
+static void host_geometry(aeros_lbm* h, std::vector<int>& shell) {
+    const int nx = h->nx, ny = h->ny, nz = h->nz;
     shell.clear();
-    h->fluid_cells = 0;
+    shell.reserve((size_t)2 * (nx * ny + ny * nz + nx * nz));
     for (int z = 0; z < nz; ++z)
-        for (int y = 0; y < ny; ++y)
-            for (int x = 0; x < nx; ++x) {
-                const int c = cidx(h, x, y, z);
-                uint32_t d = 0;
-                const bool wall = m[c] != AEROS_CELL_FLUID;
-                if (wall) d |= D_WALL;
-                else ++h->fluid_cells;
-                if (m[c] == AEROS_CELL_GROUND) d |= D_GROUND;
-                const bool on_shell = x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
-                if (on_shell) {
-                    d |= D_SHELL;
-                    shell.push_back(c);
-                }
-                for (int q = 1; q < Q19; ++q) {
-                    const int sx = x - cx19(q), sy = y - cy19(q), sz = z - cz19(q);
-                    const bool in = sx >= 0 && sx < nx && sy >= 0 && sy < ny && sz >= 0 && sz < nz;
-                    if (!in || m[cidx(h, sx, sy, sz)] != AEROS_CELL_FLUID) d |= 1u << q;
-                }
-                d |= (uint32_t)std::min<int>(wd[c], 6) << D_WD_SHIFT;
-                const int pos[3] = {x, y, z};
-                const bool inl = pos[ax] == ip, outl = pos[ax] == oc;
-                if (inl) d |= D_INLET;
-                if (outl) d |= D_OUTLET;
-                if (!wall && !inl && !outl && !on_shell) {
-                    const int nbs[6] = {c - 1, c + 1, c - nx, c + nx, c - nx * ny, c + nx * ny};
-                    bool ok = true;
-                    for (int k = 0; k < 6; ++k)
-                        if (m[nbs[k]] == AEROS_CELL_SOLID) ok = false;
-                    if (ok) d |= D_LES;
-                }
-                if (h->outlet_mode && !wall) {
-                    int slot = 0;
-                    if (pos[ax] == oc) slot = 1;
-                    else if (pos[ax] == ic) slot = 2;
-                    else if (pos[ax] == ic2) slot = 3;
-                    d |= (uint32_t)slot << D_OUT_SHIFT;
-                }
-                desc[c] = d;
+        for (int y = 0; y < ny; ++y) {
+            const int row = (z * ny + y) * nx;
+            if (z == 0 || z == nz - 1 || y == 0 || y == ny - 1) {
+                for (int x = 0; x < nx; ++x) shell.push_back(row + x);
+            } else {
+                shell.push_back(row);
+                shell.push_back(row + nx - 1);
             }
-    if (h->fluid_cells < 1) h->fluid_cells = 1;
+        }
+    long long fluid = 0;
+    for (uint8_t v : h->mask) fluid += v == 0;
+    h->fluid_cells = (int)std::max<long long>(1, fluid);
     h->n_shell = (int)shell.size();
     h->n_interior = (nx - 2) * (ny - 2) * (nz - 2);
 }
@@ -356,9 +330,8 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
 
-    std::vector<uint32_t> desc;
     std::vector<int> shell;
-    build_descriptor(h, desc, shell);
+    host_geometry(h, shell);
     int rc = AEROS_OK;
     const size_t n = (size_t)h->ncell;
 #define ALLOC(ptr, bytes)                        \
@@ -400,7 +373,25 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     cudaError_t e;
     if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return fail(e, "cudaEventCreate");
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return fail(e, "cudaEventCreate");
-    if ((e = cudaMemcpy(h->desc, desc.data(), n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "desc upload");
+    {
+        uint8_t* dm = nullptr;
+        if ((e = cudaMalloc((void**)&dm, 3 * n)) != cudaSuccess) return fail(e, "descriptor scratch");
+        DescArgs da;
+        da.nx = h->nx; da.ny = h->ny; da.nz = h->nz;
+        da.flow_axis = params->flow_axis;
+        const int na = params->flow_axis == 0 ? h->nx : (params->flow_axis == 1 ? h->ny : h->nz);
+        const bool pos = params->flow_sign > 0;
+        da.inlet_pos = pos ? 0 : na - 1;
+        da.outlet_pos = pos ? na - 1 : 0;
+        da.ic = pos ? na - 2 : 1;
+        da.ic2 = pos ? na - 3 : 2;
+        da.outlet_mode = h->outlet_mode;
+        e = cudaMemcpy(dm, h->mask.data(), n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = build_descriptors(da, dm, dm + n, dm + 2 * n, h->desc, nullptr);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        cudaFree(dm);
+        if (e != cudaSuccess) return fail(e, "descriptor build");
+    }
     if (h->n_shell && (e = cudaMemcpy(h->shell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(e, "shell upload");
     h->shell_host = shell;
@@ -828,7 +819,10 @@ extern "C" int aeros_lbm_set_equilibrium(aeros_lbm* h, const float* rho, const f
 extern "C" int aeros_lbm_read_mask(aeros_lbm* h, uint8_t* mask, uint8_t* wall_dist) {
     if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
     if (mask) memcpy(mask, h->mask.data(), h->mask.size());
-    if (wall_dist) memcpy(wall_dist, h->wall.data(), h->wall.size());
+    if (wall_dist) {
+        if (h->wall.size() != h->mask.size()) host_wall_distance(h);
+        memcpy(wall_dist, h->wall.data(), h->wall.size());
+    }
     return AEROS_OK;
 }
 
