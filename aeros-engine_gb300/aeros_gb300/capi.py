@@ -127,7 +127,7 @@ _SIGS = {
     "aeros_lbm_step_async": (C.c_int, [_P, C.c_int]),
     "aeros_lbm_get_stats": (C.c_int, [_P, C.POINTER(LbmStats)]),
     "aeros_lbm_read_fields": (C.c_int, [_P, _FP, _FP, _FP, _FP, _FP, _FP]),
-    "aeros_lbm_device_fields": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "aeros_lbm_device_fields": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "aeros_lbm_read_populations": (C.c_int, [_P, _FP]),
     "aeros_lbm_write_populations": (C.c_int, [_P, _FP]),
     "aeros_lbm_set_equilibrium": (C.c_int, [_P, _FP, _FP, _FP, _FP]),

@@ -98,9 +98,10 @@ class Solver:
         return out
 
     def device_fields(self) -> dict:
-        ptrs = [C.c_void_p() for _ in range(4)]
+        """Device addresses: rho (float32 per cell) and u4 ((ux, uy, uz, 0) per cell)."""
+        ptrs = [C.c_void_p() for _ in range(2)]
         check(lib().aeros_lbm_device_fields(self.h, *(C.byref(p) for p in ptrs)), "device_fields")
-        return dict(zip(("rho", "ux", "uy", "uz"), (p.value for p in ptrs)))
+        return dict(zip(("rho", "u4"), (p.value for p in ptrs)))
 
     def populations(self) -> np.ndarray:
         f = np.empty((19, self.n), np.float32)

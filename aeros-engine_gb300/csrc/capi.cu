@@ -74,7 +74,7 @@ struct aeros_lbm {
     unsigned long long* shell_kind = nullptr;
     std::vector<int> shell_host;
     std::vector<unsigned long long> shell_kind_host;
-    float* u[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    float4* u[2] = {nullptr, nullptr};   // velocity (ux, uy, uz, 0), double buffered
     float *rho = nullptr, *strain = nullptr, *tke = nullptr;
     float* out[2] = {nullptr, nullptr};
     int out_plane = 0;
@@ -138,8 +138,8 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->desc);
     cudaFree(h->shell);
     cudaFree(h->shell_kind);
-    for (auto& b : h->u)
-        for (auto& c : b) cudaFree(c);
+    cudaFree(h->u[0]);
+    cudaFree(h->u[1]);
     cudaFree(h->rho);
     cudaFree(h->strain);
     cudaFree(h->tke);
@@ -343,8 +343,8 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     ALLOC(h->desc, n * 4);
     ALLOC(h->shell, (size_t)std::max(1, h->n_shell) * 4);
     ALLOC(h->shell_kind, (size_t)std::max(1, h->n_shell) * 8);
-    for (auto& b : h->u)
-        for (auto& c : b) ALLOC(c, n * 4);
+    ALLOC(h->u[0], n * 16);
+    ALLOC(h->u[1], n * 16);
     ALLOC(h->rho, n * 4);
     ALLOC(h->strain, n * 4);
     ALLOC(h->tke, n * 4);
@@ -400,8 +400,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
                                       cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(e, "shell kinds upload");
     for (auto& b : h->u)
-        for (auto& c : b)
-            if ((e = cudaMemset(c, 0, n * 4)) != cudaSuccess) return fail(e, "u memset");
+        if ((e = cudaMemset(b, 0, n * 16)) != cudaSuccess) return fail(e, "u memset");
     if ((e = cudaMemset(h->strain, 0, n * 4)) != cudaSuccess) return fail(e, "memset");
     if ((e = cudaMemset(h->force_counter, 0, 4)) != cudaSuccess) return fail(e, "memset");
     if ((e = cudaMemset(h->tke, 0, n * 4)) != cudaSuccess) return fail(e, "memset");
@@ -554,7 +553,7 @@ static int launch_materialize(aeros_lbm* h, float* d_f, float* d_g) {
     A.apply_overrides = h->overrides_next;
     A.out_r = h->out[h->out_par ^ 1];
     A.out_w = h->out[h->out_par];
-    A.up[0] = A.up[1] = A.up[2] = h->u[h->ubuf][0];
+    A.up = h->u[h->ubuf];
     const int grid = h->grid[h->next_odd][h->th_on];
     CUDA_TRY(h->L->step(A, h->next_odd, h->th_on, true, grid, h->stream));
     return AEROS_OK;
@@ -598,10 +597,8 @@ static int enqueue_steps(aeros_lbm* h, int nsteps) {
         A.apply_overrides = h->overrides_next;
         A.out_w = h->out[h->out_par];
         A.out_r = h->out[h->out_par ^ 1];
-        for (int k = 0; k < 3; ++k) {
-            A.up[k] = h->u[h->ubuf][k];
-            A.uc[k] = h->u[h->ubuf ^ 1][k];
-        }
+        A.up = h->u[h->ubuf];
+        A.uc = h->u[h->ubuf ^ 1];
         A.write_obs = (i == nsteps - 1);
         A.write_u = h->p.use_les || A.write_obs;
         A.th_buoy_mode = h->th_buoy_mode;
@@ -647,8 +644,7 @@ static int finish_batch(aeros_lbm* h) {
                                                                 h->p.u_in[0] * h->p.u_in[0] + h->p.u_in[1] * h->p.u_in[1] +
                                                                     h->p.u_in[2] * h->p.u_in[2]);
         const float* uin = h->p.u_in;
-        CUDA_TRY(h->L->reset(h->f, h->desc, h->qstride, h->ncell, fa, h->rho, h->u[h->ubuf][0], h->u[h->ubuf][1],
-                             h->u[h->ubuf][2], uin, h->stream));
+        CUDA_TRY(h->L->reset(h->f, h->desc, h->qstride, h->ncell, fa, h->rho, h->u[h->ubuf], uin, h->stream));
         h->next_odd = false;
         h->overrides_next = false;
         const float usqr = uin[0] * uin[0] + uin[1] * uin[1] + uin[2] * uin[2];
@@ -730,25 +726,30 @@ extern "C" int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float*
                                      float* tke) {
     if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
     if (int rc = finish_batch(h)) return rc;
-    const size_t b = (size_t)h->ncell * 4;
+    const size_t n = (size_t)h->ncell;
+    const size_t b = n * 4;
     if (rho) CUDA_TRY(cudaMemcpyAsync(rho, h->rho, b, cudaMemcpyDeviceToHost, h->stream));
-    if (ux) CUDA_TRY(cudaMemcpyAsync(ux, h->u[h->ubuf][0], b, cudaMemcpyDeviceToHost, h->stream));
-    if (uy) CUDA_TRY(cudaMemcpyAsync(uy, h->u[h->ubuf][1], b, cudaMemcpyDeviceToHost, h->stream));
-    if (uz) CUDA_TRY(cudaMemcpyAsync(uz, h->u[h->ubuf][2], b, cudaMemcpyDeviceToHost, h->stream));
     if (strain) CUDA_TRY(cudaMemcpyAsync(strain, h->strain, b, cudaMemcpyDeviceToHost, h->stream));
     if (tke) CUDA_TRY(cudaMemcpyAsync(tke, h->tke, b, cudaMemcpyDeviceToHost, h->stream));
+    if (ux || uy || uz) {
+        std::vector<float4> u(n);
+        CUDA_TRY(cudaMemcpyAsync(u.data(), h->u[h->ubuf], n * 16, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        for (size_t c = 0; c < n; ++c) {
+            if (ux) ux[c] = u[c].x;
+            if (uy) uy[c] = u[c].y;
+            if (uz) uz[c] = u[c].z;
+        }
+    }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return AEROS_OK;
 }
 
-extern "C" int aeros_lbm_device_fields(aeros_lbm* h, const float** rho, const float** ux, const float** uy,
-                                       const float** uz) {
+extern "C" int aeros_lbm_device_fields(aeros_lbm* h, const float** rho, const float** u4) {
     if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
     if (int rc = finish_batch(h)) return rc;
     if (rho) *rho = h->rho;
-    if (ux) *ux = h->u[h->ubuf][0];
-    if (uy) *uy = h->u[h->ubuf][1];
-    if (uz) *uz = h->u[h->ubuf][2];
+    if (u4) *u4 = reinterpret_cast<const float*>(h->u[h->ubuf]);
     return AEROS_OK;
 }
 
@@ -996,7 +997,7 @@ extern "C" int aeros_lbm_cv_force_box(aeros_lbm* h, const int32_t box[6], double
     a.nx = h->nx; a.ny = h->ny; a.nz = h->nz;
     a.desc = h->desc;
     a.rho = h->rho;
-    a.ux = h->u[h->ubuf][0]; a.uy = h->u[h->ubuf][1]; a.uz = h->u[h->ubuf][2];
+    a.u = h->u[h->ubuf];
     for (int k = 0; k < 6; ++k) a.box[k] = box[k];
     a.partials = h->force_partials;
     a.out = h->force_out;

@@ -52,7 +52,8 @@ __global__ void __launch_bounds__(FORCE_BLOCK) k_cv_force(const ForceArgs a) {
         const uint32_t d = a.desc[c];
         if ((d & D_WALL) && !(d & D_GROUND)) continue;   // body cells are skipped, ground is not
         const float rho = a.rho[c];
-        const float ux = a.ux[c], uy = a.uy[c], uz = a.uz[c];
+        const float4 uv = a.u[c];
+        const float ux = uv.x, uy = uv.y, uz = uv.z;
         const float p = (1.0f / 3.0f) * (rho - 1.0f);
         const float un = ux * nx + uy * ny + uz * nz;
         fx += (double)(p * nx + rho * ux * un);

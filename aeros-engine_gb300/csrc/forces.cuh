@@ -10,7 +10,8 @@ namespace aeros {
 struct ForceArgs {
     int nx, ny, nz;
     const uint32_t* desc;
-    const float *rho, *ux, *uy, *uz;
+    const float* rho;
+    const float4* u;          // (ux, uy, uz, 0) per cell
     int box[6];              // x0 x1 y0 y1 z0 z1, inclusive
     double* partials;        // 3 per block
     double* out;             // 3 sums (not negated)

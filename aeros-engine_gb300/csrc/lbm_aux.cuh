@@ -86,15 +86,15 @@ __global__ void k_write_pre(void* fp, const uint32_t* desc, long long qstride, i
 // Re-equilibration after divergence (aeros/src/lbm.cpp:1583-1600): fluid cells
 // get f = feq(1, u_in), rho = 1, u = u_in.
 template <class S>
-__global__ void k_reset(void* fp, const uint32_t* desc, long long qstride, int ncell, FillArgs fa, float* rho, float* ux,
-                        float* uy, float* uz, float uin0, float uin1, float uin2) {
+__global__ void k_reset(void* fp, const uint32_t* desc, long long qstride, int ncell, FillArgs fa, float* rho, float4* u,
+                        float uin0, float uin1, float uin2) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell || (desc[c] & D_WALL)) return;
     typename S::T* f = reinterpret_cast<typename S::T*>(fp);
 #pragma unroll
     for (int q = 0; q < Q19; ++q) S::store(f + (long long)q * qstride + c, S::shifted ? fa.fluid[q] - w19(q) : fa.fluid[q]);
     rho[c] = 1.0f;
-    ux[c] = uin0; uy[c] = uin1; uz[c] = uin2;
+    u[c] = make_float4(uin0, uin1, uin2, 0.0f);
 }
 
 // D3Q7 populations from a temperature field. The reference's thermal step
@@ -135,7 +135,7 @@ struct Launchers {
     cudaError_t (*write_pre)(void* f, const uint32_t* desc, long long qstride, int ncell, const float* src, int nq,
                              float shift_ref, cudaStream_t s);
     cudaError_t (*reset)(void* f, const uint32_t* desc, long long qstride, int ncell, const FillArgs& fa, float* rho,
-                         float* ux, float* uy, float* uz, const float* uin, cudaStream_t s);
+                         float4* u, const float* uin, cudaStream_t s);
     cudaError_t (*thermal_fill)(const StepArgs& A, float tref, cudaStream_t s);
 };
 
@@ -182,9 +182,9 @@ const Launchers& launchers_bf16();
         k_write_pre<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, src, nq, sr);                              \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    cudaError_t reset_(void* f, const uint32_t* desc, long long qs, int n, const FillArgs& fa, float* rho, float* ux, \
-                       float* uy, float* uz, const float* uin, cudaStream_t s) {                                      \
-        k_reset<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, fa, rho, ux, uy, uz, uin[0], uin[1], uin[2]); \
+    cudaError_t reset_(void* f, const uint32_t* desc, long long qs, int n, const FillArgs& fa, float* rho, float4* u,  \
+                       const float* uin, cudaStream_t s) {                                                            \
+        k_reset<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, fa, rho, u, uin[0], uin[1], uin[2]);           \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
     cudaError_t thfill_(const StepArgs& A, float tref, cudaStream_t s) {                                              \

@@ -68,8 +68,8 @@ struct StepArgs {
     const int* shell;
     const unsigned long long* shell_kind;   // 2 bits per D3Q19 direction (LinkKind),
                                             // 2 bits per D3Q7 direction from bit 40
-    const float* up[3];
-    float* uc[3];
+    const float4* up;           // previous-step velocity (ux, uy, uz, 0) per cell
+    float4* uc;                 // this step's velocity
     float *rho, *strain, *tke;
     float* out_w;
     const float* out_r;
@@ -434,19 +434,18 @@ __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint3
 
 // Two-pass |S| from previous-step velocity (aeros/src/lbm.cpp:1012-1031).
 __device__ __forceinline__ float strain_prev(const StepArgs& A, int c) {
-    const float* ux = A.up[0];
-    const float* uy = A.up[1];
-    const float* uz = A.up[2];
-    const int xm = c - 1, xp = c + 1, ym = c - A.nx, yp = c + A.nx, zm = c - A.nxny, zp = c + A.nxny;
-    const float dux_dx = (ux[xp] - ux[xm]) * 0.5f;
-    const float duy_dy = (uy[yp] - uy[ym]) * 0.5f;
-    const float duz_dz = (uz[zp] - uz[zm]) * 0.5f;
-    const float dux_dy = (ux[yp] - ux[ym]) * 0.5f;
-    const float dux_dz = (ux[zp] - ux[zm]) * 0.5f;
-    const float duy_dx = (uy[xp] - uy[xm]) * 0.5f;
-    const float duy_dz = (uy[zp] - uy[zm]) * 0.5f;
-    const float duz_dx = (uz[xp] - uz[xm]) * 0.5f;
-    const float duz_dy = (uz[yp] - uz[ym]) * 0.5f;
+    const float4 xm = __ldg(A.up + c - 1), xp = __ldg(A.up + c + 1);
+    const float4 ym = __ldg(A.up + c - A.nx), yp = __ldg(A.up + c + A.nx);
+    const float4 zm = __ldg(A.up + c - A.nxny), zp = __ldg(A.up + c + A.nxny);
+    const float dux_dx = (xp.x - xm.x) * 0.5f;
+    const float duy_dy = (yp.y - ym.y) * 0.5f;
+    const float duz_dz = (zp.z - zm.z) * 0.5f;
+    const float dux_dy = (yp.x - ym.x) * 0.5f;
+    const float dux_dz = (zp.x - zm.x) * 0.5f;
+    const float duy_dx = (xp.y - xm.y) * 0.5f;
+    const float duy_dz = (zp.y - zm.y) * 0.5f;
+    const float duz_dx = (xp.z - xm.z) * 0.5f;
+    const float duz_dy = (yp.z - ym.z) * 0.5f;
     const float Sxx = dux_dx, Syy = duy_dy, Szz = duz_dz;
     const float Sxy = 0.5f * (dux_dy + duy_dx);
     const float Sxz = 0.5f * (dux_dz + duz_dx);
@@ -511,13 +510,79 @@ __device__ __forceinline__ TLink th_resolve(const StepArgs& A, int x, int y, int
 
 // ---- the step ------------------------------------------------------------------
 // MAT: materialize (write the gathered pre-collision populations, no step).
+// ---- thermal sub-step (D3Q7), aeros/src/thermal_lbm.cpp:199-336 ----------------
+// Gather (stream, with Dirichlet / adiabatic walls), BGK with this cell's new
+// velocity, scatter. INTERIOR: links from the descriptor, unrolled;
+// otherwise the shell's precomputed kinds, rolled loops.
+template <class S, bool ODD, bool MAT, bool INTERIOR>
+__device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int x, int y, int z, uint32_t d,
+                                                unsigned long long skind, const CellResult& r, Acc& acc) {
+    constexpr bool SH = S::shifted;
+    const float wshift = SH ? A.th_tref : 0.0f;   // stored value = g - w*Tref
+    float g[Q7];
+#pragma unroll
+    for (int i = 0; i < Q7; ++i) {
+        if (!ODD) {
+            g[i] = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;
+        } else {
+            const TLink L = th_resolve(A, x, y, z, cell, i, INTERIOR, d,
+                                       INTERIOR ? -1 : (int)((skind >> (40 + 2 * i)) & 3ull));
+            if (L.bounce == 0) {
+                g[i] = S::load_rw(gplane<S>(A, opp19(i)) + L.idx) + w7(i) * wshift;
+            } else {
+                const float v = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;   // post_{opp i}
+                g[i] = L.bounce == 2 ? (-v + 2.0f * w7(i) * L.Tw) : v;
+            }
+        }
+    }
+    if (MAT) {
+#pragma unroll
+        for (int i = 0; i < Q7; ++i) A.mat_g[(long long)i * A.ncell + cell] = g[i];
+        return;
+    }
+    float T = 0.0f;
+#pragma unroll
+    for (int i = 0; i < Q7; ++i) T += g[i];
+    if (!isfinite(T)) T = A.th_tref;
+    {
+        const float lo = A.th_cold - 1.0f, hi = A.th_hot + 1.0f;
+        const float m = (lo < T) ? T : lo;
+        T = (m < hi) ? m : hi;
+    }
+    const float v[3] = {r.ux, r.uy, r.uz};
+#pragma unroll
+    for (int i = 0; i < Q7; ++i) {
+        const float cu = i == 0 ? 0.0f : ((i & 1) ? v[(i - 1) >> 1] : -v[(i - 1) >> 1]);
+        const float eq = w7(i) * T * (1.0f + 4.0f * cu);
+        g[i] = g[i] - (g[i] - eq) * A.th_invtau;
+    }
+    A.T[cell] = T;
+    acc.tsum += T;
+    if (y == A.th_ylo) { acc.nu += (double)(A.th_hot - T) / 0.5; acc.nun++; }
+#pragma unroll
+    for (int j = 0; j < Q7; ++j) {
+        if (!ODD) {
+            S::store(gplane<S>(A, opp19(j)) + cell, g[j] - w7(j) * wshift);
+        } else {
+            const TLink L = th_resolve(A, x, y, z, cell, opp19(j), INTERIOR, d,
+                                       INTERIOR ? -1 : (int)((skind >> (40 + 2 * opp19(j))) & 3ull));
+            if (L.bounce == 0) {
+                S::store(gplane<S>(A, j) + L.idx, g[j] - w7(j) * wshift);
+            } else {
+                // becomes pre-collision population opp j of this cell
+                const float val = L.bounce == 2 ? (-g[j] + 2.0f * w7(j) * L.Tw) : g[j];
+                S::store(gplane<S>(A, opp19(j)) + cell, val - w7(j) * wshift);
+            }
+        }
+    }
+}
+
+// ---- interior cell (1 <= x,y,z <= N-2): flat neighbour offsets ---------------
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x, int y, int z, bool interior,
-                                             unsigned long long skind, Acc& acc) {
+__device__ __forceinline__ void process_interior(const StepArgs& A, int cell, int x, int y, int z, Acc& acc) {
     const uint32_t d = A.desc[cell];
     if (d & D_WALL) return;
     constexpr bool SH = S::shifted;
-
     // previous-step strain first: keeps the velocity stencil out of the
     // register peak of the collision
     float strainPre = 0.0f;
@@ -525,42 +590,88 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
     float buoy = 0.0f;
     if (!MAT && THERMAL && A.th_buoy_mode != 1)
         buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
-
-    // ---- gather ----
+    const bool plain = (d & D_LINKS) == 0;   // no wall next to the cell
     float f[Q19];
     if (!ODD) {
 #pragma unroll
         for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
-    } else if (interior) {
-        if ((d & D_LINKS) == 0) {   // no wall next to the cell: plain pull
+    } else if (plain) {
 #pragma unroll
-            for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
-        } else {
-#pragma unroll
-            for (int q = 0; q < Q19; ++q) {
-                const bool special = (d >> q) & 1u;
-                const int src = special ? cell : cell - nb19(A, q);
-                f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
-            }
-        }
+        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
     } else {
 #pragma unroll
         for (int q = 0; q < Q19; ++q) {
+            const bool special = (d >> q) & 1u;
+            const int src = special ? cell : cell - nb19(A, q);
+            f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
+        }
+    }
+    if (MAT) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) A.mat_f[(long long)q * A.ncell + cell] = SH ? f[q] + w19(q) : f[q];
+    }
+    CellResult r;
+    if (!MAT) {
+        collide19<SH>(f, A, d, false, false, strainPre, buoy, r, acc);
+        const uint32_t os = (d >> D_OUT_SHIFT) & 3u;   // planes Nx-2 / Nx-3 feed the outlet
+        if (os) {
+            const int P = A.out_plane;
+            const int pi = plane_index(A, x, y, z);
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) A.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
+        }
+        if (!ODD) {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+        } else if (plain) {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) {
+                const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
+                if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+                else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+            }
+        }
+        if (A.write_u) A.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
+        if (A.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
+    }
+    if (THERMAL) thermal_substep<S, ODD, MAT, true>(A, cell, x, y, z, d, 0ull, r, acc);
+}
+
+// ---- boundary-shell cell: precomputed link kinds, rolled loops (kept out of
+// line so the interior loop stays small in the instruction cache) ------------
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, int y, int z,
+                                           unsigned long long skind, Acc& acc) {
+    const uint32_t d = A.desc[cell];
+    if (d & D_WALL) return;
+    constexpr bool SH = S::shifted;
+    float buoy = 0.0f;
+    if (!MAT && THERMAL && A.th_buoy_mode != 1)
+        buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
+    float f[Q19];
+#pragma unroll 1
+    for (int q = 0; q < Q19; ++q) {
+        if (!ODD) {
+            f[q] = S::load_rw(fplane<S>(A, q) + cell);
+        } else {
             const Link L = resolve_kind(A, x, y, z, cell, q, (int)((skind >> (2 * q)) & 3ull));
             f[q] = S::load_rw(fplane<S>(A, L.slot) + L.idx);
         }
     }
     const bool isInlet = (d & D_INLET) != 0, isOutlet = (d & D_OUTLET) != 0;
-    if (!interior && A.apply_overrides && !A.periodic_x) {
+    if (A.apply_overrides && !A.periodic_x) {
         if (isInlet) {
-#pragma unroll
+#pragma unroll 1
             for (int q = 0; q < Q19; ++q) f[q] = A.feq_in[q];
         } else if (isOutlet && A.outlet_mode) {
             const int P = A.out_plane;
             const int pi = plane_index(A, x, y, z);
             if (A.outlet_mode == 1) {
                 // convective outlet, aeros/src/lbm.cpp:1465-1496
-#pragma unroll
+#pragma unroll 1
                 for (int q = 0; q < Q19; ++q) {
                     const float fOut = A.out_r[(0 * Q19 + q) * P + pi];
                     const float fIn = A.out_r[(1 * Q19 + q) * P + pi];
@@ -575,7 +686,7 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
                 const int pos[3] = {x, y, z};
                 const int n3[3] = {A.nx, A.ny, A.nz};
                 const int per[3] = {A.periodic_x, 0, A.periodic_z};
-#pragma unroll
+#pragma unroll 1
                 for (int q = 0; q < Q19; ++q) {
                     if (ca19(q, A.flow_axis) * A.flow_sign >= 0) continue;
                     int t[3] = {x - cx19(q), y - cy19(q), z - cz19(q)};
@@ -592,126 +703,36 @@ __device__ __forceinline__ void process_cell(const StepArgs& A, int cell, int x,
         }
     }
     if (MAT) {
-#pragma unroll
+#pragma unroll 1
         for (int q = 0; q < Q19; ++q) A.mat_f[(long long)q * A.ncell + cell] = SH ? f[q] + w19(q) : f[q];
     }
-
-    // ---- collide ----
     CellResult r;
     if (!MAT) {
-        collide19<SH>(f, A, d, isInlet, isOutlet, strainPre, buoy, r, acc);
-
-        // outlet side buffer: post values of the three outlet planes
+        collide19<SH>(f, A, d, isInlet, isOutlet, 0.0f, buoy, r, acc);
         const uint32_t os = (d >> D_OUT_SHIFT) & 3u;
         if (os) {
             const int P = A.out_plane;
             const int pi = plane_index(A, x, y, z);
-#pragma unroll
+#pragma unroll 1
             for (int q = 0; q < Q19; ++q) A.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
         }
-
-        // ---- scatter ----
-        if (!ODD) {
-            if (interior) {
-#pragma unroll
-                for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+#pragma unroll 1
+        for (int j = 0; j < Q19; ++j) {
+            const int oj = opp19(j);
+            const int kind = (int)((skind >> (2 * oj)) & 3ull);
+            if (!ODD) {
+                S::store(fplane<S>(A, oj) + cell, kind == L_COPYOWN ? f[oj] : f[j]);
             } else {
-#pragma unroll
-                for (int j = 0; j < Q19; ++j) {
-                    const bool copyown = ((skind >> (2 * opp19(j))) & 3ull) == L_COPYOWN;
-                    S::store(fplane<S>(A, opp19(j)) + cell, copyown ? f[opp19(j)] : f[j]);
-                }
-            }
-        } else if (interior) {
-            if ((d & D_LINKS) == 0) {
-#pragma unroll
-                for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < Q19; ++j) {
-                    const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
-                    if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
-                    else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < Q19; ++j) {
-                const Link L = resolve_kind(A, x, y, z, cell, opp19(j), (int)((skind >> (2 * opp19(j))) & 3ull));
+                const Link L = resolve_kind(A, x, y, z, cell, oj, kind);
                 if (L.kind == L_REGULAR || L.kind == L_FREESLIP) S::store(fplane<S>(A, L.slot) + L.idx, f[j]);
-                else if (L.kind == L_BOUNCE) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
-                else S::store(fplane<S>(A, opp19(j)) + cell, f[opp19(j)]);
+                else if (L.kind == L_BOUNCE) S::store(fplane<S>(A, oj) + cell, f[j]);
+                else S::store(fplane<S>(A, oj) + cell, f[oj]);
             }
         }
-        if (A.write_u) { A.uc[0][cell] = r.ux; A.uc[1][cell] = r.uy; A.uc[2][cell] = r.uz; }
+        if (A.write_u) A.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
         if (A.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
     }
-
-    // ---- thermal sub-step (D3Q7), aeros/src/thermal_lbm.cpp:199-336 ----
-    if (THERMAL) {
-        const float wshift = SH ? A.th_tref : 0.0f;   // stored value = g - w*Tref
-        float g[Q7];
-        if (!ODD) {
-#pragma unroll
-            for (int i = 0; i < Q7; ++i) g[i] = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;
-        } else {
-#pragma unroll
-            for (int i = 0; i < Q7; ++i) {
-                const TLink L = th_resolve(A, x, y, z, cell, i, interior, d,
-                                           interior ? -1 : (int)((skind >> (40 + 2 * i)) & 3ull));
-                if (L.bounce == 0) {
-                    g[i] = S::load_rw(gplane<S>(A, opp19(i)) + L.idx) + w7(i) * wshift;
-                } else {
-                    const float v = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;   // post_{opp i}
-                    g[i] = L.bounce == 2 ? (-v + 2.0f * w7(i) * L.Tw) : v;
-                }
-            }
-        }
-        if (MAT) {
-#pragma unroll
-            for (int i = 0; i < Q7; ++i) A.mat_g[(long long)i * A.ncell + cell] = g[i];
-            return;
-        }
-        float T = 0.0f;
-#pragma unroll
-        for (int i = 0; i < Q7; ++i) T += g[i];
-        if (!isfinite(T)) T = A.th_tref;
-        {
-            const float lo = A.th_cold - 1.0f, hi = A.th_hot + 1.0f;
-            const float m = (lo < T) ? T : lo;
-            T = (m < hi) ? m : hi;
-        }
-        const float v[3] = {r.ux, r.uy, r.uz};
-#pragma unroll
-        for (int i = 0; i < Q7; ++i) {
-            const float cu = i == 0 ? 0.0f : ((i & 1) ? v[(i - 1) >> 1] : -v[(i - 1) >> 1]);
-            const float eq = w7(i) * T * (1.0f + 4.0f * cu);
-            g[i] = g[i] - (g[i] - eq) * A.th_invtau;
-        }
-        A.T[cell] = T;
-        acc.tsum += T;
-        if (y == A.th_ylo) { acc.nu += (double)(A.th_hot - T) / 0.5; acc.nun++; }
-        // scatter
-        if (!ODD) {
-#pragma unroll
-            for (int j = 0; j < Q7; ++j) S::store(gplane<S>(A, opp19(j)) + cell, g[j] - w7(j) * wshift);
-        } else {
-#pragma unroll
-            for (int j = 0; j < Q7; ++j) {
-                const TLink L = th_resolve(A, x, y, z, cell, opp19(j), interior, d,
-                                           interior ? -1 : (int)((skind >> (40 + 2 * opp19(j))) & 3ull));
-                if (L.bounce == 0) {
-                    S::store(gplane<S>(A, j) + L.idx, g[j] - w7(j) * wshift);
-                } else {
-                    // becomes pre-collision population opp j of this cell
-                    const float val = L.bounce == 2 ? (-g[j] + 2.0f * w7(j) * L.Tw) : g[j];
-                    S::store(gplane<S>(A, opp19(j)) + cell, val - w7(j) * wshift);
-                }
-            }
-        }
-    } else if (MAT) {
-        return;
-    }
+    if (THERMAL) thermal_substep<S, ODD, MAT, false>(A, cell, x, y, z, d, skind, r, acc);
 }
 
 // Block reduction of the per-thread accumulators into one partial (FP64),
@@ -858,7 +879,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& a
             const int x = cell - (int)r * A.nx;
             const uint32_t z = A.div_y.div(r);
             const int y = (int)(r - z * (uint32_t)A.ny);
-            process_cell<S, ODD, THERMAL, MAT>(A, cell, x, y, (int)z, false, A.shell_kind[si], acc);
+            process_shell<S, ODD, THERMAL, MAT>(A, cell, x, y, (int)z, A.shell_kind[si], acc);
         }
     } else {
         const int before = min(nsh, tile / k + 1);   // shell tiles in [0, tile]
@@ -869,7 +890,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& a
             const uint32_t zq = A.div_iy.div(r);
             const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
             const int z = (int)zq + 1;
-            process_cell<S, ODD, THERMAL, MAT>(A, (z * A.ny + y) * A.nx + x, x, y, z, true, 0ull, acc);
+            process_interior<S, ODD, THERMAL, MAT>(A, (z * A.ny + y) * A.nx + x, x, y, z, acc);
         }
     }
 }

@@ -32,8 +32,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "aeros-engine_gb300"))
 
 # algorithmic bytes per cell update of the step kernel (read + write):
-#   populations 2 x 19 x bytes, previous velocity 12, new velocity 12, descriptor 4
-BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 12 + 12 + 4, "fp16": 2 * 19 * 2 + 12 + 12 + 4, "bf16": 2 * 19 * 2 + 12 + 12 + 4}
+#   populations 2 x 19 x bytes, previous velocity 16 (ux, uy, uz, pad),
+#   new velocity 16, descriptor 4
+BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 16 + 16 + 4, "fp16": 2 * 19 * 2 + 16 + 16 + 4, "bf16": 2 * 19 * 2 + 16 + 16 + 4}
 
 
 def dist_env():

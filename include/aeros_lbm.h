@@ -160,10 +160,10 @@ int aeros_lbm_get_stats(aeros_lbm* h, aeros_lbm_stats* out);
  * Any pointer may be NULL. */
 int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float* uy,
                           float* uz, float* strain, float* tke);
-/* Device pointers of the same fields (valid until the next step call).
- * Any out-pointer may be NULL. */
-int aeros_lbm_device_fields(aeros_lbm* h, const float** rho, const float** ux,
-                            const float** uy, const float** uz);
+/* Device pointers of the density and of the velocity, interleaved as
+ * (ux, uy, uz, 0) per cell (valid until the next step call). Either may be
+ * NULL. */
+int aeros_lbm_device_fields(aeros_lbm* h, const float** rho, const float** u4);
 /* Pre-collision populations, layout [19][nx*ny*nz] (the reference's f after
  * stepLBMCPU, lbm.cpp:89,1546). Converted to FP32 for shifted storage. */
 int aeros_lbm_read_populations(aeros_lbm* h, float* f);
