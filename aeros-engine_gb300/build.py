@@ -22,6 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-warn-spills"]
 # resident blocks per SM the step kernel's register budget targets (tuning knob)
 MIN_BLOCKS = os.environ.get("AEROS_STEP_MIN_BLOCKS", "3")
+STAGED_MIN_BLOCKS = os.environ.get("AEROS_STAGED_MIN_BLOCKS", "3")
+TAG = f"mb{MIN_BLOCKS}s{STAGED_MIN_BLOCKS}"
 UNITS = {
     "lbm_fp32.cu": ["--fmad=false"],
     "lbm_half.cu": ["--fmad=true"],
@@ -50,9 +52,10 @@ def _stale(obj: str, src: str) -> bool:
 
 def _compile(unit: str, flags: list[str], verbose: bool) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD_DIR, unit.replace(".cu", f".mb{MIN_BLOCKS}.o"))
+    obj = os.path.join(BUILD_DIR, unit.replace(".cu", f".{TAG}.o"))
     if _stale(obj, src):
-        cmd = [nvcc(), *ARCH, *COMMON, f"-DAEROS_STEP_MIN_BLOCKS={MIN_BLOCKS}", *flags, "-c", src, "-o", obj]
+        cmd = [nvcc(), *ARCH, *COMMON, f"-DAEROS_STEP_MIN_BLOCKS={MIN_BLOCKS}",
+               f"-DAEROS_STAGED_MIN_BLOCKS={STAGED_MIN_BLOCKS}", *flags, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {unit}:\n{r.stdout}\n{r.stderr}")
@@ -69,14 +72,14 @@ def build(verbose: bool = False) -> str:
     lib = os.path.join(OUT_DIR, "libaeros_gb300.so")
     stamp = os.path.join(BUILD_DIR, "linked_with")
     last = open(stamp).read() if os.path.exists(stamp) else ""
-    if (not os.path.exists(lib) or last != MIN_BLOCKS
+    if (not os.path.exists(lib) or last != TAG
             or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs)):
         cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", lib]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         with open(stamp, "w") as fh:
-            fh.write(MIN_BLOCKS)
+            fh.write(TAG)
     return lib
 
 

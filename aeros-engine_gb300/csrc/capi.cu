@@ -119,6 +119,7 @@ struct aeros_lbm {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     long long last_launches = 0;
     int sm_count = 0;
+    int staged = 0;               // TMA-staged interior tiles (opt-in: AEROS_STAGED=1)
 };
 
 template <class T>
@@ -329,6 +330,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (const char* e = getenv("AEROS_STAGED")) h->staged = atoi(e) != 0;
 
     std::vector<int> shell;
     host_geometry(h, shell);
@@ -339,8 +341,9 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         free_handle(h);                          \
         return rc;                               \
     }
-    ALLOC(h->f, (size_t)h->qstride * Q19 * h->esize);
-    ALLOC(h->desc, n * 4);
+    // staged copies round ranges up to 16 bytes: pad the arrays they read
+    ALLOC(h->f, ((size_t)h->qstride * Q19 + 64) * h->esize);
+    ALLOC(h->desc, (n + 64) * 4);
     ALLOC(h->shell, (size_t)std::max(1, h->n_shell) * 4);
     ALLOC(h->shell_kind, (size_t)std::max(1, h->n_shell) * 8);
     ALLOC(h->u[0], n * 16);
@@ -493,6 +496,10 @@ static void base_args(const aeros_lbm* h, StepArgs& A) {
     A.div_iy = FastDiv((uint32_t)(h->ny - 2));
     A.div_x = FastDiv((uint32_t)h->nx);
     A.div_y = FastDiv((uint32_t)h->ny);
+    for (int q = 0; q < Q19; ++q) {
+        A.fq[q] = static_cast<char*>(h->f) + (size_t)q * (size_t)h->qstride * h->esize;
+        A.nbq[q] = cx19(q) + cy19(q) * h->nx + cz19(q) * h->nx * h->ny;
+    }
     A.f = h->f; A.desc = h->desc; A.shell = h->shell; A.shell_kind = h->shell_kind;
     A.rho = h->rho; A.strain = h->strain; A.tke = h->tke;
     A.out_plane = h->out_plane;
@@ -518,6 +525,7 @@ static void base_args(const aeros_lbm* h, StepArgs& A) {
     A.freeslip = p.lateral_bc == AEROS_LATERAL_FREESLIP;
     A.outlet_mode = h->outlet_mode;
     A.total_div10 = h->ncell / 10;
+    A.staged = h->staged;
     {
         // bounded forces keep every intermediate of a clean cell finite
         float fmax = std::max(std::fabs(p.body_force[0]), std::max(std::fabs(p.body_force[1]), std::fabs(p.body_force[2])));
@@ -545,17 +553,26 @@ static void base_args(const aeros_lbm* h, StepArgs& A) {
 // pending overrides (after init, reset, or materialize + write-back).
 static int normalize_layout(aeros_lbm* h);
 
+static StepVar step_var(const aeros_lbm* h, bool write_obs) {
+    StepVar V;
+    V.up = h->u[h->ubuf];
+    V.uc = h->u[h->ubuf ^ 1];
+    V.out_w = h->out[h->out_par];
+    V.out_r = h->out[h->out_par ^ 1];
+    V.apply_overrides = h->overrides_next;
+    V.write_obs = write_obs;
+    V.write_u = h->p.use_les || write_obs;
+    return V;
+}
+
 static int launch_materialize(aeros_lbm* h, float* d_f, float* d_g) {
     StepArgs A;
     base_args(h, A);
     A.mat_f = d_f;
     A.mat_g = d_g;
-    A.apply_overrides = h->overrides_next;
-    A.out_r = h->out[h->out_par ^ 1];
-    A.out_w = h->out[h->out_par];
-    A.up = h->u[h->ubuf];
+    const StepVar V = step_var(h, false);
     const int grid = h->grid[h->next_odd][h->th_on];
-    CUDA_TRY(h->L->step(A, h->next_odd, h->th_on, true, grid, h->stream));
+    CUDA_TRY(h->L->step(A, V, h->next_odd, h->th_on, true, grid, h->stream));
     return AEROS_OK;
 }
 
@@ -594,16 +611,10 @@ static int enqueue_steps(aeros_lbm* h, int nsteps) {
     StepArgs A;
     base_args(h, A);
     for (int i = 0; i < nsteps; ++i) {
-        A.apply_overrides = h->overrides_next;
-        A.out_w = h->out[h->out_par];
-        A.out_r = h->out[h->out_par ^ 1];
-        A.up = h->u[h->ubuf];
-        A.uc = h->u[h->ubuf ^ 1];
-        A.write_obs = (i == nsteps - 1);
-        A.write_u = h->p.use_les || A.write_obs;
+        const StepVar V = step_var(h, i == nsteps - 1);
         A.th_buoy_mode = h->th_buoy_mode;
         const int grid = h->grid[h->next_odd][h->th_on];
-        CUDA_TRY(h->L->step(A, h->next_odd, h->th_on, false, grid, h->stream));
+        CUDA_TRY(h->L->step(A, V, h->next_odd, h->th_on, false, grid, h->stream));
         h->last_launches++;
         h->next_odd = !h->next_odd;
         h->overrides_next = true;
@@ -629,6 +640,12 @@ static int finish_batch(aeros_lbm* h) {
     h->stats_dirty = false;
     Control& c = *h->ctl_host;
     aeros_lbm_stats& s = h->stats;
+    if (c.stage_timeout) {
+        c.stage_timeout = 0;
+        CUDA_TRY(cudaMemcpyAsync(&h->ctl->stage_timeout, &c.stage_timeout, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        return set_error(AEROS_ERR_TIMEOUT, "a bounded wait on a staged bulk copy gave up (results used direct loads)");
+    }
     if (c.halt) {
         const long long executed = c.kexec - h->kexec_before;
         const long long launched = h->last_launches;

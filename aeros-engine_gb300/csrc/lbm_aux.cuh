@@ -127,7 +127,7 @@ __global__ void k_thermal_prestream(const StepArgs A, float tref) {
 // Launcher table, one instance per storage format (the translation unit of
 // each format is compiled with its own floating-point contraction setting).
 struct Launchers {
-    cudaError_t (*step)(const StepArgs& A, bool odd, bool thermal, bool mat, int grid, cudaStream_t s);
+    cudaError_t (*step)(const StepArgs& A, const StepVar& V, bool odd, bool thermal, bool mat, int grid, cudaStream_t s);
     int (*occupancy)(bool odd, bool thermal);
     cudaError_t (*fill_uniform)(const FillArgs& a, cudaStream_t s);
     cudaError_t (*set_equilibrium)(void* f, const uint32_t* desc, long long qstride, int ncell, const float* rho,
@@ -146,22 +146,30 @@ const Launchers& launchers_bf16();
 #define AEROS_DEFINE_LAUNCHERS(NAME, STORE)                                                                           \
     namespace NAME##_detail {                                                                                         \
     template <bool O, bool T, bool M>                                                                                 \
-    cudaError_t launch_one(const StepArgs& A, int grid, cudaStream_t s) {                                            \
-        k_lbm_step<STORE, O, T, M><<<grid, STEP_BLOCK, 0, s>>>(A);                                                    \
+    cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
+        if (!T && !M && A.staged)                                                                                     \
+            k_lbm_step_staged<STORE, O><<<grid, STEP_BLOCK, 0, s>>>(A, V);                                            \
+        else                                                                                                          \
+            k_lbm_step<STORE, O, T, M><<<grid, STEP_BLOCK, 0, s>>>(A, V);                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    cudaError_t step_(const StepArgs& A, bool odd, bool thermal, bool mat, int grid, cudaStream_t s) {               \
+    cudaError_t step_(const StepArgs& A, const StepVar& V, bool odd, bool thermal, bool mat, int grid,             \
+                      cudaStream_t s) {                                                                               \
         if (mat) {                                                                                                    \
-            if (odd) return thermal ? launch_one<true, true, true>(A, grid, s) : launch_one<true, false, true>(A, grid, s); \
-            return thermal ? launch_one<false, true, true>(A, grid, s) : launch_one<false, false, true>(A, grid, s);  \
+            if (odd) return thermal ? launch_one<true, true, true>(A, V, grid, s) : launch_one<true, false, true>(A, V, grid, s); \
+            return thermal ? launch_one<false, true, true>(A, V, grid, s) : launch_one<false, false, true>(A, V, grid, s);  \
         }                                                                                                             \
-        if (odd) return thermal ? launch_one<true, true, false>(A, grid, s) : launch_one<true, false, false>(A, grid, s); \
-        return thermal ? launch_one<false, true, false>(A, grid, s) : launch_one<false, false, false>(A, grid, s);    \
+        if (odd) return thermal ? launch_one<true, true, false>(A, V, grid, s) : launch_one<true, false, false>(A, V, grid, s); \
+        return thermal ? launch_one<false, true, false>(A, V, grid, s) : launch_one<false, false, false>(A, V, grid, s);    \
     }                                                                                                                 \
     template <bool O, bool T>                                                                                         \
     int occ_one() {                                                                                                   \
-        int n = 0;                                                                                                    \
+        int n = 0, m = 0;                                                                                             \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_step<STORE, O, T, false>, STEP_BLOCK, 0);             \
+        if (!T) {                                                                                                     \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_lbm_step_staged<STORE, O>, STEP_BLOCK, 0);            \
+            n = n < m ? n : m;                                                                                        \
+        }                                                                                                             \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \
     int occupancy_(bool odd, bool thermal) {                                                                          \

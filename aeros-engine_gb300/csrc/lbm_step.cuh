@@ -45,6 +45,7 @@ struct Control {
     int halt;               // divergence guard tripped: later steps return at once
     int halt_kind;          // 1: NaN count before streaming, 2: mean density
     int th_valid;           // Nusselt updated at least once
+    int stage_timeout;      // a bounded wait on a bulk copy gave up (error)
     long long steps;        // counted steps (lbmCurrentStep)
     long long kexec;        // step bodies executed
     float prev_kinetic;
@@ -64,15 +65,13 @@ struct StepArgs {
     FastDiv div_ix, div_iy;     // interior decode: (nx-2), (ny-2)
     FastDiv div_x, div_y;       // shell decode: nx, ny
     void* f;
+    void* fq[Q19];              // start of population plane q (f + q * qstride)
+    int nbq[Q19];               // linear offset of c_q: cx + cy * nx + cz * nx * ny
     const uint32_t* desc;
     const int* shell;
     const unsigned long long* shell_kind;   // 2 bits per D3Q19 direction (LinkKind),
                                             // 2 bits per D3Q7 direction from bit 40
-    const float4* up;           // previous-step velocity (ux, uy, uz, 0) per cell
-    float4* uc;                 // this step's velocity
     float *rho, *strain, *tke;
-    float* out_w;
-    const float* out_r;
     int out_plane;
     void* g;
     float* T;
@@ -89,8 +88,8 @@ struct StepArgs {
     int periodic_x, periodic_z;
     int use_trt, use_les;
     int freeslip, outlet_mode;  // outlet_mode: 0 none, 1 convective, 2 zero-gradient
-    int apply_overrides, write_obs, write_u;
     int fast_ok;                // forces bounded: clean states need no non-finite checks
+    int staged;                 // interior tiles through TMA bulk copies (non-thermal steps)
     int total_div10, fluid_cells;
     float conv_threshold;
     int th_on, th_fixed, th_ylo;
@@ -99,6 +98,18 @@ struct StepArgs {
                                 // field, thermal_lbm.cpp:132), 2: from T_buoy
     const float* T_buoy;
     double th_rows_n;           // Nx*Nz*(yhi-ylo+1), thermal_lbm.cpp:76
+};
+
+// What changes from one step to the next (AA parity of the double-buffered
+// velocity and outlet side buffers, first-step and last-step flags).
+struct StepVar {
+    const float4* up;           // previous-step velocity (ux, uy, uz, 0) per cell
+    float4* uc;                 // this step's velocity
+    float* out_w;               // outlet side buffer written this step
+    const float* out_r;         // ... and the one the previous step wrote
+    int apply_overrides;        // inlet / outlet overrides (off right after (re)initialisation)
+    int write_obs;              // write rho, strain, TKE (last step of a call)
+    int write_u;                // write the velocity (every step with LES, else the last)
 };
 
 // Van Driest factor table, aeros/src/lbm.cpp:112-120
@@ -126,16 +137,14 @@ struct Acc {
 
 template <class S>
 __device__ __forceinline__ typename S::T* fplane(const StepArgs& A, int q) {
-    return reinterpret_cast<typename S::T*>(A.f) + (long long)q * A.qstride;
+    return reinterpret_cast<typename S::T*>(A.fq[q]);
 }
 template <class S>
 __device__ __forceinline__ typename S::T* gplane(const StepArgs& A, int q) {
     return reinterpret_cast<typename S::T*>(A.g) + (long long)q * A.qstride;
 }
 
-__device__ __forceinline__ int nb19(const StepArgs& A, int q) {
-    return cx19(q) + cy19(q) * A.nx + cz19(q) * A.nxny;
-}
+__device__ __forceinline__ int nb19(const StepArgs& A, int q) { return A.nbq[q]; }
 
 __device__ __forceinline__ bool is_wall(const StepArgs& A, int c) { return (A.desc[c] & D_WALL) != 0; }
 
@@ -302,9 +311,8 @@ __device__ __forceinline__ void relax19_shifted_fast(float f[Q19], float rho, fl
 template <bool SHIFTED>
 __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint32_t d, bool isInlet, bool isOutlet,
                                           float strainPre, float buoy, CellResult& o, Acc& acc) {
-    // moments and the range of the populations in one pass
-    float rho = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
-    float fmn = f[0], fmx = f[0];
+    // moments and the sum of squares of the populations in one pass
+    float rho = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f, ss = 0.0f;
 #pragma unroll
     for (int q = 0; q < Q19; ++q) {
         const float m = f[q];
@@ -312,14 +320,22 @@ __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint3
         if (cx19(q) != 0) ux = cx19(q) > 0 ? ux + m : ux - m;
         if (cy19(q) != 0) uy = cy19(q) > 0 ? uy + m : uy - m;
         if (cz19(q) != 0) uz = cz19(q) > 0 ? uz + m : uz - m;
-        fmn = fminf(fmn, m);
-        fmx = fmaxf(fmx, m);
+        ss = fmaf(m, m, ss);
     }
-    // A NaN makes the sum non-finite; an infinity or any value outside
-    // [-1, 10] shows in the range. Only then can the reference's per-population
-    // replacement (lbm.cpp:1061-1074) change anything; it is replayed exactly.
-    // Shifted form: bounds on h = f - w that imply f in [-1, 10].
-    const bool clean = isfinite(rho) && fmn >= -1.0f && fmx <= (SHIFTED ? 9.6f : 10.0f);
+    // Only a non-finite population or one outside [-1, 10] lets the
+    // reference's per-population replacement (lbm.cpp:1061-1074) change
+    // anything; then it is replayed exactly. A rounded sum of squares <= 1
+    // bounds every |f| by 1 (each rounded partial sum is >= every rounded
+    // square so far) and is false for NaN / inf: the common case costs 19
+    // FMAs. Otherwise the range is taken exactly. Shifted form: bounds on
+    // h = f - w that imply f in [-1, 10].
+    bool clean = ss <= 1.0f;
+    if (!clean) {
+        float fmn = f[0], fmx = f[0];
+#pragma unroll
+        for (int q = 1; q < Q19; ++q) { fmn = fminf(fmn, f[q]); fmx = fmaxf(fmx, f[q]); }
+        clean = isfinite(rho) && fmn >= -1.0f && fmx <= (SHIFTED ? 9.6f : 10.0f);
+    }
     if (!clean) {
         rho = 0.0f; ux = 0.0f; uy = 0.0f; uz = 0.0f;
 #pragma unroll
@@ -399,12 +415,20 @@ __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint3
     // negative post-collision populations (lbmNegativePops): one minimum per
     // weight class, exact count only when one is negative
     {
-        float m0 = f[0], m1 = f[1], m2 = f[7];
+        bool anyneg;
+        if (SHIFTED) {
+            float m0 = f[0], m1 = f[1], m2 = f[7];
 #pragma unroll
-        for (int q = 2; q <= 6; ++q) m1 = fminf(m1, f[q]);
+            for (int q = 2; q <= 6; ++q) m1 = fminf(m1, f[q]);
 #pragma unroll
-        for (int q = 8; q < Q19; ++q) m2 = fminf(m2, f[q]);
-        const bool anyneg = SHIFTED ? (m0 < -w19(0) || m1 < -w19(1) || m2 < -w19(7)) : (fminf(m0, fminf(m1, m2)) < 0.0f);
+            for (int q = 8; q < Q19; ++q) m2 = fminf(m2, f[q]);
+            anyneg = m0 < -w19(0) || m1 < -w19(1) || m2 < -w19(7);
+        } else {   // any sign bit (a -0.0 only triggers the exact count below)
+            uint32_t sb = 0;
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) sb |= __float_as_uint(f[q]);
+            anyneg = (sb >> 31) != 0;
+        }
         if (anyneg || !clean) {
 #pragma unroll
             for (int q = 0; q < Q19; ++q) acc.neg += ((SHIFTED ? f[q] + w19(q) : f[q]) < 0.0f) ? 1 : 0;
@@ -433,10 +457,10 @@ __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint3
 }
 
 // Two-pass |S| from previous-step velocity (aeros/src/lbm.cpp:1012-1031).
-__device__ __forceinline__ float strain_prev(const StepArgs& A, int c) {
-    const float4 xm = __ldg(A.up + c - 1), xp = __ldg(A.up + c + 1);
-    const float4 ym = __ldg(A.up + c - A.nx), yp = __ldg(A.up + c + A.nx);
-    const float4 zm = __ldg(A.up + c - A.nxny), zp = __ldg(A.up + c + A.nxny);
+__device__ __forceinline__ float strain_prev(const StepArgs& A, const StepVar& V, int c) {
+    const float4 xm = __ldg(V.up + c - 1), xp = __ldg(V.up + c + 1);
+    const float4 ym = __ldg(V.up + c - A.nx), yp = __ldg(V.up + c + A.nx);
+    const float4 zm = __ldg(V.up + c - A.nxny), zp = __ldg(V.up + c + A.nxny);
     const float dux_dx = (xp.x - xm.x) * 0.5f;
     const float duy_dy = (yp.y - ym.y) * 0.5f;
     const float duz_dz = (zp.z - zm.z) * 0.5f;
@@ -579,14 +603,15 @@ __device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int
 
 // ---- interior cell (1 <= x,y,z <= N-2): flat neighbour offsets ---------------
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __forceinline__ void process_interior(const StepArgs& A, int cell, int x, int y, int z, Acc& acc) {
+__device__ __forceinline__ void process_interior(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
+                                                 Acc& acc) {
     const uint32_t d = A.desc[cell];
     if (d & D_WALL) return;
     constexpr bool SH = S::shifted;
     // previous-step strain first: keeps the velocity stencil out of the
     // register peak of the collision
     float strainPre = 0.0f;
-    if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, cell);
+    if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
     float buoy = 0.0f;
     if (!MAT && THERMAL && A.th_buoy_mode != 1)
         buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
@@ -618,7 +643,7 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, int cell, in
             const int P = A.out_plane;
             const int pi = plane_index(A, x, y, z);
 #pragma unroll
-            for (int q = 0; q < Q19; ++q) A.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
+            for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
         }
         if (!ODD) {
 #pragma unroll
@@ -634,16 +659,49 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, int cell, in
                 else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
             }
         }
-        if (A.write_u) A.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
-        if (A.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
+        if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
+        if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
     }
     if (THERMAL) thermal_substep<S, ODD, MAT, true>(A, cell, x, y, z, d, 0ull, r, acc);
 }
 
-// ---- boundary-shell cell: precomputed link kinds, rolled loops (kept out of
-// line so the interior loop stays small in the instruction cache) ------------
+// Collision, outlet side buffer, scatter and field writes of an interior cell
+// whose pre-collision populations are already in f (staged kernel).
+template <class S, bool ODD>
+__device__ __forceinline__ void interior_finish(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
+                                                uint32_t d, float f[Q19], float strainPre, Acc& acc) {
+    constexpr bool SH = S::shifted;
+    CellResult r;
+    collide19<SH>(f, A, d, false, false, strainPre, 0.0f, r, acc);
+    const uint32_t os = (d >> D_OUT_SHIFT) & 3u;
+    if (os) {
+        const int P = A.out_plane;
+        const int pi = plane_index(A, x, y, z);
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
+    }
+    if (!ODD) {
+#pragma unroll
+        for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+    } else if ((d & D_LINKS) == 0) {
+#pragma unroll
+        for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < Q19; ++j) {
+            const bool solid = (d >> opp19(j)) & 1u;
+            if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+            else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+        }
+    }
+    if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
+    if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
+}
+
+// ---- boundary-shell cell: precomputed link kinds (kept out of line so the
+// interior loop stays small in the instruction cache) ------------------------
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, int y, int z,
+__device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
                                            unsigned long long skind, Acc& acc) {
     const uint32_t d = A.desc[cell];
     if (d & D_WALL) return;
@@ -652,7 +710,7 @@ __device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, i
     if (!MAT && THERMAL && A.th_buoy_mode != 1)
         buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
     float f[Q19];
-#pragma unroll 1
+#pragma unroll
     for (int q = 0; q < Q19; ++q) {
         if (!ODD) {
             f[q] = S::load_rw(fplane<S>(A, q) + cell);
@@ -662,20 +720,20 @@ __device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, i
         }
     }
     const bool isInlet = (d & D_INLET) != 0, isOutlet = (d & D_OUTLET) != 0;
-    if (A.apply_overrides && !A.periodic_x) {
+    if (V.apply_overrides && !A.periodic_x) {
         if (isInlet) {
-#pragma unroll 1
+#pragma unroll
             for (int q = 0; q < Q19; ++q) f[q] = A.feq_in[q];
         } else if (isOutlet && A.outlet_mode) {
             const int P = A.out_plane;
             const int pi = plane_index(A, x, y, z);
             if (A.outlet_mode == 1) {
                 // convective outlet, aeros/src/lbm.cpp:1465-1496
-#pragma unroll 1
+#pragma unroll
                 for (int q = 0; q < Q19; ++q) {
-                    const float fOut = A.out_r[(0 * Q19 + q) * P + pi];
-                    const float fIn = A.out_r[(1 * Q19 + q) * P + pi];
-                    const float fIn2 = A.out_r[(2 * Q19 + q) * P + pi];
+                    const float fOut = V.out_r[(0 * Q19 + q) * P + pi];
+                    const float fIn = V.out_r[(1 * Q19 + q) * P + pi];
+                    const float fIn2 = V.out_r[(2 * Q19 + q) * P + pi];
                     const float df = fIn - fOut;
                     const float df2 = fIn - fIn2;
                     f[q] = fOut + A.conv * df + 0.15f * A.conv * df2;
@@ -686,7 +744,7 @@ __device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, i
                 const int pos[3] = {x, y, z};
                 const int n3[3] = {A.nx, A.ny, A.nz};
                 const int per[3] = {A.periodic_x, 0, A.periodic_z};
-#pragma unroll 1
+#pragma unroll
                 for (int q = 0; q < Q19; ++q) {
                     if (ca19(q, A.flow_axis) * A.flow_sign >= 0) continue;
                     int t[3] = {x - cx19(q), y - cy19(q), z - cz19(q)};
@@ -697,13 +755,13 @@ __device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, i
                     }
                     const int tc = (t[2] * A.ny + t[1]) * A.nx + t[0];
                     const int tpi = is_wall(A, tc) ? pi : plane_index(A, t[0], t[1], t[2]);
-                    f[q] = A.out_r[(0 * Q19 + q) * P + tpi];
+                    f[q] = V.out_r[(0 * Q19 + q) * P + tpi];
                 }
             }
         }
     }
     if (MAT) {
-#pragma unroll 1
+#pragma unroll
         for (int q = 0; q < Q19; ++q) A.mat_f[(long long)q * A.ncell + cell] = SH ? f[q] + w19(q) : f[q];
     }
     CellResult r;
@@ -713,10 +771,10 @@ __device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, i
         if (os) {
             const int P = A.out_plane;
             const int pi = plane_index(A, x, y, z);
-#pragma unroll 1
-            for (int q = 0; q < Q19; ++q) A.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
         }
-#pragma unroll 1
+#pragma unroll
         for (int j = 0; j < Q19; ++j) {
             const int oj = opp19(j);
             const int kind = (int)((skind >> (2 * oj)) & 3ull);
@@ -729,8 +787,8 @@ __device__ __noinline__ void process_shell(const StepArgs& A, int cell, int x, i
                 else S::store(fplane<S>(A, oj) + cell, f[oj]);
             }
         }
-        if (A.write_u) A.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
-        if (A.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
+        if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
+        if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
     }
     if (THERMAL) thermal_substep<S, ODD, MAT, false>(A, cell, x, y, z, d, skind, r, acc);
 }
@@ -865,7 +923,7 @@ __device__ void finish_step(const StepArgs& A) {
 }
 
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& acc) {
+__device__ __forceinline__ void process_tile(const StepArgs& A, const StepVar& V, int tile, Acc& acc) {
     // Shell tiles (costlier: per-link index arithmetic) are spread evenly
     // through the tile sequence: tile t is shell tile t / k when t % k == 0.
     const int nsh = A.ntiles - A.ntiles_interior;
@@ -879,7 +937,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& a
             const int x = cell - (int)r * A.nx;
             const uint32_t z = A.div_y.div(r);
             const int y = (int)(r - z * (uint32_t)A.ny);
-            process_shell<S, ODD, THERMAL, MAT>(A, cell, x, y, (int)z, A.shell_kind[si], acc);
+            process_shell<S, ODD, THERMAL, MAT>(A, V, cell, x, y, (int)z, A.shell_kind[si], acc);
         }
     } else {
         const int before = min(nsh, tile / k + 1);   // shell tiles in [0, tile]
@@ -890,7 +948,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& a
             const uint32_t zq = A.div_iy.div(r);
             const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
             const int z = (int)zq + 1;
-            process_interior<S, ODD, THERMAL, MAT>(A, (z * A.ny + y) * A.nx + x, x, y, z, acc);
+            process_interior<S, ODD, THERMAL, MAT>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc);
         }
     }
 }
@@ -898,12 +956,229 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, int tile, Acc& a
 // One lattice step. Tiles of STEP_BLOCK cells are assigned round-robin to a
 // persistent grid (a fixed assignment, so the statistics are deterministic).
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_step(const StepArgs A) {
+__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_step(const StepArgs A, const StepVar V) {
     if (!MAT && A.ctl->halt) return;   // uniform: every thread reads the same flag
     Acc acc;
     acc.zero();
-    for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) process_tile<S, ODD, THERMAL, MAT>(A, tile, acc);
+    for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) process_tile<S, ODD, THERMAL, MAT>(A, V, tile, acc);
     if (MAT) return;
+    block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
+    finish_step<STEP_BLOCK>(A);
+}
+
+// ---- staged interior tiles: TMA bulk copies into shared memory ----------------
+// Each interior tile (STEP_BLOCK consecutive interior cells, one or a few row
+// segments) pulls 19 contiguous population ranges — the tile's own cells on
+// even steps, the tile shifted by -c_q on odd steps — plus its descriptors.
+// One elected thread issues them as cp.async.bulk copies completing on an
+// mbarrier, for the NEXT tile of the block while the current one computes;
+// threads then read shared memory. Tiles whose span (row gaps included)
+// exceeds the staging slot, shell tiles and wall-adjacent links use direct
+// loads. Waits are bounded: on timeout the kernel records an error and
+// continues with direct loads.
+constexpr int STAGE_SLOT = 288;   // elements per staged range
+#ifndef AEROS_STAGED_MIN_BLOCKS
+#define AEROS_STAGED_MIN_BLOCKS 3
+#endif
+constexpr int STAGED_MIN_BLOCKS = AEROS_STAGED_MIN_BLOCKS;
+constexpr int STAGE_WAIT_LIMIT = 1 << 20;   // try_wait polls before a staged tile is given up
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ int interior_cell_of(const StepArgs& A, int li) {
+    const uint32_t r = A.div_ix.div((uint32_t)li);
+    const int x = li - (int)r * (A.nx - 2) + 1;
+    const uint32_t zq = A.div_iy.div(r);
+    const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
+    return ((int)zq + 1) * A.nxny + y * A.nx + x;
+}
+
+// Interior tile index of a tile of the sequence, -1 for a shell tile.
+__device__ __forceinline__ int interior_tile_of(const StepArgs& A, int tile) {
+    const int nsh = A.ntiles - A.ntiles_interior;
+    const int k = A.shell_stride;
+    if (nsh > 0 && (tile % k) == 0 && tile / k < nsh) return -1;
+    return tile - min(nsh, tile / k + 1);
+}
+
+template <class S>
+struct StageBuf {
+    typename S::T pop[Q19][STAGE_SLOT];
+    uint32_t desc[STAGE_SLOT];
+    int lo[Q19 + 1];
+    unsigned long long bar;
+};
+
+// First and last cell of interior tile `it`; true when it fits the slot.
+template <class S>
+__device__ __forceinline__ bool stage_span(const StepArgs& A, int it, int& c0, int& c1) {
+    constexpr int AL = 16 / (int)sizeof(typename S::T);
+    const int li0 = it * STEP_BLOCK;
+    const int li1 = min(li0 + STEP_BLOCK, A.n_interior) - 1;
+    c0 = interior_cell_of(A, li0);
+    c1 = interior_cell_of(A, li1);
+    return (c1 - c0 + 1) + 2 * AL <= STAGE_SLOT;
+}
+
+template <class S, bool ODD>
+__device__ __forceinline__ void stage_issue(const StepArgs& A, StageBuf<S>& sb, int c0, int c1) {
+    using T = typename S::T;
+    constexpr int AL = 16 / (int)sizeof(T);
+    uint32_t bytes[Q19 + 1];
+    int lo[Q19 + 1];
+    uint32_t total = 0;
+#pragma unroll
+    for (int q = 0; q < Q19; ++q) {
+        const int a = ODD ? c0 - nb19(A, q) : c0, b = ODD ? c1 - nb19(A, q) : c1;
+        lo[q] = a & ~(AL - 1);
+        bytes[q] = (uint32_t)(((b + 1 - lo[q]) * (int)sizeof(T) + 15) & ~15);
+        total += bytes[q];
+    }
+    lo[Q19] = c0 & ~3;
+    bytes[Q19] = (uint32_t)(((c1 + 1 - lo[Q19]) * 4 + 15) & ~15);
+    total += bytes[Q19];
+#pragma unroll
+    for (int q = 0; q <= Q19; ++q) sb.lo[q] = lo[q];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&sb.bar, total);
+#pragma unroll
+    for (int q = 0; q < Q19; ++q)
+        bulk_g2s(sb.pop[q], fplane<S>(A, ODD ? opp19(q) : q) + lo[q], bytes[q], &sb.bar);
+    bulk_g2s(sb.desc, A.desc + lo[Q19], bytes[Q19], &sb.bar);
+}
+
+template <class S, bool ODD>
+__global__ void __launch_bounds__(STEP_BLOCK, STAGED_MIN_BLOCKS) k_lbm_step_staged(const StepArgs A, const StepVar V) {
+    if (A.ctl->halt) return;   // uniform: every thread reads the same flag
+    __shared__ __align__(128) StageBuf<S> sb;
+    Acc acc;
+    acc.zero();
+    if (threadIdx.x == 0) mbar_init(&sb.bar);
+    __syncthreads();
+    uint32_t parity = 0;
+    bool stage_ok = true, pending = false;
+    int c0n = 0, c1n = 0;
+    int tile = blockIdx.x;
+    bool cur = false;
+    if (tile < A.ntiles) {
+        const int it = interior_tile_of(A, tile);
+        if (it >= 0 && stage_span<S>(A, it, c0n, c1n)) {
+            cur = true;
+            if (threadIdx.x == 0) stage_issue<S, ODD>(A, sb, c0n, c1n);
+        }
+    }
+    for (; tile < A.ntiles; tile += gridDim.x) {
+        const int next = tile + gridDim.x;
+        const int it = interior_tile_of(A, tile);
+        int itn = -1;
+        bool nxt = false;
+        if (stage_ok && next < A.ntiles) {
+            itn = interior_tile_of(A, next);
+            nxt = itn >= 0 && stage_span<S>(A, itn, c0n, c1n);
+        }
+        if (it < 0) {   // shell tile: shared memory idle, prefetch the next tile first
+            if (nxt && threadIdx.x == 0) stage_issue<S, ODD>(A, sb, c0n, c1n);
+            const int si = (tile / A.shell_stride) * STEP_BLOCK + (int)threadIdx.x;
+            if (si < A.n_shell) {
+                const int cell = A.shell[si];
+                const uint32_t r = A.div_x.div((uint32_t)cell);
+                const int x = cell - (int)r * A.nx;
+                const uint32_t z = A.div_y.div(r);
+                const int y = (int)(r - z * (uint32_t)A.ny);
+                process_shell<S, ODD, false, false>(A, V, cell, x, y, (int)z, A.shell_kind[si], acc);
+            }
+            cur = nxt;
+            continue;
+        }
+        const int li = it * STEP_BLOCK + (int)threadIdx.x;
+        const bool valid = li < A.n_interior;
+        int x = 0, y = 0, z = 0, cell = 0;
+        if (valid) {
+            const uint32_t r = A.div_ix.div((uint32_t)li);
+            x = li - (int)r * (A.nx - 2) + 1;
+            const uint32_t zq = A.div_iy.div(r);
+            y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
+            z = (int)zq + 1;
+            cell = (z * A.ny + y) * A.nx + x;
+        }
+        if (cur) {
+            bool done = false;
+            for (int spin = 0; spin < STAGE_WAIT_LIMIT && !done; ++spin) done = mbar_try_wait(&sb.bar, parity);
+            if (__syncthreads_or(!done)) {   // never expected: record, stop staging, use direct loads
+                if (threadIdx.x == 0) A.ctl->stage_timeout = 1;
+                stage_ok = false;
+                cur = false;
+                nxt = false;
+                pending = true;
+            } else {
+                parity ^= 1u;
+            }
+        }
+        uint32_t d = D_WALL;
+        float f[Q19];
+        float strainPre = 0.0f;
+        if (valid) {
+            d = cur ? sb.desc[cell - sb.lo[Q19]] : A.desc[cell];
+            if (!(d & D_WALL)) {
+                if (A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
+                if (cur && (!ODD || (d & D_LINKS) == 0)) {
+#pragma unroll
+                    for (int q = 0; q < Q19; ++q) {
+                        const int src = ODD ? cell - nb19(A, q) : cell;
+                        f[q] = S::load_rw(&sb.pop[q][src - sb.lo[q]]);
+                    }
+                } else if (cur) {
+#pragma unroll
+                    for (int q = 0; q < Q19; ++q) {
+                        if ((d >> q) & 1u) f[q] = S::load_rw(fplane<S>(A, q) + cell);
+                        else f[q] = S::load_rw(&sb.pop[q][cell - nb19(A, q) - sb.lo[q]]);
+                    }
+                } else if (!ODD) {
+#pragma unroll
+                    for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < Q19; ++q) {
+                        const bool special = (d >> q) & 1u;
+                        const int src = special ? cell : cell - nb19(A, q);
+                        f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
+                    }
+                }
+            }
+        }
+        __syncthreads();   // shared memory consumed
+        if (nxt && threadIdx.x == 0) stage_issue<S, ODD>(A, sb, c0n, c1n);
+        if (valid && !(d & D_WALL)) interior_finish<S, ODD>(A, V, cell, x, y, z, d, f, strainPre, acc);
+        cur = nxt;
+    }
+    if (pending) {   // a copy that outlived its wait: give it one more bounded wait before exiting
+        bool done = false;
+        for (int spin = 0; spin < STAGE_WAIT_LIMIT && !done; ++spin) done = mbar_try_wait(&sb.bar, parity);
+    }
     block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
     finish_step<STEP_BLOCK>(A);
 }
