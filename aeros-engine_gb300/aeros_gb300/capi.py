@@ -73,6 +73,14 @@ class VoxelPlan(C.Structure):
                 ("requested_res", C.c_int32), ("suggested_res", C.c_int32)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("shell_first", C.c_int32),
+                ("chunk_steps", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 def make_params(nx, ny, nz, *, tau=0.6, smagorinsky_c=0.12, les=False, trt=False,
                 periodic_x=False, periodic_z=False, convective_outlet=False,
                 flow_axis=0, flow_sign=1, u_in=(0.08, 0.0, 0.0), u_init=None,
@@ -143,6 +151,17 @@ _SIGS = {
     "aeros_lbm_last_step_ms": (C.c_int, [_P, _FP]),
     "aeros_lbm_last_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "aeros_lbm_device_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "aeros_batch_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
+    "aeros_batch_destroy": (C.c_int, [_P]),
+    "aeros_batch_add": (C.c_int, [_P, _P]),
+    "aeros_batch_remove": (C.c_int, [_P, _P]),
+    "aeros_batch_size": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    "aeros_batch_step": (C.c_int, [_P, C.c_int]),
+    "aeros_batch_set_tuning": (C.c_int, [_P, C.POINTER(BatchTuning)]),
+    "aeros_batch_get_tuning": (C.c_int, [_P, C.POINTER(BatchTuning)]),
+    "aeros_batch_autotune": (C.c_int, [_P, C.c_int, C.POINTER(BatchTuning)]),
+    "aeros_batch_last_step_ms": (C.c_int, [_P, _FP]),
+    "aeros_batch_last_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
 }
 
 

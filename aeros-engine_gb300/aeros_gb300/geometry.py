@@ -178,6 +178,28 @@ def sphere_config(storage="fp32", u_in=0.05, re=100.0, smag=0.1, grid=SPHERE_GRI
     return p, np.asarray(mask, np.uint8).reshape(nz, ny, nx), tris
 
 
+BATCH_SIZES = ((32, 32, 32), (64, 32, 32), (96, 48, 48), (128, 64, 64), (160, 80, 80))
+
+
+def batch_domain(i: int, storage="fp16", u_in=0.04, level=4, smag=0.1, sizes=BATCH_SIZES, re_range=(50.0, 400.0)):
+    """Domain i of the batched design sweep: size drawn from `sizes`, one
+    perturbed icosphere (radius ny/6, vertex radii x U(0.85, 1.15), axis
+    scales U(0.5, 1.5)) at (nx/3, ny/2, nz/2), Re ~ U(re_range) on the channel
+    height ny, TRT + Smagorinsky, uniform inlet, zero-gradient outlet, free-slip
+    lateral walls. Returns (params, mask, info)."""
+    from .solver import voxel_grid, voxelize
+    g = splitmix64(i)
+    nx, ny, nz = sizes[min(len(sizes) - 1, int(uniform(g, 0.0, float(len(sizes)))))]
+    re = uniform(g, re_range[0], re_range[1])
+    tau = 0.5 + 3.0 * u_in * ny / re
+    tris = perturbed_icosphere(level, ny / 6.0, (nx / 3.0, ny / 2.0, nz / 2.0), seed=1000 + i)
+    mask = voxelize(tris, voxel_grid((nx, ny, nz), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)))
+    p = capi.make_params(nx, ny, nz, tau=tau, smagorinsky_c=smag, les=True, trt=True, u_in=(u_in, 0.0, 0.0),
+                         vel_scale=1.0 / u_in, storage=storage, lateral_bc=capi.AEROS_LATERAL_FREESLIP,
+                         outlet_bc=capi.AEROS_OUTLET_ZEROGRAD)
+    return p, np.asarray(mask, np.uint8).reshape(nz, ny, nx), dict(re=re, size=(nx, ny, nz), tau=tau, tris=len(tris))
+
+
 def rb_config(ra: float, nx=128, nz=128, fluid_rows=32, pr=0.71, tau=0.56, storage="fp32"):
     """Rayleigh-Benard: the reference's vertical axis is y (thermal_lbm.cpp:60-65),
     so the config's 128 x 128 x 32 (z up) maps to nx = 128, ny = 32 + 2 wall

@@ -6,6 +6,7 @@ Translation units and their floating-point contraction:
   forces.cu    --fmad=false  per-cell momentum-flux terms as the reference
   voxel.cu     --fmad=false  bit-exact inside test
   capi.cu      --fmad=false  host code with -ffp-contract=off
+  batch.cu     --fmad=false  host side of the many-domain batch
 """
 from __future__ import annotations
 
@@ -30,9 +31,10 @@ UNITS = {
     "forces.cu": ["--fmad=false"],
     "voxel.cu": ["--fmad=false"],
     "capi.cu": ["--fmad=false"],
+    "batch.cu": ["--fmad=false"],
     "setup.cu": [],
 }
-HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh", "setup.cuh"]
+HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh", "setup.cuh", "handle.cuh"]
 
 
 def nvcc() -> str:
@@ -46,7 +48,7 @@ def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
         return True
     t = os.path.getmtime(obj)
-    deps = [src] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(os.path.dirname(HERE), "include", "aeros_lbm.h")]
+    deps = [src] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(os.path.dirname(HERE), "include", h) for h in ("aeros_lbm.h", "aeros_batch.h")]
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 

@@ -18,6 +18,7 @@
 
 #include "../../include/aeros_lbm.h"
 #include "forces.cuh"
+#include "handle.cuh"
 #include "lbm_aux.cuh"
 #include "setup.cuh"
 
@@ -29,8 +30,7 @@ using namespace aeros;
 static thread_local int g_err_code = 0;
 static thread_local char g_err_msg[1024] = {0};
 
-static int set_error(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
-static int set_error(int code, const char* fmt, ...) {
+int set_error(int code, const char* fmt, ...) {
     g_err_code = code;
     va_list ap;
     va_start(ap, fmt);
@@ -39,12 +39,6 @@ static int set_error(int code, const char* fmt, ...) {
     return code;
 }
 
-#define CUDA_TRY(expr)                                                                                    \
-    do {                                                                                                  \
-        cudaError_t e_ = (expr);                                                                          \
-        if (e_ != cudaSuccess)                                                                            \
-            return set_error(AEROS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_)); \
-    } while (0)
 
 extern "C" int aeros_consume_error(char* buf, int buf_size) {
     if (g_err_code == 0) {
@@ -57,70 +51,6 @@ extern "C" int aeros_consume_error(char* buf, int buf_size) {
     g_err_msg[0] = 0;
     return c;
 }
-
-// ---------------------------------------------------------------------------
-// handle
-// ---------------------------------------------------------------------------
-struct aeros_lbm {
-    aeros_lbm_params p{};
-    int nx = 0, ny = 0, nz = 0, ncell = 0;
-    long long qstride = 0;
-    const Launchers* L = nullptr;
-    size_t esize = 4;
-    // device memory
-    void* f = nullptr;
-    uint32_t* desc = nullptr;
-    int* shell = nullptr;
-    unsigned long long* shell_kind = nullptr;
-    std::vector<int> shell_host;
-    std::vector<unsigned long long> shell_kind_host;
-    float4* u[2] = {nullptr, nullptr};   // velocity (ux, uy, uz, 0), double buffered
-    float *rho = nullptr, *strain = nullptr, *tke = nullptr;
-    float* out[2] = {nullptr, nullptr};
-    int out_plane = 0;
-    void* g = nullptr;
-    float* T = nullptr;
-    float* T_buoy = nullptr;
-    Partial* partials = nullptr;
-    int max_grid = 0;
-    Control* ctl = nullptr;
-    Control* ctl_host = nullptr;   // pinned
-    double* force_partials = nullptr;
-    double* force_out = nullptr;
-    unsigned int* force_counter = nullptr;
-    unsigned long long* area_count = nullptr;
-    uint64_t dev_bytes = 0;
-    // host geometry
-    std::vector<uint8_t> mask, wall;
-    int n_interior = 0, n_shell = 0, fluid_cells = 1;
-    int outlet_mode = 0;
-    float feq_in[19] = {0};
-    float conv = 0.08f;
-    // layout state of the AA pattern
-    bool next_odd = false;        // next step gathers from neighbours
-    bool overrides_next = false;  // next gather applies inlet/outlet overrides
-    int out_par = 1;              // side buffer written by the next step
-    int ubuf = 0;                 // u[ubuf] holds the latest velocity
-    int grid[2][2] = {{0, 0}, {0, 0}};
-    // thermal
-    bool th_on = false;
-    aeros_thermal_params tp{};
-    int ylo = 0, yhi = 0;
-    float H = 1, tau_t = 0.7f, alpha = 0, glb = 0;
-    int th_buoy_mode = 1;
-    bool th_stepped = false;
-    // stats
-    aeros_lbm_stats stats{};
-    bool stats_dirty = false;
-    long long kexec_before = 0;
-    bool last_diverged = false;
-    // timing
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    long long last_launches = 0;
-    int sm_count = 0;
-    int staged = 0;               // TMA-staged interior tiles (opt-in: AEROS_STAGED=1)
-};
 
 template <class T>
 static int dalloc(aeros_lbm* h, T** p, size_t bytes) {
@@ -463,6 +393,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
 
 extern "C" int aeros_lbm_destroy(aeros_lbm* h) {
     if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
+    if (h->batch) return set_error(AEROS_ERR_STATE, "domain is in a batch: remove it first");
     cudaStreamSynchronize(h->stream);
     free_handle(h);
     return AEROS_OK;
@@ -480,7 +411,7 @@ extern "C" int aeros_lbm_synchronize(aeros_lbm* h) {
     return AEROS_OK;
 }
 
-static void base_args(const aeros_lbm* h, StepArgs& A) {
+void base_args(const aeros_lbm* h, StepArgs& A) {
     memset(&A, 0, sizeof(A));
     A.nx = h->nx; A.ny = h->ny; A.nz = h->nz; A.nxny = h->nx * h->ny; A.ncell = h->ncell;
     A.qstride = h->qstride;
@@ -553,7 +484,7 @@ static void base_args(const aeros_lbm* h, StepArgs& A) {
 // pending overrides (after init, reset, or materialize + write-back).
 static int normalize_layout(aeros_lbm* h);
 
-static StepVar step_var(const aeros_lbm* h, bool write_obs) {
+StepVar step_var(const aeros_lbm* h, bool write_obs) {
     StepVar V;
     V.up = h->u[h->ubuf];
     V.uc = h->u[h->ubuf ^ 1];
@@ -634,7 +565,7 @@ static int enqueue_steps(aeros_lbm* h, int nsteps) {
 
 // Reads the control block of the last enqueued batch; on a tripped
 // divergence guard re-equilibrates (lbm.cpp:1583-1600).
-static int finish_batch(aeros_lbm* h) {
+int finish_batch(aeros_lbm* h) {
     if (!h->stats_dirty) return AEROS_OK;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->stats_dirty = false;

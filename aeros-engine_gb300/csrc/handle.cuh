@@ -1,0 +1,91 @@
+// handle.cuh — the solver handle shared by the C-ABI translation units
+// (capi.cu: single domains; batch.cu: many domains in one persistent kernel).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/aeros_lbm.h"
+#include "lbm_aux.cuh"
+
+struct aeros_batch;
+
+// Records code + message (thread-local) for aeros_consume_error; returns code.
+int set_error(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+
+#define CUDA_TRY(expr)                                                                                    \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return set_error(AEROS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_)); \
+    } while (0)
+
+// One lattice domain: device buffers, AA-pattern layout state, statistics.
+struct aeros_lbm {
+    aeros_lbm_params p{};
+    int nx = 0, ny = 0, nz = 0, ncell = 0;
+    long long qstride = 0;
+    const aeros::Launchers* L = nullptr;
+    size_t esize = 4;
+    // device memory
+    void* f = nullptr;
+    uint32_t* desc = nullptr;
+    int* shell = nullptr;
+    unsigned long long* shell_kind = nullptr;
+    std::vector<int> shell_host;
+    std::vector<unsigned long long> shell_kind_host;
+    float4* u[2] = {nullptr, nullptr};   // velocity (ux, uy, uz, 0), double buffered
+    float *rho = nullptr, *strain = nullptr, *tke = nullptr;
+    float* out[2] = {nullptr, nullptr};
+    int out_plane = 0;
+    void* g = nullptr;
+    float* T = nullptr;
+    float* T_buoy = nullptr;
+    aeros::Partial* partials = nullptr;
+    int max_grid = 0;
+    aeros::Control* ctl = nullptr;
+    aeros::Control* ctl_host = nullptr;   // pinned
+    double* force_partials = nullptr;
+    double* force_out = nullptr;
+    unsigned int* force_counter = nullptr;
+    unsigned long long* area_count = nullptr;
+    uint64_t dev_bytes = 0;
+    // host geometry
+    std::vector<uint8_t> mask, wall;
+    int n_interior = 0, n_shell = 0, fluid_cells = 1;
+    int outlet_mode = 0;
+    float feq_in[19] = {0};
+    float conv = 0.08f;
+    // layout state of the AA pattern
+    bool next_odd = false;        // next step gathers from neighbours
+    bool overrides_next = false;  // next gather applies inlet/outlet overrides
+    int out_par = 1;              // side buffer written by the next step
+    int ubuf = 0;                 // u[ubuf] holds the latest velocity
+    int grid[2][2] = {{0, 0}, {0, 0}};
+    // thermal
+    bool th_on = false;
+    aeros_thermal_params tp{};
+    int ylo = 0, yhi = 0;
+    float H = 1, tau_t = 0.7f, alpha = 0, glb = 0;
+    int th_buoy_mode = 1;
+    bool th_stepped = false;
+    // stats
+    aeros_lbm_stats stats{};
+    bool stats_dirty = false;
+    long long kexec_before = 0;
+    bool last_diverged = false;
+    // timing
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    long long last_launches = 0;
+    int sm_count = 0;
+    int staged = 0;               // TMA-staged interior tiles (opt-in: AEROS_STAGED=1)
+    aeros_batch* batch = nullptr; // batch this domain is a member of
+};
+
+// Kernel arguments of the domain's current state (capi.cu).
+void base_args(const aeros_lbm* h, aeros::StepArgs& A);
+// Per-step arguments of the next step (parity of the double buffers).
+aeros::StepVar step_var(const aeros_lbm* h, bool write_obs);
+// Completes the last enqueued steps: statistics, divergence reset.
+int finish_batch(aeros_lbm* h);

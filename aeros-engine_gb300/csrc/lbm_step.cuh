@@ -845,6 +845,9 @@ __device__ __forceinline__ void block_reduce_store(const Acc& a, Partial* out) {
 // Last block: sums the partials in block order and updates the control block
 // (aeros/src/lbm.cpp:1313-1319 and 1554-1580).
 template <int BLOCK>
+__device__ void finish_totals(const StepArgs& A, const Partial* parts, int nparts);
+
+template <int BLOCK>
 __device__ void finish_step(const StepArgs& A) {
     __shared__ bool last;
     __threadfence();
@@ -852,11 +855,18 @@ __device__ void finish_step(const StepArgs& A) {
     __syncthreads();
     if (!last) return;
     __threadfence();
+    finish_totals<BLOCK>(A, A.partials, (int)gridDim.x);
+}
+
+// All threads of one block: sums nparts partials in a fixed order (FP64) and
+// updates the domain's control block.
+template <int BLOCK>
+__device__ void finish_totals(const StepArgs& A, const Partial* parts, int nparts) {
     double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     float m = 0.0f;
     long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += BLOCK) {
-        const volatile Partial* p = A.partials + b;
+    for (int b = threadIdx.x; b < nparts; b += BLOCK) {
+        const volatile Partial* p = parts + b;
         t[0] += p->rho; t[1] += p->ke; t[2] += p->tke; t[3] += p->nu; t[4] += p->tsum;
         m = fmaxf(m, p->maxu);
         c[0] += p->nan; c[1] += p->neg; c[2] += p->bad; c[3] += p->rout;
@@ -964,6 +974,108 @@ __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_step(const 
     if (MAT) return;
     block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
     finish_step<STEP_BLOCK>(A);
+}
+
+// ---- many domains in one persistent kernel -----------------------------------
+// Work items are runs of tiles of one domain (shell tiles of every domain
+// first, then interior tiles); blocks take items from a global counter. Each
+// tile stores its own partial statistics and the block that completes a
+// domain's last tile sums that domain's partials in tile order, so a domain's
+// results do not depend on the schedule, the tuning or the other domains.
+struct BatchDomain {
+    StepArgs A;                 // the domain's arguments (A.ctl: its control block)
+    float4* u[2];               // velocity double buffer
+    float* out[2];              // outlet side buffers
+    int ubuf0, outpar0;         // buffer parities at the first step of the call
+    int overrides0;             // overrides on at the first step of the call
+    int les;                    // velocity written every step
+    int part_base;              // first per-tile partial of the domain
+    int pad[3];
+};
+
+struct BatchWork {
+    int dom, tile, ntiles, pad;
+};
+
+struct BatchCtl {
+    unsigned int work_next;     // next work item (reset by the last block)
+    unsigned int blocks_done;
+    int k;                      // step of the call being executed
+    int k_last;                 // last step of the call (writes rho, |S|, TKE)
+};
+
+struct BatchArgs {
+    const BatchDomain* doms;
+    const BatchWork* work;
+    int nwork;
+    Partial* partials;          // one per tile of every domain
+    unsigned int* done;         // per domain: tiles finished this step
+    BatchCtl* ctl;
+};
+
+template <class S, bool ODD>
+__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_batch_step(const BatchArgs B) {
+    __shared__ __align__(16) unsigned char sA_raw[sizeof(StepArgs)];   // StepArgs is not trivially constructible
+    __shared__ int s_item, s_last;
+    StepArgs& sA = *reinterpret_cast<StepArgs*>(sA_raw);
+    const int k = B.ctl->k;
+    const bool write_obs = k == B.ctl->k_last;
+    int cur = -1;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(&B.ctl->work_next, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= B.nwork) break;
+        const BatchWork wk = B.work[item];
+        const BatchDomain& D = B.doms[wk.dom];
+        if (wk.dom != cur) {   // the domain's arguments into shared memory
+            const int* src = reinterpret_cast<const int*>(&D.A);
+            int* dst = reinterpret_cast<int*>(&sA);
+            for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / 4); i += STEP_BLOCK) dst[i] = src[i];
+            cur = wk.dom;
+            __syncthreads();
+        }
+        const StepArgs& A = sA;
+        // a halted domain stays halted for the rest of the call (its flag is
+        // only set by its own finisher, after its last tile of a step)
+        if (!*(volatile int*)&A.ctl->halt) {
+            StepVar V;
+            V.up = D.u[(D.ubuf0 ^ k) & 1];
+            V.uc = D.u[(D.ubuf0 ^ k ^ 1) & 1];
+            V.out_w = D.out[(D.outpar0 ^ k) & 1];
+            V.out_r = D.out[(D.outpar0 ^ k ^ 1) & 1];
+            V.apply_overrides = D.overrides0 || k > 0;
+            V.write_obs = write_obs;
+            V.write_u = D.les || write_obs;
+            for (int t = 0; t < wk.ntiles; ++t) {
+                Acc acc;
+                acc.zero();
+                process_tile<S, ODD, false, false>(A, V, wk.tile + t, acc);
+                block_reduce_store<STEP_BLOCK>(acc, B.partials + D.part_base + wk.tile + t);
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) {
+                __threadfence();
+                const unsigned int n = atomicAdd(B.done + wk.dom, (unsigned int)wk.ntiles) + (unsigned int)wk.ntiles;
+                s_last = n == (unsigned int)A.ntiles;
+            }
+            __syncthreads();
+            if (s_last) {
+                __threadfence();
+                finish_totals<STEP_BLOCK>(A, B.partials + D.part_base, A.ntiles);
+                if (threadIdx.x == 0) B.done[wk.dom] = 0;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&B.ctl->blocks_done, 1u) == gridDim.x - 1) {
+            B.ctl->work_next = 0;
+            B.ctl->blocks_done = 0;
+            B.ctl->k = k + 1;
+        }
+    }
 }
 
 // ---- staged interior tiles: TMA bulk copies into shared memory ----------------

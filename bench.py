@@ -220,6 +220,50 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20):
+    """The batched design sweep: n_domains seeded domains (sizes 32^3 ...
+    160x80x80, perturbed icosphere level 4, Re ~ U(50, 400), u = 0.04, TRT +
+    Smagorinsky, FP16 shifted storage) in one batch, autotuned launch shape,
+    `steps` steps each in CUDA-graph chunks. Beside it the same domains stepped
+    one at a time through the single-domain path (seq_steps each)."""
+    from aeros_gb300 import batch, geometry, solver
+    t0 = time.time()
+    doms = []
+    for i in range(n_domains):
+        p, mask, _ = geometry.batch_domain(i, storage=storage)
+        doms.append(solver.Solver(p, mask))
+    setup_s = time.time() - t0
+    cells = sum(d.n for d in doms)
+    seq_ms = 0.0
+    for d in doms:
+        d.step(2)
+        d.step(seq_steps)
+        seq_ms += d.last_step_ms()
+    b = batch.Batch(storage)
+    for d in doms:
+        b.add(d)
+    t1 = time.time()
+    tune = b.autotune(trial_steps=20)
+    tune_s = time.time() - t1
+    b.set_tuning(blocks_per_sm=tune["blocks_per_sm"], tiles_per_item=tune["tiles_per_item"],
+                 shell_first=tune["shell_first"], chunk_steps=100)
+    b.step(100)   # capture + warm-up
+    b.step(steps)
+    ms = b.last_step_ms()
+    launches = b.last_launch_count()
+    diverged = sum(d.stats()["diverged"] for d in doms)
+    b.close()
+    for d in doms:
+        d.close()
+    mlups = cells / (ms * 1e-3) / 1e6
+    seq_mlups = cells * seq_steps / (seq_ms * 1e-3) / 1e6
+    return {"domains": n_domains, "cells": cells, "steps": steps, "ms_per_step": round(ms, 4),
+            "mlups": round(mlups, 1), "achieved_gbs": round(BYTES_PER_CELL[storage] * cells / (ms * 1e-3) / 1e9, 1),
+            "sequential_mlups": round(seq_mlups, 1), "speedup_vs_sequential": round(mlups / seq_mlups, 3),
+            "tuning": tune, "autotune_s": round(tune_s, 2), "setup_s": round(setup_s, 2), "gpu_launches": int(launches),
+            "diverged_domains": int(diverged)}
+
+
 def cpu_baseline(mask, steps):
     """The oracle (C restatement of the reference solver, OpenMP) on the same
     grid, `steps` lattice steps (a bounded sample)."""
@@ -289,11 +333,18 @@ def main():
     ap.add_argument("--only", default="both", choices=["both", "fp32", "fp16", "bf16"],
                     help="time one storage form only (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch"])
+    ap.add_argument("--batch-domains", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=10000)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-sweep figures in the sphere line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        r = batch_sweep(args.batch_domains, args.batch_steps)
+        print(json.dumps(r), flush=True)
     else:
         run_gb300(args)
 

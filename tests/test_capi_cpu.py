@@ -36,10 +36,12 @@ def test_struct_layout_matches_c(lib):
 #include <stdio.h>
 #include <stddef.h>
 #include "aeros_lbm.h"
+#include "aeros_batch.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(aeros_lbm_params), sizeof(aeros_thermal_params),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(aeros_lbm_params), sizeof(aeros_thermal_params),
          sizeof(aeros_lbm_stats), sizeof(aeros_voxel_grid), sizeof(aeros_voxel_plan_t),
-         offsetof(aeros_lbm_params, storage), offsetof(aeros_lbm_stats, sum_rho), offsetof(aeros_lbm_stats, nusselt));
+         offsetof(aeros_lbm_params, storage), offsetof(aeros_lbm_stats, sum_rho), offsetof(aeros_lbm_stats, nusselt),
+         sizeof(aeros_batch_tuning));
   return 0; }
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -50,7 +52,7 @@ int main(void) {
         got = [int(v) for v in subprocess.check_output([exe]).split()]
     want = [C.sizeof(lib.LbmParams), C.sizeof(lib.ThermalParams), C.sizeof(lib.LbmStats), C.sizeof(lib.VoxelGrid),
             C.sizeof(lib.VoxelPlan), lib.LbmParams.storage.offset, lib.LbmStats.sum_rho.offset,
-            lib.LbmStats.nusselt.offset]
+            lib.LbmStats.nusselt.offset, C.sizeof(lib.BatchTuning)]
     assert got == want
 
 
@@ -69,6 +71,14 @@ def test_invalid_arguments_are_reported(lib):
     assert L.aeros_lbm_create(C.byref(p), m.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(h)) == -1
     assert L.aeros_consume_error(buf, 512) == -1 and b"storage" in buf.value
     assert L.aeros_lbm_step(None, 1) == -1
+    L.aeros_consume_error(buf, 512)
+    b = C.c_void_p()
+    assert L.aeros_batch_create(7, C.byref(b)) == -1 and not b.value
+    assert L.aeros_consume_error(buf, 512) == -1 and b"storage" in buf.value
+    assert L.aeros_batch_step(None, 2) == -1
+    assert L.aeros_batch_add(None, None) == -1
+    assert L.aeros_batch_set_tuning(None, None) == -1
+    assert L.aeros_batch_autotune(None, 4, None) == -1
     L.aeros_consume_error(buf, 512)
 
 
