@@ -261,6 +261,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (const char* e = getenv("AEROS_STAGED")) h->staged = atoi(e) != 0;
+    if (const char* e = getenv("AEROS_SPLIT")) h->split = atoi(e) != 0;
 
     std::vector<int> shell;
     host_geometry(h, shell);
@@ -458,6 +459,12 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     A.total_div10 = h->ncell / 10;
     A.staged = h->staged;
     {
+        const int nsh = A.ntiles - A.ntiles_interior;
+        A.split = h->split && nsh > 0 && !h->staged;
+        A.shell_grid = A.split ? std::min(nsh, std::max(1, h->sm_count) * 4) : 0;
+        A.shell_part_base = 0;   // set by the launcher (after the interior grid's slots)
+    }
+    {
         // bounded forces keep every intermediate of a clean cell finite
         float fmax = std::max(std::fabs(p.body_force[0]), std::max(std::fabs(p.body_force[1]), std::fabs(p.body_force[2])));
         if (h->th_on) fmax += std::fabs(h->glb) * (std::fabs(h->tp.hot_temp - h->tp.cold_temp) + 2.0f);
@@ -537,6 +544,7 @@ static int normalize_layout(aeros_lbm* h) {
 static int enqueue_steps(aeros_lbm* h, int nsteps) {
     if (nsteps < 0) return set_error(AEROS_ERR_INVALID, "nsteps %d < 0", nsteps);
     h->last_launches = 0;
+    h->last_kernels = 0;
     h->kexec_before = h->ctl_host->kexec;
     CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
     StepArgs A;
@@ -547,6 +555,7 @@ static int enqueue_steps(aeros_lbm* h, int nsteps) {
         const int grid = h->grid[h->next_odd][h->th_on];
         CUDA_TRY(h->L->step(A, V, h->next_odd, h->th_on, false, grid, h->stream));
         h->last_launches++;
+        h->last_kernels += A.split ? 2 : 1;
         h->next_odd = !h->next_odd;
         h->overrides_next = true;
         h->out_par ^= 1;
@@ -657,7 +666,7 @@ extern "C" int aeros_lbm_last_step_ms(aeros_lbm* h, float* ms) {
 
 extern "C" int aeros_lbm_last_launch_count(aeros_lbm* h, int64_t* n) {
     if (!h || !n) return set_error(AEROS_ERR_INVALID, "NULL argument");
-    *n = h->last_launches;
+    *n = h->last_kernels;
     return AEROS_OK;
 }
 

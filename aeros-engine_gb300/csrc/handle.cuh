@@ -80,6 +80,8 @@ struct aeros_lbm {
     long long last_launches = 0;
     int sm_count = 0;
     int staged = 0;               // TMA-staged interior tiles (opt-in: AEROS_STAGED=1)
+    int split = 1;                // shell and interior as two launches per step (AEROS_SPLIT=0: one)
+    long long last_kernels = 0;   // kernel launches of the last step call
     aeros_batch* batch = nullptr; // batch this domain is a member of
 };
 

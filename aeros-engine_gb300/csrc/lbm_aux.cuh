@@ -149,10 +149,16 @@ const Launchers& launchers_bf16();
     namespace NAME##_detail {                                                                                         \
     template <bool O, bool T, bool M>                                                                                 \
     cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
-        if (!T && !M && A.staged)                                                                                     \
+        if (!M && A.split) {                                                                                          \
+            StepArgs B = A;                                                                                           \
+            B.shell_part_base = grid;                                                                                 \
+            if (B.shell_grid > 0) k_lbm_shell<STORE, O, T><<<B.shell_grid, STEP_BLOCK, 0, s>>>(B, V);                 \
+            k_lbm_interior<STORE, O, T><<<grid, STEP_BLOCK, 0, s>>>(B, V);                                            \
+        } else if (!T && !M && A.staged) {                                                                            \
             k_lbm_step_staged<STORE, O><<<grid, STEP_BLOCK, 0, s>>>(A, V);                                            \
-        else                                                                                                          \
+        } else {                                                                                                      \
             k_lbm_step<STORE, O, T, M><<<grid, STEP_BLOCK, 0, s>>>(A, V);                                             \
+        }                                                                                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
     cudaError_t step_(const StepArgs& A, const StepVar& V, bool odd, bool thermal, bool mat, int grid,             \

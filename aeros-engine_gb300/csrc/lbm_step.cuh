@@ -90,6 +90,8 @@ struct StepArgs {
     int freeslip, outlet_mode;  // outlet_mode: 0 none, 1 convective, 2 zero-gradient
     int fast_ok;                // forces bounded: clean states need no non-finite checks
     int staged;                 // interior tiles through TMA bulk copies (non-thermal steps)
+    int split;                  // shell and interior as two launches
+    int shell_part_base, shell_grid;   // split: first partial slot and grid of the shell launch
     int total_div10, fluid_cells;
     float conv_threshold;
     int th_on, th_fixed, th_ylo;
@@ -848,14 +850,14 @@ template <int BLOCK>
 __device__ void finish_totals(const StepArgs& A, const Partial* parts, int nparts);
 
 template <int BLOCK>
-__device__ void finish_step(const StepArgs& A) {
+__device__ void finish_step(const StepArgs& A, int nparts) {
     __shared__ bool last;
     __threadfence();
     if (threadIdx.x == 0) last = (atomicAdd(&A.ctl->blocks_done, 1u) == gridDim.x - 1);
     __syncthreads();
     if (!last) return;
     __threadfence();
-    finish_totals<BLOCK>(A, A.partials, (int)gridDim.x);
+    finish_totals<BLOCK>(A, A.partials, nparts);
 }
 
 // All threads of one block: sums nparts partials in a fixed order (FP64) and
@@ -932,6 +934,35 @@ __device__ void finish_totals(const StepArgs& A, const Partial* parts, int npart
     }
 }
 
+// Shell tile st: shell cells st*STEP_BLOCK ... in increasing cell order.
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __forceinline__ void shell_tile(const StepArgs& A, const StepVar& V, int st, Acc& acc) {
+    const int si = st * STEP_BLOCK + (int)threadIdx.x;
+    if (si < A.n_shell) {
+        const int cell = A.shell[si];
+        const uint32_t r = A.div_x.div((uint32_t)cell);
+        const int x = cell - (int)r * A.nx;
+        const uint32_t z = A.div_y.div(r);
+        const int y = (int)(r - z * (uint32_t)A.ny);
+        process_shell<S, ODD, THERMAL, MAT>(A, V, cell, x, y, (int)z, A.shell_kind[si], acc);
+    }
+}
+
+// Interior tile it: interior cells (x, y, z in 1 .. n-2) it*STEP_BLOCK ... in
+// x-fastest order.
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __forceinline__ void interior_tile(const StepArgs& A, const StepVar& V, int it, Acc& acc) {
+    const int li = it * STEP_BLOCK + (int)threadIdx.x;
+    if (li < A.n_interior) {
+        const uint32_t r = A.div_ix.div((uint32_t)li);
+        const int x = li - (int)r * (A.nx - 2) + 1;
+        const uint32_t zq = A.div_iy.div(r);
+        const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
+        const int z = (int)zq + 1;
+        process_interior<S, ODD, THERMAL, MAT>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc);
+    }
+}
+
 template <class S, bool ODD, bool THERMAL, bool MAT>
 __device__ __forceinline__ void process_tile(const StepArgs& A, const StepVar& V, int tile, Acc& acc) {
     // Shell tiles (costlier: per-link index arithmetic) are spread evenly
@@ -939,28 +970,8 @@ __device__ __forceinline__ void process_tile(const StepArgs& A, const StepVar& V
     const int nsh = A.ntiles - A.ntiles_interior;
     const int k = A.shell_stride;
     const bool is_shell = nsh > 0 && (tile % k) == 0 && tile / k < nsh;
-    if (is_shell) {
-        const int si = (tile / k) * STEP_BLOCK + (int)threadIdx.x;
-        if (si < A.n_shell) {
-            const int cell = A.shell[si];
-            const uint32_t r = A.div_x.div((uint32_t)cell);
-            const int x = cell - (int)r * A.nx;
-            const uint32_t z = A.div_y.div(r);
-            const int y = (int)(r - z * (uint32_t)A.ny);
-            process_shell<S, ODD, THERMAL, MAT>(A, V, cell, x, y, (int)z, A.shell_kind[si], acc);
-        }
-    } else {
-        const int before = min(nsh, tile / k + 1);   // shell tiles in [0, tile]
-        const int li = (tile - before) * STEP_BLOCK + (int)threadIdx.x;
-        if (li < A.n_interior) {
-            const uint32_t r = A.div_ix.div((uint32_t)li);
-            const int x = li - (int)r * (A.nx - 2) + 1;
-            const uint32_t zq = A.div_iy.div(r);
-            const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
-            const int z = (int)zq + 1;
-            process_interior<S, ODD, THERMAL, MAT>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc);
-        }
-    }
+    if (is_shell) shell_tile<S, ODD, THERMAL, MAT>(A, V, tile / k, acc);
+    else interior_tile<S, ODD, THERMAL, MAT>(A, V, tile - min(nsh, tile / k + 1), acc);
 }
 
 // One lattice step. Tiles of STEP_BLOCK cells are assigned round-robin to a
@@ -973,7 +984,31 @@ __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_step(const 
     for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) process_tile<S, ODD, THERMAL, MAT>(A, V, tile, acc);
     if (MAT) return;
     block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
-    finish_step<STEP_BLOCK>(A);
+    finish_step<STEP_BLOCK>(A, (int)gridDim.x);
+}
+
+// The same step as two launches on one stream: the boundary shell first, then
+// the interior, whose code then runs without the shell path beside it in the
+// instruction cache. The shell grid stores its partials after the interior
+// grid's (slots A.shell_part_base ...); the interior grid's last block sums both.
+template <class S, bool ODD, bool THERMAL>
+__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_shell(const StepArgs A, const StepVar V) {
+    if (A.ctl->halt) return;
+    Acc acc;
+    acc.zero();
+    const int nsh = A.ntiles - A.ntiles_interior;
+    for (int st = blockIdx.x; st < nsh; st += gridDim.x) shell_tile<S, ODD, THERMAL, false>(A, V, st, acc);
+    block_reduce_store<STEP_BLOCK>(acc, A.partials + A.shell_part_base + blockIdx.x);
+}
+
+template <class S, bool ODD, bool THERMAL>
+__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_interior(const StepArgs A, const StepVar V) {
+    if (A.ctl->halt) return;
+    Acc acc;
+    acc.zero();
+    for (int it = blockIdx.x; it < A.ntiles_interior; it += gridDim.x) interior_tile<S, ODD, THERMAL, false>(A, V, it, acc);
+    block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
+    finish_step<STEP_BLOCK>(A, A.shell_part_base + A.shell_grid);
 }
 
 // ---- many domains in one persistent kernel -----------------------------------
@@ -1292,7 +1327,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, STAGED_MIN_BLOCKS) k_lbm_step_stag
         for (int spin = 0; spin < STAGE_WAIT_LIMIT && !done; ++spin) done = mbar_try_wait(&sb.bar, parity);
     }
     block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
-    finish_step<STEP_BLOCK>(A);
+    finish_step<STEP_BLOCK>(A, (int)gridDim.x);
 }
 
 }  // namespace aeros

@@ -220,7 +220,7 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
-def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20):
+def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20, chunk=100, autotune=True):
     """The batched design sweep: n_domains seeded domains (sizes 32^3 ...
     160x80x80, perturbed icosphere level 4, Re ~ U(50, 400), u = 0.04, TRT +
     Smagorinsky, FP16 shifted storage) in one batch, autotuned launch shape,
@@ -243,10 +243,10 @@ def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20):
     for d in doms:
         b.add(d)
     t1 = time.time()
-    tune = b.autotune(trial_steps=20)
+    tune = b.autotune(trial_steps=20) if autotune else b.tuning
     tune_s = time.time() - t1
     b.set_tuning(blocks_per_sm=tune["blocks_per_sm"], tiles_per_item=tune["tiles_per_item"],
-                 shell_first=tune["shell_first"], chunk_steps=100)
+                 shell_first=tune["shell_first"], chunk_steps=chunk)
     b.step(100)   # capture + warm-up
     b.step(steps)
     ms = b.last_step_ms()
@@ -336,6 +336,8 @@ def main():
     ap.add_argument("--workload", default="sphere", choices=["sphere", "batch"])
     ap.add_argument("--batch-domains", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=10000)
+    ap.add_argument("--batch-chunk", type=int, default=100, help="steps per captured CUDA graph")
+    ap.add_argument("--batch-fixed", action="store_true", help="default launch shape, no autotuning")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-sweep figures in the sphere line")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -343,7 +345,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
-        r = batch_sweep(args.batch_domains, args.batch_steps)
+        r = batch_sweep(args.batch_domains, args.batch_steps, chunk=args.batch_chunk, autotune=not args.batch_fixed)
         print(json.dumps(r), flush=True)
     else:
         run_gb300(args)
