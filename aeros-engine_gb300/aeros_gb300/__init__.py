@@ -4,6 +4,6 @@
 ``geometry``: seeded meshes and solver configurations; ``batch`` / ``serve``:
 many domains stepped together and the continuous-batching request loop.
 """
-from . import batch, capi, geometry, solver  # noqa: F401
+from . import batch, capi, geometry, serve, solver  # noqa: F401
 from .batch import Batch  # noqa: F401
 from .solver import Solver, voxel_grid, voxelize  # noqa: F401

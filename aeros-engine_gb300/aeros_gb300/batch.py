@@ -61,10 +61,10 @@ class Batch:
         check(lib().aeros_batch_get_tuning(self.h, C.byref(t)), "aeros_batch_get_tuning")
         return t.as_dict()
 
-    def set_tuning(self, blocks_per_sm=0, tiles_per_item=1, shell_first=True, chunk_steps=20) -> None:
+    def set_tuning(self, blocks_per_sm=0, tiles_per_item=1, shell_tiles_per_item=1, chunk_steps=20) -> None:
         t = BatchTuning()
         t.blocks_per_sm, t.tiles_per_item = int(blocks_per_sm), int(tiles_per_item)
-        t.shell_first, t.chunk_steps = int(bool(shell_first)), int(chunk_steps)
+        t.shell_tiles_per_item, t.chunk_steps = int(shell_tiles_per_item), int(chunk_steps)
         check(lib().aeros_batch_set_tuning(self.h, C.byref(t)), "aeros_batch_set_tuning")
 
     def autotune(self, trial_steps: int = 20) -> dict:

@@ -74,7 +74,7 @@ class VoxelPlan(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("shell_first", C.c_int32),
+    _fields_ = [("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("shell_tiles_per_item", C.c_int32),
                 ("chunk_steps", C.c_int32), ("reserved", C.c_int32 * 4)]
 
     def as_dict(self) -> dict:

@@ -7,6 +7,7 @@ geometry on every machine.
 """
 from __future__ import annotations
 
+import functools
 import math
 
 import numpy as np
@@ -29,6 +30,18 @@ def splitmix64(seed: int):
 
 def uniform(gen, lo: float, hi: float) -> float:
     return lo + (hi - lo) * ((next(gen) >> 11) * (1.0 / (1 << 53)))
+
+
+def uniform_array(seed: int, n: int, lo: float, hi: float, skip: int = 0) -> np.ndarray:
+    """Draws skip .. skip+n-1 of the splitmix64(seed) stream as uniform(lo, hi),
+    vectorized: the same float64 values as `uniform` on that stream."""
+    with np.errstate(over="ignore"):
+        k = np.arange(skip + 1, skip + n + 1, dtype=np.uint64)
+        z = np.uint64(seed & MASK64) + k * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return lo + (hi - lo) * ((z >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53)))
 
 
 # ---- meshes --------------------------------------------------------------
@@ -66,17 +79,26 @@ def icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.nda
     return v[f].reshape(-1, 9).astype(np.float32)
 
 
+@functools.lru_cache(maxsize=8)
+def _unit_icosphere_vertices(level: int):
+    """Distinct vertices of the unit icosphere and each triangle corner's index."""
+    base = icosphere(level, 1.0).reshape(-1, 3).astype(np.float64)
+    uniq, inv = np.unique(base.round(9), axis=0, return_inverse=True)
+    uniq.flags.writeable = False
+    inv = inv.reshape(-1)
+    inv.flags.writeable = False
+    return uniq, inv
+
+
 def perturbed_icosphere(level: int, radius: float, center, seed: int, radial: float = 0.15,
                         axis_scale=(0.5, 1.5)) -> np.ndarray:
     """Icosphere whose vertex radii are scaled by U(1-radial, 1+radial) and whose
     axes are scaled by U(axis_scale) — the batched design-sweep obstacle."""
-    base = icosphere(level, 1.0).reshape(-1, 3).astype(np.float64)
-    uniq, inv = np.unique(base.round(9), axis=0, return_inverse=True)
-    g = splitmix64(seed)
-    scales = np.array([uniform(g, axis_scale[0], axis_scale[1]) for _ in range(3)])
-    rad = np.array([uniform(g, 1.0 - radial, 1.0 + radial) for _ in range(len(uniq))])
+    uniq, inv = _unit_icosphere_vertices(level)
+    scales = uniform_array(seed, 3, axis_scale[0], axis_scale[1])
+    rad = uniform_array(seed, len(uniq), 1.0 - radial, 1.0 + radial, skip=3)
     pts = uniq * rad[:, None] * scales[None, :] * radius + np.asarray(center, np.float64)
-    return pts[inv.reshape(-1)].reshape(-1, 9).astype(np.float32)
+    return pts[inv].reshape(-1, 9).astype(np.float32)
 
 
 def uv_sphere(r: float, n_lat: int, n_lon: int, center=(0.0, 0.0, 0.0)) -> np.ndarray:
@@ -216,8 +238,7 @@ def rb_config(ra: float, nx=128, nz=128, fluid_rows=32, pr=0.71, tau=0.56, stora
 def rb_initial_T(nx, ny, nz, ra: float, amp: float = 1e-3, hot=0.5, cold=-0.5) -> np.ndarray:
     """Linear conduction profile between the walls plus U(-amp, amp) noise from
     splitmix64(0x5EED + Ra) on the fluid rows."""
-    g = splitmix64(0x5EED + int(ra))
-    noise = np.array([uniform(g, -amp, amp) for _ in range(nx * (ny - 2) * nz)], np.float32)
+    noise = uniform_array(0x5EED + int(ra), nx * (ny - 2) * nz, -amp, amp).astype(np.float32)
     T = np.zeros((nz, ny, nx), np.float32)
     T[:, 0, :] = hot
     T[:, ny - 1, :] = cold

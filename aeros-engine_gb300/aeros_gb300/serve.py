@@ -1,0 +1,279 @@
+"""Continuous-batching request loop over the many-domain batch.
+
+Solve requests (a seeded perturbed-icosphere obstacle, a grid, a Reynolds
+number) arrive as a Poisson process. The loop admits a request when a slot
+and device memory are free (the domain's footprint counted against an HBM
+budget), voxelizes its mesh on the GPU, creates the domain resident on the
+device and attaches it to the running batch, so new requests overlap on the
+GPU with those already running. Every `check_every` of its own steps a domain
+reports its drag coefficient from the control-volume momentum balance; it is
+retired when Cd changed by less than `tol` (relative) since the previous
+check, or at `max_steps`. Latency is arrival to retirement.
+
+A domain's trajectory does not depend on the other members of the batch
+(include/aeros_batch.h), and checks fall on the same own-step counts whatever
+the mix, so a request gives the same Cd, the same step count and the same
+fields alone as under load.
+
+The reference has no request loop; this module has no reference counterpart.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import queue
+import threading
+import time
+
+import numpy as np
+
+from . import capi, geometry
+from .batch import Batch
+from .solver import Solver, voxel_grid, voxelize
+
+SERVE_GRIDS = ((48, 48, 48), (96, 48, 48), (128, 64, 64), (192, 96, 96), (256, 128, 128))
+SERVE_LEVELS = (5, 6, 7)   # icosphere subdivisions: 20,480 / 81,920 / 327,680 triangles
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds after the start of the session
+    grid: tuple
+    level: int
+    re: float
+    seed: int
+
+
+@dataclasses.dataclass
+class Result:
+    rid: int
+    arrival: float
+    admitted: float
+    finished: float
+    steps: int
+    cd: float
+    converged: bool
+    cells: int
+    tris: int
+    footprint: int
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def make_requests(n: int, rate: float = 2.0, seed: int = 0x5E12, grids=SERVE_GRIDS, levels=SERVE_LEVELS,
+                  re_range=(50.0, 1000.0)) -> list[Request]:
+    """n requests with exponential inter-arrival gaps of mean 1/rate (seeded)."""
+    g = geometry.splitmix64(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        u = geometry.uniform(g, 0.0, 1.0)
+        t += -math.log(max(1.0 - u, 1e-300)) / rate
+        grid = grids[min(len(grids) - 1, int(geometry.uniform(g, 0.0, float(len(grids)))))]
+        level = levels[min(len(levels) - 1, int(geometry.uniform(g, 0.0, float(len(levels)))))]
+        re = geometry.uniform(g, re_range[0], re_range[1])
+        out.append(Request(i, t, grid, level, re, 0xA0000 + i))
+    return out
+
+
+def domain_for(req: Request, storage="fp16", u_in=0.05, smag=0.1):
+    """Solver, drag box and reference area of a request: obstacle of radius
+    ny/8 at (nx/3, ny/2, nz/2) (vertex radii x U(0.85, 1.15), axis scales
+    U(0.5, 1.5)), voxelized on the GPU; tau = 0.5 + 3 u ny / Re (the solver
+    raises tau < 0.51 to 0.55, aeros/src/lbm.cpp:918-920); TRT + Smagorinsky,
+    zero-gradient outlet, free-slip lateral walls."""
+    nx, ny, nz = req.grid
+    r = ny / 8.0
+    c = (nx / 3.0, ny / 2.0, nz / 2.0)
+    tris = geometry.perturbed_icosphere(req.level, r, c, seed=req.seed)
+    mask = voxelize(tris, voxel_grid((nx, ny, nz), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)))
+    tau = 0.5 + 3.0 * u_in * ny / req.re
+    p = capi.make_params(nx, ny, nz, tau=tau, smagorinsky_c=smag, les=True, trt=True, u_in=(u_in, 0.0, 0.0),
+                         vel_scale=1.0 / u_in, storage=storage, lateral_bc=capi.AEROS_LATERAL_FREESLIP,
+                         outlet_bc=capi.AEROS_OUTLET_ZEROGRAD)
+    s = Solver(p, mask)
+    ext = 1.5 * 1.15 * r + 2.0   # largest half extent of the obstacle + 2 cells
+    box = [max(1, int(c[0] - ext)), min(nx - 2, int(c[0] + ext) + 1),
+           max(1, int(c[1] - ext)), min(ny - 2, int(c[1] + ext) + 1),
+           max(1, int(c[2] - ext)), min(nz - 2, int(c[2] + ext) + 1)]
+    area = s.projected_area(0)
+    return s, box, area, len(tris), u_in
+
+
+def footprint_estimate(req: Request, storage="fp16") -> int:
+    """Device bytes of a request before it is created: per cell populations
+    (19 x 2 or 4 B), descriptor, two velocity buffers, rho / |S| / TKE and the
+    voxelizer's mask; per triangle the device BVH copy."""
+    nx, ny, nz = req.grid
+    cells = nx * ny * nz
+    pop = 19 * (2 if storage != "fp32" else 4)
+    tris = 20 * 4 ** req.level
+    return int(cells * (pop + 4 + 32 + 12 + 4) + tris * 96 + (64 << 20))
+
+
+class _Active:
+    __slots__ = ("req", "solver", "box", "area", "u", "tris", "admitted", "steps", "cd_prev", "cd", "bytes")
+
+
+class Server:
+    """Continuous batching: admission by slots and HBM footprint, domain
+    preparation (mesh, GPU voxelization, domain creation) on a worker thread
+    while the batch steps, Cd-convergence retirement."""
+
+    def __init__(self, storage="fp16", budget_bytes=170 << 30, slots=64, check_every=1000, tol=1e-4,
+                 max_steps=30000, chunk=100, levels=SERVE_LEVELS):
+        if check_every % chunk or chunk % 2:
+            raise ValueError("chunk must be even and divide check_every")
+        self.storage = storage
+        self.budget = int(budget_bytes)
+        self.slots = int(slots)
+        self.check_every = int(check_every)
+        self.tol = float(tol)
+        self.max_steps = int(max_steps)
+        self.chunk = int(chunk)
+        for lv in levels:   # unit meshes built once, before any request arrives
+            geometry._unit_icosphere_vertices(int(lv))
+
+    def _cd(self, a: _Active) -> float:
+        F = a.solver.cv_force_box(a.box)
+        return float(F[0] / (0.5 * a.u * a.u * a.area)) if a.area > 0 else float("nan")
+
+    def _prepare(self, todo: queue.Queue, done: queue.Queue) -> None:
+        while True:
+            item = todo.get()
+            if item is None:
+                return
+            req, est, t_adm = item
+            try:
+                done.put((req, est, t_adm, domain_for(req, self.storage)))
+            except Exception as e:   # reported on the serving thread
+                done.put((req, est, t_adm, e))
+
+    def run(self, requests: list[Request], realtime: bool = True, on_retire=None) -> dict:
+        """Serves the requests; returns per-request results and the summary.
+        realtime=False admits each request at once (no waiting for arrivals)."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        batch = Batch(self.storage)
+        batch.set_tuning(chunk_steps=self.chunk)
+        todo: queue.Queue = queue.Queue()
+        done: queue.Queue = queue.Queue()
+        worker = threading.Thread(target=self._prepare, args=(todo, done), daemon=True)
+        worker.start()
+        active: list[_Active] = []
+        results: list[Result] = []
+        used = 0
+        preparing = 0
+        cell_steps = 0
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0   # noqa: E731
+
+        def attach(item):
+            nonlocal used, preparing
+            req, est, t_adm, built = item
+            preparing -= 1
+            if isinstance(built, Exception):
+                used -= est
+                raise built
+            a = _Active()
+            a.req = req
+            a.admitted = t_adm
+            a.solver, a.box, a.area, a.tris, a.u = built
+            a.bytes = max(est, a.solver.device_bytes())
+            used += a.bytes - est
+            a.steps = 0
+            a.cd_prev = a.cd = float("nan")
+            batch.add(a.solver)
+            active.append(a)
+
+        try:
+            while pending or active or preparing:
+                # admission: arrived requests in order while a slot and memory are free
+                while pending and (not realtime or pending[0].arrival <= now()) \
+                        and len(active) + preparing < self.slots:
+                    est = footprint_estimate(pending[0], self.storage)
+                    if used + est > self.budget and (active or preparing):
+                        break
+                    req = pending.pop(0)
+                    used += est
+                    preparing += 1
+                    todo.put((req, est, now()))
+                while not done.empty():
+                    attach(done.get())
+                if not active:
+                    if preparing:
+                        attach(done.get())
+                    elif pending:
+                        time.sleep(max(0.0, min(0.05, pending[0].arrival - now())))
+                    continue
+                batch.step(self.chunk)
+                cell_steps += sum(a.solver.n for a in active) * self.chunk
+                retired = []
+                for a in active:
+                    a.steps += self.chunk
+                    if a.steps % self.check_every == 0:
+                        a.cd_prev, a.cd = a.cd, self._cd(a)
+                        conv = (math.isfinite(a.cd) and math.isfinite(a.cd_prev) and a.cd != 0.0
+                                and abs(a.cd - a.cd_prev) < self.tol * abs(a.cd))
+                        if conv or a.steps >= self.max_steps:
+                            retired.append((a, conv))
+                for a, conv in retired:
+                    batch.remove(a.solver)
+                    res = Result(a.req.rid, a.req.arrival, a.admitted, now(), a.steps, a.cd, conv,
+                                 a.solver.n, a.tris, a.bytes)
+                    if on_retire is not None:
+                        on_retire(res, a.solver)
+                    a.solver.close()
+                    used -= a.bytes
+                    active.remove(a)
+                    results.append(res)
+        finally:
+            todo.put(None)
+            worker.join()
+            while not done.empty():
+                item = done.get()
+                if not isinstance(item[3], Exception):
+                    item[3][0].close()
+            for a in active:
+                batch.remove(a.solver)
+                a.solver.close()
+            batch.close()
+        wall = now()
+        return {"results": sorted(results, key=lambda r: r.rid), "summary": summarize(results, wall, cell_steps)}
+
+
+def summarize(results: list[Result], wall: float, cell_steps: int) -> dict:
+    lat = np.array([r.latency for r in results], np.float64)
+    pct = (lambda q: float(np.percentile(lat, q))) if len(lat) else (lambda q: float("nan"))
+    return {"requests": len(results), "converged": int(sum(r.converged for r in results)),
+            "wall_s": round(wall, 3), "solves_per_hour": round(3600.0 * len(results) / wall, 1) if wall > 0 else 0.0,
+            "converged_per_hour": round(3600.0 * sum(r.converged for r in results) / wall, 1) if wall > 0 else 0.0,
+            "p50_s": round(pct(50), 3), "p95_s": round(pct(95), 3), "p99_s": round(pct(99), 3),
+            "mlups": round(cell_steps / wall / 1e6, 1) if wall > 0 else 0.0,
+            "steps_total": int(sum(r.steps for r in results))}
+
+
+def sequential_plain(requests: list[Request], steps_of: dict, sample_steps: int = 200) -> dict:
+    """One-at-a-time plain FP32 solves of the same requests: each domain alone
+    (single-domain path, FP32 storage) timed over `sample_steps` steps; its
+    solve time is setup + per-step time x the steps the request needed
+    (`steps_of[rid]`, from the served run: the same convergence rule)."""
+    total = 0.0
+    cells_steps = 0
+    for req in requests:
+        t = time.perf_counter()
+        s, _, _, _, _ = domain_for(req, "fp32")
+        setup = time.perf_counter() - t
+        s.step(2)
+        s.step(sample_steps)
+        per = s.last_step_ms() * 1e-3 / sample_steps
+        s.close()
+        n = steps_of.get(req.rid, 0)
+        total += setup + per * n
+        cells_steps += req.grid[0] * req.grid[1] * req.grid[2] * n
+    return {"wall_s_estimated": round(total, 3),
+            "solves_per_hour": round(3600.0 * len(requests) / total, 1) if total > 0 else 0.0,
+            "mlups": round(cells_steps / total / 1e6, 1) if total > 0 else 0.0,
+            "sample_steps": sample_steps}

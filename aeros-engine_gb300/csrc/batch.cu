@@ -28,12 +28,12 @@ struct aeros_batch {
     int sm_count = 1, occ = 1;
     // device tables
     BatchDomain* d_doms = nullptr;
-    int cap_doms = 0;
+    long long cap_doms = 0;
+    BatchAcc* d_acc = nullptr;
+    long long cap_acc = 0;
     BatchWork* d_work = nullptr;
-    int cap_work = 0, nwork = 0;
-    Partial* d_parts = nullptr;
-    long long cap_parts = 0;
-    unsigned int* d_done = nullptr;
+    long long cap_work = 0;
+    int nwork = 0, nshell_items = 0;
     BatchCtl* d_ctl = nullptr;
     // pinned staging of what every call uploads
     BatchDomain* h_doms = nullptr;
@@ -73,59 +73,23 @@ int grow(T** p, long long need, long long* cap) {
     return AEROS_OK;
 }
 
-// Tile t of a domain is a shell tile when t % k == 0 and t / k < shell tiles
-// (the spreading rule of process_tile).
-bool is_shell_tile(const StepArgs& A, int t) {
-    const int nsh = A.ntiles - A.ntiles_interior;
-    return nsh > 0 && (t % A.shell_stride) == 0 && t / A.shell_stride < nsh;
-}
-
-// Work-list and device tables for the current members and tuning.
+// Work-list and device tables for the current members and tuning. Items are
+// runs of 32-cell slices: the shell items of every member (shell launch),
+// then the interior items (interior launch).
 int rebuild(aeros_batch* b) {
     drop_graph(b);
     const int nd = (int)b->members.size();
-    std::vector<StepArgs> args(nd);
-    std::vector<int> base(nd);
-    long long parts = 0;
-    for (int i = 0; i < nd; ++i) {
-        base_args(b->members[i], args[i]);
-        base[i] = (int)parts;
-        parts += args[i].ntiles;
-    }
-    const int tpi = std::max(1, b->tune.tiles_per_item);
     std::vector<BatchWork> work;
-    auto add_runs = [&](int d, bool want_shell, bool any) {
-        const StepArgs& A = args[d];
-        int t = 0;
-        while (t < A.ntiles) {
-            if (!any && is_shell_tile(A, t) != want_shell) { ++t; continue; }
-            int n = 1;
-            if (!(want_shell && !any))   // shell tiles are not adjacent: one per item
-                while (n < tpi && t + n < A.ntiles && (any || !is_shell_tile(A, t + n))) ++n;
-            work.push_back(BatchWork{d, t, n, 0});
-            t += n;
-        }
+    auto runs = [&](int d, int kind, int n, int step) {
+        for (int s0 = 0; s0 < n; s0 += step) work.push_back(BatchWork{d, kind, s0, std::min(step, n - s0)});
     };
-    if (b->tune.shell_first) {
-        for (int d = 0; d < nd; ++d) add_runs(d, true, false);
-        for (int d = 0; d < nd; ++d) add_runs(d, false, false);
-    } else {
-        for (int d = 0; d < nd; ++d) add_runs(d, false, true);
-    }
-    long long cap = b->cap_doms;
-    if (int rc = grow(&b->d_doms, std::max(1, nd), &cap)) return rc;
-    if (cap != b->cap_doms) {
-        cudaFree(b->d_done);
-        b->d_done = nullptr;
-        if (cudaMalloc((void**)&b->d_done, (size_t)cap * sizeof(unsigned int)) != cudaSuccess)
-            return set_error(AEROS_ERR_ALLOC, "batch counters");
-        b->cap_doms = (int)cap;
-    }
-    CUDA_TRY(cudaMemsetAsync(b->d_done, 0, (size_t)b->cap_doms * sizeof(unsigned int), b->stream));
-    cap = b->cap_work;
-    if (int rc = grow(&b->d_work, std::max<long long>(1, (long long)work.size()), &cap)) return rc;
-    b->cap_work = (int)cap;
-    if (int rc = grow(&b->d_parts, std::max<long long>(1, parts), &b->cap_parts)) return rc;
+    for (int d = 0; d < nd; ++d) runs(d, 0, (b->members[d]->n_shell + 31) / 32, 8 * b->tune.shell_tiles_per_item);
+    b->nshell_items = (int)work.size();
+    for (int d = 0; d < nd; ++d) runs(d, 1, (b->members[d]->n_interior + 31) / 32, 8 * b->tune.tiles_per_item);
+    if (int rc = grow(&b->d_doms, std::max(1, nd), &b->cap_doms)) return rc;
+    if (int rc = grow(&b->d_acc, std::max(1, nd), &b->cap_acc)) return rc;
+    CUDA_TRY(cudaMemsetAsync(b->d_acc, 0, (size_t)b->cap_acc * sizeof(BatchAcc), b->stream));
+    if (int rc = grow(&b->d_work, std::max<long long>(1, (long long)work.size()), &b->cap_work)) return rc;
     if (!work.empty())
         CUDA_TRY(cudaMemcpyAsync(b->d_work, work.data(), work.size() * sizeof(BatchWork), cudaMemcpyHostToDevice,
                                  b->stream));
@@ -138,30 +102,42 @@ int rebuild(aeros_batch* b) {
             return set_error(AEROS_ERR_ALLOC, "pinned batch table");
         b->cap_h_doms = nd;
     }
-    for (int i = 0; i < nd; ++i) b->h_doms[i].part_base = base[i];
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     b->dirty = false;
     return AEROS_OK;
 }
 
-BatchArgs batch_args(const aeros_batch* b) {
+BatchArgs batch_args(const aeros_batch* b, int kind) {
     BatchArgs B;
     B.doms = b->d_doms;
     B.work = b->d_work;
-    B.nwork = b->nwork;
-    B.partials = b->d_parts;
-    B.done = b->d_done;
+    B.item_begin = kind == 0 ? 0 : b->nshell_items;
+    B.item_end = kind == 0 ? b->nshell_items : b->nwork;
+    B.acc = b->d_acc;
     B.ctl = b->d_ctl;
     return B;
 }
 
+int shell_grid_of(const aeros_batch* b) {
+    return std::max(1, std::min(b->nshell_items, b->sm_count * b->occ));
+}
+
+// One lattice step: the shell launch (when any member has shell items), then
+// the interior launch.
+cudaError_t launch_step(const aeros_batch* b, bool odd, cudaStream_t s) {
+    cudaError_t e = cudaSuccess;
+    if (b->nshell_items > 0) e = b->L->batch_step(batch_args(b, 0), odd, 0, shell_grid_of(b), s);
+    if (e == cudaSuccess) e = b->L->batch_step(batch_args(b, 1), odd, 1, grid_of(b), s);
+    return e;
+}
+
+int launches_per_step(const aeros_batch* b) { return b->nshell_items > 0 ? 2 : 1; }
+
 int capture(aeros_batch* b, int steps) {
     drop_graph(b);
-    const BatchArgs B = batch_args(b);
-    const int grid = grid_of(b);
     CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t le = cudaSuccess;
-    for (int i = 0; i < steps && le == cudaSuccess; ++i) le = b->L->batch_step(B, (i & 1) != 0, grid, b->stream);
+    for (int i = 0; i < steps && le == cudaSuccess; ++i) le = launch_step(b, (i & 1) != 0, b->stream);
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -201,7 +177,7 @@ extern "C" int aeros_batch_create(int storage, aeros_batch** out) {
          : storage == AEROS_STORE_FP16 ? &launchers_fp16() : &launchers_bf16();
     b->tune.blocks_per_sm = 0;
     b->tune.tiles_per_item = 1;
-    b->tune.shell_first = 1;
+    b->tune.shell_tiles_per_item = 1;
     b->tune.chunk_steps = 20;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -226,9 +202,8 @@ extern "C" int aeros_batch_destroy(aeros_batch* b) {
     for (aeros_lbm* h : b->members) h->batch = nullptr;
     drop_graph(b);
     cudaFree(b->d_doms);
+    cudaFree(b->d_acc);
     cudaFree(b->d_work);
-    cudaFree(b->d_parts);
-    cudaFree(b->d_done);
     cudaFree(b->d_ctl);
     if (b->h_doms) cudaFreeHost(b->h_doms);
     if (b->h_ctl) cudaFreeHost(b->h_ctl);
@@ -288,7 +263,6 @@ extern "C" int aeros_batch_step(aeros_batch* b, int nsteps) {
     for (int i = 0; i < nd; ++i) {
         aeros_lbm* h = b->members[i];
         BatchDomain& D = b->h_doms[i];
-        const int base = D.part_base;
         memset(&D, 0, sizeof(D));
         base_args(h, D.A);
         D.u[0] = h->u[0];
@@ -299,10 +273,10 @@ extern "C" int aeros_batch_step(aeros_batch* b, int nsteps) {
         D.outpar0 = h->out_par;
         D.overrides0 = h->overrides_next ? 1 : 0;
         D.les = h->p.use_les ? 1 : 0;
-        D.part_base = base;
+        D.nslices = (h->n_shell + 31) / 32 + (h->n_interior + 31) / 32;
         h->kexec_before = h->ctl_host->kexec;
     }
-    *b->h_ctl = BatchCtl{0u, 0u, 0, nsteps - 1};
+    *b->h_ctl = BatchCtl{{0u, 0u}, {0u, 0u}, 0, nsteps - 1};
     const int chunk = std::max(2, b->tune.chunk_steps & ~1);
     if (!b->graph || b->graph_steps != chunk)
         if (int rc = capture(b, chunk)) return rc;
@@ -312,8 +286,7 @@ extern "C" int aeros_batch_step(aeros_batch* b, int nsteps) {
     CUDA_TRY(cudaEventRecord(b->ev0, b->stream));
     const int reps = nsteps / chunk, rest = nsteps % chunk;
     for (int r = 0; r < reps; ++r) CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
-    const BatchArgs B = batch_args(b);
-    for (int i = 0; i < rest; ++i) CUDA_TRY(b->L->batch_step(B, (i & 1) != 0, grid_of(b), b->stream));
+    for (int i = 0; i < rest; ++i) CUDA_TRY(launch_step(b, (i & 1) != 0, b->stream));
     CUDA_TRY(cudaEventRecord(b->ev1, b->stream));
     for (aeros_lbm* h : b->members)
         CUDA_TRY(cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(Control), cudaMemcpyDeviceToHost, b->stream));
@@ -321,7 +294,7 @@ extern "C" int aeros_batch_step(aeros_batch* b, int nsteps) {
     float ms = 0.0f;
     CUDA_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms / (float)nsteps;
-    b->last_launches = nsteps;
+    b->last_launches = (long long)nsteps * launches_per_step(b);
     int rc_all = AEROS_OK;
     for (aeros_lbm* h : b->members) {
         // the same bookkeeping as nsteps (even) steps of aeros_lbm_step
@@ -337,13 +310,13 @@ extern "C" int aeros_batch_step(aeros_batch* b, int nsteps) {
 extern "C" int aeros_batch_set_tuning(aeros_batch* b, const aeros_batch_tuning* t) {
     if (!b || !t) return set_error(AEROS_ERR_INVALID, "NULL argument");
     if (t->blocks_per_sm < 0 || t->blocks_per_sm > 64) return set_error(AEROS_ERR_INVALID, "blocks_per_sm %d", t->blocks_per_sm);
-    if (t->tiles_per_item != 1 && t->tiles_per_item != 2 && t->tiles_per_item != 4 && t->tiles_per_item != 8)
-        return set_error(AEROS_ERR_INVALID, "tiles_per_item %d (1, 2, 4 or 8)", t->tiles_per_item);
+    for (int v : {t->tiles_per_item, t->shell_tiles_per_item})
+        if (v != 1 && v != 2 && v != 4 && v != 8)
+            return set_error(AEROS_ERR_INVALID, "tiles per item %d (1, 2, 4 or 8)", v);
     if (t->chunk_steps < 2 || (t->chunk_steps & 1) || t->chunk_steps > 10000)
         return set_error(AEROS_ERR_INVALID, "chunk_steps %d (even, 2..10000)", t->chunk_steps);
     CUDA_TRY(cudaStreamSynchronize(b->stream));
     b->tune = *t;
-    b->tune.shell_first = t->shell_first ? 1 : 0;
     b->dirty = true;
     return AEROS_OK;
 }
@@ -369,7 +342,7 @@ extern "C" int aeros_batch_autotune(aeros_batch* b, int trial_steps, aeros_batch
             aeros_batch_tuning t = start;
             t.blocks_per_sm = p;
             t.tiles_per_item = tpi;
-            t.shell_first = 1;
+            t.shell_tiles_per_item = 1;
             t.chunk_steps = std::max(2, std::min(start.chunk_steps, trial_steps));
             cand.push_back(t);
         }
@@ -387,9 +360,11 @@ extern "C" int aeros_batch_autotune(aeros_batch* b, int trial_steps, aeros_batch
     };
     for (const auto& t : cand)
         if (int rc = trial(t)) return rc;
-    aeros_batch_tuning alt = pick;
-    alt.shell_first = 0;
-    if (int rc = trial(alt)) return rc;
+    for (int stpi : {2, 4}) {
+        aeros_batch_tuning alt = pick;
+        alt.shell_tiles_per_item = stpi;
+        if (int rc = trial(alt)) return rc;
+    }
     pick.chunk_steps = start.chunk_steps;
     if (int rc = aeros_batch_set_tuning(b, &pick)) return rc;
     if (best) *best = pick;

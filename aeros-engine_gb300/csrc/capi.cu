@@ -309,7 +309,9 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return fail(e, "cudaEventCreate");
     {
         uint8_t* dm = nullptr;
-        if ((e = cudaMalloc((void**)&dm, 3 * n)) != cudaSuccess) return fail(e, "descriptor scratch");
+        // stream-ordered scratch and stream syncs only: creating a domain does
+        // not wait for work other streams have in flight (a running batch)
+        if ((e = cudaMallocAsync((void**)&dm, 3 * n, nullptr)) != cudaSuccess) return fail(e, "descriptor scratch");
         DescArgs da;
         da.nx = h->nx; da.ny = h->ny; da.nz = h->nz;
         da.flow_axis = params->flow_axis;
@@ -322,8 +324,8 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         da.outlet_mode = h->outlet_mode;
         e = cudaMemcpy(dm, h->mask.data(), n, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = build_descriptors(da, dm, dm + n, dm + 2 * n, h->desc, nullptr);
-        if (e == cudaSuccess) e = cudaDeviceSynchronize();
-        cudaFree(dm);
+        cudaFreeAsync(dm, nullptr);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
         if (e != cudaSuccess) return fail(e, "descriptor build");
     }
     if (h->n_shell && (e = cudaMemcpy(h->shell, shell.data(), shell.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -383,7 +385,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
                 return fail(e, "outlet buffer init");
         }
     }
-    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "init");
+    if ((e = cudaStreamSynchronize(nullptr)) != cudaSuccess) return fail(e, "init");
     for (int o = 0; o < 2; ++o)
         for (int t = 0; t < 2; ++t) h->grid[o][t] = std::min(h->max_grid, std::max(1, h->sm_count) * h->L->occupancy(o, t));
     h->stats.avg_rho = 1.0f;
@@ -1024,14 +1026,15 @@ extern "C" int aeros_voxelize(const float* tris, int64_t ntri, const aeros_voxel
     if (!mask_out) return set_error(AEROS_ERR_INVALID, "mask is NULL");
     const size_t total = (size_t)g->nx * g->ny * g->nz;
     uint8_t* d = nullptr;
-    if (cudaMalloc((void**)&d, total) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "mask buffer");
+    if (cudaMallocAsync((void**)&d, total, nullptr) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "mask buffer");
     char err[512] = {0};
     int rc = voxelize_impl(tris, ntri, g, d, nullptr, err, sizeof(err));
     if (rc == AEROS_OK) {
-        cudaError_t e = cudaMemcpy(mask_out, d, total, cudaMemcpyDeviceToHost);
+        cudaError_t e = cudaMemcpyAsync(mask_out, d, total, cudaMemcpyDeviceToHost, nullptr);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
         if (e != cudaSuccess) snprintf(err, sizeof(err), "mask copy: %s", cudaGetErrorString(e)), rc = AEROS_ERR_CUDA;
     }
-    cudaFree(d);
+    cudaFreeAsync(d, nullptr);
     if (rc) return set_error(rc, "%s", err);
     return AEROS_OK;
 }

@@ -137,7 +137,7 @@ struct Launchers {
     cudaError_t (*reset)(void* f, const uint32_t* desc, long long qstride, int ncell, const FillArgs& fa, float* rho,
                          float4* u, const float* uin, cudaStream_t s);
     cudaError_t (*thermal_fill)(const StepArgs& A, float tref, cudaStream_t s);
-    cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int grid, cudaStream_t s);
+    cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s);
     int (*batch_occupancy)();
 };
 
@@ -207,15 +207,20 @@ const Launchers& launchers_bf16();
         k_thermal_prestream<STORE><<<(A.ncell + 255) / 256, 256, 0, s>>>(A, tref);                                    \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    cudaError_t batch_(const BatchArgs& B, bool odd, int grid, cudaStream_t s) {                                     \
-        if (odd) k_batch_step<STORE, true><<<grid, STEP_BLOCK, 0, s>>>(B);                                            \
-        else k_batch_step<STORE, false><<<grid, STEP_BLOCK, 0, s>>>(B);                                               \
+    cudaError_t batch_(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s) {                          \
+        if (kind == 0) {                                                                                              \
+            if (odd) k_batch_step<STORE, true, 0><<<grid, STEP_BLOCK, 0, s>>>(B);                                     \
+            else k_batch_step<STORE, false, 0><<<grid, STEP_BLOCK, 0, s>>>(B);                                        \
+        } else {                                                                                                      \
+            if (odd) k_batch_step<STORE, true, 1><<<grid, STEP_BLOCK, 0, s>>>(B);                                     \
+            else k_batch_step<STORE, false, 1><<<grid, STEP_BLOCK, 0, s>>>(B);                                        \
+        }                                                                                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
     int batch_occ_() {                                                                                                \
         int n = 0, m = 0;                                                                                             \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<STORE, false>, STEP_BLOCK, 0);                 \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_batch_step<STORE, true>, STEP_BLOCK, 0);                  \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<STORE, false, 1>, STEP_BLOCK, 0);              \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_batch_step<STORE, true, 1>, STEP_BLOCK, 0);               \
         n = n < m ? n : m;                                                                                            \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \

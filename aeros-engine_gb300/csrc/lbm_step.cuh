@@ -846,6 +846,7 @@ __device__ __forceinline__ void block_reduce_store(const Acc& a, Partial* out) {
 
 // Last block: sums the partials in block order and updates the control block
 // (aeros/src/lbm.cpp:1313-1319 and 1554-1580).
+static __device__ __noinline__ void apply_totals(const StepArgs& A, const double t[5], float m, const long long c[8]);
 template <int BLOCK>
 __device__ void finish_totals(const StepArgs& A, const Partial* parts, int nparts);
 
@@ -896,6 +897,14 @@ __device__ void finish_totals(const StepArgs& A, const Partial* parts, int npart
         m = fmaxf(m, s_m[j]);
         for (int k = 0; k < 8; ++k) c[k] += s_i[k][j];
     }
+    apply_totals(A, t, m, c);
+}
+
+// Updates the domain's control block from the step's totals: t = sums of
+// (rho - 1), |u|^2, TKE, Nusselt rows, T; m = max |u|^2; c = counters (NaN,
+// negative, bad, rho out of range, rho non-finite, u limited, Nusselt cells,
+// fluid cells). One thread.
+static __device__ __noinline__ void apply_totals(const StepArgs& A, const double t[5], float m, const long long c[8]) {
     Control* ctl = A.ctl;
     ctl->blocks_done = 0;
     ctl->tile_next = 0;
@@ -934,10 +943,9 @@ __device__ void finish_totals(const StepArgs& A, const Partial* parts, int npart
     }
 }
 
-// Shell tile st: shell cells st*STEP_BLOCK ... in increasing cell order.
+// Shell cell si (shell cells are listed in increasing cell order).
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __forceinline__ void shell_tile(const StepArgs& A, const StepVar& V, int st, Acc& acc) {
-    const int si = st * STEP_BLOCK + (int)threadIdx.x;
+__device__ __forceinline__ void shell_cell(const StepArgs& A, const StepVar& V, int si, Acc& acc) {
     if (si < A.n_shell) {
         const int cell = A.shell[si];
         const uint32_t r = A.div_x.div((uint32_t)cell);
@@ -948,11 +956,9 @@ __device__ __forceinline__ void shell_tile(const StepArgs& A, const StepVar& V, 
     }
 }
 
-// Interior tile it: interior cells (x, y, z in 1 .. n-2) it*STEP_BLOCK ... in
-// x-fastest order.
+// Interior cell li: the interior (x, y, z in 1 .. n-2) in x-fastest order.
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __forceinline__ void interior_tile(const StepArgs& A, const StepVar& V, int it, Acc& acc) {
-    const int li = it * STEP_BLOCK + (int)threadIdx.x;
+__device__ __forceinline__ void interior_cell(const StepArgs& A, const StepVar& V, int li, Acc& acc) {
     if (li < A.n_interior) {
         const uint32_t r = A.div_ix.div((uint32_t)li);
         const int x = li - (int)r * (A.nx - 2) + 1;
@@ -961,6 +967,16 @@ __device__ __forceinline__ void interior_tile(const StepArgs& A, const StepVar& 
         const int z = (int)zq + 1;
         process_interior<S, ODD, THERMAL, MAT>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc);
     }
+}
+
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __forceinline__ void shell_tile(const StepArgs& A, const StepVar& V, int st, Acc& acc) {
+    shell_cell<S, ODD, THERMAL, MAT>(A, V, st * STEP_BLOCK + (int)threadIdx.x, acc);
+}
+
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __forceinline__ void interior_tile(const StepArgs& A, const StepVar& V, int it, Acc& acc) {
+    interior_cell<S, ODD, THERMAL, MAT>(A, V, it * STEP_BLOCK + (int)threadIdx.x, acc);
 }
 
 template <class S, bool ODD, bool THERMAL, bool MAT>
@@ -1012,11 +1028,15 @@ __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_interior(co
 }
 
 // ---- many domains in one persistent kernel -----------------------------------
-// Work items are runs of tiles of one domain (shell tiles of every domain
-// first, then interior tiles); blocks take items from a global counter. Each
-// tile stores its own partial statistics and the block that completes a
-// domain's last tile sums that domain's partials in tile order, so a domain's
-// results do not depend on the schedule, the tuning or the other domains.
+// Warps take work items from a global counter; an item is a run of 32-cell
+// slices of one domain's shell or interior (shell items of every domain
+// first). A warp sums each slice in FP32 (a fixed shuffle tree over a fixed
+// set of 32 cells), converts the slice sums to 64-bit fixed point and adds
+// them into the domain's accumulators with integer atomics. Integer addition
+// is exact and associative, so a domain's statistics do not depend on the
+// order of the slices: not on the schedule, the tuning or the other domains.
+// The warp that finishes a domain's last slice of the step updates its control
+// block. No block-wide barrier is involved.
 struct BatchDomain {
     StepArgs A;                 // the domain's arguments (A.ctl: its control block)
     float4* u[2];               // velocity double buffer
@@ -1024,91 +1044,158 @@ struct BatchDomain {
     int ubuf0, outpar0;         // buffer parities at the first step of the call
     int overrides0;             // overrides on at the first step of the call
     int les;                    // velocity written every step
-    int part_base;              // first per-tile partial of the domain
+    int nslices;                // shell + interior slices of 32 cells
     int pad[3];
 };
 
 struct BatchWork {
-    int dom, tile, ntiles, pad;
+    int dom, kind, slice0, nslices;   // kind 0: shell slices, 1: interior slices
+};
+
+struct BatchAcc {               // per domain, zero between steps
+    unsigned long long drho, ke, tke;   // fixed point, two's complement
+    unsigned long long cnt[7];          // NaN, negative, bad, rho range, rho finite, u limited, cells
+    unsigned int maxu2;                 // float bits (values >= 0 order as integers)
+    unsigned int done;                  // slices finished this step
 };
 
 struct BatchCtl {
-    unsigned int work_next;     // next work item (reset by the last block)
-    unsigned int blocks_done;
+    unsigned int work_next[2];  // next work item of the shell / interior launch (reset by its last warp)
+    unsigned int warps_done[2];
     int k;                      // step of the call being executed
     int k_last;                 // last step of the call (writes rho, |S|, TKE)
 };
 
 struct BatchArgs {
     const BatchDomain* doms;
-    const BatchWork* work;
-    int nwork;
-    Partial* partials;          // one per tile of every domain
-    unsigned int* done;         // per domain: tiles finished this step
+    const BatchWork* work;      // shell items of every domain, then interior items
+    int item_begin, item_end;   // this launch's items
+    BatchAcc* acc;
     BatchCtl* ctl;
 };
 
-template <class S, bool ODD>
+struct WarpSums {               // one warp's sums over the slices of a work item
+    long long drho, ke, tke;    // fixed point
+    long long cnt[7];           // NaN, negative, bad, rho range, rho finite, u limited, cells
+};
+
+constexpr float FX_SUM = 1099511627776.0f;   // 2^40: sums of rho - 1 and |u|^2 per slice
+constexpr float FX_TKE = 1048576.0f;         // 2^20: TKE per slice (up to 32 x 1e6)
+
+__device__ __forceinline__ float warp_allsum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_allsum(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// KIND 0: the shell slices of every domain; KIND 1: the interior slices (one
+// launch each per step, so each launch's code is only its own path).
+template <class S, bool ODD, int KIND>
 __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_batch_step(const BatchArgs B) {
-    __shared__ __align__(16) unsigned char sA_raw[sizeof(StepArgs)];   // StepArgs is not trivially constructible
-    __shared__ int s_item, s_last;
-    StepArgs& sA = *reinterpret_cast<StepArgs*>(sA_raw);
+    // one copy of the current domain's arguments per warp
+    __shared__ __align__(16) unsigned char s_args[STEP_BLOCK / 32][sizeof(StepArgs)];
+    __shared__ WarpSums s_sums[STEP_BLOCK / 32];
+    const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
+    StepArgs& A = *reinterpret_cast<StepArgs*>(s_args[wid]);   // StepArgs is not trivially constructible
     const int k = B.ctl->k;
     const bool write_obs = k == B.ctl->k_last;
     int cur = -1;
     for (;;) {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(&B.ctl->work_next, 1u);
-        __syncthreads();
-        const int item = s_item;
-        if (item >= B.nwork) break;
+        int item = 0;
+        if (lane == 0) item = B.item_begin + (int)atomicAdd(&B.ctl->work_next[KIND], 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= B.item_end) break;
         const BatchWork wk = B.work[item];
         const BatchDomain& D = B.doms[wk.dom];
-        if (wk.dom != cur) {   // the domain's arguments into shared memory
+        if (wk.dom != cur) {
+            __syncwarp();
             const int* src = reinterpret_cast<const int*>(&D.A);
-            int* dst = reinterpret_cast<int*>(&sA);
-            for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / 4); i += STEP_BLOCK) dst[i] = src[i];
+            int* dst = reinterpret_cast<int*>(s_args[wid]);
+            for (int i = lane; i < (int)(sizeof(StepArgs) / 4); i += 32) dst[i] = src[i];
+            __syncwarp();
             cur = wk.dom;
-            __syncthreads();
         }
-        const StepArgs& A = sA;
         // a halted domain stays halted for the rest of the call (its flag is
-        // only set by its own finisher, after its last tile of a step)
-        if (!*(volatile int*)&A.ctl->halt) {
-            StepVar V;
-            V.up = D.u[(D.ubuf0 ^ k) & 1];
-            V.uc = D.u[(D.ubuf0 ^ k ^ 1) & 1];
-            V.out_w = D.out[(D.outpar0 ^ k) & 1];
-            V.out_r = D.out[(D.outpar0 ^ k ^ 1) & 1];
-            V.apply_overrides = D.overrides0 || k > 0;
-            V.write_obs = write_obs;
-            V.write_u = D.les || write_obs;
-            for (int t = 0; t < wk.ntiles; ++t) {
-                Acc acc;
-                acc.zero();
-                process_tile<S, ODD, false, false>(A, V, wk.tile + t, acc);
-                block_reduce_store<STEP_BLOCK>(acc, B.partials + D.part_base + wk.tile + t);
-                __syncthreads();
+        // only set by its own finisher, after its last slice of a step)
+        if (*(volatile int*)&A.ctl->halt) continue;
+        StepVar V;
+        V.up = D.u[(D.ubuf0 ^ k) & 1];
+        V.uc = D.u[(D.ubuf0 ^ k ^ 1) & 1];
+        V.out_w = D.out[(D.outpar0 ^ k) & 1];
+        V.out_r = D.out[(D.outpar0 ^ k ^ 1) & 1];
+        V.apply_overrides = D.overrides0 || k > 0;
+        V.write_obs = write_obs;
+        V.write_u = D.les || write_obs;
+        WarpSums& W = s_sums[wid];
+        if (lane == 0) {
+            W.drho = W.ke = W.tke = 0;
+            for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
+        }
+        float mx = 0.0f;   // per lane, reduced once per item
+        for (int sl = 0; sl < wk.nslices; ++sl) {
+            Acc acc;
+            acc.zero();
+            const int idx = (wk.slice0 + sl) * 32 + lane;
+            if (KIND == 0) shell_cell<S, ODD, false, false>(A, V, idx, acc);
+            else interior_cell<S, ODD, false, false>(A, V, idx, acc);
+            const float sd = warp_allsum(acc.drho), sk = warp_allsum(acc.ke), st = warp_allsum(acc.tke);
+            mx = fmaxf(mx, acc.maxu2);
+            const int cells = __popc(__ballot_sync(0xffffffffu, acc.cells != 0));
+            const bool rare = __any_sync(0xffffffffu, (acc.nan | acc.neg | acc.bad | acc.rout | acc.rnf | acc.ulim) != 0);
+            int c6[6] = {0, 0, 0, 0, 0, 0};
+            if (rare) {
+                c6[0] = warp_allsum(acc.nan); c6[1] = warp_allsum(acc.neg); c6[2] = warp_allsum(acc.bad);
+                c6[3] = warp_allsum(acc.rout); c6[4] = warp_allsum(acc.rnf); c6[5] = warp_allsum(acc.ulim);
             }
-            if (threadIdx.x == 0) {
-                __threadfence();
-                const unsigned int n = atomicAdd(B.done + wk.dom, (unsigned int)wk.ntiles) + (unsigned int)wk.ntiles;
-                s_last = n == (unsigned int)A.ntiles;
-            }
-            __syncthreads();
-            if (s_last) {
-                __threadfence();
-                finish_totals<STEP_BLOCK>(A, B.partials + D.part_base, A.ntiles);
-                if (threadIdx.x == 0) B.done[wk.dom] = 0;
+            if (lane == 0) {
+                W.drho += __float2ll_rn(sd * FX_SUM);
+                W.ke += __float2ll_rn(sk * FX_SUM);
+                W.tke += __float2ll_rn(st * FX_TKE);
+                W.cnt[6] += cells;
+                if (rare)
+                    for (int j = 0; j < 6; ++j) W.cnt[j] += c6[j];
             }
         }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __syncwarp();
+        BatchAcc* ac = B.acc + wk.dom;
+        // one atomic per lane
+        if (lane == 0) atomicAdd(&ac->drho, (unsigned long long)W.drho);
+        else if (lane == 1) atomicAdd(&ac->ke, (unsigned long long)W.ke);
+        else if (lane == 2) atomicAdd(&ac->tke, (unsigned long long)W.tke);
+        else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ac->cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
+        else if (lane == 10 && mx > 0.0f) atomicMax(&ac->maxu2, __float_as_uint(mx));
         __threadfence();
-        if (atomicAdd(&B.ctl->blocks_done, 1u) == gridDim.x - 1) {
-            B.ctl->work_next = 0;
-            B.ctl->blocks_done = 0;
-            B.ctl->k = k + 1;
+        __syncwarp();
+        int last = 0;
+        if (lane == 0) last = atomicAdd(&ac->done, (unsigned int)wk.nslices) + (unsigned int)wk.nslices == (unsigned int)D.nslices;
+        if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
+            __threadfence();
+            volatile BatchAcc* va = ac;
+            const double t[5] = {(double)(long long)va->drho / (double)FX_SUM, (double)(long long)va->ke / (double)FX_SUM,
+                                 (double)(long long)va->tke / (double)FX_TKE, 0.0, 0.0};
+            const long long c[8] = {(long long)va->cnt[0], (long long)va->cnt[1], (long long)va->cnt[2],
+                                    (long long)va->cnt[3], (long long)va->cnt[4], (long long)va->cnt[5], 0,
+                                    (long long)va->cnt[6]};
+            apply_totals(A, t, __uint_as_float(va->maxu2), c);
+            va->drho = 0; va->ke = 0; va->tke = 0;
+            for (int j = 0; j < 7; ++j) va->cnt[j] = 0;
+            va->maxu2 = 0;
+            va->done = 0;
+        }
+    }
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(&B.ctl->warps_done[KIND], 1u) == gridDim.x * (STEP_BLOCK / 32) - 1) {
+            B.ctl->work_next[KIND] = 0;
+            B.ctl->warps_done[KIND] = 0;
+            if (KIND == 1) B.ctl->k = k + 1;
         }
     }
 }

@@ -221,9 +221,10 @@ int voxelize_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, ui
     DNode* dn = nullptr;
     float* dt = nullptr;
     int* dof = nullptr;
-    cudaError_t e = cudaMalloc((void**)&dn, b.nodes.size() * sizeof(DNode));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&dt, flat.size() * 4);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&dof, 4);
+    // stream-ordered scratch: voxelizing does not wait for other streams' work
+    cudaError_t e = cudaMallocAsync((void**)&dn, b.nodes.size() * sizeof(DNode), s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dt, flat.size() * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dof, 4, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dn, b.nodes.data(), b.nodes.size() * sizeof(DNode), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dt, flat.data(), flat.size() * 4, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(dof, 0, 4, s);
@@ -238,10 +239,10 @@ int voxelize_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, ui
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(&overflow, dof, 4, cudaMemcpyDeviceToHost, s);
+    if (dn) cudaFreeAsync(dn, s);
+    if (dt) cudaFreeAsync(dt, s);
+    if (dof) cudaFreeAsync(dof, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(dn);
-    cudaFree(dt);
-    cudaFree(dof);
     if (e != cudaSuccess) { snprintf(err, errn, "voxelize: %s", cudaGetErrorString(e)); return AEROS_ERR_CUDA; }
     if (overflow) { snprintf(err, errn, "voxelize: BVH traversal stack overflow"); return AEROS_ERR_UNSUPPORTED; }
     return AEROS_OK;

@@ -246,7 +246,7 @@ def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20, chunk=1
     tune = b.autotune(trial_steps=20) if autotune else b.tuning
     tune_s = time.time() - t1
     b.set_tuning(blocks_per_sm=tune["blocks_per_sm"], tiles_per_item=tune["tiles_per_item"],
-                 shell_first=tune["shell_first"], chunk_steps=chunk)
+                 shell_tiles_per_item=tune["shell_tiles_per_item"], chunk_steps=chunk)
     b.step(100)   # capture + warm-up
     b.step(steps)
     ms = b.last_step_ms()
@@ -262,6 +262,29 @@ def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20, chunk=1
             "sequential_mlups": round(seq_mlups, 1), "speedup_vs_sequential": round(mlups / seq_mlups, 3),
             "tuning": tune, "autotune_s": round(tune_s, 2), "setup_s": round(setup_s, 2), "gpu_launches": int(launches),
             "diverged_domains": int(diverged)}
+
+
+def serve_session(n_requests=16, rate=2.0, max_steps=30000, seq_sample=200):
+    """The request loop: n_requests Poisson arrivals (rate per second) served
+    by continuous batching (FP16), once in real time (latency percentiles) and
+    once with every request queued at the start (throughput); the same
+    requests solved one at a time in plain FP32 beside it."""
+    from aeros_gb300 import serve
+    reqs = serve.make_requests(n_requests, rate=rate)
+    srv = serve.Server(storage="fp16", max_steps=max_steps)
+    live = srv.run(reqs, realtime=True)
+    sat = srv.run(reqs, realtime=False)
+    steps_of = {r.rid: r.steps for r in sat["results"]}
+    seq = serve.sequential_plain(reqs, steps_of, sample_steps=seq_sample)
+    conv_seq = sum(r.converged for r in sat["results"])
+    seq_conv_per_h = 3600.0 * conv_seq / seq["wall_s_estimated"] if seq["wall_s_estimated"] > 0 else 0.0
+    return {"requests": n_requests, "rate_per_s": rate, "realtime": live["summary"], "saturated": sat["summary"],
+            "sequential_fp32": seq, "sequential_converged_per_hour": round(seq_conv_per_h, 1),
+            "speedup_solves_per_hour": round(sat["summary"]["solves_per_hour"] / seq["solves_per_hour"], 3)
+            if seq["solves_per_hour"] > 0 else None,
+            "per_request": [dict(rid=r.rid, grid=reqs[r.rid].grid, level=reqs[r.rid].level, re=round(reqs[r.rid].re, 1),
+                                 steps=r.steps, cd=round(r.cd, 5), converged=r.converged,
+                                 latency_s=round(r.latency, 3)) for r in live["results"]]}
 
 
 def cpu_baseline(mask, steps):
@@ -333,7 +356,10 @@ def main():
     ap.add_argument("--only", default="both", choices=["both", "fp32", "fp16", "bf16"],
                     help="time one storage form only (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "serve"])
+    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-rate", type=float, default=2.0)
+    ap.add_argument("--serve-max-steps", type=int, default=30000)
     ap.add_argument("--batch-domains", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=10000)
     ap.add_argument("--batch-chunk", type=int, default=100, help="steps per captured CUDA graph")
@@ -344,6 +370,9 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serve":
+        r = serve_session(args.serve_requests, args.serve_rate, args.serve_max_steps)
+        print(json.dumps(r), flush=True)
     elif args.workload == "batch":
         r = batch_sweep(args.batch_domains, args.batch_steps, chunk=args.batch_chunk, autotune=not args.batch_fixed)
         print(json.dumps(r), flush=True)

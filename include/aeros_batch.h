@@ -8,12 +8,13 @@
  * and steps the batch. Reading fields, forces or statistics of a member goes
  * through the member's own aeros_lbm handle, as for a lone domain.
  *
- * Device side: one persistent kernel per lattice step walks a work-list of
- * tiles of every member (shell tiles first), and a chunk of steps is captured
- * once as a CUDA graph and replayed. Per-tile partial statistics reduced in
- * tile order make every member's state and statistics independent of the
- * other members, of the schedule and of the tuning: a domain gives the same
- * bits alone as in any mix.
+ * Device side: per lattice step, two persistent launches (the boundary
+ * shells of every member, then the interiors) whose warps take work items
+ * from a global counter, and a chunk of steps is captured once as a CUDA
+ * graph and replayed. Statistics are summed per 32-cell slice and added in
+ * exact fixed point, which makes every member's state and statistics
+ * independent of the other members, of the schedule and of the tuning: a
+ * domain gives the same bits alone as in any mix.
  *
  * Status codes and aeros_consume_error() are those of aeros_lbm.h.
  */
@@ -30,12 +31,14 @@ extern "C" {
 
 typedef struct aeros_batch aeros_batch;
 
-/* Launch shape of the batch kernel. */
+/* Launch shape of the batch kernels. A lattice step is two launches: the
+ * boundary shells of all members, then their interiors. Work items are runs
+ * of 256-cell tiles taken by warps from a global counter. */
 typedef struct aeros_batch_tuning {
-    int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid (0: occupancy limit) */
-    int32_t tiles_per_item;  /* tiles (256 cells each) per work item: 1, 2, 4 or 8                */
-    int32_t shell_first;     /* 1: boundary-shell tiles of all members ahead of interior tiles  */
-    int32_t chunk_steps;     /* steps per captured graph (even, >= 2)                            */
+    int32_t blocks_per_sm;         /* resident blocks per SM of the interior grid (0: occupancy limit) */
+    int32_t tiles_per_item;        /* interior tiles per work item: 1, 2, 4 or 8                       */
+    int32_t shell_tiles_per_item;  /* shell tiles per work item: 1, 2, 4 or 8                          */
+    int32_t chunk_steps;           /* steps per captured graph (even, >= 2)                            */
     int32_t reserved[4];
 } aeros_batch_tuning;
 

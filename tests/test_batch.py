@@ -54,7 +54,7 @@ def test_batch_members_equal_lone_domains(mods, storage):
         b.set_tuning(chunk_steps=10)
         b.step(40)
         got = [state(s) for s in members]
-        assert b.last_launch_count() == 40
+        assert b.last_launch_count() == 80   # shell + interior launch per step
     for i, g in enumerate(got):
         s, _, _ = domain(mods, i, storage)
         s.step(40)
@@ -86,8 +86,8 @@ def test_alone_and_in_mix_identical(mods):
 def test_tuning_changes_no_result(mods):
     Batch = mods[0].Batch
     outs = []
-    for tune in (dict(blocks_per_sm=1, tiles_per_item=1, shell_first=True, chunk_steps=4),
-                 dict(blocks_per_sm=0, tiles_per_item=4, shell_first=False, chunk_steps=12)):
+    for tune in (dict(blocks_per_sm=1, tiles_per_item=1, shell_tiles_per_item=1, chunk_steps=4),
+                 dict(blocks_per_sm=0, tiles_per_item=4, shell_tiles_per_item=8, chunk_steps=12)):
         with Batch("fp16") as b:
             ms = [domain(mods, i)[0] for i in range(3)]
             for m in ms:

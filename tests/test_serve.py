@@ -1,0 +1,78 @@
+"""Continuous-batching request loop (aeros_gb300/serve.py)."""
+import numpy as np
+import pytest
+
+SMALL_GRIDS = ((32, 16, 16), (40, 24, 24), (48, 24, 16))
+
+
+def test_requests_are_seeded_poisson():
+    from aeros_gb300 import serve
+    a = serve.make_requests(400, rate=2.0, seed=7)
+    b = serve.make_requests(400, rate=2.0, seed=7)
+    assert [(r.arrival, r.grid, r.level, r.re) for r in a] == [(r.arrival, r.grid, r.level, r.re) for r in b]
+    gaps = np.diff([0.0] + [r.arrival for r in a])
+    assert (gaps > 0).all()
+    assert 0.4 < gaps.mean() < 0.6            # mean gap 1 / rate
+    assert 0.7 < gaps.std() / gaps.mean() < 1.3   # exponential: coefficient of variation 1
+    assert all(50.0 <= r.re <= 1000.0 for r in a)
+    assert {r.grid for r in a} == set(serve.SERVE_GRIDS)
+    assert {r.level for r in a} == set(serve.SERVE_LEVELS)
+
+
+def test_footprint_estimate_orders_requests():
+    from aeros_gb300 import serve
+    small = serve.Request(0, 0.0, (48, 48, 48), 5, 100.0, 1)
+    big = serve.Request(1, 0.0, (256, 128, 128), 7, 100.0, 2)
+    assert serve.footprint_estimate(small) < serve.footprint_estimate(big)
+    assert serve.footprint_estimate(big, "fp32") > serve.footprint_estimate(big, "fp16")
+
+
+def _reqs(serve, n):
+    return serve.make_requests(n, rate=50.0, seed=11, grids=SMALL_GRIDS, levels=(2, 3))
+
+
+@pytest.mark.gpu
+def test_result_alone_equals_result_in_mix():
+    """A request served alone and among five others: the same Cd, step count,
+    and bitwise the same final populations."""
+    from aeros_gb300 import serve
+    reqs = _reqs(serve, 6)
+    kept = {}
+
+    def keep(res, solver):
+        kept[res.rid] = solver.populations()
+
+    srv = serve.Server(check_every=200, max_steps=1000, chunk=100, tol=1e-3)
+    mix = srv.run(reqs, realtime=False, on_retire=keep)
+    mix_pop = dict(kept)
+    kept.clear()
+    target = reqs[3]
+    alone = srv.run([target], realtime=False, on_retire=keep)
+    a = alone["results"][0]
+    m = [r for r in mix["results"] if r.rid == target.rid][0]
+    assert (a.steps, a.converged) == (m.steps, m.converged)
+    assert a.cd == m.cd and np.isfinite(a.cd)
+    assert np.array_equal(kept[target.rid], mix_pop[target.rid])
+    s = mix["summary"]
+    assert s["requests"] == 6 and s["p50_s"] <= s["p95_s"] <= s["p99_s"]
+
+
+@pytest.mark.gpu
+def test_admission_respects_slots_and_budget():
+    from aeros_gb300 import serve
+    reqs = _reqs(serve, 5)
+
+    def max_overlap(results):
+        ev = sorted([(r.admitted, 1) for r in results] + [(r.finished, -1) for r in results])
+        cur = best = 0
+        for _, d in ev:
+            cur += d
+            best = max(best, cur)
+        return best
+
+    two = serve.Server(slots=2, check_every=200, max_steps=400, chunk=100).run(reqs, realtime=False)
+    assert max_overlap(two["results"]) <= 2 and two["summary"]["requests"] == 5
+    tight = serve.Server(budget_bytes=serve.footprint_estimate(reqs[0]) + 1, check_every=200, max_steps=400,
+                         chunk=100).run(reqs, realtime=False)
+    assert max_overlap(tight["results"]) == 1 and tight["summary"]["requests"] == 5
+    assert all(r.steps == 400 or r.converged for r in tight["results"])
