@@ -147,6 +147,7 @@ _SIGS = {
     "aeros_lbm_projected_area": (C.c_int, [_P, C.c_int, _DP]),
     "aeros_voxelize": (C.c_int, [_FP, C.c_int64, C.POINTER(VoxelGrid), _U8P]),
     "aeros_voxelize_device": (C.c_int, [_FP, C.c_int64, C.POINTER(VoxelGrid), _P]),
+    "aeros_voxelize_device_noalloc": (C.c_int, [_FP, C.c_int64, C.POINTER(VoxelGrid), _P]),
     "aeros_voxel_plan": (C.c_int, [_FP, C.c_int, C.c_uint64, C.POINTER(VoxelPlan)]),
     "aeros_lbm_last_step_ms": (C.c_int, [_P, _FP]),
     "aeros_lbm_last_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),

@@ -1001,6 +1001,8 @@ extern "C" int aeros_lbm_projected_area(aeros_lbm* h, int axis, double* area) {
 namespace aeros {
 int voxelize_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask, cudaStream_t s,
                   char* err, size_t errn);
+int voxelize_noalloc_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask, char* err,
+                          size_t errn);
 }
 
 static int check_grid(const float* tris, int64_t ntri, const aeros_voxel_grid* g) {
@@ -1017,6 +1019,18 @@ extern "C" int aeros_voxelize_device(const float* tris, int64_t ntri, const aero
     if (!d_mask) return set_error(AEROS_ERR_INVALID, "mask is NULL");
     char err[512] = {0};
     const int rc = voxelize_impl(tris, ntri, g, d_mask, nullptr, err, sizeof(err));
+    if (rc) return set_error(rc, "%s", err);
+    return AEROS_OK;
+}
+
+// Fixed-scratch variant of aeros_voxelize_device for callers that cannot
+// allocate device memory (see voxelize_noalloc_impl in voxel.cu).
+extern "C" int aeros_voxelize_device_noalloc(const float* tris, int64_t ntri, const aeros_voxel_grid* g,
+                                             uint8_t* d_mask) {
+    if (int rc = check_grid(tris, ntri, g)) return rc;
+    if (!d_mask) return set_error(AEROS_ERR_INVALID, "mask is NULL");
+    char err[512] = {0};
+    const int rc = voxelize_noalloc_impl(tris, ntri, g, d_mask, err, sizeof(err));
     if (rc) return set_error(rc, "%s", err);
     return AEROS_OK;
 }

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/aeros_lbm.h"
@@ -242,6 +243,107 @@ int voxelize_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, ui
     if (dn) cudaFreeAsync(dn, s);
     if (dt) cudaFreeAsync(dt, s);
     if (dof) cudaFreeAsync(dof, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { snprintf(err, errn, "voxelize: %s", cudaGetErrorString(e)); return AEROS_ERR_CUDA; }
+    if (overflow) { snprintf(err, errn, "voxelize: BVH traversal stack overflow"); return AEROS_ERR_UNSUPPORTED; }
+    return AEROS_OK;
+}
+
+// ---- voxelizing without device allocation -----------------------------------
+// Callers that cannot allocate device memory while they voxelize: a serving
+// loop that has handed its whole HBM budget to resident domains (an extra
+// allocation can fail mid-session), and a caller whose other streams must not
+// be stalled by the device-wide synchronization cudaFree implies. The BVH,
+// the triangles and the overflow flag go to one fixed device array instead,
+// VOXEL_SCRATCH_BYTES long (24 MiB: up to about 330,000 triangles, the
+// level-7 icosphere); a mesh needing more is rejected before any device work.
+// The array is shared by every call on a device, so calls must not overlap
+// (the caller serializes them: each call returns after its work completed).
+// The array's address is looked up once per device on the first call, which
+// must therefore come before any stream capture on that device.
+constexpr size_t VOXEL_SCRATCH_BYTES = size_t(24) << 20;
+static __device__ __align__(256) unsigned char g_voxel_scratch[VOXEL_SCRATCH_BYTES];
+
+namespace {
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+int scratch_address(void** out, char* err, size_t errn) {
+    static std::mutex mu;
+    static void* addr[64] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) {
+        snprintf(err, errn, "device: %s", cudaGetErrorString(e));
+        return AEROS_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_voxel_scratch);
+        if (e != cudaSuccess || !p) {
+            snprintf(err, errn, "scratch symbol: %s", cudaGetErrorString(e));
+            return AEROS_ERR_CUDA;
+        }
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return AEROS_OK;
+}
+}  // namespace
+
+int voxelize_noalloc_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask, char* err,
+                          size_t errn) {
+    if ((size_t)ntri * sizeof(float) * 9 > VOXEL_SCRATCH_BYTES) {
+        snprintf(err, errn, "%lld triangles exceed the %zu-byte voxelizer scratch", (long long)ntri, VOXEL_SCRATCH_BYTES);
+        return AEROS_ERR_INVALID;
+    }
+    std::vector<HTri> tv;
+    tv.reserve((size_t)std::max<int64_t>(ntri, 0));
+    for (int64_t i = 0; i < ntri; ++i) {
+        HTri t;
+        if (make_tri(tris + 9 * i, t)) tv.push_back(t);
+    }
+    const long long total = (long long)g->nx * g->ny * g->nz;
+    const cudaStream_t s = nullptr;
+    if (tv.empty()) {
+        cudaError_t e = cudaMemsetAsync(d_mask, 0, (size_t)total, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) { snprintf(err, errn, "memset: %s", cudaGetErrorString(e)); return AEROS_ERR_CUDA; }
+        return AEROS_OK;
+    }
+    Builder b(tv);
+    b.nodes.reserve(tv.size() * 2 / 4 + 2);
+    b.build(0, (int)tv.size(), 0);
+    std::vector<float> flat(tv.size() * 9);
+    for (size_t i = 0; i < tv.size(); ++i) memcpy(&flat[9 * i], tv[i].v, 36);
+    // layout: overflow flag | nodes | triangles, each 256-byte aligned
+    const size_t off_nodes = 256;
+    const size_t off_tris = align256(off_nodes + b.nodes.size() * sizeof(DNode));
+    const size_t need = off_tris + flat.size() * sizeof(float);
+    if (need > VOXEL_SCRATCH_BYTES) {
+        snprintf(err, errn, "mesh needs %zu bytes of the %zu-byte voxelizer scratch", need, VOXEL_SCRATCH_BYTES);
+        return AEROS_ERR_INVALID;
+    }
+    void* base = nullptr;
+    if (int rc = scratch_address(&base, err, errn)) return rc;
+    unsigned char* sc = static_cast<unsigned char*>(base);
+    int* dof = reinterpret_cast<int*>(sc);
+    DNode* dn = reinterpret_cast<DNode*>(sc + off_nodes);
+    float* dt = reinterpret_cast<float*>(sc + off_tris);
+    cudaError_t e = cudaMemsetAsync(dof, 0, sizeof(int), s);   // the flag starts at zero
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dn, b.nodes.data(), b.nodes.size() * sizeof(DNode), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dt, flat.data(), flat.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    int overflow = 0;
+    if (e == cudaSuccess) {
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        long long blocks = (total + 127) / 128;
+        blocks = std::min<long long>(blocks, (long long)std::max(1, sms) * 16);
+        k_voxelize<<<(int)std::max<long long>(1, blocks), 128, 0, s>>>(dn, dt, *g, d_mask, dof);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&overflow, dof, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { snprintf(err, errn, "voxelize: %s", cudaGetErrorString(e)); return AEROS_ERR_CUDA; }
     if (overflow) { snprintf(err, errn, "voxelize: BVH traversal stack overflow"); return AEROS_ERR_UNSUPPORTED; }

@@ -210,6 +210,18 @@ int aeros_voxelize(const float* tris, int64_t ntri, const aeros_voxel_grid* grid
 /* Same with a device-resident output mask (nx*ny*nz bytes). */
 int aeros_voxelize_device(const float* tris, int64_t ntri,
                           const aeros_voxel_grid* grid, uint8_t* d_mask_out);
+/* No reference counterpart. aeros_voxelize_device without device allocation,
+ * for callers that cannot allocate while they voxelize (a serving loop whose
+ * HBM budget is spent on resident domains; callers whose other streams must
+ * not be stalled by the device-wide synchronization of cudaFree). BVH,
+ * triangles and overflow flag live in one fixed 24 MiB device array per
+ * device (about 330,000 triangles); a larger mesh returns AEROS_ERR_INVALID
+ * before any device work. Calls share that array: they must not overlap in
+ * time (the call returns after its device work has completed). The first
+ * call on a device looks the array up and must come before any stream
+ * capture on that device. Same mask as aeros_voxelize_device. */
+int aeros_voxelize_device_noalloc(const float* tris, int64_t ntri,
+                                  const aeros_voxel_grid* grid, uint8_t* d_mask);
 
 /* Grid plan (aeros/src/voxel_grid.cpp:172-215): dimensions for a bounding box
  * and resolution against a byte budget (0 = unlimited). */
