@@ -66,6 +66,25 @@ def _compile(unit: str, flags: list[str], verbose: bool) -> str:
     return obj
 
 
+FACADE = os.path.join(HERE, "facade")
+
+
+def build_facade(lib: str) -> str:
+    """libaeros_facade.so: the C++17 mirror of the reference solver interface
+    over the C ABI (g++, linked against libaeros_gb300.so by rpath)."""
+    out = os.path.join(OUT_DIR, "libaeros_facade.so")
+    src = os.path.join(FACADE, "aeros_facade.cpp")
+    deps = [src, os.path.join(FACADE, "aeros_facade.h"), lib]
+    if os.path.exists(out) and all(os.path.getmtime(d) <= os.path.getmtime(out) for d in deps):
+        return out
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", src, "-o", out,
+           "-L" + OUT_DIR, "-laeros_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"facade build failed:\n{r.stdout}\n{r.stderr}")
+    return out
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(BUILD_DIR, exist_ok=True)
     os.makedirs(OUT_DIR, exist_ok=True)
@@ -82,6 +101,7 @@ def build(verbose: bool = False) -> str:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         with open(stamp, "w") as fh:
             fh.write(TAG)
+    build_facade(lib)
     return lib
 
 

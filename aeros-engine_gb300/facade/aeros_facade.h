@@ -1,0 +1,140 @@
+// aeros_facade.h — the reference solver's C++ interface (aeros/src/lbm.h,
+// aeros/src/thermal_lbm.h) over the GB300 C ABI (include/aeros_lbm.h).
+//
+// Drop-in for the solver's callers: the same function names and the same
+// globals, which this layer fills from the device after each stepLBMCPU call
+// (scalars always, fields when lbmFacadeReadbackFields is true). The grid
+// comes from the voxel globals the reference's initLBM reads
+// (g_voxelData / g_voxNx.. , aeros/src/globals.h:150-158), taken as the
+// solver grid itself (the reference's domainPadding = 0 case). C++17, no
+// dependency beyond the C ABI; glm::vec3 is used for the vector results when
+// <glm/glm.hpp> is on the include path, a three-float struct otherwise.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/aeros_lbm.h"
+
+#if __has_include(<glm/glm.hpp>)
+#include <glm/glm.hpp>
+using LbmVec3 = glm::vec3;
+#else
+struct LbmVec3 {
+    float x = 0.0f, y = 0.0f, z = 0.0f;
+};
+#endif
+
+// Solver settings: the fields of the reference's LBMParams (aeros/src/lbm.h:11-75)
+// with its defaults, so settings code compiles unchanged. Fields the GPU step
+// does not read (frame pacing, world-unit viscosity, domain padding) are kept
+// for source compatibility.
+struct LBMParams {
+    bool enabled = false;
+    bool useGPU = false;
+    int stepsPerFrame = 3;
+    float tau = 0.6f;
+    float U0 = 0.1f;
+    float viscosity = 0.033f;
+    float smagorinskyC = 0.12f;
+    bool useTurbulence = true;
+    int maxSteps = 10000;
+    float convergenceThreshold = 1e-5f;
+    bool useGround = false;
+    float groundHeight = 0.0f;
+    bool useTRT = false;
+    bool useConvectiveOutlet = true;
+    float inletTurbulence = 0.02f;
+    float domainPadding = 0.25f;
+    bool autoViscosity = true;
+    float bodyForceX = 0.0f;
+    float bodyForceY = 0.0f;
+    float bodyForceZ = 0.0f;
+    bool periodicX = false;
+    bool periodicZ = false;
+};
+
+// ---- inputs (aeros/src/globals.h:150-158) -----------------------------------
+extern std::vector<int> g_voxelData;   // nx*ny*nz, nonzero = solid; 2 = ground
+extern int g_voxNx, g_voxNy, g_voxNz;
+// Inlet velocity in lattice units (the reference derives it from U0 and the
+// flow angles, computeInletVelocityLB, aeros/src/lbm.cpp:186-199); default
+// (U0, 0, 0) when all three are zero.
+extern float lbmInletVelocityLB[3];
+// Velocity scale world / lattice used for TKE in world units (lbm.cpp:1130).
+extern float lbmVelocityScale;
+// Population storage of the GPU step: AEROS_STORE_FP32 (drop-in, bitwise the
+// reference's arithmetic) or AEROS_STORE_FP16 / AEROS_STORE_BF16.
+extern int lbmStorage;
+// Read the fields back after every stepLBMCPU call (the reference's globals
+// always hold the latest fields); false leaves them to lbmFacadeReadFields().
+extern bool lbmFacadeReadbackFields;
+
+// ---- state (aeros/src/lbm.h:77-154) -----------------------------------------
+extern LBMParams lbmParams;
+extern bool lbmInitialized;
+extern bool lbmConverged;
+extern int lbmCurrentStep;
+extern float lbmAvgRho;
+extern float lbmAvgKineticEnergy;
+extern float lbmMaxVelocityLB;
+extern float lbmConvergence;
+extern long long lbmNegativePops;
+extern long long lbmBadPops;
+extern long long lbmRhoOutOfRange;
+extern long long lbmRhoNonFinite;
+extern long long lbmULimited;
+extern float lbmTimeMs;
+extern float lbmTKE;
+extern int lbmNx, lbmNy, lbmNz;
+extern std::vector<float> lbmRho;
+extern std::vector<float> lbmUx, lbmUy, lbmUz;
+extern std::vector<float> lbmTKEField;
+extern std::vector<float> lbmStrainMag;
+extern std::vector<char> lbmIsSolid;
+extern std::vector<char> lbmIsGround;
+
+// ---- solver (aeros/src/lbm.h:156-202) ---------------------------------------
+void initLBM();
+void resetLBM();
+void shutdownLBM();
+void stepLBMCPU(int steps = 1);
+LbmVec3 lbmControlVolumeForce(float boxHalfX, float boxHalfY, float boxHalfZ);
+float lbmProjectedAreaCells(int axis);
+
+// ---- thermal (aeros/src/thermal_lbm.h:33-72) --------------------------------
+struct ThermalParams {
+    bool enabled = false;
+    float rayleigh = 1.0e5f;
+    float prandtl = 0.71f;
+    bool fixedWallTemps = true;
+    float hotTemp = 1.0f;
+    float coldTemp = 0.0f;
+    float perturbation = 0.02f;
+};
+extern ThermalParams thermalParams;
+extern std::vector<float> thermalT;
+extern std::vector<float> thermalBuoyancyY;
+extern bool thermalReady;
+extern float thermalNusselt;
+extern float thermalMeanT;
+// On the solver's grid (the GPU lattice must exist: call after initLBM). The
+// mask argument is the solid mask the solver already holds; nuLB as the
+// reference (lattice viscosity).
+bool thermalInit(int nx, int ny, int nz, const std::vector<char>& solidMask, float nuLB);
+void thermalShutdown();
+bool thermalUpload(const std::vector<float>& T);
+// The GPU step advances the thermal lattice inside stepLBMCPU (the reference
+// calls thermalStep from there too, aeros/src/lbm.cpp:1551-1552); a separate
+// call has nothing left to do.
+void thermalStep(const float* ux, const float* uy, const float* uz);
+
+// ---- extras of this layer ----------------------------------------------------
+// The C-ABI handle (NULL before initLBM): for callers that also use the batch
+// or the device field pointers.
+aeros_lbm* lbmFacadeHandle();
+// Reads rho, u, strain and TKE into the globals now.
+bool lbmFacadeReadFields();
+// Message of the last failed call ("" when none).
+const std::string& lbmFacadeLastError();
