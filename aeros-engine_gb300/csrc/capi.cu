@@ -262,6 +262,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (const char* e = getenv("AEROS_STAGED")) h->staged = atoi(e) != 0;
     if (const char* e = getenv("AEROS_SPLIT")) h->split = atoi(e) != 0;
+    if (const char* e = getenv("AEROS_FUSED")) h->fused = atoi(e) != 0;
 
     std::vector<int> shell;
     host_geometry(h, shell);
@@ -462,7 +463,9 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     A.staged = h->staged;
     {
         const int nsh = A.ntiles - A.ntiles_interior;
-        A.split = h->split && nsh > 0 && !h->staged;
+        A.fused = h->fused && !h->th_on && !h->staged;
+        A.shell_blocks = A.fused ? std::min(nsh, std::max(1, h->sm_count)) : 0;
+        A.split = h->split && nsh > 0 && !h->staged && !A.fused;
         A.shell_grid = A.split ? std::min(nsh, std::max(1, h->sm_count) * 4) : 0;
         A.shell_part_base = 0;   // set by the launcher (after the interior grid's slots)
     }

@@ -149,7 +149,9 @@ const Launchers& launchers_bf16();
     namespace NAME##_detail {                                                                                         \
     template <bool O, bool T, bool M>                                                                                 \
     cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
-        if (!M && A.split) {                                                                                          \
+        if (!M && !T && A.fused) {                                                                                    \
+            k_lbm_fused<STORE, O><<<grid + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V);                                 \
+        } else if (!M && A.split) {                                                                                   \
             StepArgs B = A;                                                                                           \
             B.shell_part_base = grid;                                                                                 \
             if (B.shell_grid > 0) k_lbm_shell<STORE, O, T><<<B.shell_grid, STEP_BLOCK, 0, s>>>(B, V);                 \

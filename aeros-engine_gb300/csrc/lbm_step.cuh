@@ -55,6 +55,12 @@ struct Control {
     float nusselt, mean_t;
     int pad;
     long long nan, neg, bad, rout, rnf, ulim;
+    // fused launch (dynamic warp work items): exact fixed-point sums of the
+    // step, zeroed by the finisher
+    unsigned int shell_next, warps_done;
+    unsigned long long fx_drho, fx_ke, fx_tke;
+    unsigned long long fx_cnt[7];   // NaN, negative, bad, rho range, rho finite, u limited, cells
+    unsigned int fx_maxu2, pad2;
 };
 
 struct StepArgs {
@@ -91,6 +97,8 @@ struct StepArgs {
     int fast_ok;                // forces bounded: clean states need no non-finite checks
     int staged;                 // interior tiles through TMA bulk copies (non-thermal steps)
     int split;                  // shell and interior as two launches
+    int fused;                  // one launch: shell blocks beside dynamic interior blocks (non-thermal)
+    int shell_blocks;           // fused: blocks given to the boundary shell
     int shell_part_base, shell_grid;   // split: first partial slot and grid of the shell launch
     int total_div10, fluid_cells;
     float conv_threshold;
@@ -607,32 +615,33 @@ __device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int
 template <class S, bool ODD, bool THERMAL, bool MAT>
 __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
                                                  Acc& acc) {
+    // Every load below is in bounds for an interior cell whatever its
+    // descriptor, so all of them are issued before the descriptor arrives
+    // (one memory round trip less on the cell's critical path); the
+    // populations a wall link redirects are loaded again afterwards.
     const uint32_t d = A.desc[cell];
-    if (d & D_WALL) return;
     constexpr bool SH = S::shifted;
-    // previous-step strain first: keeps the velocity stencil out of the
-    // register peak of the collision
-    float strainPre = 0.0f;
-    if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
-    float buoy = 0.0f;
-    if (!MAT && THERMAL && A.th_buoy_mode != 1)
-        buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
-    const bool plain = (d & D_LINKS) == 0;   // no wall next to the cell
+    // previous-step strain (two-pass |S|) from the velocity stencil
+    const float strainAll = (!MAT && A.use_les) ? strain_prev(A, V, cell) : 0.0f;
     float f[Q19];
     if (!ODD) {
 #pragma unroll
         for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
-    } else if (plain) {
-#pragma unroll
-        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
     } else {
 #pragma unroll
-        for (int q = 0; q < Q19; ++q) {
-            const bool special = (d >> q) & 1u;
-            const int src = special ? cell : cell - nb19(A, q);
-            f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
-        }
+        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
     }
+    if (d & D_WALL) return;
+    const bool plain = (d & D_LINKS) == 0;   // no wall next to the cell
+    if (ODD && !plain) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q)
+            if ((d >> q) & 1u) f[q] = S::load_rw(fplane<S>(A, q) + cell);
+    }
+    const float strainPre = (d & D_LES) ? strainAll : 0.0f;
+    float buoy = 0.0f;
+    if (!MAT && THERMAL && A.th_buoy_mode != 1)
+        buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
     if (MAT) {
 #pragma unroll
         for (int q = 0; q < Q19; ++q) A.mat_f[(long long)q * A.ncell + cell] = SH ? f[q] + w19(q) : f[q];
@@ -705,12 +714,10 @@ __device__ __forceinline__ void interior_finish(const StepArgs& A, const StepVar
 template <class S, bool ODD, bool THERMAL, bool MAT>
 __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
                                            unsigned long long skind, Acc& acc) {
+    // the link kinds give in-domain sources for every shell cell: the
+    // populations are loaded before the descriptor arrives
     const uint32_t d = A.desc[cell];
-    if (d & D_WALL) return;
     constexpr bool SH = S::shifted;
-    float buoy = 0.0f;
-    if (!MAT && THERMAL && A.th_buoy_mode != 1)
-        buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
     float f[Q19];
 #pragma unroll
     for (int q = 0; q < Q19; ++q) {
@@ -721,6 +728,10 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
             f[q] = S::load_rw(fplane<S>(A, L.slot) + L.idx);
         }
     }
+    if (d & D_WALL) return;
+    float buoy = 0.0f;
+    if (!MAT && THERMAL && A.th_buoy_mode != 1)
+        buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
     const bool isInlet = (d & D_INLET) != 0, isOutlet = (d & D_OUTLET) != 0;
     if (V.apply_overrides && !A.periodic_x) {
         if (isInlet) {
@@ -1027,6 +1038,118 @@ __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_interior(co
     finish_step<STEP_BLOCK>(A, A.shell_part_base + A.shell_grid);
 }
 
+struct WarpSums {               // one warp's sums over the slices of a work item
+    long long drho, ke, tke;    // fixed point
+    long long cnt[7];           // NaN, negative, bad, rho range, rho finite, u limited, cells
+};
+
+constexpr float FX_SUM = 1099511627776.0f;   // 2^40: sums of rho - 1 and |u|^2 per slice
+constexpr float FX_TKE = 1048576.0f;         // 2^20: TKE per slice (up to 32 x 1e6)
+
+__device__ __forceinline__ float warp_allsum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_allsum(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ---- one launch per step: shell blocks beside dynamic interior blocks -------------
+// The grid is A.shell_blocks + the persistent interior grid. The first
+// A.shell_blocks blocks (dispatched first: about one per SM) take the
+// boundary-shell tiles, whose cost is latency, while the co-resident interior
+// blocks stream the interior; interior blocks take 256-cell tiles from a
+// global counter, so the blocks dispatched once the shell blocks retire share
+// the remaining tiles. Each 32-cell slice's sums are converted to 64-bit fixed
+// point and accumulated exactly, so the statistics do not depend on which
+// block took which tile.
+template <class S, bool ODD>
+__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_fused(const StepArgs A, const StepVar V) {
+    if (A.ctl->halt) return;   // uniform: every thread reads the same flag
+    __shared__ WarpSums s_sums[STEP_BLOCK / 32];
+    __shared__ int s_tile[2];
+    const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
+    WarpSums& W = s_sums[wid];
+    if (lane == 0) {
+        W.drho = W.ke = W.tke = 0;
+        for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
+    }
+    __syncwarp();
+    float mx = 0.0f;
+    Control* ctl = A.ctl;
+    auto add_slice = [&](const Acc& acc) {
+        const float sd = warp_allsum(acc.drho), sk = warp_allsum(acc.ke), st = warp_allsum(acc.tke);
+        mx = fmaxf(mx, acc.maxu2);
+        const int cells = __popc(__ballot_sync(0xffffffffu, acc.cells != 0));
+        const bool rare = __any_sync(0xffffffffu, (acc.nan | acc.neg | acc.bad | acc.rout | acc.rnf | acc.ulim) != 0);
+        int c6[6] = {0, 0, 0, 0, 0, 0};
+        if (rare) {
+            c6[0] = warp_allsum(acc.nan); c6[1] = warp_allsum(acc.neg); c6[2] = warp_allsum(acc.bad);
+            c6[3] = warp_allsum(acc.rout); c6[4] = warp_allsum(acc.rnf); c6[5] = warp_allsum(acc.ulim);
+        }
+        if (lane == 0) {
+            W.drho += __float2ll_rn(sd * FX_SUM);
+            W.ke += __float2ll_rn(sk * FX_SUM);
+            W.tke += __float2ll_rn(st * FX_TKE);
+            W.cnt[6] += cells;
+            if (rare)
+                for (int j = 0; j < 6; ++j) W.cnt[j] += c6[j];
+        }
+    };
+    const int nsh = A.ntiles - A.ntiles_interior;
+    if ((int)blockIdx.x < A.shell_blocks) {
+        for (int st = blockIdx.x; st < nsh; st += A.shell_blocks) {
+            Acc acc;
+            acc.zero();
+            shell_tile<S, ODD, false, false>(A, V, st, acc);
+            add_slice(acc);
+        }
+    } else {
+        int par = 0;
+        for (;;) {
+            if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
+            __syncthreads();
+            const int it = s_tile[par];
+            par ^= 1;
+            if (it >= A.ntiles_interior) break;
+            Acc acc;
+            acc.zero();
+            interior_tile<S, ODD, false, false>(A, V, it, acc);
+            add_slice(acc);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __syncwarp();
+    if (lane == 0) atomicAdd(&ctl->fx_drho, (unsigned long long)W.drho);
+    else if (lane == 1) atomicAdd(&ctl->fx_ke, (unsigned long long)W.ke);
+    else if (lane == 2) atomicAdd(&ctl->fx_tke, (unsigned long long)W.tke);
+    else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ctl->fx_cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
+    else if (lane == 10 && mx > 0.0f) atomicMax(&ctl->fx_maxu2, __float_as_uint(mx));
+    __threadfence();
+    __syncwarp();
+    int last = 0;
+    if (lane == 0) last = atomicAdd(&ctl->warps_done, 1u) == gridDim.x * (STEP_BLOCK / 32) - 1;
+    if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
+        __threadfence();
+        volatile Control* vc = ctl;
+        const double t[5] = {(double)(long long)vc->fx_drho / (double)FX_SUM, (double)(long long)vc->fx_ke / (double)FX_SUM,
+                             (double)(long long)vc->fx_tke / (double)FX_TKE, 0.0, 0.0};
+        const long long c[8] = {(long long)vc->fx_cnt[0], (long long)vc->fx_cnt[1], (long long)vc->fx_cnt[2],
+                                (long long)vc->fx_cnt[3], (long long)vc->fx_cnt[4], (long long)vc->fx_cnt[5], 0,
+                                (long long)vc->fx_cnt[6]};
+        const float m = __uint_as_float(vc->fx_maxu2);
+        vc->fx_drho = 0; vc->fx_ke = 0; vc->fx_tke = 0;
+        for (int j = 0; j < 7; ++j) vc->fx_cnt[j] = 0;
+        vc->fx_maxu2 = 0;
+        vc->warps_done = 0;
+        apply_totals(A, t, m, c);   // also rewinds tile_next
+    }
+}
+
 // ---- many domains in one persistent kernel -----------------------------------
 // Warps take work items from a global counter; an item is a run of 32-cell
 // slices of one domain's shell or interior (shell items of every domain
@@ -1073,25 +1196,6 @@ struct BatchArgs {
     BatchAcc* acc;
     BatchCtl* ctl;
 };
-
-struct WarpSums {               // one warp's sums over the slices of a work item
-    long long drho, ke, tke;    // fixed point
-    long long cnt[7];           // NaN, negative, bad, rho range, rho finite, u limited, cells
-};
-
-constexpr float FX_SUM = 1099511627776.0f;   // 2^40: sums of rho - 1 and |u|^2 per slice
-constexpr float FX_TKE = 1048576.0f;         // 2^20: TKE per slice (up to 32 x 1e6)
-
-__device__ __forceinline__ float warp_allsum(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ int warp_allsum(int v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 // KIND 0: the shell slices of every domain; KIND 1: the interior slices (one
 // launch each per step, so each launch's code is only its own path).
