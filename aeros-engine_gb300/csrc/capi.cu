@@ -263,6 +263,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     if (const char* e = getenv("AEROS_STAGED")) h->staged = atoi(e) != 0;
     if (const char* e = getenv("AEROS_SPLIT")) h->split = atoi(e) != 0;
     if (const char* e = getenv("AEROS_FUSED")) h->fused = atoi(e) != 0;
+    if (const char* e = getenv("AEROS_SHELL_BLOCKS")) h->shell_blocks_per_sm = std::max(1, std::min(8, atoi(e)));
 
     std::vector<int> shell;
     host_geometry(h, shell);
@@ -464,7 +465,7 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     {
         const int nsh = A.ntiles - A.ntiles_interior;
         A.fused = h->fused && !h->th_on && !h->staged;
-        A.shell_blocks = A.fused ? std::min(nsh, std::max(1, h->sm_count)) : 0;
+        A.shell_blocks = A.fused ? std::min(nsh, std::max(1, h->sm_count) * h->shell_blocks_per_sm) : 0;
         A.split = h->split && nsh > 0 && !h->staged && !A.fused;
         A.shell_grid = A.split ? std::min(nsh, std::max(1, h->sm_count) * 4) : 0;
         A.shell_part_base = 0;   // set by the launcher (after the interior grid's slots)
@@ -474,6 +475,7 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
         float fmax = std::max(std::fabs(p.body_force[0]), std::max(std::fabs(p.body_force[1]), std::fabs(p.body_force[2])));
         if (h->th_on) fmax += std::fabs(h->glb) * (std::fabs(h->tp.hot_temp - h->tp.cold_temp) + 2.0f);
         A.fast_ok = std::isfinite(fmax) && fmax <= 1.0f;
+        A.shifted_fast = h->esize == 2 && fmax == 0.0f && !h->th_on;
     }
     A.fluid_cells = h->fluid_cells;
     A.conv_threshold = p.convergence_threshold;

@@ -95,6 +95,7 @@ struct StepArgs {
     int use_trt, use_les;
     int freeslip, outlet_mode;  // outlet_mode: 0 none, 1 convective, 2 zero-gradient
     int fast_ok;                // forces bounded: clean states need no non-finite checks
+    int shifted_fast;           // shifted storage, no body force, no thermal: collide19_shifted_fast
     int staged;                 // interior tiles through TMA bulk copies (non-thermal steps)
     int split;                  // shell and interior as two launches
     int fused;                  // one launch: shell blocks beside dynamic interior blocks (non-thermal)
@@ -318,9 +319,120 @@ __device__ __forceinline__ void relax19_shifted_fast(float f[Q19], float rho, fl
 // override, LES tau, Guo force and TRT rate: aeros/src/lbm.cpp:1061-1299, same
 // expression trees (compiled without contraction the plain form is bitwise
 // the reference's float arithmetic).
+// Shifted storage, no body force, a cell off the inlet/outlet planes: the
+// same model in fewer instructions. The sums and differences of opposite
+// populations are formed once (in place) and serve both the moments and the
+// TRT update; reciprocals are single-instruction approximations (the shifted
+// form is measured against the FP64 oracle, not bitwise the reference); the
+// density guard and the velocity limiter are applied as in the full path.
+// Returns false, with f untouched, when a population may be outside the clean
+// range (the full path then replays the reference's per-population checks).
+__device__ __forceinline__ bool collide19_shifted_fast(float f[Q19], const StepArgs& A, uint32_t d, float strainPre,
+                                                       CellResult& o, Acc& acc) {
+    float ss = 0.0f;
+#pragma unroll
+    for (int q = 0; q < Q19; ++q) ss = fmaf(f[q], f[q], ss);
+    if (!(ss <= 1.0f)) return false;
+    // f[qi] <- h_qi + h_qo, f[qo] <- h_qi - h_qo for the opposite pairs
+    float drho = f[0], jx = 0.0f, jy = 0.0f, jz = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const int qi = 2 * k + 1;
+        const float p = f[qi] + f[qi + 1], m = f[qi] - f[qi + 1];
+        f[qi] = p;
+        f[qi + 1] = m;
+        drho += p;
+        if (cx19(qi) != 0) jx = cx19(qi) > 0 ? jx + m : jx - m;
+        if (cy19(qi) != 0) jy = cy19(qi) > 0 ? jy + m : jy - m;
+        if (cz19(qi) != 0) jz = cz19(qi) > 0 ? jz + m : jz - m;
+    }
+    float rho = 1.0f + drho;
+    if (rho < 0.5f || rho > 1.5f) {   // density guard, lbm.cpp:1078-1080
+        acc.rout++;
+        acc.nan++;
+        rho = 1.0f;
+        drho = 0.0f;
+    }
+    const float invRho = __fdividef(1.0f, rho);
+    float ux = jx * invRho, uy = jy * invRho, uz = jz * invRho;
+    float usqr = ux * ux + uy * uy + uz * uz;
+    if (usqr > 0.09f) {   // both limiters of the full path (lbm.cpp:1086-1090, 1148-1153)
+        const float sc = sqrtf(0.09f / usqr);
+        ux *= sc; uy *= sc; uz *= sc;
+        usqr = ux * ux + uy * uy + uz * uz;
+        if (usqr > 0.09f) {
+            acc.ulim++;
+            const float sc2 = sqrtf(0.09f / usqr);
+            ux *= sc2; uy *= sc2; uz *= sc2;
+            usqr = ux * ux + uy * uy + uz * uz;
+        }
+    }
+    float tauEff = A.tau0, strainMag = 0.0f;
+    if (A.use_les) {
+        strainMag = strainPre;
+        if (strainMag < 10.0f && strainMag > 1e-6f) {
+            float cs = A.Cs;
+            const int wd = (int)((d >> D_WD_SHIFT) & 7u);
+            if (wd <= 5) cs *= van_driest(wd);
+            tauEff = fminf(fmaxf(fmaf(cs * cs, strainMag * 3.0f, A.tau0), 0.51f), 1.5f);
+        }
+    }
+    const float invTau = __fdividef(1.0f, tauEff);
+    float sMinus = invTau;
+    if (A.use_trt) {
+        const float m = invTau - 0.5f;
+        const float denom = (fabsf(m) > 1e-6f) ? (__fdividef(0.1875f, m) + 0.5f) : 1.0f;
+        sMinus = __fdividef(1.0f, fmaxf(0.05f, denom));
+    }
+    // TRT on the deviations h = f - w: f^eq - w = w (P + 3 rho cu + 4.5 rho cu^2)
+    // with P = rho - 1 - 1.5 rho |u|^2 (the symmetric part relaxes with 1/tau,
+    // the antisymmetric with s-)
+    const float P = drho - 1.5f * rho * usqr;
+    const float R45 = 4.5f * rho;
+    const float A1 = 0.5f * (1.0f - invTau), A2 = 0.5f * (1.0f - sMinus);
+    const float W1 = invTau * w19(1), W2 = invTau * w19(7);
+    const float M1 = 3.0f * rho * sMinus * w19(1), M2 = 3.0f * rho * sMinus * w19(7);
+    f[0] = f[0] - invTau * (f[0] - w19(0) * P);
+    float post = f[0] * f[0];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const int qi = 2 * k + 1;
+        const float cu = cu19(qi, ux, uy, uz);
+        const float ep = fmaf(R45, cu * cu, P);
+        const float fp = fmaf(A1, f[qi], (qi <= 6 ? W1 : W2) * ep);
+        const float fm = fmaf(A2, f[qi + 1], (qi <= 6 ? M1 : M2) * cu);
+        f[qi] = fp + fm;
+        f[qi + 1] = fp - fm;
+        post = fmaf(f[qi], f[qi], post);
+        post = fmaf(f[qi + 1], f[qi + 1], post);
+    }
+    // negative post-collision populations: sum h^2 below the smallest weight
+    // squared proves every f = h + w >= 0; otherwise count exactly
+    if (!(post < (1.0f / 36.0f) * (1.0f / 36.0f))) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) acc.neg += (f[q] + w19(q) < 0.0f) ? 1 : 0;
+    }
+    o.rho = rho;
+    o.ux = ux; o.uy = uy; o.uz = uz;
+    o.strain = strainMag;
+    const float cS = A.Cs * strainMag;
+    float tke = cS * cS * A.velScale2;
+    if (!isfinite(tke) || tke < 0.0f) tke = 0.0f;
+    if (tke > 1.0e6f) tke = 1.0e6f;
+    o.tke = tke;
+    o.usqr = usqr;
+    acc.maxu2 = fmaxf(acc.maxu2, usqr);
+    acc.drho += drho;
+    acc.ke += usqr;
+    acc.tke += tke;
+    acc.cells++;
+    return true;
+}
+
 template <bool SHIFTED>
 __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint32_t d, bool isInlet, bool isOutlet,
                                           float strainPre, float buoy, CellResult& o, Acc& acc) {
+    if (SHIFTED && A.shifted_fast && !isInlet && !isOutlet && collide19_shifted_fast(f, A, d, strainPre, o, acc)) return;
     // moments and the sum of squares of the populations in one pass
     float rho = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f, ss = 0.0f;
 #pragma unroll
