@@ -727,30 +727,37 @@ __device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int
 template <class S, bool ODD, bool THERMAL, bool MAT>
 __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
                                                  Acc& acc) {
-    // Every load below is in bounds for an interior cell whatever its
-    // descriptor, so all of them are issued before the descriptor arrives
-    // (one memory round trip less on the cell's critical path); the
-    // populations a wall link redirects are loaded again afterwards.
     const uint32_t d = A.desc[cell];
     constexpr bool SH = S::shifted;
-    // previous-step strain (two-pass |S|) from the velocity stencil
-    const float strainAll = (!MAT && A.use_les) ? strain_prev(A, V, cell) : 0.0f;
     float f[Q19];
+    float strainPre = 0.0f;
     if (!ODD) {
+        // even step: every load is of the cell itself, in bounds whatever
+        // the descriptor says, so all are issued before the descriptor
+        // arrives (one memory round trip less on the critical path)
+        const float strainAll = (!MAT && A.use_les) ? strain_prev(A, V, cell) : 0.0f;
 #pragma unroll
         for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
+        if (d & D_WALL) return;
+        if (d & D_LES) strainPre = strainAll;
     } else {
+        // odd step: the descriptor first (the gather differs next to walls;
+        // issuing both forms costs more registers than the round trip saves)
+        if (d & D_WALL) return;
+        if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
+        if ((d & D_LINKS) == 0) {
 #pragma unroll
-        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
+            for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) {
+                const bool special = (d >> q) & 1u;
+                const int src = special ? cell : cell - nb19(A, q);
+                f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
+            }
+        }
     }
-    if (d & D_WALL) return;
     const bool plain = (d & D_LINKS) == 0;   // no wall next to the cell
-    if (ODD && !plain) {
-#pragma unroll
-        for (int q = 0; q < Q19; ++q)
-            if ((d >> q) & 1u) f[q] = S::load_rw(fplane<S>(A, q) + cell);
-    }
-    const float strainPre = (d & D_LES) ? strainAll : 0.0f;
     float buoy = 0.0f;
     if (!MAT && THERMAL && A.th_buoy_mode != 1)
         buoy = A.th_glb * ((A.th_buoy_mode == 0 ? A.T[cell] : A.T_buoy[cell]) - A.th_tref);
@@ -1295,8 +1302,8 @@ struct BatchAcc {               // per domain, zero between steps
 };
 
 struct BatchCtl {
-    unsigned int work_next[2];  // next work item of the shell / interior launch (reset by its last warp)
-    unsigned int warps_done[2];
+    unsigned int work_next[2];  // next work item of the shell / interior launch (reset by its last block)
+    unsigned int warps_done[2]; // blocks of the launch that have finished
     int k;                      // step of the call being executed
     int k_last;                 // last step of the call (writes rho, |S|, TKE)
 };
@@ -1313,28 +1320,84 @@ struct BatchArgs {
 // launch each per step, so each launch's code is only its own path).
 template <class S, bool ODD, int KIND>
 __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_batch_step(const BatchArgs B) {
-    // one copy of the current domain's arguments per warp
-    __shared__ __align__(16) unsigned char s_args[STEP_BLOCK / 32][sizeof(StepArgs)];
+    // Blocks take items; warp w of the block takes slice w of every group of
+    // eight, so a block covers 256 consecutive cells at a time (the rows the
+    // velocity stencil shares stay in L1). The current domain's arguments are
+    // copied to shared memory once per domain change. Each warp keeps its
+    // fixed-point sums for the current domain and adds them (then its slice
+    // count) to the domain's accumulators when the block moves to another
+    // domain or runs out of items.
+    __shared__ __align__(16) unsigned char s_args[sizeof(StepArgs)];
     __shared__ WarpSums s_sums[STEP_BLOCK / 32];
+    __shared__ int s_item[2];
     const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
-    StepArgs& A = *reinterpret_cast<StepArgs*>(s_args[wid]);   // StepArgs is not trivially constructible
+    StepArgs& A = *reinterpret_cast<StepArgs*>(s_args);   // StepArgs is not trivially constructible
+    WarpSums& W = s_sums[wid];
     const int k = B.ctl->k;
     const bool write_obs = k == B.ctl->k_last;
-    int cur = -1;
+    if (lane == 0) {
+        W.drho = W.ke = W.tke = 0;
+        for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
+    }
+    __syncwarp();
+    float mx = 0.0f;
+    int w_slices = 0;
+    auto flush = [&](int dom) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __syncwarp();
+        BatchAcc* ac = B.acc + dom;
+        if (lane == 0) atomicAdd(&ac->drho, (unsigned long long)W.drho);
+        else if (lane == 1) atomicAdd(&ac->ke, (unsigned long long)W.ke);
+        else if (lane == 2) atomicAdd(&ac->tke, (unsigned long long)W.tke);
+        else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ac->cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
+        else if (lane == 10 && mx > 0.0f) atomicMax(&ac->maxu2, __float_as_uint(mx));
+        __threadfence();
+        __syncwarp();
+        int last = 0;
+        if (lane == 0)
+            last = atomicAdd(&ac->done, (unsigned int)w_slices) + (unsigned int)w_slices == (unsigned int)B.doms[dom].nslices;
+        if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
+            __threadfence();
+            volatile BatchAcc* va = ac;
+            const double t[5] = {(double)(long long)va->drho / (double)FX_SUM, (double)(long long)va->ke / (double)FX_SUM,
+                                 (double)(long long)va->tke / (double)FX_TKE, 0.0, 0.0};
+            const long long c[8] = {(long long)va->cnt[0], (long long)va->cnt[1], (long long)va->cnt[2],
+                                    (long long)va->cnt[3], (long long)va->cnt[4], (long long)va->cnt[5], 0,
+                                    (long long)va->cnt[6]};
+            apply_totals(A, t, __uint_as_float(va->maxu2), c);
+            va->drho = 0; va->ke = 0; va->tke = 0;
+            for (int j = 0; j < 7; ++j) va->cnt[j] = 0;
+            va->maxu2 = 0;
+            va->done = 0;
+        }
+        if (lane == 0) {
+            W.drho = W.ke = W.tke = 0;
+            for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
+        }
+        __syncwarp();
+        mx = 0.0f;
+        w_slices = 0;
+    };
+    int cur = -1, par = 0;
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = B.item_begin + (int)atomicAdd(&B.ctl->work_next[KIND], 1u);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= B.item_end) break;
+        if (threadIdx.x == 0) s_item[par] = B.item_begin + (int)atomicAdd(&B.ctl->work_next[KIND], 1u);
+        __syncthreads();
+        const int item = s_item[par];
+        par ^= 1;
+        const bool end = item >= B.item_end;
+        const int dom = end ? -1 : B.work[item].dom;
+        if (cur >= 0 && dom != cur && w_slices > 0) flush(cur);
+        if (end) break;
         const BatchWork wk = B.work[item];
-        const BatchDomain& D = B.doms[wk.dom];
-        if (wk.dom != cur) {
-            __syncwarp();
+        const BatchDomain& D = B.doms[dom];
+        if (dom != cur) {
+            __syncthreads();   // every warp is done with the previous arguments
             const int* src = reinterpret_cast<const int*>(&D.A);
-            int* dst = reinterpret_cast<int*>(s_args[wid]);
-            for (int i = lane; i < (int)(sizeof(StepArgs) / 4); i += 32) dst[i] = src[i];
-            __syncwarp();
-            cur = wk.dom;
+            int* dst = reinterpret_cast<int*>(s_args);
+            for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / 4); i += STEP_BLOCK) dst[i] = src[i];
+            __syncthreads();
+            cur = dom;
         }
         // a halted domain stays halted for the rest of the call (its flag is
         // only set by its own finisher, after its last slice of a step)
@@ -1347,13 +1410,9 @@ __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_batch_step(cons
         V.apply_overrides = D.overrides0 || k > 0;
         V.write_obs = write_obs;
         V.write_u = D.les || write_obs;
-        WarpSums& W = s_sums[wid];
-        if (lane == 0) {
-            W.drho = W.ke = W.tke = 0;
-            for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
-        }
-        float mx = 0.0f;   // per lane, reduced once per item
-        for (int sl = 0; sl < wk.nslices; ++sl) {
+        for (int base = 0; base < wk.nslices; base += STEP_BLOCK / 32) {
+            const int sl = base + wid;
+            if (sl >= wk.nslices) break;   // warp-uniform
             Acc acc;
             acc.zero();
             const int idx = (wk.slice0 + sl) * 32 + lane;
@@ -1376,39 +1435,12 @@ __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_batch_step(cons
                 if (rare)
                     for (int j = 0; j < 6; ++j) W.cnt[j] += c6[j];
             }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        __syncwarp();
-        BatchAcc* ac = B.acc + wk.dom;
-        // one atomic per lane
-        if (lane == 0) atomicAdd(&ac->drho, (unsigned long long)W.drho);
-        else if (lane == 1) atomicAdd(&ac->ke, (unsigned long long)W.ke);
-        else if (lane == 2) atomicAdd(&ac->tke, (unsigned long long)W.tke);
-        else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ac->cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
-        else if (lane == 10 && mx > 0.0f) atomicMax(&ac->maxu2, __float_as_uint(mx));
-        __threadfence();
-        __syncwarp();
-        int last = 0;
-        if (lane == 0) last = atomicAdd(&ac->done, (unsigned int)wk.nslices) + (unsigned int)wk.nslices == (unsigned int)D.nslices;
-        if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
-            __threadfence();
-            volatile BatchAcc* va = ac;
-            const double t[5] = {(double)(long long)va->drho / (double)FX_SUM, (double)(long long)va->ke / (double)FX_SUM,
-                                 (double)(long long)va->tke / (double)FX_TKE, 0.0, 0.0};
-            const long long c[8] = {(long long)va->cnt[0], (long long)va->cnt[1], (long long)va->cnt[2],
-                                    (long long)va->cnt[3], (long long)va->cnt[4], (long long)va->cnt[5], 0,
-                                    (long long)va->cnt[6]};
-            apply_totals(A, t, __uint_as_float(va->maxu2), c);
-            va->drho = 0; va->ke = 0; va->tke = 0;
-            for (int j = 0; j < 7; ++j) va->cnt[j] = 0;
-            va->maxu2 = 0;
-            va->done = 0;
+            ++w_slices;
         }
     }
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(&B.ctl->warps_done[KIND], 1u) == gridDim.x * (STEP_BLOCK / 32) - 1) {
+        if (atomicAdd(&B.ctl->warps_done[KIND], 1u) == gridDim.x - 1) {   // counts blocks
             B.ctl->work_next[KIND] = 0;
             B.ctl->warps_done[KIND] = 0;
             if (KIND == 1) B.ctl->k = k + 1;
