@@ -79,13 +79,24 @@ __global__ void __launch_bounds__(FORCE_BLOCK) k_cv_force(const ForceArgs a) {
         last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
+    if (!last) return;
+    // the last block sums the block partials: strided per thread, then the
+    // same shuffle and warp order as above (a fixed order: deterministic)
     __threadfence();
     double t[3] = {0.0, 0.0, 0.0};
     const volatile double* pp = a.partials;
-    for (unsigned b = 0; b < gridDim.x; ++b)
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += FORCE_BLOCK)
         for (int k = 0; k < 3; ++k) t[k] += pp[3 * b + k];
-    for (int k = 0; k < 3; ++k) a.out[k] = t[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 3; ++k) t[k] += __shfl_down_sync(0xffffffffu, t[k], o);
+    __syncthreads();   // s[] is reused
+    if (lane == 0) { s[0][wid] = t[0]; s[1][wid] = t[1]; s[2][wid] = t[2]; }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double r[3] = {0.0, 0.0, 0.0};
+    for (int w = 0; w < FORCE_BLOCK / 32; ++w) { r[0] += s[0][w]; r[1] += s[1][w]; r[2] += s[2][w]; }
+    for (int k = 0; k < 3; ++k) a.out[k] = r[k];
     *a.counter = 0;
 }
 

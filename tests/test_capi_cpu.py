@@ -103,3 +103,16 @@ def test_geometry_generators():
     p = geometry.perturbed_icosphere(4, 10.0, (0, 0, 0), seed=3)
     assert p.shape == (5120, 9)
     assert np.array_equal(p, geometry.perturbed_icosphere(4, 10.0, (0, 0, 0), seed=3))
+
+
+def test_bench_control_block_size_matches_device_struct(tmp_path):
+    """bench.py counts the bytes every step call reads back with the size of
+    the device control block: keep the two in step."""
+    import bench
+    src = tmp_path / "t.cu"
+    src.write_text('#include <cstdio>\n#include "lbm_step.cuh"\n'
+                   'int main() { printf("%zu\\n", sizeof(aeros::Control)); return 0; }\n')
+    exe = tmp_path / "t"
+    subprocess.check_call(["nvcc", "-std=c++17", "-I", os.path.join(ROOT, "aeros-engine_gb300", "csrc"), str(src),
+                           "-o", str(exe)])
+    assert int(subprocess.check_output([str(exe)]).decode().strip()) == bench.CONTROL_BYTES
