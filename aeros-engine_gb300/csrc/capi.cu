@@ -69,6 +69,8 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->desc);
     cudaFree(h->shell);
     cudaFree(h->shell_kind);
+    cudaFree(h->shell_gth);
+    cudaFree(h->shell_sct);
     cudaFree(h->u[0]);
     cudaFree(h->u[1]);
     cudaFree(h->rho);
@@ -194,6 +196,52 @@ static void build_shell_kinds(aeros_lbm* h) {
             for (int i = 0; i < Q7; ++i) v |= (unsigned long long)host_th_kind(h, x, y, z, i) << (40 + 2 * i);
         h->shell_kind_host[k] = v;
     }
+}
+
+// Host twin of resolve_kind (lbm_step.cuh): plane and cell of the source of
+// population q of a shell cell under link kind `kind`.
+static void host_resolve(const aeros_lbm* h, int x, int y, int z, int q, int kind, int& slot, int& idx) {
+    const int c = cidx(h, x, y, z);
+    if (kind == L_BOUNCE || kind == L_COPYOWN) { slot = q; idx = c; return; }
+    int s0 = x - cx19(q), s1 = y - cy19(q), s2 = z - cz19(q);
+    if (h->p.periodic_x) s0 = s0 < 0 ? s0 + h->nx : (s0 >= h->nx ? s0 - h->nx : s0);
+    if (h->p.periodic_z) s2 = s2 < 0 ? s2 + h->nz : (s2 >= h->nz ? s2 - h->nz : s2);
+    if (kind == L_REGULAR) { slot = opp19(q); idx = cidx(h, s0, s1, s2); return; }
+    const bool o0 = s0 < 0 || s0 >= h->nx, o1 = s1 < 0 || s1 >= h->ny, o2 = s2 < 0 || s2 >= h->nz;
+    const int rq = dir19_of(o0 ? -cx19(q) : cx19(q), o1 ? -cy19(q) : cy19(q), o2 ? -cz19(q) : cz19(q));
+    slot = opp19(rq);
+    idx = cidx(h, o0 ? x : s0, o1 ? y : s1, o2 ? z : s2);
+}
+
+// Odd-step gather and scatter element offsets of every shell cell (as the
+// device resolves them), when plane * qstride + cell fits in 32 bits.
+static int build_shell_tables(aeros_lbm* h) {
+    const size_t ns = h->shell_host.size();
+    if (!ns || (unsigned long long)h->qstride * Q19 > 0xffffffffull) return AEROS_OK;
+    std::vector<uint32_t> gth(ns * Q19), sct(ns * Q19);
+    for (size_t k = 0; k < ns; ++k) {
+        const int c = h->shell_host[k];
+        const int x = c % h->nx, r = c / h->nx, y = r % h->ny, z = r / h->ny;
+        const unsigned long long sk = h->shell_kind_host[k];
+        for (int q = 0; q < Q19; ++q) {
+            int slot, idx;
+            host_resolve(h, x, y, z, q, (int)((sk >> (2 * q)) & 3ull), slot, idx);
+            gth[(size_t)q * ns + k] = (uint32_t)((unsigned long long)slot * h->qstride + idx);
+            // post-collision f_j goes where the source of population opp(j) lies;
+            // bounce-back and copy-own keep it in the cell's own slot opp(j)
+            const int oj = opp19(q);
+            const int kind = (int)((sk >> (2 * oj)) & 3ull);
+            host_resolve(h, x, y, z, oj, kind, slot, idx);
+            if (kind == L_BOUNCE || kind == L_COPYOWN) { slot = oj; idx = c; }
+            sct[(size_t)q * ns + k] = (uint32_t)((unsigned long long)slot * h->qstride + idx);
+        }
+    }
+    int rc = dalloc(h, &h->shell_gth, gth.size() * 4);
+    if (rc == AEROS_OK) rc = dalloc(h, &h->shell_sct, sct.size() * 4);
+    if (rc != AEROS_OK) return rc;
+    CUDA_TRY(cudaMemcpy(h->shell_gth, gth.data(), gth.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->shell_sct, sct.data(), sct.size() * 4, cudaMemcpyHostToDevice));
+    return AEROS_OK;
 }
 
 static void fill_args(const aeros_lbm* h, FillArgs& fa, const float u[3]) {
@@ -337,6 +385,12 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     if (h->n_shell && (e = cudaMemcpy(h->shell_kind, h->shell_kind_host.data(), h->shell_kind_host.size() * 8,
                                       cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(e, "shell kinds upload");
+    if (getenv("AEROS_SHELL_TABLES") == nullptr || atoi(getenv("AEROS_SHELL_TABLES")) != 0) {
+        if (int rc2 = build_shell_tables(h)) {
+            free_handle(h);
+            return rc2;
+        }
+    }
     for (auto& b : h->u)
         if ((e = cudaMemset(b, 0, n * 16)) != cudaSuccess) return fail(e, "u memset");
     if ((e = cudaMemset(h->strain, 0, n * 4)) != cudaSuccess) return fail(e, "memset");
@@ -437,6 +491,7 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
         A.nbq[q] = cx19(q) + cy19(q) * h->nx + cz19(q) * h->nx * h->ny;
     }
     A.f = h->f; A.desc = h->desc; A.shell = h->shell; A.shell_kind = h->shell_kind;
+    A.shell_gth = h->shell_gth; A.shell_sct = h->shell_sct;
     A.rho = h->rho; A.strain = h->strain; A.tke = h->tke;
     A.out_plane = h->out_plane;
     A.g = h->g; A.T = h->T; A.T_buoy = h->T_buoy;

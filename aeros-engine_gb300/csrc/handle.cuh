@@ -32,6 +32,8 @@ struct aeros_lbm {
     uint32_t* desc = nullptr;
     int* shell = nullptr;
     unsigned long long* shell_kind = nullptr;
+    uint32_t* shell_gth = nullptr;   // odd-step gather / scatter offsets of the shell cells (NULL: resolve)
+    uint32_t* shell_sct = nullptr;
     std::vector<int> shell_host;
     std::vector<unsigned long long> shell_kind_host;
     float4* u[2] = {nullptr, nullptr};   // velocity (ux, uy, uz, 0), double buffered

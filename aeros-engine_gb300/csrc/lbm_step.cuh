@@ -75,6 +75,9 @@ struct StepArgs {
     int nbq[Q19];               // linear offset of c_q: cx + cy * nx + cz * nx * ny
     const uint32_t* desc;
     const int* shell;
+    const uint32_t* shell_gth;  // odd steps: element offset (plane * qstride + cell) of the source of
+                                // population q of shell cell si, at [q * n_shell + si]; NULL: resolve
+    const uint32_t* shell_sct;  // odd steps: element offset that post-collision population j goes to
     const unsigned long long* shell_kind;   // 2 bits per D3Q19 direction (LinkKind),
                                             // 2 bits per D3Q7 direction from bit 40
     float *rho, *strain, *tke;
@@ -831,20 +834,30 @@ __device__ __forceinline__ void interior_finish(const StepArgs& A, const StepVar
 // ---- boundary-shell cell: precomputed link kinds (kept out of line so the
 // interior loop stays small in the instruction cache) ------------------------
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
+__device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, int si, int cell, int x, int y, int z,
                                            unsigned long long skind, Acc& acc) {
     // the link kinds give in-domain sources for every shell cell: the
     // populations are loaded before the descriptor arrives
     const uint32_t d = A.desc[cell];
     constexpr bool SH = S::shifted;
     float f[Q19];
+    const bool tables = ODD && A.shell_gth != nullptr;
+    if (tables) {   // precomputed sources: coalesced table loads instead of per-link index arithmetic
+        const typename S::T* fb = reinterpret_cast<const typename S::T*>(A.f);
+        uint32_t off[Q19];
 #pragma unroll
-    for (int q = 0; q < Q19; ++q) {
-        if (!ODD) {
-            f[q] = S::load_rw(fplane<S>(A, q) + cell);
-        } else {
-            const Link L = resolve_kind(A, x, y, z, cell, q, (int)((skind >> (2 * q)) & 3ull));
-            f[q] = S::load_rw(fplane<S>(A, L.slot) + L.idx);
+        for (int q = 0; q < Q19; ++q) off[q] = __ldg(A.shell_gth + (size_t)q * A.n_shell + si);
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fb + off[q]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) {
+            if (!ODD) {
+                f[q] = S::load_rw(fplane<S>(A, q) + cell);
+            } else {
+                const Link L = resolve_kind(A, x, y, z, cell, q, (int)((skind >> (2 * q)) & 3ull));
+                f[q] = S::load_rw(fplane<S>(A, L.slot) + L.idx);
+            }
         }
     }
     if (d & D_WALL) return;
@@ -906,17 +919,30 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
 #pragma unroll
             for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
         }
+        if (tables) {
+            typename S::T* fb = reinterpret_cast<typename S::T*>(A.f);
+            uint32_t off[Q19];
 #pragma unroll
-        for (int j = 0; j < Q19; ++j) {
-            const int oj = opp19(j);
-            const int kind = (int)((skind >> (2 * oj)) & 3ull);
-            if (!ODD) {
-                S::store(fplane<S>(A, oj) + cell, kind == L_COPYOWN ? f[oj] : f[j]);
-            } else {
-                const Link L = resolve_kind(A, x, y, z, cell, oj, kind);
-                if (L.kind == L_REGULAR || L.kind == L_FREESLIP) S::store(fplane<S>(A, L.slot) + L.idx, f[j]);
-                else if (L.kind == L_BOUNCE) S::store(fplane<S>(A, oj) + cell, f[j]);
-                else S::store(fplane<S>(A, oj) + cell, f[oj]);
+            for (int j = 0; j < Q19; ++j) off[j] = __ldg(A.shell_sct + (size_t)j * A.n_shell + si);
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) {
+                const int oj = opp19(j);
+                const bool copy_own = ((skind >> (2 * oj)) & 3ull) == (unsigned long long)L_COPYOWN;
+                S::store(fb + off[j], copy_own ? f[oj] : f[j]);
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) {
+                const int oj = opp19(j);
+                const int kind = (int)((skind >> (2 * oj)) & 3ull);
+                if (!ODD) {
+                    S::store(fplane<S>(A, oj) + cell, kind == L_COPYOWN ? f[oj] : f[j]);
+                } else {
+                    const Link L = resolve_kind(A, x, y, z, cell, oj, kind);
+                    if (L.kind == L_REGULAR || L.kind == L_FREESLIP) S::store(fplane<S>(A, L.slot) + L.idx, f[j]);
+                    else if (L.kind == L_BOUNCE) S::store(fplane<S>(A, oj) + cell, f[j]);
+                    else S::store(fplane<S>(A, oj) + cell, f[oj]);
+                }
             }
         }
         if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
@@ -1082,7 +1108,7 @@ __device__ __forceinline__ void shell_cell(const StepArgs& A, const StepVar& V, 
         const int x = cell - (int)r * A.nx;
         const uint32_t z = A.div_y.div(r);
         const int y = (int)(r - z * (uint32_t)A.ny);
-        process_shell<S, ODD, THERMAL, MAT>(A, V, cell, x, y, (int)z, A.shell_kind[si], acc);
+        process_shell<S, ODD, THERMAL, MAT>(A, V, si, cell, x, y, (int)z, A.shell_kind[si], acc);
     }
 }
 
@@ -1591,7 +1617,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, STAGED_MIN_BLOCKS) k_lbm_step_stag
                 const int x = cell - (int)r * A.nx;
                 const uint32_t z = A.div_y.div(r);
                 const int y = (int)(r - z * (uint32_t)A.ny);
-                process_shell<S, ODD, false, false>(A, V, cell, x, y, (int)z, A.shell_kind[si], acc);
+                process_shell<S, ODD, false, false>(A, V, si, cell, x, y, (int)z, A.shell_kind[si], acc);
             }
             cur = nxt;
             continue;
