@@ -139,6 +139,7 @@ struct Launchers {
     cudaError_t (*thermal_fill)(const StepArgs& A, float tref, cudaStream_t s);
     cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s);
     int (*batch_occupancy)();
+    int (*fused_occupancy)();
 };
 
 const Launchers& launchers_fp32();
@@ -150,7 +151,7 @@ const Launchers& launchers_bf16();
     template <bool O, bool T, bool M>                                                                                 \
     cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
         if (!M && !T && A.fused) {                                                                                    \
-            k_lbm_fused<STORE, O><<<grid + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V);                                 \
+            k_lbm_fused<STORE, O><<<A.fused_grid + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V);                         \
         } else if (!M && A.split) {                                                                                   \
             StepArgs B = A;                                                                                           \
             B.shell_part_base = grid;                                                                                 \
@@ -219,6 +220,13 @@ const Launchers& launchers_bf16();
         }                                                                                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
+    int fused_occ_() {                                                                                                \
+        int n = 0, m = 0;                                                                                             \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false>, STEP_BLOCK, 0);                  \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_lbm_fused<STORE, true>, STEP_BLOCK, 0);                   \
+        n = n < m ? n : m;                                                                                            \
+        return n > 0 ? n : 1;                                                                                         \
+    }                                                                                                                 \
     int batch_occ_() {                                                                                                \
         int n = 0, m = 0;                                                                                             \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<STORE, false, 1>, STEP_BLOCK, 0);              \
@@ -229,7 +237,7 @@ const Launchers& launchers_bf16();
     }                                                                                                                 \
     const Launchers& NAME() {                                                                                         \
         using namespace NAME##_detail;                                                                                \
-        static const Launchers L = {step_, occupancy_, fill_, seteq_, writepre_, reset_, thfill_, batch_, batch_occ_};                    \
+        static const Launchers L = {step_, occupancy_, fill_, seteq_, writepre_, reset_, thfill_, batch_, batch_occ_, fused_occ_};                    \
         return L;                                                                                                     \
     }
 

@@ -103,6 +103,7 @@ struct StepArgs {
     int split;                  // shell and interior as two launches
     int fused;                  // one launch: shell blocks beside dynamic interior blocks (non-thermal)
     int shell_blocks;           // fused: blocks given to the boundary shell
+    int fused_grid;             // fused: interior blocks (resident blocks per SM x SMs)
     int shell_part_base, shell_grid;   // split: first partial slot and grid of the shell launch
     int total_div10, fluid_cells;
     float conv_threshold;
@@ -1211,8 +1212,15 @@ __device__ __forceinline__ int warp_allsum(int v) {
 // the remaining tiles. Each 32-cell slice's sums are converted to 64-bit fixed
 // point and accumulated exactly, so the statistics do not depend on which
 // block took which tile.
+#ifndef AEROS_FUSED_MIN_BLOCKS
+#define AEROS_FUSED_MIN_BLOCKS 4
+#endif
+#ifndef AEROS_BATCH_MIN_BLOCKS
+#define AEROS_BATCH_MIN_BLOCKS 4
+#endif
+
 template <class S, bool ODD>
-__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_fused(const StepArgs A, const StepVar V) {
+__global__ void __launch_bounds__(STEP_BLOCK, AEROS_FUSED_MIN_BLOCKS) k_lbm_fused(const StepArgs A, const StepVar V) {
     if (A.ctl->halt) return;   // uniform: every thread reads the same flag
     __shared__ WarpSums s_sums[STEP_BLOCK / 32];
     __shared__ int s_tile[2];
@@ -1345,7 +1353,7 @@ struct BatchArgs {
 // KIND 0: the shell slices of every domain; KIND 1: the interior slices (one
 // launch each per step, so each launch's code is only its own path).
 template <class S, bool ODD, int KIND>
-__global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_batch_step(const BatchArgs B) {
+__global__ void __launch_bounds__(STEP_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_step(const BatchArgs B) {
     // Blocks take items; warp w of the block takes slice w of every group of
     // eight, so a block covers 256 consecutive cells at a time (the rows the
     // velocity stencil shares stay in L1). The current domain's arguments are
