@@ -71,6 +71,7 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->shell_kind);
     cudaFree(h->shell_gth);
     cudaFree(h->shell_sct);
+    cudaFree(h->zg_src);
     cudaFree(h->u[0]);
     cudaFree(h->u[1]);
     cudaFree(h->rho);
@@ -244,6 +245,45 @@ static int build_shell_tables(aeros_lbm* h) {
     return AEROS_OK;
 }
 
+static int host_plane_index(const aeros_lbm* h, int x, int y, int z) {
+    const int ax = h->p.flow_axis;
+    return ax == 0 ? y + h->ny * z : (ax == 1 ? x + h->nx * z : x + h->nx * y);
+}
+
+// Zero-gradient outlet: for every outlet-plane cell and unknown population q,
+// the plane index of the side-buffer value it takes (the device rule in
+// process_shell, evaluated once).
+static int build_zerograd_table(aeros_lbm* h) {
+    if (h->outlet_mode != 2) return AEROS_OK;
+    const int ax = h->p.flow_axis, sg = h->p.flow_sign;
+    const int n3[3] = {h->nx, h->ny, h->nz};
+    const int per[3] = {h->p.periodic_x, 0, h->p.periodic_z};
+    const int opos = sg > 0 ? n3[ax] - 1 : 0;
+    const int P = h->out_plane;
+    std::vector<int> tab((size_t)Q19 * P, 0);
+    for (int z = 0; z < h->nz; ++z)
+        for (int y = 0; y < h->ny; ++y)
+            for (int x = 0; x < h->nx; ++x) {
+                const int pos[3] = {x, y, z};
+                if (pos[ax] != opos) continue;
+                const int pi = host_plane_index(h, x, y, z);
+                for (int q = 0; q < Q19; ++q) {
+                    if (ca19(q, ax) * sg >= 0) continue;
+                    int t[3] = {x - cx19(q), y - cy19(q), z - cz19(q)};
+                    t[ax] = pos[ax];
+                    for (int a = 0; a < 3; ++a) {
+                        if (a == ax) continue;
+                        if (t[a] < 0 || t[a] >= n3[a]) t[a] = per[a] ? (t[a] + n3[a]) % n3[a] : pos[a];
+                    }
+                    const bool wall = h->mask[cidx(h, t[0], t[1], t[2])] != 0;
+                    tab[(size_t)q * P + pi] = wall ? pi : host_plane_index(h, t[0], t[1], t[2]);
+                }
+            }
+    if (int rc = dalloc(h, &h->zg_src, tab.size() * 4)) return rc;
+    CUDA_TRY(cudaMemcpy(h->zg_src, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+    return AEROS_OK;
+}
+
 static void fill_args(const aeros_lbm* h, FillArgs& fa, const float u[3]) {
     fa.f = h->f;
     fa.desc = h->desc;
@@ -386,7 +426,9 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
                                       cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(e, "shell kinds upload");
     if (getenv("AEROS_SHELL_TABLES") == nullptr || atoi(getenv("AEROS_SHELL_TABLES")) != 0) {
-        if (int rc2 = build_shell_tables(h)) {
+        int rc2 = build_shell_tables(h);
+        if (rc2 == AEROS_OK) rc2 = build_zerograd_table(h);
+        if (rc2) {
             free_handle(h);
             return rc2;
         }
@@ -493,6 +535,7 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     }
     A.f = h->f; A.desc = h->desc; A.shell = h->shell; A.shell_kind = h->shell_kind;
     A.shell_gth = h->shell_gth; A.shell_sct = h->shell_sct;
+    A.zg_src = h->zg_src;
     A.rho = h->rho; A.strain = h->strain; A.tke = h->tke;
     A.out_plane = h->out_plane;
     A.g = h->g; A.T = h->T; A.T_buoy = h->T_buoy;
@@ -512,6 +555,10 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     for (int q = 0; q < Q19; ++q) A.feq_in[q] = h->feq_in[q];
     A.conv = h->conv;
     A.flow_axis = p.flow_axis; A.flow_sign = p.flow_sign;
+    {
+        const int na = p.flow_axis == 0 ? h->nx : (p.flow_axis == 1 ? h->ny : h->nz);
+        A.inlet_pos = p.flow_sign > 0 ? 0 : na - 1;   // as the descriptor's D_INLET plane
+    }
     A.periodic_x = p.periodic_x; A.periodic_z = p.periodic_z;
     A.use_trt = p.use_trt; A.use_les = p.use_les;
     A.freeslip = p.lateral_bc == AEROS_LATERAL_FREESLIP;

@@ -34,6 +34,7 @@ struct aeros_lbm {
     unsigned long long* shell_kind = nullptr;
     uint32_t* shell_gth = nullptr;   // odd-step gather / scatter offsets of the shell cells (NULL: resolve)
     uint32_t* shell_sct = nullptr;
+    int* zg_src = nullptr;            // zero-gradient outlet sources (NULL: computed on the device)
     std::vector<int> shell_host;
     std::vector<unsigned long long> shell_kind_host;
     float4* u[2] = {nullptr, nullptr};   // velocity (ux, uy, uz, 0), double buffered

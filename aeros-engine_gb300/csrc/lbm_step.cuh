@@ -104,6 +104,9 @@ struct StepArgs {
     int fused;                  // one launch: shell blocks beside dynamic interior blocks (non-thermal)
     int shell_blocks;           // fused: blocks given to the boundary shell
     int fused_grid;             // fused: interior blocks (resident blocks per SM x SMs)
+    int inlet_pos;              // inlet plane coordinate along the flow axis
+    const int* zg_src;          // zero-gradient outlet: plane index each unknown q of outlet-plane
+                                // cell pi reads, at [q * out_plane + pi] (NULL: computed)
     int shell_part_base, shell_grid;   // split: first partial slot and grid of the shell launch
     int total_div10, fluid_cells;
     float conv_threshold;
@@ -843,7 +846,14 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
     constexpr bool SH = S::shifted;
     float f[Q19];
     const bool tables = ODD && A.shell_gth != nullptr;
-    if (tables) {   // precomputed sources: coalesced table loads instead of per-link index arithmetic
+    // the inlet override replaces every population of an inlet-plane cell
+    // (lbm.cpp:1411-1429): nothing to load there
+    const int apos = A.flow_axis == 0 ? x : (A.flow_axis == 1 ? y : z);
+    const bool inlet_override = V.apply_overrides && !A.periodic_x && apos == A.inlet_pos;
+    if (inlet_override) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) f[q] = A.feq_in[q];
+    } else if (tables) {   // precomputed sources: coalesced table loads instead of per-link index arithmetic
         const typename S::T* fb = reinterpret_cast<const typename S::T*>(A.f);
         uint32_t off[Q19];
 #pragma unroll
@@ -893,14 +903,19 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
 #pragma unroll
                 for (int q = 0; q < Q19; ++q) {
                     if (ca19(q, A.flow_axis) * A.flow_sign >= 0) continue;
-                    int t[3] = {x - cx19(q), y - cy19(q), z - cz19(q)};
-                    t[A.flow_axis] = pos[A.flow_axis];
-                    for (int a = 0; a < 3; ++a) {
-                        if (a == A.flow_axis) continue;
-                        if (t[a] < 0 || t[a] >= n3[a]) t[a] = per[a] ? (t[a] + n3[a]) % n3[a] : pos[a];
+                    int tpi;
+                    if (A.zg_src) {   // precomputed at creation
+                        tpi = __ldg(A.zg_src + q * P + pi);
+                    } else {
+                        int t[3] = {x - cx19(q), y - cy19(q), z - cz19(q)};
+                        t[A.flow_axis] = pos[A.flow_axis];
+                        for (int a = 0; a < 3; ++a) {
+                            if (a == A.flow_axis) continue;
+                            if (t[a] < 0 || t[a] >= n3[a]) t[a] = per[a] ? (t[a] + n3[a]) % n3[a] : pos[a];
+                        }
+                        const int tc = (t[2] * A.ny + t[1]) * A.nx + t[0];
+                        tpi = is_wall(A, tc) ? pi : plane_index(A, t[0], t[1], t[2]);
                     }
-                    const int tc = (t[2] * A.ny + t[1]) * A.nx + t[0];
-                    const int tpi = is_wall(A, tc) ? pi : plane_index(A, t[0], t[1], t[2]);
                     f[q] = V.out_r[(0 * Q19 + q) * P + tpi];
                 }
             }
