@@ -73,6 +73,32 @@ class VoxelPlan(C.Structure):
                 ("requested_res", C.c_int32), ("suggested_res", C.c_int32)]
 
 
+class WorldParams(C.Structure):
+    _fields_ = [("flow_speed", C.c_float), ("air_density", C.c_float), ("min", C.c_float * 3),
+                ("cell", C.c_float * 3), ("reserved", C.c_int32 * 4)]
+
+
+class WorldStats(C.Structure):
+    _fields_ = [("pressure_min", C.c_float), ("pressure_max", C.c_float), ("residual_rho", C.c_float),
+                ("residual_u", C.c_float), ("pressure_non_finite", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+AEROS_FIELD_VELOCITY_LB, AEROS_FIELD_DENSITY, AEROS_FIELD_PRESSURE, AEROS_FIELD_VORTICITY = 0, 1, 2, 3
+AEROS_FIELD_Q, AEROS_FIELD_STRAIN, AEROS_FIELD_TKE, AEROS_FIELD_SOLID = 4, 5, 6, 7
+
+
+def make_world(flow_speed=1.0, air_density=1.225, mn=(0.0, 0.0, 0.0), cell=(1.0, 1.0, 1.0)) -> WorldParams:
+    w = WorldParams()
+    w.flow_speed, w.air_density = float(flow_speed), float(air_density)
+    for i in range(3):
+        w.min[i] = float(mn[i])
+        w.cell[i] = float(cell[i])
+    return w
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("blocks_per_sm", C.c_int32), ("tiles_per_item", C.c_int32), ("shell_tiles_per_item", C.c_int32),
                 ("chunk_steps", C.c_int32), ("reserved", C.c_int32 * 4)]
@@ -152,6 +178,9 @@ _SIGS = {
     "aeros_lbm_last_step_ms": (C.c_int, [_P, _FP]),
     "aeros_lbm_last_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "aeros_lbm_device_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "aeros_lbm_world_fields": (C.c_int, [_P, C.POINTER(WorldParams), _FP, _FP, _FP, _FP, C.POINTER(WorldStats)]),
+    "aeros_lbm_vorticity_q": (C.c_int, [_P, _FP, _FP, _FP]),
+    "aeros_lbm_sample": (C.c_int, [_P, C.POINTER(WorldParams), C.c_int, _FP, C.c_int64, _FP, _U8P]),
     "aeros_batch_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
     "aeros_batch_destroy": (C.c_int, [_P]),
     "aeros_batch_add": (C.c_int, [_P, _P]),

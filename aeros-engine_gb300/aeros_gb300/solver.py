@@ -150,6 +150,33 @@ class Solver:
         check(lib().aeros_lbm_cv_force_box(self.h, b, out.ctypes.data_as(_DP)), "cv_force_box")
         return out
 
+    # ---- readback and post-processing -----------------------------------
+    def world_fields(self, world: capi.WorldParams, read=True) -> tuple[dict, dict]:
+        """World velocity and pressure of the last step (kept on the device;
+        copied to host arrays when `read`) and the readback statistics."""
+        out = {k: np.empty(self.n, np.float32) for k in ("ux", "uy", "uz", "pressure")} if read else {}
+        st = capi.WorldStats()
+        ptr = (lambda k: _f(out[k])) if read else (lambda k: None)
+        check(lib().aeros_lbm_world_fields(self.h, C.byref(world), ptr("ux"), ptr("uy"), ptr("uz"),
+                                           ptr("pressure"), C.byref(st)), "world_fields")
+        return out, st.as_dict()
+
+    def vorticity_q(self, read=True) -> dict:
+        out = {k: np.empty(self.n, np.float32) for k in ("vorticity", "q", "strain")} if read else {}
+        ptr = (lambda k: _f(out[k])) if read else (lambda k: None)
+        check(lib().aeros_lbm_vorticity_q(self.h, ptr("vorticity"), ptr("q"), ptr("strain")), "vorticity_q")
+        return out
+
+    def sample(self, world: capi.WorldParams, field: int, points: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        n = pts.shape[0]
+        per = 3 if field == capi.AEROS_FIELD_VELOCITY_LB else 1
+        out = np.empty(n * per, np.float32)
+        valid = np.empty(n, np.uint8)
+        check(lib().aeros_lbm_sample(self.h, C.byref(world), int(field), _f(pts), n, _f(out),
+                                     valid.ctypes.data_as(_U8P)), "sample")
+        return (out.reshape(n, 3) if per == 3 else out), valid
+
     def projected_area(self, axis: int) -> float:
         v = C.c_double()
         check(lib().aeros_lbm_projected_area(self.h, int(axis), C.byref(v)), "projected_area")

@@ -7,6 +7,7 @@ Translation units and their floating-point contraction:
   voxel.cu     --fmad=false  bit-exact inside test
   capi.cu      --fmad=false  host code with -ffp-contract=off
   batch.cu     --fmad=false  host side of the many-domain batch
+  post.cu      --fmad=false  world fields, vorticity / Q, samplers as the reference rounds them
 """
 from __future__ import annotations
 
@@ -34,6 +35,7 @@ UNITS = {
     "voxel.cu": ["--fmad=false"],
     "capi.cu": ["--fmad=false"],
     "batch.cu": ["--fmad=false"],
+    "post.cu": ["--fmad=false"],
     "setup.cu": [],
 }
 HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh", "setup.cuh", "handle.cuh"]

@@ -72,6 +72,10 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->shell_gth);
     cudaFree(h->shell_sct);
     cudaFree(h->zg_src);
+    for (float* b : {h->uxw, h->uyw, h->uzw, h->pressure, h->vort, h->qcrit, h->prev_rho}) cudaFree(b);
+    cudaFree(h->post_parts);
+    cudaFree(h->post_out);
+    cudaFree(h->post_counter);
     cudaFree(h->u[0]);
     cudaFree(h->u[1]);
     cudaFree(h->rho);

@@ -35,6 +35,15 @@ struct aeros_lbm {
     uint32_t* shell_gth = nullptr;   // odd-step gather / scatter offsets of the shell cells (NULL: resolve)
     uint32_t* shell_sct = nullptr;
     int* zg_src = nullptr;            // zero-gradient outlet sources (NULL: computed on the device)
+    // post-processing (allocated on first use)
+    float *uxw = nullptr, *uyw = nullptr, *uzw = nullptr, *pressure = nullptr, *vort = nullptr, *qcrit = nullptr;
+    float* prev_rho = nullptr;
+    void* post_parts = nullptr;
+    void* post_out = nullptr;
+    unsigned int* post_counter = nullptr;
+    long long post_prev_step = -1;
+    float post_prev_maxu = 0.0f;
+    float post_min[3] = {0.0f, 0.0f, 0.0f}, post_cell[3] = {1.0f, 1.0f, 1.0f};
     std::vector<int> shell_host;
     std::vector<unsigned long long> shell_kind_host;
     float4* u[2] = {nullptr, nullptr};   // velocity (ux, uy, uz, 0), double buffered

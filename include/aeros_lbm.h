@@ -236,6 +236,54 @@ typedef struct aeros_voxel_plan_t {
 int aeros_voxel_plan(const float size[3], int res, uint64_t budget_bytes,
                      aeros_voxel_plan_t* out);
 
+/* ---- readback and post-processing on the device --------------------------------
+ * World units of the visualizer: the fields stay on the device, the host
+ * arrays below are optional (NULL: not copied). */
+typedef struct aeros_world_params {
+    float flow_speed;        /* freestream speed, m/s (flowSpeed)                    */
+    float air_density;       /* kg/m^3 (airDensity)                                   */
+    float min[3];            /* world position of the grid origin (lbmMinX..)         */
+    float cell[3];           /* world cell size (lbmCellSizeX..)                      */
+    int32_t reserved[4];
+} aeros_world_params;
+
+typedef struct aeros_world_stats {
+    float pressure_min, pressure_max;   /* lbmPressureMin / lbmPressureMax (strided) */
+    float residual_rho;                 /* lbmResidualRho: RMS of rho change since the last call */
+    float residual_u;                   /* lbmResidualU: change of max |u| since the last call */
+    int64_t pressure_non_finite;        /* lbmPressureNonFinite                      */
+} aeros_world_stats;
+
+/* Replaces the readback prep at the end of stepLBMCPU (aeros/src/lbm.cpp:1602-1705)
+ * for the state of the last step: world velocity u * flow_speed / |u_in|
+ * and pressure rho0 cs2 (rho - 1) scale^2 (zero on body and ground cells),
+ * pressure min / max over at most 262,144 strided cells, the density
+ * residual against the previous call and the change of max |u|. */
+int aeros_lbm_world_fields(aeros_lbm* h, const aeros_world_params* wp, float* ux, float* uy, float* uz,
+                           float* pressure, aeros_world_stats* stats);
+/* Replaces computeLBMVorticityAndQ (aeros/src/lbm.cpp:2005-2093): |curl u|,
+ * the Q criterion and sqrt(2 S:S) from the world velocity of the last
+ * aeros_lbm_world_fields call (central differences, interior cells; the
+ * strain also replaces the step's |S| there, as in the reference). */
+int aeros_lbm_vorticity_q(aeros_lbm* h, float* vorticity, float* q, float* strain);
+
+enum {
+    AEROS_FIELD_VELOCITY_LB = 0,   /* getLBMVelocityLB (lbm.cpp:1782-1840): 3 values per point */
+    AEROS_FIELD_DENSITY = 1,       /* sampleFieldTrilinear (lbm.cpp:1881-1933) of lbmRho   */
+    AEROS_FIELD_PRESSURE = 2,      /* ... of lbmPressure                                    */
+    AEROS_FIELD_VORTICITY = 3,
+    AEROS_FIELD_Q = 4,
+    AEROS_FIELD_STRAIN = 5,
+    AEROS_FIELD_TKE = 6,
+    AEROS_FIELD_SOLID = 7          /* isLBMSolidWorld (lbm.cpp:1954-1969): 1 or 0          */
+};
+/* Samples a field at n world points (xyz each) on the device, with the
+ * reference's trilinear rules (solid corners skipped, weights renormalised).
+ * out: n values (3n for the velocity); valid (optional): 1 where the
+ * reference's sampler reports data. */
+int aeros_lbm_sample(aeros_lbm* h, const aeros_world_params* wp, int field, const float* points, int64_t n,
+                     float* out, uint8_t* valid);
+
 /* ---- timing helper for benches ------------------------------------------------ */
 /* Milliseconds of the step kernels enqueued by the last aeros_lbm_step*/
 /* call, measured with CUDA events on the handle's stream. */

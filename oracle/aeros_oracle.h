@@ -53,6 +53,13 @@ void    ao_lbm_cv_force(const ao_lbm* s, float hx, float hy, float hz, double ou
 void    ao_lbm_cv_force_box(const ao_lbm* s, const int32_t box[6], double out[3]);
 double  ao_lbm_projected_area(const ao_lbm* s, int axis);
 /* lbmEquilibriumMoments (aeros/src/lbm.cpp:307-327). Returns 1 on success. */
+/* readback and post-processing (lbm.cpp:1602-1705, 2005-2093, 1782-1969) */
+int     ao_lbm_world_fields(ao_lbm* s, const aeros_world_params* wp, float* ux, float* uy,
+                            float* uz, float* pressure, aeros_world_stats* st);
+int     ao_lbm_vorticity_q(ao_lbm* s, const aeros_world_params* wp, float* vort, float* q,
+                           float* strain);
+int     ao_lbm_sample(const ao_lbm* s, const aeros_world_params* wp, int field, const float* pts,
+                      int64_t n, float* out, uint8_t* valid);
 int     ao_equilibrium_moments(float rho, float ux, float uy, float uz,
                                float* sum, float* mx, float* my, float* mz);
 int     ao_real_bytes(void);

@@ -28,10 +28,12 @@ typedef AO_REAL real;
 #define K(x) (x)
 #define RSQRT(x) sqrt(x)
 #define RABS(x) fabs(x)
+#define RFLOOR(x) floor(x)
 #else
 #define K(x) (x##f)
 #define RSQRT(x) sqrtf(x)
 #define RABS(x) fabsf(x)
+#define RFLOOR(x) floorf(x)
 #endif
 
 #define Q19 19
@@ -85,6 +87,10 @@ struct ao_lbm {
     real *g, *gn, *T, *buoy;
     int ylo, yhi;
     real H, tau_t, alpha, glb, nusselt, mean_t;
+    /* readback / post-processing */
+    real *uxw, *uyw, *uzw, *pres, *vort, *qc, *prev_rho;
+    int64_t prev_step;
+    real prev_maxu;
 };
 
 static inline int ao_idx(const ao_lbm* s, int x, int y, int z) { return (z * s->ny + y) * s->nx + x; }
@@ -229,6 +235,7 @@ ao_lbm* ao_lbm_create(const aeros_lbm_params* p, const uint8_t* mask) {
 void ao_lbm_destroy(ao_lbm* s) {
     if (!s) return;
     free(s->mask); free(s->wall); free(s->f); free(s->fn);
+    free(s->uxw); free(s->uyw); free(s->uzw); free(s->pres); free(s->vort); free(s->qc); free(s->prev_rho);
     free(s->rho); free(s->ux); free(s->uy); free(s->uz); free(s->strain); free(s->tke);
     free(s->g); free(s->gn); free(s->T); free(s->buoy);
     free(s);
@@ -980,4 +987,255 @@ double ao_lbm_projected_area(const ao_lbm* s, int axis) {
             }
     free(hit);
     return (double)(float)area;
+}
+
+
+/* ---- readback and post-processing --------------------------------------------
+ * The readback prep at the end of stepLBMCPU (aeros/src/lbm.cpp:1602-1705):
+ * world velocity and pressure, strided pressure min / max, the density
+ * residual against the previous readback and the change of max |u|. */
+int ao_lbm_world_fields(ao_lbm* s, const aeros_world_params* wp, float* oux, float* ouy, float* ouz, float* op,
+                        aeros_world_stats* st) {
+    const int total = s->total;
+    if (!s->uxw) {
+        s->uxw = (real*)calloc((size_t)total, sizeof(real));
+        s->uyw = (real*)calloc((size_t)total, sizeof(real));
+        s->uzw = (real*)calloc((size_t)total, sizeof(real));
+        s->pres = (real*)calloc((size_t)total, sizeof(real));
+        s->vort = (real*)calloc((size_t)total, sizeof(real));
+        s->qc = (real*)calloc((size_t)total, sizeof(real));
+        s->prev_step = -1;
+        s->prev_maxu = K(0.0);
+        if (!s->uxw || !s->uyw || !s->uzw || !s->pres || !s->vort || !s->qc) return -1;
+    }
+    const real in0 = (real)s->p.u_in[0], in1 = (real)s->p.u_in[1], in2 = (real)s->p.u_in[2];
+    real U0mag2 = RSQRT(in0 * in0 + in1 * in1 + in2 * in2);
+    if (!isfinite(U0mag2) || U0mag2 < K(1e-6)) U0mag2 = K(0.08);
+    real scale = (real)wp->flow_speed / U0mag2;
+    if (!isfinite(scale) || scale > K(1000.0)) scale = K(20.0);
+    const real rho0 = (real)wp->air_density;
+    const real cs2 = K(1.0) / K(3.0);
+    long long pbad = 0;
+    for (int c = 0; c < total; ++c) {
+        if (is_wall(s, c)) {
+            s->uxw[c] = K(0.0); s->uyw[c] = K(0.0); s->uzw[c] = K(0.0);
+            s->pres[c] = K(0.0);
+            continue;
+        }
+        real ux = s->ux[c], uy = s->uy[c], uz = s->uz[c];
+        if (!isfinite(ux)) ux = K(0.0);
+        s->uxw[c] = ux * scale;
+        s->uyw[c] = uy * scale;
+        s->uzw[c] = uz * scale;
+        real rho = s->rho[c];
+        if (!isfinite(rho)) rho = K(1.0);
+        const real pLat = cs2 * (rho - K(1.0));
+        real pPhys = pLat * scale * scale * rho0;
+        if (!isfinite(pPhys)) { pbad++; pPhys = K(0.0); }
+        s->pres[c] = pPhys;
+    }
+    int stride = 1;
+    while (total / stride > 262144) stride *= 2;
+    real pMin = K(1e30), pMax = K(-1e30);
+    const int valid = s->prev_rho != NULL && s->prev_step >= 0 && s->step >= s->prev_step;
+    if (!s->prev_rho) {
+        s->prev_rho = (real*)malloc((size_t)total * sizeof(real));
+        if (!s->prev_rho) return -1;
+        for (int c = 0; c < total; ++c) s->prev_rho[c] = K(1.0);
+    }
+    double sumSq = 0.0;
+    int nSampled = 0;
+    for (int c = 0; c < total; c += stride) {
+        const real p = s->pres[c];
+        if (isfinite(p)) { if (p < pMin) pMin = p; if (p > pMax) pMax = p; }
+        if (valid) {
+            const real r = s->rho[c];
+            if (isfinite(r)) {
+                const real d = r - s->prev_rho[c];
+                sumSq += (double)d * (double)d;
+                ++nSampled;
+            }
+        }
+    }
+    if (st) {
+        st->pressure_min = (pMin <= pMax && isfinite(pMin)) ? (float)pMin : 0.0f;
+        st->pressure_max = (pMin <= pMax && isfinite(pMax)) ? (float)pMax : 0.0f;
+        st->residual_rho = (valid && nSampled > 0) ? (float)sqrt(sumSq / (double)nSampled) : 0.0f;
+        st->residual_u = (float)RABS(s->max_u - s->prev_maxu);
+        st->pressure_non_finite = pbad;
+    }
+    s->prev_maxu = s->max_u;
+    for (int c = 0; c < total; ++c) {
+        const real r = s->rho[c];
+        s->prev_rho[c] = isfinite(r) ? r : K(1.0);
+    }
+    s->prev_step = s->step;
+    for (int c = 0; c < total; ++c) {
+        if (oux) oux[c] = (float)s->uxw[c];
+        if (ouy) ouy[c] = (float)s->uyw[c];
+        if (ouz) ouz[c] = (float)s->uzw[c];
+        if (op) op[c] = (float)s->pres[c];
+    }
+    return 0;
+}
+
+/* computeLBMVorticityAndQ, aeros/src/lbm.cpp:2005-2093 (from the world
+ * velocity of the last ao_lbm_world_fields call). */
+int ao_lbm_vorticity_q(ao_lbm* s, const aeros_world_params* wp, float* ovort, float* oq, float* ostrain) {
+    if (!s->uxw) return -1;
+    const int Nx = s->nx, Ny = s->ny, Nz = s->nz, total = s->total;
+    real csx = (real)wp->cell[0], csy = (real)wp->cell[1], csz = (real)wp->cell[2];
+    if (csx < K(1e-6)) csx = K(0.1);
+    if (csy < K(1e-6)) csy = K(0.1);
+    if (csz < K(1e-6)) csz = K(0.1);
+    const real ix = K(1.0) / csx, iy = K(1.0) / csy, iz = K(1.0) / csz;
+    const real* uxW = s->uxw;
+    const real* uyW = s->uyw;
+    const real* uzW = s->uzw;
+    for (int z = 1; z < Nz - 1; ++z)
+        for (int y = 1; y < Ny - 1; ++y)
+            for (int x = 1; x < Nx - 1; ++x) {
+                const int cell = (z * Ny + y) * Nx + x;
+                if (is_wall(s, cell)) { s->vort[cell] = K(0.0); s->qc[cell] = K(0.0); continue; }
+                const int xm = cell - 1, xp = cell + 1, ym = cell - Nx, yp = cell + Nx;
+                const int zm = cell - Nx * Ny, zp = cell + Nx * Ny;
+                const real dux_dx = (uxW[xp] - uxW[xm]) * K(0.5) * ix;
+                const real dux_dy = (uxW[yp] - uxW[ym]) * K(0.5) * iy;
+                const real dux_dz = (uxW[zp] - uxW[zm]) * K(0.5) * iz;
+                const real duy_dx = (uyW[xp] - uyW[xm]) * K(0.5) * ix;
+                const real duy_dy = (uyW[yp] - uyW[ym]) * K(0.5) * iy;
+                const real duy_dz = (uyW[zp] - uyW[zm]) * K(0.5) * iz;
+                const real duz_dx = (uzW[xp] - uzW[xm]) * K(0.5) * ix;
+                const real duz_dy = (uzW[yp] - uzW[ym]) * K(0.5) * iy;
+                const real duz_dz = (uzW[zp] - uzW[zm]) * K(0.5) * iz;
+                if (!isfinite(dux_dx)) { s->vort[cell] = K(0.0); s->qc[cell] = K(0.0); continue; }
+                const real wx = duz_dy - duy_dz, wy = dux_dz - duz_dx, wz = duy_dx - dux_dy;
+                real vm = RSQRT(wx * wx + wy * wy + wz * wz);
+                if (!isfinite(vm)) vm = K(0.0);
+                if (vm > K(1000.0)) vm = K(1000.0);
+                s->vort[cell] = vm;
+                const real Sxx = dux_dx, Syy = duy_dy, Szz = duz_dz;
+                const real Sxy = K(0.5) * (dux_dy + duy_dx);
+                const real Sxz = K(0.5) * (dux_dz + duz_dx);
+                const real Syz = K(0.5) * (duy_dz + duz_dy);
+                const real Oxy = K(0.5) * (dux_dy - duy_dx);
+                const real Oxz = K(0.5) * (dux_dz - duz_dx);
+                const real Oyz = K(0.5) * (duy_dz - duz_dy);
+                const real S2 = Sxx * Sxx + Syy * Syy + Szz * Szz + K(2.0) * (Sxy * Sxy + Sxz * Sxz + Syz * Syz);
+                const real O2 = K(2.0) * (Oxy * Oxy + Oxz * Oxz + Oyz * Oyz);
+                real Q = K(0.5) * (O2 - S2);
+                if (!isfinite(Q)) Q = K(0.0);
+                if (Q > K(1e6)) Q = K(1e6);
+                if (Q < K(-1e6)) Q = K(-1e6);
+                s->qc[cell] = Q;
+                real strain = RSQRT(K(2.0) * S2);
+                if (!isfinite(strain)) strain = K(0.0);
+                s->strain[cell] = strain;
+            }
+    for (int c = 0; c < total; ++c) {
+        if (ovort) ovort[c] = (float)s->vort[c];
+        if (oq) oq[c] = (float)s->qc[c];
+        if (ostrain) ostrain[c] = (float)s->strain[c];
+    }
+    return 0;
+}
+
+static real clamp01r(real t) { return t < K(0.0) ? K(0.0) : (t > K(1.0) ? K(1.0) : t); }
+
+/* getLBMVelocityLB (lbm.cpp:1782-1840), sampleFieldTrilinear with solid
+ * corners skipped (lbm.cpp:1881-1933), isLBMSolidWorld (lbm.cpp:1954-1969). */
+int ao_lbm_sample(const ao_lbm* s, const aeros_world_params* wp, int field, const float* pts, int64_t n, float* out,
+                  uint8_t* valid) {
+    const real* fld = NULL;
+    if (field == AEROS_FIELD_DENSITY) fld = s->rho;
+    else if (field == AEROS_FIELD_PRESSURE) fld = s->pres;
+    else if (field == AEROS_FIELD_VORTICITY) fld = s->vort;
+    else if (field == AEROS_FIELD_Q) fld = s->qc;
+    else if (field == AEROS_FIELD_STRAIN) fld = s->strain;
+    else if (field == AEROS_FIELD_TKE) fld = s->tke;
+    if (field != AEROS_FIELD_VELOCITY_LB && field != AEROS_FIELD_SOLID && !fld) return -1;
+    const int Nx = s->nx, Ny = s->ny, Nz = s->nz;
+    const real mnx = (real)wp->min[0], mny = (real)wp->min[1], mnz = (real)wp->min[2];
+    const real csx = (real)wp->cell[0], csy = (real)wp->cell[1], csz = (real)wp->cell[2];
+    for (int64_t i = 0; i < n; ++i) {
+        const real wx = (real)pts[3 * i], wy = (real)pts[3 * i + 1], wz = (real)pts[3 * i + 2];
+        uint8_t ok = 0;
+        if (field == AEROS_FIELD_VELOCITY_LB) {
+            real rx = K(0.0), ry = K(0.0), rz = K(0.0);
+            if (isfinite(wx)) {
+                const real fx = (wx - mnx) / csx, fy = (wy - mny) / csy, fz = (wz - mnz) / csz;
+                const int ix = (int)RFLOOR(fx), iy = (int)RFLOOR(fy), iz = (int)RFLOOR(fz);
+                const real tx = clamp01r(fx - (real)ix), ty = clamp01r(fy - (real)iy), tz = clamp01r(fz - (real)iz);
+                if (!(ix < 0 || ix >= Nx - 1 || iy < 0 || iy >= Ny - 1 || iz < 0 || iz >= Nz - 1)) {
+                    const real w[8] = {(1 - tx) * (1 - ty) * (1 - tz), tx * (1 - ty) * (1 - tz), (1 - tx) * ty * (1 - tz),
+                                       tx * ty * (1 - tz), (1 - tx) * (1 - ty) * tz, tx * (1 - ty) * tz,
+                                       (1 - tx) * ty * tz, tx * ty * tz};
+                    real vx[8], vy[8], vz[8], ws[8], totalW = K(0.0);
+                    int cnt = 0;
+                    for (int k = 0; k < 8; ++k) {
+                        const int cell = ((iz + ((k >> 2) & 1)) * Ny + (iy + ((k >> 1) & 1))) * Nx + (ix + (k & 1));
+                        if (is_wall(s, cell)) continue;
+                        if (!isfinite(s->ux[cell])) continue;
+                        vx[cnt] = s->ux[cell]; vy[cnt] = s->uy[cell]; vz[cnt] = s->uz[cell]; ws[cnt] = w[k];
+                        totalW += w[k];
+                        ++cnt;
+                    }
+                    if (cnt > 0) {
+                        ok = 1;
+                        if (totalW < K(1e-6)) {
+                            rx = vx[0]; ry = vy[0]; rz = vz[0];
+                        } else {
+                            for (int k = 0; k < cnt; ++k) {
+                                const real sc = ws[k] / totalW;
+                                rx += vx[k] * sc; ry += vy[k] * sc; rz += vz[k] * sc;
+                            }
+                            if (!isfinite(rx)) { rx = K(0.0); ry = K(0.0); rz = K(0.0); }
+                        }
+                    }
+                }
+            }
+            out[3 * i] = (float)rx; out[3 * i + 1] = (float)ry; out[3 * i + 2] = (float)rz;
+        } else if (field == AEROS_FIELD_SOLID) {
+            real r = K(0.0);
+            if (isfinite(wx) && isfinite(wy) && isfinite(wz) && csx >= K(1e-9) && csy >= K(1e-9) && csz >= K(1e-9)) {
+                const real fx = (wx - mnx) / csx, fy = (wy - mny) / csy, fz = (wz - mnz) / csz;
+                const int ix = (int)RFLOOR(fx), iy = (int)RFLOOR(fy), iz = (int)RFLOOR(fz);
+                if (!(ix < 0 || ix >= Nx || iy < 0 || iy >= Ny || iz < 0 || iz >= Nz)) {
+                    ok = 1;
+                    r = is_wall(s, (iz * Ny + iy) * Nx + ix) ? K(1.0) : K(0.0);
+                }
+            }
+            out[i] = (float)r;
+        } else {
+            real r = K(0.0);
+            if (isfinite(wx) && isfinite(wy) && isfinite(wz) && !(csx < K(1e-9) || csy < K(1e-9) || csz < K(1e-9)) &&
+                !(Nx < 2 || Ny < 2 || Nz < 2)) {
+                const real fx = (wx - mnx) / csx, fy = (wy - mny) / csy, fz = (wz - mnz) / csz;
+                const int ix = (int)RFLOOR(fx), iy = (int)RFLOOR(fy), iz = (int)RFLOOR(fz);
+                if (!(ix < 0 || iy < 0 || iz < 0) && !(ix > Nx - 2 || iy > Ny - 2 || iz > Nz - 2)) {
+                    const real tx = clamp01r(fx - (real)ix), ty = clamp01r(fy - (real)iy), tz = clamp01r(fz - (real)iz);
+                    const real wxs[2] = {K(1.0) - tx, tx}, wys[2] = {K(1.0) - ty, ty}, wzs[2] = {K(1.0) - tz, tz};
+                    real acc = K(0.0), wsum = K(0.0);
+                    for (int dz = 0; dz <= 1; ++dz)
+                        for (int dy = 0; dy <= 1; ++dy)
+                            for (int dx = 0; dx <= 1; ++dx) {
+                                const int cell = ((iz + dz) * Ny + (iy + dy)) * Nx + (ix + dx);
+                                if (is_wall(s, cell)) continue;
+                                const real v = fld[cell];
+                                if (!isfinite(v)) continue;
+                                const real w = wxs[dx] * wys[dy] * wzs[dz];
+                                acc += v * w;
+                                wsum += w;
+                            }
+                    if (!(wsum < K(1e-6))) {
+                        acc /= wsum;
+                        if (isfinite(acc)) { r = acc; ok = 1; }
+                    }
+                }
+            }
+            out[i] = (float)r;
+        }
+        if (valid) valid[i] = ok;
+    }
+    return 0;
 }

@@ -18,7 +18,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "aeros-engine_gb300"))
-from aeros_gb300.capi import LbmParams, LbmStats, ThermalParams, VoxelGrid, VoxelPlan  # noqa: E402
+from aeros_gb300.capi import (AEROS_FIELD_VELOCITY_LB, LbmParams, LbmStats, ThermalParams, VoxelGrid,  # noqa: E402
+                              VoxelPlan, WorldParams, WorldStats)
 
 _FP = C.POINTER(C.c_float)
 _U8P = C.POINTER(C.c_uint8)
@@ -74,6 +75,10 @@ def oracle_lib(precision: str = "f32") -> C.CDLL:
         L.ao_count_hits_brute.argtypes = [_FP, C.c_int64, _FP, C.c_int]
         L.ao_voxel_plan.argtypes = [_FP, C.c_int, C.c_uint64, C.POINTER(VoxelPlan)]
         L.ao_set_threads.argtypes = [C.c_int]
+        L.ao_lbm_world_fields.argtypes = [C.c_void_p, C.POINTER(WorldParams), _FP, _FP, _FP, _FP,
+                                          C.POINTER(WorldStats)]
+        L.ao_lbm_vorticity_q.argtypes = [C.c_void_p, C.POINTER(WorldParams), _FP, _FP, _FP]
+        L.ao_lbm_sample.argtypes = [C.c_void_p, C.POINTER(WorldParams), C.c_int, _FP, C.c_int64, _FP, _U8P]
         _libs[precision] = L
     return _libs[precision]
 
@@ -167,6 +172,31 @@ class OracleLBM:
     def projected_area(self, axis: int) -> float:
         return float(self.L.ao_lbm_projected_area(self.h, int(axis)))
 
+    def world_fields(self, world: WorldParams) -> tuple[dict, dict]:
+        out = {k: np.empty(self.n, np.float32) for k in ("ux", "uy", "uz", "pressure")}
+        st = WorldStats()
+        if self.L.ao_lbm_world_fields(self.h, C.byref(world), fptr(out["ux"]), fptr(out["uy"]), fptr(out["uz"]),
+                                      fptr(out["pressure"]), C.byref(st)) != 0:
+            raise RuntimeError("oracle world fields failed")
+        return out, st.as_dict()
+
+    def vorticity_q(self, world: WorldParams) -> dict:
+        out = {k: np.empty(self.n, np.float32) for k in ("vorticity", "q", "strain")}
+        if self.L.ao_lbm_vorticity_q(self.h, C.byref(world), fptr(out["vorticity"]), fptr(out["q"]),
+                                     fptr(out["strain"])) != 0:
+            raise RuntimeError("oracle vorticity failed")
+        return out
+
+    def sample(self, world: WorldParams, field: int, points: np.ndarray):
+        pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        n = pts.shape[0]
+        per = 3 if field == AEROS_FIELD_VELOCITY_LB else 1
+        out = np.empty(n * per, np.float32)
+        valid = np.empty(n, np.uint8)
+        if self.L.ao_lbm_sample(self.h, C.byref(world), int(field), fptr(pts), n, fptr(out), u8ptr(valid)) != 0:
+            raise RuntimeError("oracle sample failed")
+        return (out.reshape(n, 3) if per == 3 else out), valid
+
 
 def equilibrium_moments(rho, ux, uy, uz):
     L = oracle_lib("f32")
@@ -235,6 +265,9 @@ class RefHarness:
         L.ref_validation_setup.argtypes = [C.c_int, C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float,
                                            C.POINTER(C.c_int), _FP, _FP]
         L.ref_get_mask.argtypes = [_U8P]
+        L.ref_world_get.argtypes = [_FP, _FP, _FP, _FP, _FP, C.POINTER(C.c_longlong), _FP]
+        L.ref_vorticity_q.argtypes = [_FP, _FP, _FP]
+        L.ref_sample.argtypes = [C.c_int, _FP, C.c_longlong, _FP, _U8P]
         self.L = L
         self.n = 0
 
@@ -347,3 +380,30 @@ class RefHarness:
         out = (C.c_int * 6)()
         self.L.ref_voxel_plan(fptr(np.asarray(size, np.float32)), int(res), int(budget), out)
         return tuple(out)
+
+    def world(self):
+        """The readback prep of the last step: fields, stats and the world
+        parameters (flowSpeed, airDensity, lbmMin, lbmCellSize) it used."""
+        out = {k: np.empty(self.n, np.float32) for k in ("ux", "uy", "uz", "pressure")}
+        st = np.zeros(4, np.float32)
+        bad = C.c_longlong()
+        wp = np.zeros(8, np.float32)
+        self.L.ref_world_get(fptr(out["ux"]), fptr(out["uy"]), fptr(out["uz"]), fptr(out["pressure"]), fptr(st),
+                             C.byref(bad), fptr(wp))
+        stats = dict(pressure_min=float(st[0]), pressure_max=float(st[1]), residual_rho=float(st[2]),
+                     residual_u=float(st[3]), pressure_non_finite=int(bad.value))
+        return out, stats, [float(v) for v in wp]
+
+    def vorticity_q(self) -> dict:
+        out = {k: np.empty(self.n, np.float32) for k in ("vorticity", "q", "strain")}
+        self.L.ref_vorticity_q(fptr(out["vorticity"]), fptr(out["q"]), fptr(out["strain"]))
+        return out
+
+    def sample(self, field: int, points: np.ndarray):
+        pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        n = pts.shape[0]
+        per = 3 if field == AEROS_FIELD_VELOCITY_LB else 1
+        out = np.empty(n * per, np.float32)
+        valid = np.empty(n, np.uint8)
+        self.L.ref_sample(int(field), fptr(pts), n, fptr(out), u8ptr(valid))
+        return (out.reshape(n, 3) if per == 3 else out), valid

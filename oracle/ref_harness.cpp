@@ -288,4 +288,50 @@ void ref_get_mask(uint8_t* out) {
     for (size_t i = 0; i < n; ++i) out[i] = lbmIsSolid[i] ? 1 : (lbmIsGround[i] ? 2 : 0);
 }
 
+// The readback prep of the last stepLBMCPU call (lbm.cpp:1602-1705): world
+// velocity, pressure, stats4 = {pressure min, max, residual rho, residual u},
+// and the world parameters it used: wp8 = {flowSpeed, airDensity, lbmMin xyz,
+// lbmCellSize xyz}.
+void ref_world_get(float* uxw, float* uyw, float* uzw, float* p, float* stats4, long long* pbad, float* wp8) {
+    const size_t n = lbmUxWorld.size();
+    for (size_t i = 0; i < n; ++i) {
+        uxw[i] = lbmUxWorld[i]; uyw[i] = lbmUyWorld[i]; uzw[i] = lbmUzWorld[i]; p[i] = lbmPressure[i];
+    }
+    stats4[0] = lbmPressureMin; stats4[1] = lbmPressureMax; stats4[2] = lbmResidualRho; stats4[3] = lbmResidualU;
+    *pbad = lbmPressureNonFinite;
+    wp8[0] = flowSpeed; wp8[1] = airDensity;
+    wp8[2] = lbmMinX; wp8[3] = lbmMinY; wp8[4] = lbmMinZ;
+    wp8[5] = lbmCellSizeX; wp8[6] = lbmCellSizeY; wp8[7] = lbmCellSizeZ;
+}
+
+// computeLBMVorticityAndQ (lbm.cpp:2005-2093) and its three fields.
+void ref_vorticity_q(float* vort, float* q, float* strain) {
+    computeLBMVorticityAndQ();
+    const size_t n = lbmVorticityMag.size();
+    for (size_t i = 0; i < n; ++i) { vort[i] = lbmVorticityMag[i]; q[i] = lbmQCriterion[i]; strain[i] = lbmStrainMag[i]; }
+}
+
+// The reference's samplers at n world points: field 0 getLBMVelocityLB (3
+// values), 1..6 sampleFieldTrilinear of rho / pressure / vorticity / Q /
+// strain / TKE with solid corners skipped, 7 isLBMSolidWorld.
+void ref_sample(int field, const float* pts, long long n, float* out, uint8_t* valid) {
+    const std::vector<float>* fields[7] = {nullptr, &lbmRho, &lbmPressure, &lbmVorticityMag, &lbmQCriterion,
+                                           &lbmStrainMag, &lbmTKEField};
+    for (long long i = 0; i < n; ++i) {
+        const glm::vec3 w(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+        if (field == 0) {
+            const glm::vec3 v = getLBMVelocityLB(w);
+            out[3 * i] = v.x; out[3 * i + 1] = v.y; out[3 * i + 2] = v.z;
+            valid[i] = 0;
+        } else if (field == 7) {
+            out[i] = isLBMSolidWorld(w) ? 1.0f : 0.0f;
+            valid[i] = 0;
+        } else {
+            float v = 0.0f;
+            valid[i] = sampleFieldTrilinear(*fields[field], w, true, &v) ? 1 : 0;
+            out[i] = v;
+        }
+    }
+}
+
 }  // extern "C"

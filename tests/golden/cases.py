@@ -137,3 +137,26 @@ def outputs_digest(fields: dict, f: np.ndarray | None, mask: np.ndarray, T=None,
 
 EQ_MOMENT_CASES = [(1.0, 0.0, 0.0, 0.0), (1.0, 0.05, 0.0, 0.0), (0.7, 0.04, -0.03, 0.02), (1.35, -0.02, 0.05, 0.01),
                    (0.55, 0.1, 0.1, 0.0), (1.6, 0.0, 0.0, -0.08), (1.1, 0.28, 0.0, 0.0)]
+
+
+# ---- readback and post-processing fixtures ------------------------------------
+# Cases whose world fields, vorticity / Q / strain and sampler outputs are
+# recorded from the reference (tests/golden/post.json); the freestream speed
+# they are scaled with; the sample points are drawn from splitmix64.
+POST_CASES = ("sphere_trt_les_conv", "channel_force3", "sphere_les_ground_copy", "sphere_plus_y")
+POST_FLOW_SPEED = 12.5
+POST_NPTS = 300
+
+
+def post_points(grid, seed: int = 0x9057) -> np.ndarray:
+    """Sample points in and around the grid (world units = cells): 60 % of the
+    extent around the centre, so some fall outside and next to walls."""
+    from aeros_gb300 import geometry
+    u = geometry.uniform_array(seed, 3 * POST_NPTS, -1.0, 1.0).reshape(-1, 3)
+    g = np.asarray(grid, np.float64)
+    return (u * g * 0.6 + g * 0.5).astype(np.float32)
+
+
+def fdigest(a) -> str:
+    """Digest of a float32 array with -0 folded into +0."""
+    return digest(np.asarray(a, np.float32) + np.float32(0.0))

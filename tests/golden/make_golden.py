@@ -103,9 +103,42 @@ def validation_sphere(R, res=48, d_cells=20, pad=0.15, warm=500, meas=50):
                 digest=outputs_digest(fl, R.populations(), mask.reshape(-1))), mask
 
 
+def post_fixtures(R) -> dict:
+    """World fields + readback statistics of the last step (lbm.cpp:1602-1705),
+    computeLBMVorticityAndQ (lbm.cpp:2005-2093) and the samplers
+    (lbm.cpp:1782-1969) of the reference, for POST_CASES."""
+    from cases import POST_CASES, POST_FLOW_SPEED, fdigest, post_points
+    out = {}
+    for name in POST_CASES:
+        case = CASES[name]
+        nx, ny, nz = case["grid"]
+        solid = case["solid"]().astype(np.uint8).reshape(-1)
+        kw = dict(case["kw"])
+        kw["flow_speed"] = POST_FLOW_SPEED
+        R.setup(nx, ny, nz, solid, ground_rows=case.get("ground_rows", 0), **kw)
+        if "u_init" in case:
+            R.set_uniform(*case["u_init"])
+        R.step(case["steps"])
+        wf, st, wp = R.world()
+        vq = R.vorticity_q()
+        pts = post_points(case["grid"])
+        samples = {}
+        for f in range(8):
+            v, ok = R.sample(f, pts)
+            samples[str(f)] = dict(value=fdigest(v), valid=fdigest(ok.astype(np.float32)))
+        out[name] = dict(world=wp, stats=st, fields={k: fdigest(v) for k, v in wf.items()},
+                         vorticity={k: fdigest(v) for k, v in vq.items()}, samples=samples)
+        print(f"  {name}: p in [{st['pressure_min']:.4g}, {st['pressure_max']:.4g}], residual {st['residual_rho']:.3g}")
+    return out
+
+
 def main():
     O.build()
     R = O.RefHarness()
+    if "--post" in sys.argv:   # only the post-processing fixtures
+        with open(os.path.join(HERE, "post.json"), "w") as fh:
+            json.dump(post_fixtures(R), fh, indent=1, sort_keys=True)
+        return
     out = {"cases": {}, "note": "generated from the reference sources by make_golden.py"}
     t0 = time.time()
     for name, case in CASES.items():
@@ -164,6 +197,9 @@ def main():
                          "1@512/512M": list(R.voxel_plan([1, 1, 1], 512, 512 << 20))}
     with open(os.path.join(HERE, "golden.json"), "w") as fh:
         json.dump(out, fh, indent=1, sort_keys=True)
+    print("post-processing ...")
+    with open(os.path.join(HERE, "post.json"), "w") as fh:
+        json.dump(post_fixtures(R), fh, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "masks.npz"), **masks)
     print(f"done in {time.time() - t0:.0f} s")
 

@@ -109,3 +109,13 @@ def test_golden_published_values():
     assert p > 1.5
     assert round(GOLD["validation_sphere"]["cd"], 3) == 1.128
     assert GOLD["validation_sphere"]["area"] == 316.0
+
+
+@pytest.mark.parametrize("name", ["sphere_trt_les_conv", "channel_force3", "sphere_les_ground_copy", "sphere_plus_y"])
+def test_oracle_post_processing_equals_reference(oracle_built, name):
+    """World fields, readback statistics, vorticity / Q / strain and the
+    samplers of the C restatement, bitwise the reference's."""
+    from post_common import check_post
+    O = oracle_built
+    check_post(name, lambda p, m: O.OracleLBM(p, m), lambda o, n: o.step(n), lambda o, wp: o.world_fields(wp),
+               lambda o, wp: o.vorticity_q(wp), lambda o, wp, f, pts: o.sample(wp, f, pts))
