@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <initializer_list>
 
 std::vector<int> g_voxelData;
 int g_voxNx = 0, g_voxNy = 0, g_voxNz = 0;
@@ -37,6 +38,17 @@ std::vector<float> lbmStrainMag;
 std::vector<char> lbmIsSolid;
 std::vector<char> lbmIsGround;
 
+float lbmMinX = 0.0f, lbmMinY = 0.0f, lbmMinZ = 0.0f;
+float lbmCellSizeX = 1.0f, lbmCellSizeY = 1.0f, lbmCellSizeZ = 1.0f;
+float lbmFacadeFlowSpeed = 1.0f;
+float lbmFacadeAirDensity = 1.225f;
+std::vector<float> lbmUxWorld, lbmUyWorld, lbmUzWorld;
+std::vector<float> lbmPressure;
+std::vector<float> lbmVorticityMag;
+std::vector<float> lbmQCriterion;
+float lbmPressureMin = 0.0f, lbmPressureMax = 0.0f, lbmResidualRho = 0.0f, lbmResidualU = 0.0f;
+long long lbmPressureNonFinite = 0;
+
 ThermalParams thermalParams;
 std::vector<float> thermalT;
 std::vector<float> thermalBuoyancyY;
@@ -47,6 +59,7 @@ float thermalMeanT = 0.0f;
 namespace {
 aeros_lbm* g_handle = nullptr;
 std::string g_error;
+bool g_world_read = false;   // the device holds world fields of the current state
 
 bool ok(int status) {
     if (status == AEROS_OK) return true;
@@ -77,6 +90,36 @@ void pull_stats() {
         thermalNusselt = s.nusselt;
         thermalMeanT = s.mean_t;
     }
+}
+
+aeros_world_params world_params() {
+    aeros_world_params w{};
+    w.flow_speed = lbmFacadeFlowSpeed;
+    w.air_density = lbmFacadeAirDensity;
+    w.min[0] = lbmMinX; w.min[1] = lbmMinY; w.min[2] = lbmMinZ;
+    w.cell[0] = lbmCellSizeX; w.cell[1] = lbmCellSizeY; w.cell[2] = lbmCellSizeZ;
+    return w;
+}
+
+// The world-unit readback of the reference's stepLBMCPU end (lbm.cpp:1602-1705).
+bool read_world() {
+    const size_t n = cells();
+    lbmUxWorld.resize(n);
+    lbmUyWorld.resize(n);
+    lbmUzWorld.resize(n);
+    lbmPressure.resize(n);
+    const aeros_world_params w = world_params();
+    aeros_world_stats st{};
+    if (!ok(aeros_lbm_world_fields(g_handle, &w, lbmUxWorld.data(), lbmUyWorld.data(), lbmUzWorld.data(),
+                                   lbmPressure.data(), &st)))
+        return false;
+    lbmPressureMin = st.pressure_min;
+    lbmPressureMax = st.pressure_max;
+    lbmResidualRho = st.residual_rho;
+    lbmResidualU = st.residual_u;
+    lbmPressureNonFinite = st.pressure_non_finite;
+    g_world_read = true;
+    return true;
 }
 }  // namespace
 
@@ -162,6 +205,10 @@ void initLBM() {
     }
     lbmInitialized = true;
     lbmCurrentStep = 0;
+    g_world_read = false;
+    // the derived fields start at zero, as the reference allocates them (lbm.cpp:566-580)
+    for (std::vector<float>* v : {&lbmUxWorld, &lbmUyWorld, &lbmUzWorld, &lbmPressure, &lbmVorticityMag, &lbmQCriterion})
+        v->assign((size_t)n, 0.0f);
     pull_stats();
     if (lbmFacadeReadbackFields) lbmFacadeReadFields();
 }
@@ -171,10 +218,67 @@ void resetLBM() { initLBM(); }
 void stepLBMCPU(int steps) {
     if (!g_handle || steps <= 0) return;
     if (!ok(aeros_lbm_step(g_handle, steps))) return;
+    g_world_read = false;
     float ms = 0.0f;
     if (ok(aeros_lbm_last_step_ms(g_handle, &ms))) lbmTimeMs = ms;
     pull_stats();
-    if (lbmFacadeReadbackFields) lbmFacadeReadFields();
+    if (lbmFacadeReadbackFields && lbmFacadeReadFields()) read_world();
+}
+
+void computeLBMVorticityAndQ() {
+    if (!g_handle) return;
+    const size_t n = cells();
+    lbmVorticityMag.resize(n);
+    lbmQCriterion.resize(n);
+    lbmStrainMag.resize(n);
+    if (!g_world_read && !read_world()) return;
+    ok(aeros_lbm_vorticity_q(g_handle, lbmVorticityMag.data(), lbmQCriterion.data(), lbmStrainMag.data()));
+}
+
+bool lbmFacadeSample(int field, const float* points, long long n, float* out, uint8_t* valid) {
+    if (!g_handle) return false;
+    const aeros_world_params w = world_params();
+    return ok(aeros_lbm_sample(g_handle, &w, field, points, n, out, valid));
+}
+
+namespace {
+bool sample_one(int field, const LbmVec3& p, float* out) {
+    const float pt[3] = {p.x, p.y, p.z};
+    uint8_t valid = 0;
+    if (!lbmFacadeSample(field, pt, 1, out, &valid)) return false;
+    return valid != 0;
+}
+float sample_or(int field, const LbmVec3& p, float fallback) {
+    float v = 0.0f;
+    return sample_one(field, p, &v) ? v : fallback;
+}
+}  // namespace
+
+LbmVec3 getLBMVelocityLB(const LbmVec3& worldPos) {
+    float v[3] = {0.0f, 0.0f, 0.0f};
+    LbmVec3 r;
+    if (g_handle) sample_one(AEROS_FIELD_VELOCITY_LB, worldPos, v);
+    r.x = v[0]; r.y = v[1]; r.z = v[2];
+    return r;
+}
+float getLBMDensityWorld(const LbmVec3& worldPos) {   // lbm.cpp:1948-1952
+    float rho = 1.0f;
+    if (sample_one(AEROS_FIELD_DENSITY, worldPos, &rho)) return std::min(std::max(rho, 0.8f), 1.2f);
+    return 1.0f;
+}
+bool getLBMPressureWorldChecked(const LbmVec3& worldPos, float* outPa) {
+    if (!outPa) return false;
+    *outPa = 0.0f;
+    return sample_one(AEROS_FIELD_PRESSURE, worldPos, outPa);
+}
+float getLBMPressureWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_PRESSURE, worldPos, 0.0f); }
+float getLBMVorticityWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_VORTICITY, worldPos, 0.0f); }
+float getLBMQWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_Q, worldPos, 0.0f); }
+float getLBMTKEWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_TKE, worldPos, 0.0f); }
+float getLBMStrainWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_STRAIN, worldPos, 0.0f); }
+bool isLBMSolidWorld(const LbmVec3& worldPos) {
+    float v = 0.0f;
+    return sample_one(AEROS_FIELD_SOLID, worldPos, &v) && v != 0.0f;
 }
 
 LbmVec3 lbmControlVolumeForce(float boxHalfX, float boxHalfY, float boxHalfZ) {

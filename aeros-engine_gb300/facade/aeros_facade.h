@@ -95,6 +95,22 @@ extern std::vector<float> lbmStrainMag;
 extern std::vector<char> lbmIsSolid;
 extern std::vector<char> lbmIsGround;
 
+// World-unit readback (aeros/src/lbm.h:126-154): filled after every
+// stepLBMCPU call when lbmFacadeReadbackFields is true, as the reference's
+// stepLBMCPU does at its end (lbm.cpp:1602-1705). The grid's world placement
+// and the freestream: the reference keeps flowSpeed and airDensity in other
+// modules, so a caller copies them into the two inputs below.
+extern float lbmMinX, lbmMinY, lbmMinZ;
+extern float lbmCellSizeX, lbmCellSizeY, lbmCellSizeZ;
+extern float lbmFacadeFlowSpeed;     // flowSpeed, m/s
+extern float lbmFacadeAirDensity;    // airDensity, kg/m^3
+extern std::vector<float> lbmUxWorld, lbmUyWorld, lbmUzWorld;
+extern std::vector<float> lbmPressure;
+extern std::vector<float> lbmVorticityMag;
+extern std::vector<float> lbmQCriterion;
+extern float lbmPressureMin, lbmPressureMax, lbmResidualRho, lbmResidualU;
+extern long long lbmPressureNonFinite;
+
 // ---- solver (aeros/src/lbm.h:156-202) ---------------------------------------
 void initLBM();
 void resetLBM();
@@ -102,6 +118,22 @@ void shutdownLBM();
 void stepLBMCPU(int steps = 1);
 LbmVec3 lbmControlVolumeForce(float boxHalfX, float boxHalfY, float boxHalfZ);
 float lbmProjectedAreaCells(int axis);
+// computeLBMVorticityAndQ (lbm.cpp:2005-2093), on the device.
+void computeLBMVorticityAndQ();
+// The samplers (lbm.cpp:1782-1969), on the device, one point per call.
+LbmVec3 getLBMVelocityLB(const LbmVec3& worldPos);
+float getLBMDensityWorld(const LbmVec3& worldPos);
+float getLBMPressureWorld(const LbmVec3& worldPos);
+bool getLBMPressureWorldChecked(const LbmVec3& worldPos, float* outPa);
+float getLBMVorticityWorld(const LbmVec3& worldPos);
+float getLBMQWorld(const LbmVec3& worldPos);
+float getLBMTKEWorld(const LbmVec3& worldPos);
+float getLBMStrainWorld(const LbmVec3& worldPos);
+bool isLBMSolidWorld(const LbmVec3& worldPos);
+// Many points at once (xyz each): the way to sample a whole slice or a set
+// of streamline seeds without a device round trip per point. field is one of
+// AEROS_FIELD_*; out gets n values (3n for the velocity), valid n flags.
+bool lbmFacadeSample(int field, const float* points, long long n, float* out, uint8_t* valid);
 
 // ---- thermal (aeros/src/thermal_lbm.h:33-72) --------------------------------
 struct ThermalParams {

@@ -1,12 +1,23 @@
 // A caller written against the reference solver interface, built on the
 // C++17 facade: the 64x32x32 Poiseuille channel (walls at y = 0 and y = 31,
-// periodic x and z, body force 1e-6, tau 0.8, BGK, no LES). Steps it, prints
-// the globals the visualizer reads and writes lbmUx to the file argv[2].
+// periodic x and z, body force 1e-6, tau 0.8, BGK, no LES), placed in world
+// space at (-3.2, -1.6, -1.6) with 0.1 m cells. Steps it, prints the globals
+// the visualizer reads and writes to the file argv[2], as float32:
+// lbmUx, lbmUxWorld, lbmUyWorld, lbmPressure, lbmVorticityMag, lbmQCriterion,
+// lbmStrainMag (cells each), then NPTS sample points (xyz) and, for each field
+// 0..7 of lbmFacadeSample, its values (3 per point for the velocity) and
+// validity flags (as floats).
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
 
 #include "aeros_facade.h"
+
+namespace {
+constexpr int NPTS = 64;
+
+void put(FILE* fh, const std::vector<float>& v) { std::fwrite(v.data(), sizeof(float), v.size(), fh); }
+}  // namespace
 
 int main(int argc, char** argv) {
     const int steps = argc > 1 ? std::atoi(argv[1]) : 200;
@@ -27,6 +38,12 @@ int main(int argc, char** argv) {
     lbmParams.bodyForceX = 1e-6f;
     lbmParams.U0 = 0.0f;
     lbmInletVelocityLB[0] = 0.0f;
+    lbmMinX = -3.2f;
+    lbmMinY = -1.6f;
+    lbmMinZ = -1.6f;
+    lbmCellSizeX = lbmCellSizeY = lbmCellSizeZ = 0.1f;
+    lbmFacadeFlowSpeed = 10.0f;
+    lbmFacadeAirDensity = 1.225f;
     initLBM();
     if (!lbmInitialized) {
         std::fprintf(stderr, "initLBM failed: %s\n", lbmFacadeLastError().c_str());
@@ -34,13 +51,44 @@ int main(int argc, char** argv) {
     }
     for (int i = 0; i < steps / 2; ++i) stepLBMCPU(1);   // frame-loop style
     stepLBMCPU(steps - steps / 2);                          // and one batched call
+    computeLBMVorticityAndQ();
     const LbmVec3 F = lbmControlVolumeForce(0.3f, 0.3f, 0.3f);
     std::printf("step %d avg_rho %.9g avg_ke %.9g max_u %.9g fx %.9g area %.1f\n", lbmCurrentStep, lbmAvgRho,
                 lbmAvgKineticEnergy, lbmMaxVelocityLB, F.x, lbmProjectedAreaCells(0));
+    std::printf("pmin %.9g pmax %.9g res_rho %.9g res_u %.9g nonfinite %lld\n", lbmPressureMin, lbmPressureMax,
+                lbmResidualRho, lbmResidualU, lbmPressureNonFinite);
+    // points on a diagonal through the channel, some outside it and some in the walls
+    std::vector<float> pts(3 * NPTS);
+    for (int i = 0; i < NPTS; ++i) {
+        const float t = (float)i / (float)(NPTS - 1);
+        pts[3 * i + 0] = -3.4f + 6.8f * t;
+        pts[3 * i + 1] = -1.7f + 3.4f * t;
+        pts[3 * i + 2] = 0.37f - 0.5f * t;
+    }
+    LbmVec3 mid;
+    mid.x = pts[3 * 20];
+    mid.y = pts[3 * 20 + 1];
+    mid.z = pts[3 * 20 + 2];
+    float pa = 0.0f;
+    const bool pok = getLBMPressureWorldChecked(mid, &pa);
+    const LbmVec3 u = getLBMVelocityLB(mid);
+    std::printf("probe p %.9g ok %d ux %.9g rho %.9g q %.9g vort %.9g strain %.9g tke %.9g solid %d %d\n", pa, (int)pok,
+                u.x, getLBMDensityWorld(mid), getLBMQWorld(mid), getLBMVorticityWorld(mid), getLBMStrainWorld(mid),
+                getLBMTKEWorld(mid), (int)isLBMSolidWorld(mid), (int)isLBMSolidWorld(LbmVec3{-3.0f, -1.58f, 0.0f}));
     if (argc > 2) {
         FILE* fh = std::fopen(argv[2], "wb");
         if (!fh) return 2;
-        std::fwrite(lbmUx.data(), sizeof(float), lbmUx.size(), fh);
+        for (const std::vector<float>* v : {&lbmUx, &lbmUxWorld, &lbmUyWorld, &lbmPressure, &lbmVorticityMag,
+                                            &lbmQCriterion, &lbmStrainMag})
+            put(fh, *v);
+        put(fh, pts);
+        for (int f = AEROS_FIELD_VELOCITY_LB; f <= AEROS_FIELD_SOLID; ++f) {
+            std::vector<float> out((size_t)NPTS * (f == AEROS_FIELD_VELOCITY_LB ? 3 : 1));
+            std::vector<uint8_t> valid(NPTS);
+            if (!lbmFacadeSample(f, pts.data(), NPTS, out.data(), valid.data())) return 4;
+            put(fh, out);
+            put(fh, std::vector<float>(valid.begin(), valid.end()));
+        }
         std::fclose(fh);
     }
     shutdownLBM();

@@ -29,21 +29,63 @@ def test_facade_builds_and_links(driver):
     assert os.path.exists(driver)
 
 
+NPTS = 64   # tests/facade/channel_driver.cpp
+
+
 @pytest.mark.gpu
 def test_facade_channel_equals_c_abi(driver, tmp_path):
+    """The facade's globals after stepLBMCPU and computeLBMVorticityAndQ and
+    its samplers equal, bit for bit, what the C ABI gives for the same calls:
+    a world readback after every stepping call (the residuals compare
+    consecutive readbacks), then vorticity / Q / strain, then the samplers."""
     from aeros_gb300 import capi, geometry, solver
-    out = tmp_path / "ux.bin"
+    out = tmp_path / "fields.bin"
     r = subprocess.run([driver, "200", str(out)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    ux = np.fromfile(out, np.float32)
+    blob = np.fromfile(out, np.float32)
+    n = 64 * 32 * 32
+    got = {k: blob[i * n:(i + 1) * n] for i, k in
+           enumerate(("ux", "uxw", "uyw", "pressure", "vorticity", "q", "strain"))}
+    pos = 7 * n
+    pts = blob[pos:pos + 3 * NPTS].reshape(NPTS, 3)
+    pos += 3 * NPTS
+
     p = capi.make_params(64, 32, 32, tau=0.8, periodic_x=True, periodic_z=True, u_in=(0.0, 0.0, 0.0),
                          body_force=(1e-6, 0.0, 0.0), convective_outlet=True)
+    wp = capi.make_world(10.0, 1.225, (-3.2, -1.6, -1.6), (0.1, 0.1, 0.1))
     s = solver.Solver(p, geometry.channel_mask(64, 32, 32))
     for _ in range(100):
         s.step(1)
+        s.world_fields(wp, read=False)
     s.step(100)
-    ref = s.fields()["ux"]
-    assert np.array_equal(ux, ref)
+    world, wst = s.world_fields(wp)
+    ref = s.fields()
+    vq = s.vorticity_q()
+    assert np.array_equal(got["ux"], ref["ux"])
+    assert np.array_equal(got["uxw"], world["ux"])
+    assert np.array_equal(got["uyw"], world["uy"])
+    assert np.array_equal(got["pressure"], world["pressure"])
+    for k in ("vorticity", "q", "strain"):
+        assert np.array_equal(got[k], vq[k]), k
     st = s.stats()
     assert f"step {st['step']} " in r.stdout
     assert np.float32(r.stdout.split("avg_rho ")[1].split()[0]) == np.float32(st["avg_rho"])
+    line = r.stdout.split("pmin ")[1].split()
+    assert np.float32(line[0]) == np.float32(wst["pressure_min"])
+    assert np.float32(line[2]) == np.float32(wst["pressure_max"])
+    assert np.float32(line[4]) == np.float32(wst["residual_rho"])
+    assert np.float32(line[6]) == np.float32(wst["residual_u"])
+    for f in range(8):
+        per = 3 if f == capi.AEROS_FIELD_VELOCITY_LB else 1
+        v = blob[pos:pos + per * NPTS]
+        pos += per * NPTS
+        ok = blob[pos:pos + NPTS]
+        pos += NPTS
+        rv, rok = s.sample(wp, f, pts)
+        assert np.array_equal(v, rv.reshape(-1)), f
+        assert np.array_equal(ok, rok.astype(np.float32)), f
+    # the one-point getters agree with the many-point call (point 20 lies inside)
+    probe = r.stdout.split("probe ")[1].split()
+    pv, pok = s.sample(wp, capi.AEROS_FIELD_PRESSURE, pts[20:21])
+    assert probe[3] == "1" and pok[0] == 1 and np.float32(probe[1]) == pv[0]
+    assert probe[-2] == "0" and probe[-1] == "1"   # the mid point is fluid, the wall point solid
