@@ -181,6 +181,7 @@ _SIGS = {
     "aeros_lbm_world_fields": (C.c_int, [_P, C.POINTER(WorldParams), _FP, _FP, _FP, _FP, C.POINTER(WorldStats)]),
     "aeros_lbm_vorticity_q": (C.c_int, [_P, _FP, _FP, _FP]),
     "aeros_lbm_sample": (C.c_int, [_P, C.POINTER(WorldParams), C.c_int, _FP, C.c_int64, _FP, _U8P]),
+    "aeros_equilibrium_moments": (C.c_int, [_FP, C.c_int64, _FP, _U8P]),
     "aeros_batch_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
     "aeros_batch_destroy": (C.c_int, [_P]),
     "aeros_batch_add": (C.c_int, [_P, _P]),

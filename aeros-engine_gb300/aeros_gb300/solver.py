@@ -183,6 +183,18 @@ class Solver:
         return float(v.value)
 
 
+def equilibrium_moments(states) -> tuple[np.ndarray, np.ndarray]:
+    """lbmEquilibriumMoments (aeros/src/lbm.cpp:249-267) on the device for
+    rows (rho, ux, uy, uz): returns (n, 4) sums (mass, momentum xyz) and the
+    (n,) finite flags."""
+    st = np.ascontiguousarray(states, dtype=np.float32).reshape(-1, 4)
+    n = st.shape[0]
+    out = np.empty((n, 4), np.float32)
+    ok = np.empty(n, np.uint8)
+    check(lib().aeros_equilibrium_moments(_f(st), n, _f(out), ok.ctypes.data_as(capi._U8P)), "equilibrium_moments")
+    return out, ok
+
+
 def voxel_grid(n, mn, cell) -> VoxelGrid:
     g = VoxelGrid()
     g.nx, g.ny, g.nz = (int(v) for v in n)

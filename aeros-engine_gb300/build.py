@@ -82,7 +82,8 @@ def build_facade(lib: str) -> str:
     deps = [src, os.path.join(FACADE, "aeros_facade.h"), lib]
     if os.path.exists(out) and all(os.path.getmtime(d) <= os.path.getmtime(out) for d in deps):
         return out
-    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", src, "-o", out,
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", src,
+           "-o", out,
            "-L" + OUT_DIR, "-laeros_gb300", "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

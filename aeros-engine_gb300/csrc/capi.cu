@@ -1096,6 +1096,58 @@ extern "C" int aeros_lbm_cv_force(aeros_lbm* h, float half_x, float half_y, floa
     return aeros_lbm_cv_force_box(h, box, out);
 }
 
+namespace {
+// lbmEquilibriumMoments, aeros/src/lbm.cpp:249-267: one thread per state.
+__global__ void k_eq_moments(const float* st, long long n, float* out, uint8_t* ok) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float rho = st[4 * i], ux = st[4 * i + 1], uy = st[4 * i + 2], uz = st[4 * i + 3];
+        float m = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+        bool good = isfinite(rho) && isfinite(ux) && isfinite(uy) && isfinite(uz);
+        if (good) {
+            const float usqr = ux * ux + uy * uy + uz * uz;
+            for (int q = 0; q < 19 && good; ++q) {
+                const float feq = aeros::eq_checked(q, rho, ux, uy, uz, usqr);
+                good = isfinite(feq);
+                m += feq;
+                px += feq * (float)aeros::cx19(q);
+                py += feq * (float)aeros::cy19(q);
+                pz += feq * (float)aeros::cz19(q);
+            }
+        }
+        out[4 * i] = good ? m : 0.0f;
+        out[4 * i + 1] = good ? px : 0.0f;
+        out[4 * i + 2] = good ? py : 0.0f;
+        out[4 * i + 3] = good ? pz : 0.0f;
+        ok[i] = good ? 1 : 0;
+    }
+}
+}  // namespace
+
+extern "C" int aeros_equilibrium_moments(const float* states, int64_t n, float* out, uint8_t* ok) {
+    if (n < 0 || n > ((int64_t)1 << 24)) return set_error(AEROS_ERR_INVALID, "%lld states", (long long)n);
+    if (n > 0 && (!states || !out || !ok)) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (n == 0) return AEROS_OK;
+    const size_t fb = (size_t)n * 4 * sizeof(float);
+    char* d = nullptr;
+    cudaStream_t s = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&d, 2 * fb + (size_t)n, s));
+    float* dst = (float*)d;
+    float* dout = (float*)(d + fb);
+    uint8_t* dok = (uint8_t*)(d + 2 * fb);
+    cudaError_t e = cudaMemcpyAsync(dst, states, fb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+        k_eq_moments<<<blocks, 256, 0, s>>>(dst, n, dout, dok);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, fb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ok, dok, (size_t)n, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "equilibrium moments: %s", cudaGetErrorString(e));
+    return AEROS_OK;
+}
+
 extern "C" int aeros_lbm_projected_area(aeros_lbm* h, int axis, double* area) {
     if (!h || !area) return set_error(AEROS_ERR_INVALID, "NULL argument");
     if (axis < 0 || axis > 2) return set_error(AEROS_ERR_INVALID, "axis %d", axis);

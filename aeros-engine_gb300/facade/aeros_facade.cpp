@@ -40,8 +40,12 @@ std::vector<char> lbmIsGround;
 
 float lbmMinX = 0.0f, lbmMinY = 0.0f, lbmMinZ = 0.0f;
 float lbmCellSizeX = 1.0f, lbmCellSizeY = 1.0f, lbmCellSizeZ = 1.0f;
+float lbmMaxX = 0.0f, lbmMaxY = 0.0f, lbmMaxZ = 0.0f;
 float lbmFacadeFlowSpeed = 1.0f;
 float lbmFacadeAirDensity = 1.225f;
+float lbmFacadeAirPressure = 101325.0f;
+float lbmFacadeSpeedOfSound = 340.0f;
+float lbmFacadeFreestream[3] = {0.0f, 0.0f, 0.0f};
 std::vector<float> lbmUxWorld, lbmUyWorld, lbmUzWorld;
 std::vector<float> lbmPressure;
 std::vector<float> lbmVorticityMag;
@@ -60,6 +64,7 @@ namespace {
 aeros_lbm* g_handle = nullptr;
 std::string g_error;
 bool g_world_read = false;   // the device holds world fields of the current state
+float g_uin[3] = {0.0f, 0.0f, 0.0f};   // the solver's inlet velocity (lattice units)
 
 bool ok(int status) {
     if (status == AEROS_OK) return true;
@@ -190,6 +195,7 @@ void initLBM() {
     for (int i = 0; i < 3; ++i) {
         p.u_in[i] = given ? lbmInletVelocityLB[i] : (i == 0 ? lbmParams.U0 : 0.0f);
         p.u_init[i] = p.u_in[i];
+        g_uin[i] = p.u_in[i];
     }
     p.body_force[0] = lbmParams.bodyForceX;
     p.body_force[1] = lbmParams.bodyForceY;
@@ -206,6 +212,9 @@ void initLBM() {
     lbmInitialized = true;
     lbmCurrentStep = 0;
     g_world_read = false;
+    lbmMaxX = lbmMinX + lbmNx * lbmCellSizeX;
+    lbmMaxY = lbmMinY + lbmNy * lbmCellSizeY;
+    lbmMaxZ = lbmMinZ + lbmNz * lbmCellSizeZ;
     // the derived fields start at zero, as the reference allocates them (lbm.cpp:566-580)
     for (std::vector<float>* v : {&lbmUxWorld, &lbmUyWorld, &lbmUzWorld, &lbmPressure, &lbmVorticityMag, &lbmQCriterion})
         v->assign((size_t)n, 0.0f);
@@ -279,6 +288,148 @@ float getLBMStrainWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_
 bool isLBMSolidWorld(const LbmVec3& worldPos) {
     float v = 0.0f;
     return sample_one(AEROS_FIELD_SOLID, worldPos, &v) && v != 0.0f;
+}
+
+namespace {
+LbmVec3 vec3(float x, float y, float z) {
+    LbmVec3 v;
+    v.x = x; v.y = y; v.z = z;
+    return v;
+}
+float length3(const LbmVec3& v) { return std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+// flowSpeed / |u_in| with the reference's fallbacks (lbm.cpp:1857-1862)
+float velocity_scale() {
+    float u0 = std::sqrt(g_uin[0] * g_uin[0] + g_uin[1] * g_uin[1] + g_uin[2] * g_uin[2]);
+    if (!std::isfinite(u0) || u0 < 1e-6f) u0 = 0.08f;
+    float scale = lbmFacadeFlowSpeed / u0;
+    if (!std::isfinite(scale) || scale > 1000.0f) scale = 20.0f;
+    return scale;
+}
+}  // namespace
+
+LbmVec3 getLBMVelocityWorld(const LbmVec3& p) {   // lbm.cpp:1847-1870
+    const LbmVec3 fs = vec3(lbmFacadeFreestream[0], lbmFacadeFreestream[1], lbmFacadeFreestream[2]);
+    if (!lbmInitialized || !g_handle) return fs;
+    if (p.x < lbmMinX || p.x > lbmMaxX || p.y < lbmMinY || p.y > lbmMaxY || p.z < lbmMinZ || p.z > lbmMaxZ) return fs;
+    if (isLBMSolidWorld(p)) return vec3(0.0f, 0.0f, 0.0f);
+    const LbmVec3 v = getLBMVelocityLB(p);
+    const float mag2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (mag2 < 1e-12f) return vec3(0.0f, 0.0f, 0.0f);
+    const float scale = velocity_scale();
+    LbmVec3 w = vec3(v.x * scale, v.y * scale, v.z * scale);
+    if (!std::isfinite(w.x)) return fs;
+    const float maxV = lbmFacadeFlowSpeed * 2.0f;
+    const float mag = length3(w);
+    if (mag > maxV) {
+        const float k = maxV / mag;
+        w = vec3(w.x * k, w.y * k, w.z * k);
+    }
+    return w;
+}
+
+float getLBMVelocityMagWorld(const LbmVec3& p) {   // lbm.cpp:1992-1996
+    const float m = length3(getLBMVelocityWorld(p));
+    return std::isfinite(m) ? m : 0.0f;
+}
+
+float getLBMMachWorld(const LbmVec3& p) {   // lbm.cpp:2319-2326
+    const float mag = length3(getLBMVelocityWorld(p));
+    if (!std::isfinite(mag)) return 0.0f;
+    float a = lbmFacadeSpeedOfSound;
+    if (a < 1.0f) a = 340.0f;
+    return mag / a;
+}
+
+// lbm.cpp:2328-2356: normalized helicity from the world velocity at the point
+// and the central-difference vorticity of the cell (the world fields of the
+// last readback, held on the host by this layer).
+float getLBMHelicityWorld(const LbmVec3& p) {
+    if (!lbmInitialized) return 0.0f;
+    const float fx = (p.x - lbmMinX) / lbmCellSizeX;
+    const float fy = (p.y - lbmMinY) / lbmCellSizeY;
+    const float fz = (p.z - lbmMinZ) / lbmCellSizeZ;
+    const int ix = (int)std::floor(fx), iy = (int)std::floor(fy), iz = (int)std::floor(fz);
+    if (ix <= 0 || ix >= lbmNx - 1 || iy <= 0 || iy >= lbmNy - 1 || iz <= 0 || iz >= lbmNz - 1) return 0.0f;
+    const long long cell = ((long long)iz * lbmNy + iy) * lbmNx + ix;
+    const long long total = (long long)lbmNx * lbmNy * lbmNz;
+    if ((long long)lbmVorticityMag.size() != total || (long long)lbmUxWorld.size() != total) return 0.0f;
+    const LbmVec3 vel = getLBMVelocityWorld(p);
+    const long long xm = cell - 1, xp = cell + 1;
+    const long long ym = cell - lbmNx, yp = cell + lbmNx;
+    const long long zm = cell - (long long)lbmNx * lbmNy, zp = cell + (long long)lbmNx * lbmNy;
+    const float duz_dy = (lbmUzWorld[yp] - lbmUzWorld[ym]) * 0.5f;
+    const float duy_dz = (lbmUyWorld[zp] - lbmUyWorld[zm]) * 0.5f;
+    const float dux_dz = (lbmUxWorld[zp] - lbmUxWorld[zm]) * 0.5f;
+    const float duz_dx = (lbmUzWorld[xp] - lbmUzWorld[xm]) * 0.5f;
+    const float duy_dx = (lbmUyWorld[xp] - lbmUyWorld[xm]) * 0.5f;
+    const float dux_dy = (lbmUxWorld[yp] - lbmUxWorld[ym]) * 0.5f;
+    const LbmVec3 om = vec3(duz_dy - duy_dz, dux_dz - duz_dx, duy_dx - dux_dy);
+    const float h = vel.x * om.x + vel.y * om.y + vel.z * om.z;
+    if (!std::isfinite(h)) return 0.0f;
+    const float vm = length3(vel), om_m = length3(om);
+    if (vm < 1e-6f || om_m < 1e-6f) return 0.0f;
+    return h / (vm * om_m);
+}
+
+float getLBMTotalPressureWorld(const LbmVec3& p) {   // lbm.cpp:2358-2372
+    const LbmVec3 v = getLBMVelocityWorld(p);
+    const float mag2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (!std::isfinite(mag2)) return lbmFacadeAirPressure;
+    float pStatic = lbmFacadeAirPressure;
+    float lbmP = 0.0f;
+    getLBMPressureWorldChecked(p, &lbmP);
+    pStatic += lbmP;
+    const float pt = pStatic + 0.5f * lbmFacadeAirDensity * mag2;
+    return std::isfinite(pt) ? pt : lbmFacadeAirPressure;
+}
+
+float lbmLatticeDtWorld() {   // lbm.cpp:1717-1732
+    if (!lbmInitialized) return 0.0f;
+    const float dx = lbmCellSizeX;
+    if (!std::isfinite(dx) || dx <= 0.0f) return 0.0f;
+    float u0 = std::sqrt(g_uin[0] * g_uin[0] + g_uin[1] * g_uin[1] + g_uin[2] * g_uin[2]);
+    if (!std::isfinite(u0) || u0 < 1e-6f) u0 = 0.08f;
+    float vs = lbmFacadeFlowSpeed / u0;
+    if (!std::isfinite(vs) || vs > 1000.0f) vs = 20.0f;
+    if (vs < 0.01f) vs = 0.01f;
+    float dt = dx / vs;
+    if (!std::isfinite(dt) || dt <= 0.0f) return 0.0f;
+    return dt > 1.0f ? 1.0f : dt;
+}
+
+void updateLBM(float deltaTime, int forceSteps) {   // lbm.cpp:1734-1780
+    if (!lbmParams.enabled) return;
+    // a new voxel grid re-initializes the solver (lbm.cpp:1740-1762)
+    if (!lbmInitialized || g_voxNx != lbmNx || g_voxNy != lbmNy || g_voxNz != lbmNz) {
+        initLBM();
+        return;
+    }
+    int steps;
+    if (forceSteps >= 0) {
+        steps = std::min(forceSteps, 64);
+    } else {
+        steps = lbmParams.stepsPerFrame;
+        if (steps <= 0) steps = 1;
+        if (steps > 50) steps = 50;
+        if (deltaTime > 0.02f) steps = std::min(steps * 2, 50);
+    }
+    if (steps <= 0) return;
+    stepLBMCPU(steps);
+    if (lbmCurrentStep % 30 == 0) computeLBMVorticityAndQ();
+}
+
+bool lbmEquilibriumMoments(float rho, float ux, float uy, float uz, float* sumFeq, float* momX, float* momY,
+                           float* momZ) {
+    if (!sumFeq || !momX || !momY || !momZ) return false;
+    const float st[4] = {rho, ux, uy, uz};
+    float out[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    uint8_t good = 0;
+    if (!ok(aeros_equilibrium_moments(st, 1, out, &good)) || !good) return false;
+    *sumFeq = out[0];
+    *momX = out[1];
+    *momY = out[2];
+    *momZ = out[3];
+    return true;
 }
 
 LbmVec3 lbmControlVolumeForce(float boxHalfX, float boxHalfY, float boxHalfZ) {

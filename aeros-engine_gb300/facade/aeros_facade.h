@@ -102,8 +102,13 @@ extern std::vector<char> lbmIsGround;
 // modules, so a caller copies them into the two inputs below.
 extern float lbmMinX, lbmMinY, lbmMinZ;
 extern float lbmCellSizeX, lbmCellSizeY, lbmCellSizeZ;
-extern float lbmFacadeFlowSpeed;     // flowSpeed, m/s
-extern float lbmFacadeAirDensity;    // airDensity, kg/m^3
+// lbmMin + lbmN * lbmCellSize, set by initLBM (lbm.cpp:505-507)
+extern float lbmMaxX, lbmMaxY, lbmMaxZ;
+extern float lbmFacadeFlowSpeed;       // flowSpeed, m/s
+extern float lbmFacadeAirDensity;      // airDensity, kg/m^3
+extern float lbmFacadeAirPressure;     // airPressure, Pa
+extern float lbmFacadeSpeedOfSound;    // speedOfSound, m/s
+extern float lbmFacadeFreestream[3];   // flowParams.vx, vy, vz, m/s
 extern std::vector<float> lbmUxWorld, lbmUyWorld, lbmUzWorld;
 extern std::vector<float> lbmPressure;
 extern std::vector<float> lbmVorticityMag;
@@ -116,6 +121,16 @@ void initLBM();
 void resetLBM();
 void shutdownLBM();
 void stepLBMCPU(int steps = 1);
+// updateLBM (lbm.cpp:1734-1780) for a fixed grid: forceSteps >= 0 steps that
+// many (at most 64), -1 takes lbmParams.stepsPerFrame (doubled for long
+// frames, at most 50); vorticity / Q every 30 steps. Initializes the solver
+// when it is not.
+void updateLBM(float deltaTime, int forceSteps = -1);
+// lbmLatticeDtWorld (lbm.cpp:1717-1732): seconds of physical time per step.
+float lbmLatticeDtWorld();
+// lbmEquilibriumMoments (lbm.cpp:249-267), evaluated on the device.
+bool lbmEquilibriumMoments(float rho, float ux, float uy, float uz, float* sumFeq, float* momX, float* momY,
+                           float* momZ);
 LbmVec3 lbmControlVolumeForce(float boxHalfX, float boxHalfY, float boxHalfZ);
 float lbmProjectedAreaCells(int axis);
 // computeLBMVorticityAndQ (lbm.cpp:2005-2093), on the device.
@@ -130,6 +145,13 @@ float getLBMQWorld(const LbmVec3& worldPos);
 float getLBMTKEWorld(const LbmVec3& worldPos);
 float getLBMStrainWorld(const LbmVec3& worldPos);
 bool isLBMSolidWorld(const LbmVec3& worldPos);
+// Compositions of the samplers above, as the reference composes them
+// (lbm.cpp:1847-1870, 1992-1996, 2319-2372).
+LbmVec3 getLBMVelocityWorld(const LbmVec3& worldPos);
+float getLBMVelocityMagWorld(const LbmVec3& worldPos);
+float getLBMMachWorld(const LbmVec3& worldPos);
+float getLBMHelicityWorld(const LbmVec3& worldPos);
+float getLBMTotalPressureWorld(const LbmVec3& worldPos);
 // Many points at once (xyz each): the way to sample a whole slice or a set
 // of streamline seeds without a device round trip per point. field is one of
 // AEROS_FIELD_*; out gets n values (3n for the velocity), valid n flags.

@@ -192,6 +192,16 @@ int aeros_lbm_cv_force_box(aeros_lbm* h, const int32_t box[6], double out[3]);
 /* Replaces lbmProjectedAreaCells (aeros/src/lbm.cpp:2236-2256). */
 int aeros_lbm_projected_area(aeros_lbm* h, int axis, double* area);
 
+/* lbmEquilibriumMoments (aeros/src/lbm.cpp:249-267), evaluated on the device
+ * with the equilibrium the solver's kernels use (computeEquilibriumFast,
+ * lbm.cpp:146-184, velocity limiter included): for n states
+ * states[4i..4i+3] = (rho, ux, uy, uz), out[4i..4i+3] = the sum of the 19
+ * equilibrium populations and their three momentum sums, each accumulated in
+ * FP32 over q = 0..18 as the reference does. ok[i] = 0 where an input or a
+ * population is not finite (the reference's false); out is then 0. No
+ * handle: a validation helper on the current device. */
+int aeros_equilibrium_moments(const float* states, int64_t n, float* out, uint8_t* ok);
+
 /* ---- voxelizer ------------------------------------------------------------------ */
 typedef struct aeros_voxel_grid {
     int32_t nx, ny, nz;

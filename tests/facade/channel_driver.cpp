@@ -49,8 +49,10 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "initLBM failed: %s\n", lbmFacadeLastError().c_str());
         return 1;
     }
-    for (int i = 0; i < steps / 2; ++i) stepLBMCPU(1);   // frame-loop style
-    stepLBMCPU(steps - steps / 2);                          // and one batched call
+    lbmFacadeFreestream[0] = 10.0f;
+    lbmParams.enabled = true;
+    for (int i = 0; i < steps / 2; ++i) updateLBM(0.01f, 1);   // frame-loop style
+    stepLBMCPU(steps - steps / 2);                               // and one batched call
     computeLBMVorticityAndQ();
     const LbmVec3 F = lbmControlVolumeForce(0.3f, 0.3f, 0.3f);
     std::printf("step %d avg_rho %.9g avg_ke %.9g max_u %.9g fx %.9g area %.1f\n", lbmCurrentStep, lbmAvgRho,
@@ -75,6 +77,18 @@ int main(int argc, char** argv) {
     std::printf("probe p %.9g ok %d ux %.9g rho %.9g q %.9g vort %.9g strain %.9g tke %.9g solid %d %d\n", pa, (int)pok,
                 u.x, getLBMDensityWorld(mid), getLBMQWorld(mid), getLBMVorticityWorld(mid), getLBMStrainWorld(mid),
                 getLBMTKEWorld(mid), (int)isLBMSolidWorld(mid), (int)isLBMSolidWorld(LbmVec3{-3.0f, -1.58f, 0.0f}));
+    const LbmVec3 vw = getLBMVelocityWorld(mid);
+    std::printf("world ux %.9g uy %.9g mag %.9g mach %.9g dt %.9g outside %.9g\n", vw.x, vw.y, getLBMVelocityMagWorld(mid),
+                getLBMMachWorld(mid), lbmLatticeDtWorld(), getLBMVelocityWorld(LbmVec3{9.0f, 0.0f, 0.0f}).x);
+    // the equilibrium moments of the reference's own test states
+    const float eq[7][4] = {{1.0f, 0.0f, 0.0f, 0.0f},    {1.0f, 0.05f, 0.0f, 0.0f},  {0.7f, 0.04f, -0.03f, 0.02f},
+                            {1.35f, -0.02f, 0.05f, 0.01f}, {0.55f, 0.1f, 0.1f, 0.0f}, {1.6f, 0.0f, 0.0f, -0.08f},
+                            {1.1f, 0.28f, 0.0f, 0.0f}};
+    for (const auto& c : eq) {
+        float m = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+        const bool good = lbmEquilibriumMoments(c[0], c[1], c[2], c[3], &m, &px, &py, &pz);
+        std::printf("eq %d %.9g %.9g %.9g %.9g\n", (int)good, m, px, py, pz);
+    }
     if (argc > 2) {
         FILE* fh = std::fopen(argv[2], "wb");
         if (!fh) return 2;

@@ -54,9 +54,11 @@ def test_facade_channel_equals_c_abi(driver, tmp_path):
                          body_force=(1e-6, 0.0, 0.0), convective_outlet=True)
     wp = capi.make_world(10.0, 1.225, (-3.2, -1.6, -1.6), (0.1, 0.1, 0.1))
     s = solver.Solver(p, geometry.channel_mask(64, 32, 32))
-    for _ in range(100):
+    for k in range(100):
         s.step(1)
         s.world_fields(wp, read=False)
+        if (k + 1) % 30 == 0:   # updateLBM's vorticity / Q cadence
+            s.vorticity_q(read=False)
     s.step(100)
     world, wst = s.world_fields(wp)
     ref = s.fields()
@@ -89,3 +91,17 @@ def test_facade_channel_equals_c_abi(driver, tmp_path):
     pv, pok = s.sample(wp, capi.AEROS_FIELD_PRESSURE, pts[20:21])
     assert probe[3] == "1" and pok[0] == 1 and np.float32(probe[1]) == pv[0]
     assert probe[-2] == "0" and probe[-1] == "1"   # the mid point is fluid, the wall point solid
+    # world velocity: the lattice velocity times flowSpeed / 0.08 (no inlet velocity), within 2 flowSpeed
+    uv, _ = s.sample(wp, capi.AEROS_FIELD_VELOCITY_LB, pts[20:21])
+    world = r.stdout.split("world ")[1].split()
+    scale = np.float32(10.0) / np.float32(0.08)
+    assert np.float32(world[1]) == np.float32(uv[0, 0] * scale)
+    assert np.float32(world[3]) == np.float32(uv[0, 1] * scale)
+    assert np.float32(world[9]) == np.float32(np.float32(0.1) / scale)   # lbmLatticeDtWorld
+    assert np.float32(world[11]) == np.float32(10.0)   # outside the grid: the freestream
+    from golden.cases import EQ_MOMENT_CASES
+    from post_common import GOLD
+    eq = [ln.split()[1:] for ln in r.stdout.splitlines() if ln.startswith("eq ")]
+    assert len(eq) == len(EQ_MOMENT_CASES)
+    for row, ref in zip(eq, GOLD["eq_moments"]):
+        assert row[0] == "1" and [np.float32(v) for v in row[1:]] == list(np.float32(ref))

@@ -35,3 +35,26 @@ def test_gpu_post_processing_shifted_storage_is_close():
     assert np.abs(f16["ux"] - f32["ux"]).max() <= 2e-3 * umax
     pmax = np.abs(f32["pressure"]).max()
     assert np.abs(f16["pressure"] - f32["pressure"]).max() <= 2e-2 * pmax
+
+
+def test_gpu_equilibrium_moments_equal_reference():
+    """aeros_equilibrium_moments on the reference test's seven states equals
+    lbmEquilibriumMoments bit for bit, keeps mass and momentum within that
+    test's tolerances (3e-5), limits |u| to 0.3 and rejects non-finite input."""
+    from aeros_gb300 import solver
+    from golden.cases import EQ_MOMENT_CASES
+    from post_common import GOLD
+    st = np.array(EQ_MOMENT_CASES, np.float32)
+    out, ok = solver.equilibrium_moments(st)
+    assert ok.all()
+    assert out.tolist() == np.array(GOLD["eq_moments"], np.float32).tolist()
+    for (rho, ux, uy, uz), (m, px, py, pz) in zip(st, out):
+        assert abs(m - rho) <= 3e-5 * max(1.0, rho)
+        if ux * ux + uy * uy + uz * uz <= 0.09:
+            assert max(abs(px - rho * ux), abs(py - rho * uy), abs(pz - rho * uz)) <= 3e-5
+    bad = np.array([[1.0, np.nan, 0.0, 0.0], [np.nan, 0.0, 0.0, 0.0], [1.0, 0.0, np.inf, 0.0]], np.float32)
+    out, ok = solver.equilibrium_moments(bad)
+    assert not ok.any() and not out.any()
+    # above the limiter: the momentum is that of |u| = 0.3 along u, the mass is kept
+    out, ok = solver.equilibrium_moments(np.array([[1.0, 0.5, 0.0, 0.0]], np.float32))
+    assert ok[0] and abs(out[0, 0] - 1.0) <= 3e-5 and abs(out[0, 1] - 0.3) <= 3e-5
