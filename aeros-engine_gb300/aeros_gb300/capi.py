@@ -182,6 +182,10 @@ _SIGS = {
     "aeros_lbm_vorticity_q": (C.c_int, [_P, _FP, _FP, _FP]),
     "aeros_lbm_sample": (C.c_int, [_P, C.POINTER(WorldParams), C.c_int, _FP, C.c_int64, _FP, _U8P]),
     "aeros_equilibrium_moments": (C.c_int, [_FP, C.c_int64, _FP, _U8P]),
+    "aeros_sdf_device": (C.c_int, [_P, C.POINTER(VoxelGrid), _P, _P]),
+    "aeros_sdf": (C.c_int, [_U8P, C.POINTER(VoxelGrid), _FP]),
+    "aeros_sdf_sample": (C.c_int, [_P, C.POINTER(VoxelGrid), _FP, C.c_int64, _FP, _FP]),
+    "aeros_sdf_last_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "aeros_batch_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
     "aeros_batch_destroy": (C.c_int, [_P]),
     "aeros_batch_add": (C.c_int, [_P, _P]),

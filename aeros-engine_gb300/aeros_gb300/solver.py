@@ -195,6 +195,36 @@ def equilibrium_moments(states) -> tuple[np.ndarray, np.ndarray]:
     return out, ok
 
 
+def sdf(mask: np.ndarray, grid: VoxelGrid) -> np.ndarray:
+    """The voxel grid's signed distance field (buildVoxelGrid's distance part,
+    aeros/src/voxel_grid.cpp:384-553) computed on the device from a host mask."""
+    m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+    if m.size != grid.nx * grid.ny * grid.nz:
+        raise ValueError("mask size does not match the grid")
+    out = np.empty(m.size, np.float32)
+    check(lib().aeros_sdf(m.ctypes.data_as(_U8P), C.byref(grid), _f(out)), "sdf")
+    return out
+
+
+def sdf_last_stats() -> tuple[int, int]:
+    """(propagation passes, tile runs) of this thread's last distance field."""
+    p, t = C.c_int64(), C.c_int64()
+    check(lib().aeros_sdf_last_stats(C.byref(p), C.byref(t)), "sdf_last_stats")
+    return p.value, t.value
+
+
+def sdf_sample(d_sdf: int, grid: VoxelGrid, points: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """sampleSDFCPU / sdfNormalCPU (voxel_grid.cpp:32-123) of the device field
+    at address d_sdf (0: no field) at host points (n, 3): (dist, normals)."""
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    n = pts.shape[0]
+    dist = np.empty(n, np.float32)
+    nrm = np.empty((n, 3), np.float32)
+    check(lib().aeros_sdf_sample(C.c_void_p(d_sdf or None), C.byref(grid), _f(pts), n, _f(dist), _f(nrm)),
+          "sdf_sample")
+    return dist, nrm
+
+
 def voxel_grid(n, mn, cell) -> VoxelGrid:
     g = VoxelGrid()
     g.nx, g.ny, g.nz = (int(v) for v in n)

@@ -8,6 +8,7 @@ Translation units and their floating-point contraction:
   capi.cu      --fmad=false  host code with -ffp-contract=off
   batch.cu     --fmad=false  host side of the many-domain batch
   post.cu      --fmad=false  world fields, vorticity / Q, samplers as the reference rounds them
+  sdf.cu       --fmad=false  distance field: weights, smoothing and samplers as the reference
 """
 from __future__ import annotations
 
@@ -36,6 +37,7 @@ UNITS = {
     "capi.cu": ["--fmad=false"],
     "batch.cu": ["--fmad=false"],
     "post.cu": ["--fmad=false"],
+    "sdf.cu": ["--fmad=false"],
     "setup.cu": [],
 }
 HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh", "setup.cuh", "handle.cuh"]

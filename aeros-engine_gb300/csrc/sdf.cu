@@ -1,0 +1,495 @@
+// sdf.cu — the voxel grid's signed distance field on the device (the
+// distance-field part of buildVoxelGrid, aeros/src/voxel_grid.cpp:384-553)
+// and its samplers (sampleSDFCPU / sdfNormalCPU, voxel_grid.cpp:32-123).
+//
+// Seeds, weights and smoothing are the reference's. The propagation is not
+// its order-dependent sweeps + FIFO (thresholds 1e-4 and 1e-3) but their
+// common limit, the least fixed point of
+//     |d(c)| = min(|d0(c)|, min_n fl(|d(n)| + w(n, c)))
+// over the 26 neighbours, with the sign of the seed a minimal path starts
+// from (negative on equal magnitudes). Float addition of a positive weight
+// is monotone, so the fixed point is unique and every schedule reaches the
+// same bits; the reference stops short of it (never below it in magnitude
+// before smoothing) by at most a small fraction of a cell: under 2 % of the
+// smallest cell on the test meshes, after smoothing.
+//
+// State during propagation: one 32-bit key per cell, (bits(|d|) << 1) | (d >= 0),
+// so that the better value is the smaller unsigned key. The grid is cut into
+// 8x8x8 tiles; a pass runs one 512-thread block per active tile, which loads
+// the tile and a one-cell halo into shared memory, relaxes it to local
+// convergence (Jacobi, two barriers per sweep), writes improved cells back and
+// activates exactly the neighbour tiles whose halo it changed. Passes repeat
+// until no tile is active (bounded on the host). Compiled with --fmad=false.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/aeros_lbm.h"
+#include "handle.cuh"
+
+namespace {
+
+constexpr int T = 8;             // tile edge
+constexpr int H = T + 2;         // with halo
+constexpr int HC = H * H * H;    // 1000 keys in shared memory
+constexpr int TB = T * T * T;    // 512 threads, one cell each
+constexpr int MAXIT = 48;        // local sweeps before the tile is re-queued
+constexpr uint32_t SENTINEL = 0xFFFFFFFFu;          // outside the grid
+constexpr uint32_t REACH_MAX = 0x47C35000u;         // bits of 1e5f: larger magnitudes do not propagate
+constexpr int PB = 256;
+
+struct Weights {
+    float w[26];
+    int off[26];   // shared-memory offsets of the 26 neighbours
+};
+
+__device__ __forceinline__ uint32_t make_key(float d) {
+    return (__float_as_uint(fabsf(d)) << 1) | (d >= 0.0f ? 1u : 0u);
+}
+
+__device__ __forceinline__ float key_value(uint32_t k) {
+    const float m = __uint_as_float(k >> 1);
+    return (k & 1u) ? m : -m;
+}
+
+// Activates the tile of cell (i, j, k) and the neighbour tiles whose halo
+// holds it.
+__device__ void activate_cell(int i, int j, int k, int ntx, int nty, int ntz, uint32_t* act, uint32_t* list,
+                              uint32_t* nlist) {
+    const int bx = i / T, by = j / T, bz = k / T;
+    const int lx = i % T == 0 ? -1 : (i % T == T - 1 ? 1 : 0);
+    const int ly = j % T == 0 ? -1 : (j % T == T - 1 ? 1 : 0);
+    const int lz = k % T == 0 ? -1 : (k % T == T - 1 ? 1 : 0);
+    for (int dz = 0; dz <= (lz != 0); ++dz)
+        for (int dy = 0; dy <= (ly != 0); ++dy)
+            for (int dx = 0; dx <= (lx != 0); ++dx) {
+                const int nbx = bx + (dx ? lx : 0), nby = by + (dy ? ly : 0), nbz = bz + (dz ? lz : 0);
+                if (nbx < 0 || nbx >= ntx || nby < 0 || nby >= nty || nbz < 0 || nbz >= ntz) continue;
+                const uint32_t t = (uint32_t)((nbz * nty + nby) * ntx + nbx);
+                if (atomicExch(&act[t], 1u) == 0u) list[atomicAdd(nlist, 1u)] = t;
+            }
+}
+
+// Seeds (voxel_grid.cpp:384-410): a cell with a 6-neighbour of the other
+// solidity (mask == 1 is solid) starts at -+0.5 of the smallest cell size,
+// every other cell at +1e6; tiles holding a seed, in their cells or their
+// halo, start active.
+__global__ void k_sdf_seed(const uint8_t* __restrict__ mask, int nx, int ny, int nz, float half, uint32_t* key,
+                           uint32_t* act, uint32_t* list, uint32_t* nlist, int ntx, int nty, int ntz) {
+    const long long total = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)PB + threadIdx.x; c < total; c += (long long)gridDim.x * PB) {
+        const int i = (int)(c % nx);
+        const long long r = c / nx;
+        const int j = (int)(r % ny);
+        const int k = (int)(r / ny);
+        const bool here = mask[c] == 1;
+        bool surf = false;
+        if (i + 1 < nx) surf |= (mask[c + 1] == 1) != here;
+        if (i > 0) surf |= (mask[c - 1] == 1) != here;
+        if (j + 1 < ny) surf |= (mask[c + nx] == 1) != here;
+        if (j > 0) surf |= (mask[c - nx] == 1) != here;
+        if (k + 1 < nz) surf |= (mask[c + (long long)nx * ny] == 1) != here;
+        if (k > 0) surf |= (mask[c - (long long)nx * ny] == 1) != here;
+        key[c] = make_key(surf ? (here ? -half : half) : 1e6f);
+        if (surf) activate_cell(i, j, k, ntx, nty, ntz, act, list, nlist);
+    }
+}
+
+// One propagation pass over the listed tiles. act_out / list_out / n_out
+// collect the tiles to run next (each tile listed once).
+__global__ void __launch_bounds__(TB) k_sdf_relax(uint32_t* key, int nx, int ny, int nz, int ntx, int nty, int ntz,
+                                                  const Weights W, const uint32_t* __restrict__ list_in, uint32_t n_in,
+                                                  uint32_t* act_out, uint32_t* list_out, uint32_t* n_out) {
+    __shared__ uint32_t s[HC];
+    __shared__ uint32_t s_dirs;   // bit (dz+1)*9 + (dy+1)*3 + (dx+1): neighbour tiles to activate
+    const int tx = threadIdx.x & (T - 1), ty = (threadIdx.x >> 3) & (T - 1), tz = threadIdx.x >> 6;
+    const int me = ((tz + 1) * H + (ty + 1)) * H + (tx + 1);
+    for (uint32_t li = blockIdx.x; li < n_in; li += gridDim.x) {
+        const uint32_t t = list_in[li];
+        const int bx = (int)(t % ntx), by = (int)((t / ntx) % nty), bz = (int)(t / ((uint32_t)ntx * nty));
+        const int x0 = bx * T - 1, y0 = by * T - 1, z0 = bz * T - 1;
+        if (threadIdx.x == 0) s_dirs = 0u;
+        for (int h = threadIdx.x; h < HC; h += TB) {
+            const int hx = h % H, hy = (h / H) % H, hz = h / (H * H);
+            const int gx = x0 + hx, gy = y0 + hy, gz = z0 + hz;
+            uint32_t v = SENTINEL;
+            if (gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz)
+                v = __ldcg(&key[((long long)gz * ny + gy) * nx + gx]);
+            s[h] = v;
+        }
+        __syncthreads();
+        const int gx = bx * T + tx, gy = by * T + ty, gz = bz * T + tz;
+        const bool inside = gx < nx && gy < ny && gz < nz;
+        const uint32_t orig = s[me];
+        uint32_t cur = orig;
+        bool converged = false;
+        for (int it = 0; it < MAXIT; ++it) {
+            uint32_t best = cur;
+            if (inside) {
+#pragma unroll
+                for (int n = 0; n < 26; ++n) {
+                    const uint32_t kn = s[me + W.off[n]];
+                    if ((kn >> 1) <= REACH_MAX) {
+                        const float m = __fadd_rn(__uint_as_float(kn >> 1), W.w[n]);
+                        best = min(best, (__float_as_uint(m) << 1) | (kn & 1u));
+                    }
+                }
+            }
+            const bool changed = best < cur;
+            __syncthreads();   // every read of this sweep is done
+            if (changed) {
+                s[me] = best;
+                cur = best;
+            }
+            if (!__syncthreads_or(changed)) {   // also publishes the writes
+                converged = true;
+                break;
+            }
+        }
+        if (inside && cur < orig) {
+            key[((long long)gz * ny + gy) * nx + gx] = cur;
+            // halo cells of neighbour tiles: faces, edges and corners this cell lies on
+            const int lx = tx == 0 ? -1 : (tx == T - 1 ? 1 : 0);
+            const int ly = ty == 0 ? -1 : (ty == T - 1 ? 1 : 0);
+            const int lz = tz == 0 ? -1 : (tz == T - 1 ? 1 : 0);
+            uint32_t bits = 0u;
+            for (int dz = 0; dz <= (lz != 0); ++dz)
+                for (int dy = 0; dy <= (ly != 0); ++dy)
+                    for (int dx = 0; dx <= (lx != 0); ++dx) {
+                        const int ox = dx ? lx : 0, oy = dy ? ly : 0, oz = dz ? lz : 0;
+                        if (ox | oy | oz) bits |= 1u << ((oz + 1) * 9 + (oy + 1) * 3 + (ox + 1));
+                    }
+            if (bits) atomicOr(&s_dirs, bits);
+        }
+        __syncthreads();
+        if (threadIdx.x < 27) {
+            const uint32_t dirs = s_dirs | (converged ? 0u : (1u << 13));   // not converged: run again
+            if (dirs & (1u << threadIdx.x)) {
+                const int ox = (int)(threadIdx.x % 3) - 1, oy = (int)(threadIdx.x / 3 % 3) - 1,
+                          oz = (int)(threadIdx.x / 9) - 1;
+                const int nbx = bx + ox, nby = by + oy, nbz = bz + oz;
+                if (nbx >= 0 && nbx < ntx && nby >= 0 && nby < nty && nbz >= 0 && nbz < ntz) {
+                    const uint32_t nt = (uint32_t)((nbz * nty + nby) * ntx + nbx);
+                    if (atomicExch(&act_out[nt], 1u) == 0u) list_out[atomicAdd(n_out, 1u)] = nt;
+                }
+            }
+        }
+        __syncthreads();   // s[] and s_dirs are reused by the next tile
+    }
+}
+
+__global__ void k_sdf_decode(const uint32_t* __restrict__ key, float* d, long long total) {
+    for (long long c = blockIdx.x * (long long)PB + threadIdx.x; c < total; c += (long long)gridDim.x * PB)
+        d[c] = key_value(key[c]);
+}
+
+// One smoothing pass (voxel_grid.cpp:479-540): interior cells farther than
+// lim keep 0.65 of themselves and 0.35 of the (0.25, 0.5, 0.25) average
+// along the axis; the others are copied.
+__global__ void k_sdf_smooth(const float* __restrict__ in, float* out, int nx, int ny, int nz, long long stride,
+                             float lim) {
+    const long long total = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)PB + threadIdx.x; c < total; c += (long long)gridDim.x * PB) {
+        const int i = (int)(c % nx);
+        const long long r = c / nx;
+        const int j = (int)(r % ny);
+        const int k = (int)(r / ny);
+        const float v = in[c];
+        float o = v;
+        if (i >= 1 && i < nx - 1 && j >= 1 && j < ny - 1 && k >= 1 && k < nz - 1 && !(fabsf(v) < lim)) {
+            const float sum = in[c - stride] * 0.25f + v * 0.5f + in[c + stride] * 0.25f;
+            o = sum * 0.35f + v * 0.65f;
+        }
+        out[c] = o;
+    }
+}
+
+// ---- samplers ---------------------------------------------------------------
+
+struct SdfView {
+    const float* d;
+    int nx, ny, nz;
+    float min[3], cs[3];
+};
+
+__device__ __forceinline__ bool valid_f(float v) { return isfinite(v) && fabsf(v) < 1e6f; }
+
+// floorf to int for |v| < 2^30; beyond, +-2^30 (outside every grid)
+__device__ __forceinline__ int ifloor(float v) {
+    const float f = floorf(v);
+    if (!(f > -1073741824.0f)) return -1073741824;
+    if (!(f < 1073741824.0f)) return 1073741824;
+    return (int)f;
+}
+
+__device__ float sdf_get(const SdfView& g, int x, int y, int z, float fallback) {
+    if (x < 0 || x >= g.nx || y < 0 || y >= g.ny || z < 0 || z >= g.nz) return fallback;
+    const float v = g.d[((long long)z * g.ny + y) * g.nx + x];
+    return valid_f(v) ? v : fallback;
+}
+
+// sampleSDFCPU, voxel_grid.cpp:32-81
+__device__ float sdf_sample1(const SdfView& g, float px, float py, float pz) {
+    if (!valid_f(px) || !valid_f(py) || !valid_f(pz)) return 1000.0f;
+    float csx = g.cs[0], csy = g.cs[1], csz = g.cs[2];
+    if (!valid_f(csx) || fabsf(csx) < 1e-8f) return 1000.0f;
+    if (!valid_f(csy) || fabsf(csy) < 1e-8f) csy = csx;
+    if (!valid_f(csz) || fabsf(csz) < 1e-8f) csz = csx;
+    const float fx = (px - g.min[0]) / csx - 0.5f;
+    const float fy = (py - g.min[1]) / csy - 0.5f;
+    const float fz = (pz - g.min[2]) / csz - 0.5f;
+    const int ix0 = ifloor(fx), iy0 = ifloor(fy), iz0 = ifloor(fz);
+    const int ix1 = ix0 + 1, iy1 = iy0 + 1, iz1 = iz0 + 1;
+    float tx = fx - ix0, ty = fy - iy0, tz = fz - iz0;
+    tx = fminf(fmaxf(tx, 0.0f), 1.0f);
+    ty = fminf(fmaxf(ty, 0.0f), 1.0f);
+    tz = fminf(fmaxf(tz, 0.0f), 1.0f);
+    if (ix0 < 0 || iy0 < 0 || iz0 < 0 || ix1 >= g.nx || iy1 >= g.ny || iz1 >= g.nz) {
+        const int ix = ifloor((px - g.min[0]) / csx);
+        const int iy = ifloor((py - g.min[1]) / csy);
+        const int iz = ifloor((pz - g.min[2]) / csz);
+        if (ix < 0 || ix >= g.nx || iy < 0 || iy >= g.ny || iz < 0 || iz >= g.nz) return 1000.0f;
+        return g.d[((long long)iz * g.ny + iy) * g.nx + ix];
+    }
+    const float c000 = sdf_get(g, ix0, iy0, iz0, 1000.0f), c100 = sdf_get(g, ix1, iy0, iz0, 1000.0f);
+    const float c010 = sdf_get(g, ix0, iy1, iz0, 1000.0f), c110 = sdf_get(g, ix1, iy1, iz0, 1000.0f);
+    const float c001 = sdf_get(g, ix0, iy0, iz1, 1000.0f), c101 = sdf_get(g, ix1, iy0, iz1, 1000.0f);
+    const float c011 = sdf_get(g, ix0, iy1, iz1, 1000.0f), c111 = sdf_get(g, ix1, iy1, iz1, 1000.0f);
+    const float c00 = c000 * (1 - tx) + c100 * tx;
+    const float c10 = c010 * (1 - tx) + c110 * tx;
+    const float c01 = c001 * (1 - tx) + c101 * tx;
+    const float c11 = c011 * (1 - tx) + c111 * tx;
+    const float c0 = c00 * (1 - ty) + c10 * ty;
+    const float c1 = c01 * (1 - ty) + c11 * ty;
+    return c0 * (1 - tz) + c1 * tz;
+}
+
+// sdfNormalCPU, voxel_grid.cpp:83-123
+__device__ void sdf_normal1(const SdfView& g, float px, float py, float pz, float* n3) {
+    n3[0] = 0.0f; n3[1] = 1.0f; n3[2] = 0.0f;
+    if (g.nx <= 1 || g.ny <= 1 || g.nz <= 1) return;
+    if (!valid_f(px) || !valid_f(py) || !valid_f(pz)) return;
+    float csx = g.cs[0], csy = g.cs[1], csz = g.cs[2];
+    if (!valid_f(csx) || fabsf(csx) < 1e-8f) return;
+    if (!valid_f(csy) || fabsf(csy) < 1e-8f) csy = csx;
+    if (!valid_f(csz) || fabsf(csz) < 1e-8f) csz = csx;
+    float eps = fminf(csx, fminf(csy, csz)) * 0.5f;
+    if (eps < 1e-4f) eps = 0.01f;
+    float dx = sdf_sample1(g, px + eps, py, pz) - sdf_sample1(g, px - eps, py, pz);
+    float dy = sdf_sample1(g, px, py + eps, pz) - sdf_sample1(g, px, py - eps, pz);
+    float dz = sdf_sample1(g, px, py, pz + eps) - sdf_sample1(g, px, py, pz - eps);
+    float len = sqrtf(dx * dx + dy * dy + dz * dz);
+    if (!valid_f(len) || len < 1e-6f) {
+        const int ix = ifloor((px - g.min[0]) / csx);
+        const int iy = ifloor((py - g.min[1]) / csy);
+        const int iz = ifloor((pz - g.min[2]) / csz);
+        if (ix <= 0 || ix >= g.nx - 1 || iy <= 0 || iy >= g.ny - 1 || iz <= 0 || iz >= g.nz - 1) return;
+        dx = sdf_get(g, ix + 1, iy, iz, 0.0f) - sdf_get(g, ix - 1, iy, iz, 0.0f);
+        dy = sdf_get(g, ix, iy + 1, iz, 0.0f) - sdf_get(g, ix, iy - 1, iz, 0.0f);
+        dz = sdf_get(g, ix, iy, iz + 1, 0.0f) - sdf_get(g, ix, iy, iz - 1, 0.0f);
+        len = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (len < 1e-6f) return;
+    }
+    n3[0] = dx / len; n3[1] = dy / len; n3[2] = dz / len;
+}
+
+__global__ void k_sdf_sample(const SdfView g, const float* __restrict__ pts, long long n, float* dist, float* normal) {
+    for (long long i = blockIdx.x * (long long)PB + threadIdx.x; i < n; i += (long long)gridDim.x * PB) {
+        const float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+        if (dist) dist[i] = sdf_sample1(g, px, py, pz);
+        if (normal) {
+            float n3[3];
+            sdf_normal1(g, px, py, pz, n3);
+            normal[3 * i] = n3[0]; normal[3 * i + 1] = n3[1]; normal[3 * i + 2] = n3[2];
+        }
+    }
+}
+
+int grid_blocks(long long work) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return (int)std::max<long long>(1, std::min<long long>((work + PB - 1) / PB, (long long)sms * 8));
+}
+
+thread_local long long t_passes = 0, t_visits = 0;
+
+int check_sdf_grid(const aeros_voxel_grid* g) {
+    if (!g) return set_error(AEROS_ERR_INVALID, "grid is NULL");
+    if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || (long long)g->nx * g->ny * g->nz > (1ll << 31))
+        return set_error(AEROS_ERR_INVALID, "grid %dx%dx%d", g->nx, g->ny, g->nz);
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(g->cell[a]) || !(g->cell[a] > 0.0f) || !std::isfinite(g->min[a]))
+            return set_error(AEROS_ERR_INVALID, "cell size / minimum of axis %d", a);
+    return AEROS_OK;
+}
+
+// Builds the field from a device mask into a device array, on stream s.
+int sdf_impl(const uint8_t* d_mask, const aeros_voxel_grid* g, float* d_sdf, cudaStream_t s) {
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const long long total = (long long)nx * ny * nz;
+    const int ntx = (nx + T - 1) / T, nty = (ny + T - 1) / T, ntz = (nz + T - 1) / T;
+    const long long ntiles = (long long)ntx * nty * ntz;
+    // weights and shared-memory offsets in the reference's dz, dy, dx order (voxel_grid.cpp:412-422)
+    Weights W;
+    int n = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                if (dx == 0 && dy == 0 && dz == 0) continue;
+                const float wx = dx * g->cell[0], wy = dy * g->cell[1], wz = dz * g->cell[2];
+                W.w[n] = sqrtf(wx * wx + wy * wy + wz * wz);
+                W.off[n] = (dz * H + dy) * H + dx;
+                ++n;
+            }
+    const float half = 0.5f * fminf(g->cell[0], fminf(g->cell[1], g->cell[2]));
+    // key array (reused as the smoothing ping-pong buffer), two activity
+    // flag arrays, two tile lists, two counters
+    const size_t kb = (size_t)total * 4, tb = (size_t)ntiles * 4;
+    char* buf = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&buf, kb + 4 * tb + 16, s));
+    uint32_t* key = (uint32_t*)buf;
+    uint32_t* act[2] = {(uint32_t*)(buf + kb), (uint32_t*)(buf + kb + tb)};
+    uint32_t* list[2] = {(uint32_t*)(buf + kb + 2 * tb), (uint32_t*)(buf + kb + 3 * tb)};
+    uint32_t* cnt = (uint32_t*)(buf + kb + 4 * tb);   // cnt[0], cnt[1]
+    cudaError_t e = cudaMemsetAsync(act[0], 0, 2 * tb, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, 16, s);
+    if (e == cudaSuccess) {
+        k_sdf_seed<<<grid_blocks(total), PB, 0, s>>>(d_mask, nx, ny, nz, half, key, act[0], list[0], &cnt[0], ntx, nty,
+                                                        ntz);
+        e = cudaGetLastError();
+    }
+    uint32_t n_act = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&n_act, &cnt[0], 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // Each pass completes at least one more tile of every shortest path; a
+    // shortest path has at most nx + ny + nz hops, so this bound is generous.
+    const long long max_passes = 4ll * (nx + ny + nz) + 64;
+    long long passes = 0, visits = 0;
+    int cur = 0;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    while (e == cudaSuccess && n_act > 0 && passes < max_passes) {
+        const int nxt = cur ^ 1;
+        // clear the next flags: only the tiles listed last time were set there
+        e = cudaMemsetAsync(act[nxt], 0, tb, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&cnt[nxt], 0, 4, s);
+        if (e != cudaSuccess) break;
+        const int blocks = (int)std::min<long long>(n_act, (long long)std::max(1, sms) * 4);
+        visits += n_act;
+        k_sdf_relax<<<blocks, TB, 0, s>>>(key, nx, ny, nz, ntx, nty, ntz, W, list[cur], n_act, act[nxt], list[nxt],
+                                          &cnt[nxt]);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&n_act, &cnt[nxt], 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        passes++;
+        cur = nxt;
+    }
+    if (e == cudaSuccess && n_act > 0) {
+        cudaFreeAsync(buf, s);
+        return set_error(AEROS_ERR_TIMEOUT, "distance field: not converged after %lld passes", passes);
+    }
+    if (e == cudaSuccess) {
+        // decode into d_sdf, then 6 smoothing passes d_sdf -> scratch -> d_sdf ...
+        k_sdf_decode<<<grid_blocks(total), PB, 0, s>>>(key, d_sdf, total);
+        e = cudaGetLastError();
+        float* scratch = (float*)key;
+        const long long stride[3] = {1, nx, (long long)nx * ny};
+        float* a = d_sdf;
+        float* b = scratch;
+        for (int iter = 0; iter < 2 && e == cudaSuccess; ++iter)
+            for (int axis = 0; axis < 3 && e == cudaSuccess; ++axis) {
+                const float lim = g->cell[axis] * 3.0f;
+                k_sdf_smooth<<<grid_blocks(total), PB, 0, s>>>(a, b, nx, ny, nz, stride[axis], lim);
+                e = cudaGetLastError();
+                std::swap(a, b);
+            }
+        // six passes: the result is back in d_sdf
+    }
+    cudaFreeAsync(buf, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "distance field: %s", cudaGetErrorString(e));
+    t_passes = passes;
+    t_visits = visits;
+    return AEROS_OK;
+}
+
+}  // namespace
+
+extern "C" int aeros_sdf_device(const uint8_t* d_mask, const aeros_voxel_grid* grid, float* d_sdf, void* stream) {
+    if (int rc = check_sdf_grid(grid)) return rc;
+    if (!d_mask || !d_sdf) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    return sdf_impl(d_mask, grid, d_sdf, (cudaStream_t)stream);
+}
+
+extern "C" int aeros_sdf(const uint8_t* mask, const aeros_voxel_grid* grid, float* sdf) {
+    if (int rc = check_sdf_grid(grid)) return rc;
+    if (!mask || !sdf) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    const size_t total = (size_t)grid->nx * grid->ny * grid->nz;
+    cudaStream_t s = nullptr;
+    char* d = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&d, total * 5, s));
+    float* dsdf = (float*)d;
+    uint8_t* dmask = (uint8_t*)(d + total * 4);
+    cudaError_t e = cudaMemcpyAsync(dmask, mask, total, cudaMemcpyHostToDevice, s);
+    int rc = e == cudaSuccess ? sdf_impl(dmask, grid, dsdf, s) : set_error(AEROS_ERR_CUDA, "mask copy: %s", cudaGetErrorString(e));
+    if (rc == AEROS_OK) {
+        e = cudaMemcpyAsync(sdf, dsdf, total * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = set_error(AEROS_ERR_CUDA, "field copy: %s", cudaGetErrorString(e));
+    }
+    cudaFreeAsync(d, s);
+    return rc;
+}
+
+extern "C" int aeros_sdf_sample(const float* d_sdf, const aeros_voxel_grid* grid, const float* points, int64_t n,
+                                float* dist, float* normal) {
+    if (!grid || (n > 0 && (!points || (!dist && !normal))))
+        return set_error(AEROS_ERR_INVALID, "NULL argument");
+    if (n < 0 || n > ((int64_t)1 << 28)) return set_error(AEROS_ERR_INVALID, "%lld points", (long long)n);
+    if (n == 0) return AEROS_OK;
+    SdfView g;
+    g.d = d_sdf;
+    g.nx = grid->nx; g.ny = grid->ny; g.nz = grid->nz;
+    for (int a = 0; a < 3; ++a) { g.min[a] = grid->min[a]; g.cs[a] = grid->cell[a]; }
+    const bool empty = !d_sdf || g.nx <= 0 || g.ny <= 0 || g.nz <= 0;
+    if (empty) {   // no field: sampleSDFCPU's 1000 and the default normal (voxel_grid.cpp:33, 84)
+        for (int64_t i = 0; i < n; ++i) {
+            if (dist) dist[i] = 1000.0f;
+            if (normal) { normal[3 * i] = 0.0f; normal[3 * i + 1] = 1.0f; normal[3 * i + 2] = 0.0f; }
+        }
+        return AEROS_OK;
+    }
+    cudaStream_t s = nullptr;
+    const size_t pb = (size_t)n * 12;
+    char* d = nullptr;
+    CUDA_TRY(cudaMallocAsync((void**)&d, pb * 2 + (size_t)n * 4, s));
+    float* dp = (float*)d;
+    float* dn = (float*)(d + pb);
+    float* dd = (float*)(d + 2 * pb);
+    cudaError_t e = cudaMemcpyAsync(dp, points, pb, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        k_sdf_sample<<<grid_blocks(n), PB, 0, s>>>(g, dp, n, dist ? dd : nullptr, normal ? dn : nullptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && dist) e = cudaMemcpyAsync(dist, dd, (size_t)n * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && normal) e = cudaMemcpyAsync(normal, dn, pb, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "distance samples: %s", cudaGetErrorString(e));
+    return AEROS_OK;
+}
+
+extern "C" int aeros_sdf_last_stats(int64_t* passes, int64_t* tile_runs) {
+    if (passes) *passes = t_passes;
+    if (tile_runs) *tile_runs = t_visits;
+    return AEROS_OK;
+}

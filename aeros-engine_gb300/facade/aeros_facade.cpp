@@ -263,10 +263,12 @@ float sample_or(int field, const LbmVec3& p, float fallback) {
 }
 }  // namespace
 
-LbmVec3 getLBMVelocityLB(const LbmVec3& worldPos) {
+LbmVec3 getLBMVelocityLB(const LbmVec3& worldPos) {   // the value is the answer: no validity flag
+    const float pt[3] = {worldPos.x, worldPos.y, worldPos.z};
     float v[3] = {0.0f, 0.0f, 0.0f};
+    uint8_t valid = 0;
     LbmVec3 r;
-    if (g_handle) sample_one(AEROS_FIELD_VELOCITY_LB, worldPos, v);
+    if (!lbmFacadeSample(AEROS_FIELD_VELOCITY_LB, pt, 1, v, &valid)) v[0] = v[1] = v[2] = 0.0f;
     r.x = v[0]; r.y = v[1]; r.z = v[2];
     return r;
 }
@@ -285,9 +287,11 @@ float getLBMVorticityWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIE
 float getLBMQWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_Q, worldPos, 0.0f); }
 float getLBMTKEWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_TKE, worldPos, 0.0f); }
 float getLBMStrainWorld(const LbmVec3& worldPos) { return sample_or(AEROS_FIELD_STRAIN, worldPos, 0.0f); }
-bool isLBMSolidWorld(const LbmVec3& worldPos) {
+bool isLBMSolidWorld(const LbmVec3& worldPos) {   // the value is the answer: no validity flag
+    const float pt[3] = {worldPos.x, worldPos.y, worldPos.z};
     float v = 0.0f;
-    return sample_one(AEROS_FIELD_SOLID, worldPos, &v) && v != 0.0f;
+    uint8_t valid = 0;
+    return lbmFacadeSample(AEROS_FIELD_SOLID, pt, 1, &v, &valid) && v != 0.0f;
 }
 
 namespace {

@@ -75,6 +75,13 @@ void    ao_voxel_plan(const float size[3], int res, uint64_t budget,
 /* OpenMP thread count used by the oracle loops. */
 int     ao_set_threads(int n);
 
+/* sdf_oracle.c: buildVoxelGrid's distance field as the reference computes it,
+ * and the least-fixed-point form the device computes (see its header). */
+int     ao_sdf_reference(const uint8_t* mask, int nx, int ny, int nz, const float cs[3], float* d);
+int     ao_sdf_exact(const uint8_t* mask, int nx, int ny, int nz, const float cs[3], float* d);
+int     ao_sdf_sample(const float* sdf, int nx, int ny, int nz, const float mn[3], const float cs[3],
+                      const float* pts, int64_t n, float* dist, float* normal);
+
 #ifdef __cplusplus
 }
 #endif

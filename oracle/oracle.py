@@ -75,6 +75,9 @@ def oracle_lib(precision: str = "f32") -> C.CDLL:
         L.ao_count_hits_brute.argtypes = [_FP, C.c_int64, _FP, C.c_int]
         L.ao_voxel_plan.argtypes = [_FP, C.c_int, C.c_uint64, C.POINTER(VoxelPlan)]
         L.ao_set_threads.argtypes = [C.c_int]
+        L.ao_sdf_reference.argtypes = [_U8P, C.c_int, C.c_int, C.c_int, _FP, _FP]
+        L.ao_sdf_exact.argtypes = [_U8P, C.c_int, C.c_int, C.c_int, _FP, _FP]
+        L.ao_sdf_sample.argtypes = [_FP, C.c_int, C.c_int, C.c_int, _FP, _FP, _FP, C.c_int64, _FP, _FP]
         L.ao_lbm_world_fields.argtypes = [C.c_void_p, C.POINTER(WorldParams), _FP, _FP, _FP, _FP,
                                           C.POINTER(WorldStats)]
         L.ao_lbm_vorticity_q.argtypes = [C.c_void_p, C.POINTER(WorldParams), _FP, _FP, _FP]
@@ -206,6 +209,32 @@ def equilibrium_moments(rho, ux, uy, uz):
     return bool(ok), tuple(float(v) for v in out)
 
 
+def sdf(mask: np.ndarray, dims, cs, exact: bool = False) -> np.ndarray:
+    """Distance field of a mask: the reference's sweeps + FIFO restated
+    (exact=False) or the least-fixed-point form the device computes."""
+    L = oracle_lib("f32")
+    nx, ny, nz = dims
+    m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+    out = np.empty(m.size, np.float32)
+    c = np.asarray(cs, np.float32)
+    fn = L.ao_sdf_exact if exact else L.ao_sdf_reference
+    if fn(u8ptr(m), nx, ny, nz, fptr(c), fptr(out)) != 0:
+        raise RuntimeError("oracle sdf failed")
+    return out
+
+
+def sdf_sample(field: np.ndarray, dims, mn, cs, points: np.ndarray):
+    L = oracle_lib("f32")
+    nx, ny, nz = dims
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    dist = np.empty(pts.shape[0], np.float32)
+    nrm = np.empty((pts.shape[0], 3), np.float32)
+    f = np.ascontiguousarray(field, dtype=np.float32)
+    L.ao_sdf_sample(fptr(f), nx, ny, nz, fptr(np.asarray(mn, np.float32)), fptr(np.asarray(cs, np.float32)),
+                    fptr(pts), pts.shape[0], fptr(dist), fptr(nrm))
+    return dist, nrm
+
+
 def voxelize_brute(tris: np.ndarray, grid: VoxelGrid) -> np.ndarray:
     L = oracle_lib("f32")
     t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
@@ -268,6 +297,10 @@ class RefHarness:
         L.ref_world_get.argtypes = [_FP, _FP, _FP, _FP, _FP, C.POINTER(C.c_longlong), _FP]
         L.ref_vorticity_q.argtypes = [_FP, _FP, _FP]
         L.ref_sample.argtypes = [C.c_int, _FP, C.c_longlong, _FP, _U8P]
+        L.ref_build_voxel_grid.restype = C.c_longlong
+        L.ref_build_voxel_grid.argtypes = [_FP, C.c_longlong, C.c_int]
+        L.ref_voxel_get.argtypes = [C.POINTER(C.c_int), _FP, _FP, _U8P, _FP]
+        L.ref_sdf_sample.argtypes = [_FP, C.c_longlong, _FP, _FP]
         self.L = L
         self.n = 0
 
@@ -343,6 +376,28 @@ class RefHarness:
 
     def projected_area(self, axis):
         return float(self.L.ref_lbm_projected_area(int(axis)))
+
+    def build_voxel_grid(self, tris: np.ndarray, res: int) -> dict:
+        """buildVoxelGrid (voxel_grid.cpp:224-553) of a mesh: dims, grid
+        minimum, cell sizes, mask and distance field."""
+        v = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)
+        n = self.L.ref_build_voxel_grid(fptr(v), v.size, res)
+        if n <= 0:
+            raise RuntimeError("the reference refused the voxel grid")
+        dims = (C.c_int * 3)()
+        mn = np.zeros(3, np.float32)
+        cs = np.zeros(3, np.float32)
+        mask = np.zeros(n, np.uint8)
+        field = np.zeros(n, np.float32)
+        self.L.ref_voxel_get(dims, fptr(mn), fptr(cs), u8ptr(mask), fptr(field))
+        return dict(dims=tuple(dims), min=mn, cs=cs, mask=mask, sdf=field)
+
+    def sdf_sample(self, points: np.ndarray):
+        pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        dist = np.empty(pts.shape[0], np.float32)
+        nrm = np.empty((pts.shape[0], 3), np.float32)
+        self.L.ref_sdf_sample(fptr(pts), pts.shape[0], fptr(dist), fptr(nrm))
+        return dist, nrm
 
     def equilibrium_moments(self, rho, ux, uy, uz):
         out = np.zeros(4, np.float32)

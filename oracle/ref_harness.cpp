@@ -282,6 +282,54 @@ int ref_validation_setup(int shape, int res, float radius, int diameter_cells, f
     return 0;
 }
 
+// The reference's whole voxel grid build (voxel_grid.cpp:224-553): grid plan
+// from the mesh box with its 14 % margin, BVH mask, distance field. Returns
+// the cell count (0 when the build refused); ref_voxel_get reads the result:
+// dims3, the grid minimum, the cell sizes, the mask and the distance field.
+long long ref_build_voxel_grid(const float* verts, long long nfloats, int res) {
+    std::vector<float> v(verts, verts + nfloats);
+    glm::vec3 lo(1e30f), hi(-1e30f);
+    for (long long i = 0; i + 2 < nfloats; i += 3) {
+        lo = glm::min(lo, glm::vec3(v[i], v[i + 1], v[i + 2]));
+        hi = glm::max(hi, glm::vec3(v[i], v[i + 1], v[i + 2]));
+    }
+    minBB = lo; maxBB = hi; center = 0.5f * (lo + hi);
+    const glm::vec3 ext = hi - lo;
+    maxDim = std::max(ext.x, std::max(ext.y, ext.z));
+    g_voxelData.clear();
+    g_distanceField.clear();
+    buildVoxelGrid(v, res);
+    if (!g_voxelBuildError.empty()) return 0;
+    return (long long)g_voxelData.size();
+}
+
+void ref_voxel_get(int* dims3, float* min3, float* cs3, uint8_t* mask, float* sdf) {
+    dims3[0] = g_voxNx; dims3[1] = g_voxNy; dims3[2] = g_voxNz;
+    min3[0] = g_voxMinX; min3[1] = g_voxMinY; min3[2] = g_voxMinZ;
+    cs3[0] = (g_voxMaxX - g_voxMinX) / g_voxNx;
+    cs3[1] = (g_voxMaxY - g_voxMinY) / g_voxNy;
+    cs3[2] = (g_voxMaxZ - g_voxMinZ) / g_voxNz;
+    const size_t n = g_voxelData.size();
+    for (size_t i = 0; i < n; ++i) {
+        if (mask) mask[i] = (uint8_t)g_voxelData[i];
+        if (sdf) sdf[i] = g_distanceField[i];
+    }
+}
+
+// sampleSDFCPU / sdfNormalCPU (voxel_grid.cpp:32-123) on the last grid, with
+// the flow field's cell size set to the grid's.
+void ref_sdf_sample(const float* pts, long long n, float* dist, float* normal) {
+    flowParams.cellSizeX = (g_voxMaxX - g_voxMinX) / g_voxNx;
+    flowParams.cellSizeY = (g_voxMaxY - g_voxMinY) / g_voxNy;
+    flowParams.cellSizeZ = (g_voxMaxZ - g_voxMinZ) / g_voxNz;
+    for (long long i = 0; i < n; ++i) {
+        const glm::vec3 p(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+        dist[i] = sampleSDFCPU(p);
+        const glm::vec3 nn = sdfNormalCPU(p);
+        normal[3 * i] = nn.x; normal[3 * i + 1] = nn.y; normal[3 * i + 2] = nn.z;
+    }
+}
+
 // Solver mask: 0 fluid, 1 solid, 2 ground.
 void ref_get_mask(uint8_t* out) {
     const size_t n = lbmIsSolid.size();

@@ -160,3 +160,44 @@ def post_points(grid, seed: int = 0x9057) -> np.ndarray:
 def fdigest(a) -> str:
     """Digest of a float32 array with -0 folded into +0."""
     return digest(np.asarray(a, np.float32) + np.float32(0.0))
+
+
+# ---- voxel-grid distance field fixtures --------------------------------------
+# Meshes voxelized by the reference's buildVoxelGrid (its grid plan, mask and
+# distance field, voxel_grid.cpp:224-553); tests/golden/sdf.json keeps the
+# mask (packed), the field's digest and the reference samplers' outputs at
+# seeded points.
+SDF_CASES = {
+    "icosphere_l4_res64": dict(mesh=("icosphere", 4), res=64),
+    "torus_res80": dict(mesh=("torus", 1.0, 0.3, 48, 24), res=80),
+    "box_res48": dict(mesh=("box", (1.0, 0.4, 0.6)), res=48),
+    "perturbed_l4_res96": dict(mesh=("perturbed_icosphere", 4, 1.0, (0.0, 0.0, 0.0), 11), res=96),
+}
+SDF_NPTS = 400
+
+
+def sdf_mesh(case) -> np.ndarray:
+    from aeros_gb300 import geometry
+    kind, *args = case["mesh"]
+    return getattr(geometry, kind)(*args)
+
+
+def sdf_points(lo, hi, seed: int = 0x5DF) -> np.ndarray:
+    """Points over the grid box widened by 10 % on each side (some outside)."""
+    from aeros_gb300 import geometry
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    u = geometry.uniform_array(seed, 3 * SDF_NPTS, 0.0, 1.0).reshape(-1, 3)
+    return (lo - 0.1 * (hi - lo) + u * 1.2 * (hi - lo)).astype(np.float32)
+
+
+def pack_mask(mask: np.ndarray) -> str:
+    import base64
+    import zlib
+    return base64.b64encode(zlib.compress(np.packbits(np.asarray(mask, np.uint8).reshape(-1)).tobytes(), 9)).decode()
+
+
+def unpack_mask(s: str, n: int) -> np.ndarray:
+    import base64
+    import zlib
+    return np.unpackbits(np.frombuffer(zlib.decompress(base64.b64decode(s)), np.uint8))[:n].astype(np.uint8)

@@ -132,9 +132,32 @@ def post_fixtures(R) -> dict:
     return out
 
 
+def sdf_fixtures(R) -> dict:
+    """buildVoxelGrid's mask and distance field (voxel_grid.cpp:224-553) and
+    sampleSDFCPU / sdfNormalCPU (:32-123) of the reference, for SDF_CASES."""
+    from cases import SDF_CASES, fdigest, pack_mask, sdf_mesh, sdf_points
+    out = {}
+    for name, case in SDF_CASES.items():
+        g = R.build_voxel_grid(sdf_mesh(case), case["res"])
+        nx, ny, nz = g["dims"]
+        hi = g["min"] + g["cs"] * np.array([nx, ny, nz], np.float32)
+        pts = sdf_points(g["min"], hi)
+        dist, nrm = R.sdf_sample(pts)
+        out[name] = dict(dims=[nx, ny, nz], min=[float(v) for v in g["min"]], cs=[float(v) for v in g["cs"]],
+                         mask=pack_mask(g["mask"]), sdf=fdigest(g["sdf"]),
+                         sdf_min=float(g["sdf"].min()), sdf_max=float(g["sdf"].max()),
+                         dist=fdigest(dist), normal=fdigest(nrm))
+        print(f"  {name}: {nx}x{ny}x{nz}, solid {int(g['mask'].sum())}, sdf [{g['sdf'].min():.4g}, {g['sdf'].max():.4g}]")
+    return out
+
+
 def main():
     O.build()
     R = O.RefHarness()
+    if "--sdf" in sys.argv:   # only the distance-field fixtures
+        with open(os.path.join(HERE, "sdf.json"), "w") as fh:
+            json.dump(sdf_fixtures(R), fh, indent=1, sort_keys=True)
+        return
     if "--post" in sys.argv:   # only the post-processing fixtures
         with open(os.path.join(HERE, "post.json"), "w") as fh:
             json.dump(post_fixtures(R), fh, indent=1, sort_keys=True)
