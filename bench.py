@@ -302,6 +302,70 @@ def serve_session(n_requests=16, rate=2.0, max_steps=30000, seq_sample=200):
                                  latency_s=round(r.latency, 3)) for r in live["results"]]}
 
 
+def sdf_bench(res=256, reps=5, cpu=True):
+    """The voxel grid's distance field (buildVoxelGrid's distance part) of the
+    level-6 icosphere on the reference's grid plan at resolution `res` (box
+    = mesh bounds + 14 % of the largest extent on each side): mask voxelized
+    on the device, then `reps` timed builds from the device mask into a device
+    field; e2e through the host-array call. CPU baseline: the reference's
+    sweeps + FIFO + smoothing restated (single thread, as the reference runs
+    them) on the same mask."""
+    import ctypes as C
+
+    import torch
+    from aeros_gb300 import capi, geometry, solver
+    tris = geometry.icosphere(6)
+    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    margin = np.float32(0.14) * (hi - lo).max()
+    mn, mx = lo - margin, hi + margin
+    plan = solver.voxel_plan(mx - mn, res)
+    dims = (plan.nx, plan.ny, plan.nz)
+    cs = ((mx - mn) / np.array(dims, np.float32)).astype(np.float32)
+    grid = solver.voxel_grid(dims, mn, cs)
+    n = dims[0] * dims[1] * dims[2]
+    L = capi.lib()
+    dm = torch.empty(n, dtype=torch.uint8, device="cuda")
+    df = torch.empty(n, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    t = np.ascontiguousarray(tris, np.float32)
+    capi.check(L.aeros_voxelize_device(t.ctypes.data_as(C.POINTER(C.c_float)), t.shape[0], C.byref(grid),
+                                       C.c_void_p(dm.data_ptr())), "voxelize")
+    capi.check(L.aeros_sdf_device(C.c_void_p(dm.data_ptr()), C.byref(grid), C.c_void_p(df.data_ptr()), None), "sdf")
+    ms = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        capi.check(L.aeros_sdf_device(C.c_void_p(dm.data_ptr()), C.byref(grid), C.c_void_p(df.data_ptr()), None),
+                   "sdf")
+        ms.append(1000 * (time.perf_counter() - t0))
+    passes, runs = solver.sdf_last_stats()
+    mask = dm.cpu().numpy()
+    t0 = time.perf_counter()
+    field = solver.sdf(mask, grid)
+    e2e_ms = 1000 * (time.perf_counter() - t0)
+    dev_ms = float(np.median(ms))
+    line = {"metric": "distance-field build rate (level-6 icosphere, reference grid plan)",
+            "value": round(n / (dev_ms * 1e-3) / 1e6, 1), "unit": "Mcells/s", "higher_is_better": True,
+            "ms_per_build": round(dev_ms, 3), "builds": reps, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"icosphere L6 (81,920 triangles), grid {dims[0]}x{dims[1]}x{dims[2]} "
+                                   f"({n} cells), res {res}", "solid_cells": int((mask == 1).sum())},
+            "passes": int(passes), "tile_runs": int(runs), "tiles": int(-(-dims[0] // 8) * -(-dims[1] // 8) * -(-dims[2] // 8)),
+            "e2e": {"value": round(n / (e2e_ms * 1e-3) / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": n,
+                    "d2h_bytes_per_step": 4 * n, "what": "aeros_sdf: host mask in, host field out"},
+            "field_range": [float(field.min()), float(field.max())]}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        t0 = time.perf_counter()
+        oracle.sdf(mask, dims, cs)
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": round(n / cpu_s / 1e6, 2), "unit": "Mcells/s", "cores": 1, "kind": "port",
+                                "sample": f"one full build of the same {n}-cell grid (the reference's sweeps, FIFO "
+                                          "and smoothing restated, single thread as the reference's propagation)"}
+    return line
+
+
 def cpu_baseline(mask, steps):
     """The oracle (C restatement of the reference solver, OpenMP) on the same
     grid, `steps` lattice steps (a bounded sample)."""
@@ -371,7 +435,8 @@ def main():
     ap.add_argument("--only", default="both", choices=["both", "fp32", "fp16", "bf16"],
                     help="time one storage form only (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "serve"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "serve", "sdf"])
+    ap.add_argument("--sdf-res", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-rate", type=float, default=2.0)
     ap.add_argument("--serve-max-steps", type=int, default=30000)
@@ -388,6 +453,8 @@ def main():
     elif args.workload == "serve":
         r = serve_session(args.serve_requests, args.serve_rate, args.serve_max_steps)
         print(json.dumps(r), flush=True)
+    elif args.workload == "sdf":
+        print(json.dumps(sdf_bench(args.sdf_res, reps=max(1, min(args.steps, 20)), cpu=not args.no_cpu)), flush=True)
     elif args.workload == "batch":
         r = batch_sweep(args.batch_domains, args.batch_steps, chunk=args.batch_chunk, autotune=not args.batch_fixed)
         print(json.dumps(r), flush=True)

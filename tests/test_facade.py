@@ -72,7 +72,7 @@ def test_facade_channel_equals_c_abi(driver, tmp_path):
     st = s.stats()
     assert f"step {st['step']} " in r.stdout
     assert np.float32(r.stdout.split("avg_rho ")[1].split()[0]) == np.float32(st["avg_rho"])
-    line = r.stdout.split("pmin ")[1].split()
+    line = r.stdout.split("pmin ")[1].splitlines()[0].split()
     assert np.float32(line[0]) == np.float32(wst["pressure_min"])
     assert np.float32(line[2]) == np.float32(wst["pressure_max"])
     assert np.float32(line[4]) == np.float32(wst["residual_rho"])
@@ -87,13 +87,16 @@ def test_facade_channel_equals_c_abi(driver, tmp_path):
         assert np.array_equal(v, rv.reshape(-1)), f
         assert np.array_equal(ok, rok.astype(np.float32)), f
     # the one-point getters agree with the many-point call (point 20 lies inside)
-    probe = r.stdout.split("probe ")[1].split()
+    probe = r.stdout.split("probe ")[1].splitlines()[0].split()
     pv, pok = s.sample(wp, capi.AEROS_FIELD_PRESSURE, pts[20:21])
     assert probe[3] == "1" and pok[0] == 1 and np.float32(probe[1]) == pv[0]
-    assert probe[-2] == "0" and probe[-1] == "1"   # the mid point is fluid, the wall point solid
+    wall = np.array([[-3.0, -1.58, 0.0]], np.float32)   # cell (2, 0, 16): the y = 0 wall row
+    sv, _ = s.sample(wp, capi.AEROS_FIELD_SOLID, np.concatenate([pts[20:21], wall]))
+    assert sv.tolist() == [0.0, 1.0], sv
+    assert probe[-2:] == ["0", "1"], r.stdout   # the mid point is fluid, the wall point solid
     # world velocity: the lattice velocity times flowSpeed / 0.08 (no inlet velocity), within 2 flowSpeed
     uv, _ = s.sample(wp, capi.AEROS_FIELD_VELOCITY_LB, pts[20:21])
-    world = r.stdout.split("world ")[1].split()
+    world = r.stdout.split("world ")[1].splitlines()[0].split()
     scale = np.float32(10.0) / np.float32(0.08)
     assert np.float32(world[1]) == np.float32(uv[0, 0] * scale)
     assert np.float32(world[3]) == np.float32(uv[0, 1] * scale)
