@@ -150,6 +150,17 @@ _FP = C.POINTER(C.c_float)
 _U8P = C.POINTER(C.c_uint8)
 _DP = C.POINTER(C.c_double)
 
+class StlInfo(C.Structure):
+    _fields_ = [("format", C.c_int32), ("reason", C.c_int32), ("declared_triangles", C.c_uint32),
+                ("reserved0", C.c_uint32), ("payload_bytes", C.c_uint64), ("trailing_bytes", C.c_uint64),
+                ("triangles", C.c_int64), ("dropped", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved0"}
+
+
+AEROS_STL_UNKNOWN, AEROS_STL_BINARY, AEROS_STL_ASCII = 0, 1, 2
+
 _SIGS = {
     "aeros_consume_error": (C.c_int, [C.c_char_p, C.c_int]),
     "aeros_lbm_create": (C.c_int, [C.POINTER(LbmParams), _U8P, C.POINTER(_P)]),
@@ -186,6 +197,9 @@ _SIGS = {
     "aeros_sdf": (C.c_int, [_U8P, C.POINTER(VoxelGrid), _FP]),
     "aeros_sdf_sample": (C.c_int, [_P, C.POINTER(VoxelGrid), _FP, C.c_int64, _FP, _FP]),
     "aeros_sdf_last_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "aeros_stl_detect": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(StlInfo)]),
+    "aeros_stl_parse": (C.c_int, [C.c_char_p, C.c_uint64, C.c_uint64, _FP, _FP, C.c_int64, C.POINTER(StlInfo)]),
+    "aeros_stl_read_file": (C.c_int, [C.c_char_p, C.c_uint64, _FP, _FP, C.c_int64, C.POINTER(StlInfo)]),
     "aeros_batch_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
     "aeros_batch_destroy": (C.c_int, [_P]),
     "aeros_batch_add": (C.c_int, [_P, _P]),

@@ -225,6 +225,37 @@ def sdf_sample(d_sdf: int, grid: VoxelGrid, points: np.ndarray) -> tuple[np.ndar
     return dist, nrm
 
 
+def stl_detect(data: bytes) -> dict:
+    """stlformat::detect (aeros/src/stl_format.h:86-140) of file bytes."""
+    info = capi.StlInfo()
+    check(lib().aeros_stl_detect(data, len(data), C.byref(info)), "stl_detect")
+    return info.as_dict()
+
+
+def stl_parse(data: bytes, budget: int = 0) -> tuple[np.ndarray, np.ndarray, dict]:
+    """loadSTL's parse (aeros/src/stl_loader.cpp:30-223) of file bytes:
+    (triangles [n, 9], per-vertex normals [n, 9], info)."""
+    info = capi.StlInfo()
+    check(lib().aeros_stl_parse(data, len(data), budget, None, None, 0, C.byref(info)), "stl_parse")
+    n = info.triangles
+    v = np.empty((n, 9), np.float32)
+    nrm = np.empty((n, 9), np.float32)
+    check(lib().aeros_stl_parse(data, len(data), budget, _f(v), _f(nrm), n, C.byref(info)), "stl_parse")
+    return v, nrm, info.as_dict()
+
+
+def stl_read(path: str, budget: int = 0) -> tuple[np.ndarray, np.ndarray, dict]:
+    """stl_parse of a file on disk (aeros_stl_read_file)."""
+    info = capi.StlInfo()
+    p = str(path).encode()
+    check(lib().aeros_stl_read_file(p, budget, None, None, 0, C.byref(info)), "stl_read")
+    n = info.triangles
+    v = np.empty((n, 9), np.float32)
+    nrm = np.empty((n, 9), np.float32)
+    check(lib().aeros_stl_read_file(p, budget, _f(v), _f(nrm), n, C.byref(info)), "stl_read")
+    return v, nrm, info.as_dict()
+
+
 def voxel_grid(n, mn, cell) -> VoxelGrid:
     g = VoxelGrid()
     g.nx, g.ny, g.nz = (int(v) for v in n)

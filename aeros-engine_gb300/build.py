@@ -9,6 +9,7 @@ Translation units and their floating-point contraction:
   batch.cu     --fmad=false  host side of the many-domain batch
   post.cu      --fmad=false  world fields, vorticity / Q, samplers as the reference rounds them
   sdf.cu       --fmad=false  distance field: weights, smoothing and samplers as the reference
+  stl.cpp      host only     STL detection and parse (-ffp-contract=off like all host code)
 """
 from __future__ import annotations
 
@@ -38,6 +39,7 @@ UNITS = {
     "batch.cu": ["--fmad=false"],
     "post.cu": ["--fmad=false"],
     "sdf.cu": ["--fmad=false"],
+    "stl.cpp": [],
     "setup.cu": [],
 }
 HEADERS = ["lattice.cuh", "lbm_step.cuh", "lbm_aux.cuh", "forces.cuh", "setup.cuh", "handle.cuh"]
@@ -60,7 +62,7 @@ def _stale(obj: str, src: str) -> bool:
 
 def _compile(unit: str, flags: list[str], verbose: bool) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD_DIR, unit.replace(".cu", f".{TAG}.o"))
+    obj = os.path.join(BUILD_DIR, f"{os.path.splitext(unit)[0]}.{TAG}.o")
     if _stale(obj, src):
         cmd = [nvcc(), *ARCH, *COMMON, f"-DAEROS_STEP_MIN_BLOCKS={MIN_BLOCKS}",
                f"-DAEROS_STAGED_MIN_BLOCKS={STAGED_MIN_BLOCKS}", f"-DAEROS_FUSED_MIN_BLOCKS={FUSED_MIN_BLOCKS}",

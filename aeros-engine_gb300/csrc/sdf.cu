@@ -9,9 +9,9 @@
 // over the 26 neighbours, with the sign of the seed a minimal path starts
 // from (negative on equal magnitudes). Float addition of a positive weight
 // is monotone, so the fixed point is unique and every schedule reaches the
-// same bits; the reference stops short of it (never below it in magnitude
-// before smoothing) by at most a small fraction of a cell: under 2 % of the
-// smallest cell on the test meshes, after smoothing.
+// same bits. The reference stops short of it (never below it in magnitude
+// before smoothing): on the test meshes 99.99 % of the cells agree within
+// 1e-4 and all within 2e-3 (cells at the smoothing's 3-cell threshold).
 //
 // State during propagation: one 32-bit key per cell, (bits(|d|) << 1) | (d >= 0),
 // so that the better value is the smaller unsigned key. The grid is cut into
@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <vector>
 
 #include "../../include/aeros_lbm.h"
@@ -486,6 +487,62 @@ extern "C" int aeros_sdf_sample(const float* d_sdf, const aeros_voxel_grid* grid
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "distance samples: %s", cudaGetErrorString(e));
     return AEROS_OK;
+}
+
+// A distance field kept on the device for sampling (the reference keeps
+// g_distanceField for sampleSDFCPU / sdfNormalCPU).
+struct aeros_sdf_field {
+    aeros_voxel_grid grid;
+    float* d = nullptr;
+};
+
+extern "C" int aeros_sdf_field_create(const uint8_t* mask, const aeros_voxel_grid* grid, aeros_sdf_field** out) {
+    if (!out) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    if (int rc = check_sdf_grid(grid)) return rc;
+    if (!mask) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    const size_t total = (size_t)grid->nx * grid->ny * grid->nz;
+    aeros_sdf_field* f = new (std::nothrow) aeros_sdf_field;
+    if (!f) return set_error(AEROS_ERR_ALLOC, "field handle");
+    f->grid = *grid;
+    cudaStream_t s = nullptr;
+    uint8_t* dm = nullptr;
+    cudaError_t e = cudaMalloc((void**)&f->d, total * 4);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dm, total, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dm, mask, total, cudaMemcpyHostToDevice, s);
+    int rc = e == cudaSuccess ? sdf_impl(dm, grid, f->d, s) : set_error(AEROS_ERR_CUDA, "field: %s", cudaGetErrorString(e));
+    if (dm) cudaFreeAsync(dm, s);
+    if (rc == AEROS_OK && (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        rc = set_error(AEROS_ERR_CUDA, "field: %s", cudaGetErrorString(e));
+    if (rc != AEROS_OK) {
+        cudaFree(f->d);
+        delete f;
+        return rc;
+    }
+    *out = f;
+    return AEROS_OK;
+}
+
+extern "C" int aeros_sdf_field_destroy(aeros_sdf_field* f) {
+    if (!f) return AEROS_OK;
+    cudaFree(f->d);
+    delete f;
+    return AEROS_OK;
+}
+
+extern "C" const float* aeros_sdf_field_device(const aeros_sdf_field* f) { return f ? f->d : nullptr; }
+
+extern "C" int aeros_sdf_field_read(const aeros_sdf_field* f, float* sdf) {
+    if (!f || !sdf) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    const size_t total = (size_t)f->grid.nx * f->grid.ny * f->grid.nz;
+    CUDA_TRY(cudaMemcpy(sdf, f->d, total * 4, cudaMemcpyDeviceToHost));
+    return AEROS_OK;
+}
+
+extern "C" int aeros_sdf_field_sample(const aeros_sdf_field* f, const float* points, int64_t n, float* dist,
+                                      float* normal) {
+    if (!f) return set_error(AEROS_ERR_INVALID, "field is NULL");
+    return aeros_sdf_sample(f->d, &f->grid, points, n, dist, normal);
 }
 
 extern "C" int aeros_sdf_last_stats(int64_t* passes, int64_t* tile_runs) {

@@ -53,6 +53,12 @@ std::vector<float> lbmQCriterion;
 float lbmPressureMin = 0.0f, lbmPressureMax = 0.0f, lbmResidualRho = 0.0f, lbmResidualU = 0.0f;
 long long lbmPressureNonFinite = 0;
 
+float g_voxMinX = 0.0f, g_voxMinY = 0.0f, g_voxMinZ = 0.0f, g_voxMaxX = 0.0f, g_voxMaxY = 0.0f, g_voxMaxZ = 0.0f;
+std::vector<float> g_distanceField;
+std::string g_voxelBuildError;
+long long g_voxelSolidCells = 0;
+int g_voxelUsedRes = 0;
+
 ThermalParams thermalParams;
 std::vector<float> thermalT;
 std::vector<float> thermalBuoyancyY;
@@ -127,6 +133,137 @@ bool read_world() {
     return true;
 }
 }  // namespace
+
+namespace {
+aeros_sdf_field* g_sdf = nullptr;   // the device copy of g_distanceField
+}  // namespace
+
+bool loadSTL(const std::string& filename, std::vector<float>& vertices, std::vector<float>& normals) {
+    aeros_stl_info info{};
+    if (!ok(aeros_stl_read_file(filename.c_str(), 0, nullptr, nullptr, 0, &info))) return false;
+    const size_t base = vertices.size();
+    vertices.resize(base + (size_t)info.triangles * 9);
+    normals.resize(normals.size() + (size_t)info.triangles * 9);
+    return ok(aeros_stl_read_file(filename.c_str(), 0, vertices.data() + base,
+                                  normals.data() + normals.size() - (size_t)info.triangles * 9, info.triangles, &info));
+}
+
+void buildVoxelGrid(const std::vector<float>& verts, int res) {
+    g_voxelBuildError.clear();
+    g_voxelSolidCells = 0;
+    g_voxelUsedRes = 0;
+    if (verts.empty()) {
+        g_voxelBuildError = "no vertices";
+        return;
+    }
+    res = std::min(std::max(res, 8), 256);
+    // bounds as the model loader computes them (model.cpp:47-66)
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    bool any = false;
+    for (size_t i = 0; i + 2 < verts.size(); i += 3) {
+        if (!std::isfinite(verts[i]) || !std::isfinite(verts[i + 1]) || !std::isfinite(verts[i + 2])) continue;
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], verts[i + a]);
+            hi[a] = std::max(hi[a], verts[i + a]);
+        }
+        any = true;
+    }
+    if (!any) {
+        g_voxelBuildError = "no finite vertex";
+        return;
+    }
+    const float ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+    const float diag = std::sqrt(ex * ex + ey * ey + ez * ez);
+    if (!(diag >= 1e-6f)) {   // voxel_grid.cpp:241-244
+        g_voxelBuildError = "invalid bounding box";
+        return;
+    }
+    const float maxDim = (diag < 0.0001f || !std::isfinite(diag)) ? 1.0f : diag;
+    // grid box and plan (voxel_grid.cpp:246-288)
+    float margin = 0.14f * maxDim;
+    if (!std::isfinite(margin) || margin < 0.001f) margin = 0.1f;
+    float mn[3], mx[3], size[3];
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = lo[a] - margin;
+        mx[a] = hi[a] + margin;
+        size[a] = mx[a] - mn[a];
+        if (size[a] < 1e-6f) size[a] = 1.0f;
+    }
+    aeros_voxel_plan_t plan{};
+    if (!ok(aeros_voxel_plan(size, res, 0, &plan))) {
+        g_voxelBuildError = g_error;
+        return;
+    }
+    aeros_voxel_grid grid{};
+    grid.nx = plan.nx;
+    grid.ny = plan.ny;
+    grid.nz = plan.nz;
+    for (int a = 0; a < 3; ++a) {
+        const int n = a == 0 ? plan.nx : (a == 1 ? plan.ny : plan.nz);
+        grid.min[a] = mn[a];
+        grid.cell[a] = size[a] / n;
+        if (grid.cell[a] < 1e-6f) grid.cell[a] = 0.1f;
+    }
+    const long long total = (long long)grid.nx * grid.ny * grid.nz;
+    if (total <= 0 || total > 20ll * 1024 * 1024) {
+        g_voxelBuildError = "cell count " + std::to_string(total) + " outside 1 .. 20 M";
+        return;
+    }
+    std::vector<uint8_t> mask((size_t)total);
+    if (!ok(aeros_voxelize(verts.data(), (int64_t)(verts.size() / 9), &grid, mask.data()))) {
+        g_voxelBuildError = g_error;
+        return;
+    }
+    aeros_sdf_field* f = nullptr;
+    if (!ok(aeros_sdf_field_create(mask.data(), &grid, &f))) {
+        g_voxelBuildError = g_error;
+        return;
+    }
+    g_distanceField.resize((size_t)total);
+    if (!ok(aeros_sdf_field_read(f, g_distanceField.data()))) {
+        aeros_sdf_field_destroy(f);
+        g_voxelBuildError = g_error;
+        return;
+    }
+    aeros_sdf_field_destroy(g_sdf);
+    g_sdf = f;
+    g_voxNx = grid.nx;
+    g_voxNy = grid.ny;
+    g_voxNz = grid.nz;
+    g_voxMinX = mn[0]; g_voxMinY = mn[1]; g_voxMinZ = mn[2];
+    g_voxMaxX = mx[0]; g_voxMaxY = mx[1]; g_voxMaxZ = mx[2];
+    g_voxelData.assign(mask.begin(), mask.end());
+    g_voxelSolidCells = 0;
+    for (uint8_t v : mask) g_voxelSolidCells += v != 0;
+    g_voxelUsedRes = grid.nx;
+}
+
+bool voxelFacadeSampleSDF(const float* points, long long n, float* dist, float* normal) {
+    if (!g_sdf) {   // no field: the reference's 1000 and (0, 1, 0)
+        for (long long i = 0; i < n; ++i) {
+            if (dist) dist[i] = 1000.0f;
+            if (normal) { normal[3 * i] = 0.0f; normal[3 * i + 1] = 1.0f; normal[3 * i + 2] = 0.0f; }
+        }
+        return true;
+    }
+    return ok(aeros_sdf_field_sample(g_sdf, points, n, dist, normal));
+}
+
+float sampleSDFCPU(const LbmVec3& p) {
+    const float pt[3] = {p.x, p.y, p.z};
+    float d = 1000.0f;
+    if (!voxelFacadeSampleSDF(pt, 1, &d, nullptr)) return 1000.0f;
+    return d;
+}
+
+LbmVec3 sdfNormalCPU(const LbmVec3& p) {
+    const float pt[3] = {p.x, p.y, p.z};
+    float n[3] = {0.0f, 1.0f, 0.0f};
+    LbmVec3 r;
+    if (!voxelFacadeSampleSDF(pt, 1, nullptr, n)) n[0] = 0.0f, n[1] = 1.0f, n[2] = 0.0f;
+    r.x = n[0]; r.y = n[1]; r.z = n[2];
+    return r;
+}
 
 aeros_lbm* lbmFacadeHandle() { return g_handle; }
 const std::string& lbmFacadeLastError() { return g_error; }

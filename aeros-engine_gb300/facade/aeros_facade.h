@@ -184,6 +184,25 @@ bool thermalUpload(const std::vector<float>& T);
 // call has nothing left to do.
 void thermalStep(const float* ux, const float* uy, const float* uz);
 
+// ---- geometry in (aeros/src/stl_loader.h, aeros/src/voxel_grid.h) ---------------
+// loadSTL (stl_loader.cpp:30-223): binary or ASCII by content; 9 floats per
+// triangle, per-vertex normals. false when the file cannot be used.
+bool loadSTL(const std::string& filename, std::vector<float>& vertices, std::vector<float>& normals);
+// buildVoxelGrid (voxel_grid.cpp:224-553) on the device: grid plan over the
+// mesh bounds (computed from verts as the model loader does, model.cpp:47-66)
+// plus 14 % of their diagonal, mask by the BVH three-ray vote, signed
+// distance field. Fills the voxel globals below; g_voxelBuildError says why
+// when it does not. The memory plan has no byte budget (the reference caps it
+// at half of the free RAM).
+void buildVoxelGrid(const std::vector<float>& verts, int res);
+float sampleSDFCPU(const LbmVec3& p);    // on the device, one point per call
+LbmVec3 sdfNormalCPU(const LbmVec3& p);
+extern float g_voxMinX, g_voxMinY, g_voxMinZ, g_voxMaxX, g_voxMaxY, g_voxMaxZ;
+extern std::vector<float> g_distanceField;
+extern std::string g_voxelBuildError;
+extern long long g_voxelSolidCells;
+extern int g_voxelUsedRes;
+
 // ---- extras of this layer ----------------------------------------------------
 // The C-ABI handle (NULL before initLBM): for callers that also use the batch
 // or the device field pointers.
@@ -192,3 +211,5 @@ aeros_lbm* lbmFacadeHandle();
 bool lbmFacadeReadFields();
 // Message of the last failed call ("" when none).
 const std::string& lbmFacadeLastError();
+// Many distance samples at once (xyz each; dist n, normal 3n, either NULL).
+bool voxelFacadeSampleSDF(const float* points, long long n, float* dist, float* normal);

@@ -305,7 +305,7 @@ def serve_session(n_requests=16, rate=2.0, max_steps=30000, seq_sample=200):
 def sdf_bench(res=256, reps=5, cpu=True):
     """The voxel grid's distance field (buildVoxelGrid's distance part) of the
     level-6 icosphere on the reference's grid plan at resolution `res` (box
-    = mesh bounds + 14 % of the largest extent on each side): mask voxelized
+    = mesh bounds + 14 % of the bounds' diagonal on each side): mask voxelized
     on the device, then `reps` timed builds from the device mask into a device
     field; e2e through the host-array call. CPU baseline: the reference's
     sweeps + FIFO + smoothing restated (single thread, as the reference runs
@@ -316,7 +316,7 @@ def sdf_bench(res=256, reps=5, cpu=True):
     from aeros_gb300 import capi, geometry, solver
     tris = geometry.icosphere(6)
     lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
-    margin = np.float32(0.14) * (hi - lo).max()
+    margin = np.float32(0.14) * np.float32(np.sqrt(np.sum((hi - lo) ** 2, dtype=np.float32)))
     mn, mx = lo - margin, hi + margin
     plan = solver.voxel_plan(mx - mn, res)
     dims = (plan.nx, plan.ny, plan.nz)

@@ -242,8 +242,8 @@ int aeros_voxelize_device_noalloc(const float* tris, int64_t ntri,
  * sqrtf(wx^2 + wy^2 + wz^2) runs to its least fixed point: the float
  * shortest-path length from a seed, with that seed's sign (negative on
  * equal lengths). The reference's four sweeps and 1e-3 FIFO stop short of
- * that limit by a small fraction of a cell (under 2 % of the smallest cell
- * on the test meshes; same signs).
+ * that limit (same signs; on the test meshes 99.99 % of the cells within
+ * 1e-4, all within 2e-3).
  * Then the reference's two rounds of x, y, z smoothing beyond 3 cells.
  * Device mask and output, nx*ny*nz each; stream: a cudaStream_t or NULL.
  * Returns when the field is complete. AEROS_ERR_TIMEOUT if the propagation
@@ -259,9 +259,67 @@ int aeros_sdf(const uint8_t* mask, const aeros_voxel_grid* grid, float* sdf);
  * reference without a field. */
 int aeros_sdf_sample(const float* d_sdf, const aeros_voxel_grid* grid, const float* points, int64_t n,
                      float* dist, float* normal);
+/* A field built on the device and kept there (the reference keeps
+ * g_distanceField for its samplers): create from a host mask, read back,
+ * sample (aeros_sdf_sample on the field's own device array and grid),
+ * destroy. */
+typedef struct aeros_sdf_field aeros_sdf_field;
+int aeros_sdf_field_create(const uint8_t* mask, const aeros_voxel_grid* grid, aeros_sdf_field** out);
+int aeros_sdf_field_destroy(aeros_sdf_field* field);
+const float* aeros_sdf_field_device(const aeros_sdf_field* field);   /* NULL for NULL */
+int aeros_sdf_field_read(const aeros_sdf_field* field, float* sdf);
+int aeros_sdf_field_sample(const aeros_sdf_field* field, const float* points, int64_t n, float* dist,
+                           float* normal);
 /* Propagation passes and tile runs (8x8x8 tiles) of the calling thread's
  * last distance-field build. No reference counterpart: diagnostics. */
 int aeros_sdf_last_stats(int64_t* passes, int64_t* tile_runs);
+
+/* ---- STL ingest ------------------------------------------------------------------- */
+/* Format detection by content (stlformat::detect, aeros/src/stl_format.h:86-140):
+ * ASCII when the file starts with "solid" and holds facet / vertex keywords;
+ * else binary when the 80-byte header's triangle count fits the data (a tail
+ * after the triangles is allowed); else ASCII for keyword text without
+ * "solid"; else unknown (truncated binary, text without keywords, other). */
+enum { AEROS_STL_UNKNOWN = 0, AEROS_STL_BINARY = 1, AEROS_STL_ASCII = 2 };
+enum {
+    AEROS_STL_REASON_EMPTY = 0,
+    AEROS_STL_REASON_ASCII = 1,              /* "solid" + facet/vertex               */
+    AEROS_STL_REASON_BINARY = 2,             /* size matches the count exactly       */
+    AEROS_STL_REASON_BINARY_TAIL = 3,        /* trailing bytes after the triangles   */
+    AEROS_STL_REASON_TEXT_NO_SOLID = 4,      /* keyword text without "solid"         */
+    AEROS_STL_REASON_TEXT_NO_KEYWORDS = 5,   /* text without facet/vertex (unknown)  */
+    AEROS_STL_REASON_TRUNCATED = 6,          /* the count promises more than there is */
+    AEROS_STL_REASON_UNRECOGNIZED = 7
+};
+typedef struct aeros_stl_info {
+    int32_t  format;               /* AEROS_STL_*                                     */
+    int32_t  reason;               /* AEROS_STL_REASON_*                              */
+    uint32_t declared_triangles;   /* header count (binary files)                     */
+    uint32_t reserved0;
+    uint64_t payload_bytes;        /* 50 per declared triangle (binary)               */
+    uint64_t trailing_bytes;       /* after the last triangle (binary)                */
+    int64_t  triangles;            /* triangles parsed (after aeros_stl_parse)        */
+    int64_t  dropped;              /* binary: triangles with a non-finite coordinate;
+                                      ASCII: non-finite vertices, rounded down to 3s  */
+} aeros_stl_info;
+int aeros_stl_detect(const uint8_t* data, uint64_t size, aeros_stl_info* info);
+/* loadSTL's parse (aeros/src/stl_loader.cpp:30-223) of an in-memory file.
+ * Binary: each normal made finite and unit ((0, 0, 1) when not), triangles
+ * with a non-finite coordinate dropped. ASCII: vertex lines in threes (the
+ * number extraction of the C++ standard library streams), each triangle's
+ * normal from its edges ((0, 1, 0) when degenerate). vertices gets 9 floats
+ * per triangle, normals 9 per triangle (the normal once per vertex); either
+ * may be NULL; at most `capacity` triangles are written while
+ * info->triangles counts them all (call with capacity 0 to size the
+ * buffers). budget: refuse a binary file whose vertices + normals need more
+ * bytes (0: no limit; the reference uses half of the available RAM). Files
+ * under 10 bytes or over 2 GiB, unknown formats and files without a usable
+ * triangle return AEROS_ERR_INVALID. */
+int aeros_stl_parse(const uint8_t* data, uint64_t size, uint64_t budget, float* vertices, float* normals,
+                    int64_t capacity, aeros_stl_info* info);
+/* Same for a file path. */
+int aeros_stl_read_file(const char* path, uint64_t budget, float* vertices, float* normals, int64_t capacity,
+                        aeros_stl_info* info);
 
 /* Grid plan (aeros/src/voxel_grid.cpp:172-215): dimensions for a bounding box
  * and resolution against a byte budget (0 = unlimited). */

@@ -301,6 +301,10 @@ class RefHarness:
         L.ref_build_voxel_grid.argtypes = [_FP, C.c_longlong, C.c_int]
         L.ref_voxel_get.argtypes = [C.POINTER(C.c_int), _FP, _FP, _U8P, _FP]
         L.ref_sdf_sample.argtypes = [_FP, C.c_longlong, _FP, _FP]
+        L.ref_stl_detect.argtypes = [C.c_char_p, C.c_ulonglong, C.POINTER(C.c_ulonglong)]
+        L.ref_stl_load.restype = C.c_longlong
+        L.ref_stl_load.argtypes = [C.c_char_p]
+        L.ref_stl_get.argtypes = [_FP, _FP]
         self.L = L
         self.n = 0
 
@@ -391,6 +395,20 @@ class RefHarness:
         field = np.zeros(n, np.float32)
         self.L.ref_voxel_get(dims, fptr(mn), fptr(cs), u8ptr(mask), fptr(field))
         return dict(dims=tuple(dims), min=mn, cs=cs, mask=mask, sdf=field)
+
+    def stl_detect(self, data: bytes) -> list:
+        out = (C.c_ulonglong * 4)()
+        self.L.ref_stl_detect(data, len(data), out)
+        return [int(v) for v in out]
+
+    def stl_load(self, path: str):
+        n = self.L.ref_stl_load(path.encode())
+        if n <= 0:
+            return int(n), None, None
+        v = np.empty(9 * n, np.float32)
+        nrm = np.empty(9 * n, np.float32)
+        self.L.ref_stl_get(fptr(v), fptr(nrm))
+        return int(n), v, nrm
 
     def sdf_sample(self, points: np.ndarray):
         pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)

@@ -16,6 +16,8 @@
 #include <cstring>
 
 #include "mesh_bvh.h"
+#include "stl_format.h"
+#include "stl_loader.h"
 
 extern "C" double glfwGetTime(void) { static double t = 0.0; return (t += 1.0 / 60.0); }
 extern "C" void setVoxelData(const int*, const float*, int, int, int, float, float, float, float, float, float) {}
@@ -282,8 +284,9 @@ int ref_validation_setup(int shape, int res, float radius, int diameter_cells, f
     return 0;
 }
 
-// The reference's whole voxel grid build (voxel_grid.cpp:224-553): grid plan
-// from the mesh box with its 14 % margin, BVH mask, distance field. Returns
+// The reference's whole voxel grid build (voxel_grid.cpp:224-553) of a mesh
+// whose bounds are set as the model loader sets them: grid plan from the
+// mesh box with a margin of 14 % of its diagonal, BVH mask, distance field. Returns
 // the cell count (0 when the build refused); ref_voxel_get reads the result:
 // dims3, the grid minimum, the cell sizes, the mask and the distance field.
 long long ref_build_voxel_grid(const float* verts, long long nfloats, int res) {
@@ -293,9 +296,10 @@ long long ref_build_voxel_grid(const float* verts, long long nfloats, int res) {
         lo = glm::min(lo, glm::vec3(v[i], v[i + 1], v[i + 2]));
         hi = glm::max(hi, glm::vec3(v[i], v[i + 1], v[i + 2]));
     }
-    minBB = lo; maxBB = hi; center = 0.5f * (lo + hi);
-    const glm::vec3 ext = hi - lo;
-    maxDim = std::max(ext.x, std::max(ext.y, ext.z));
+    // bounds as the model loader sets them (model.cpp:47-66)
+    minBB = lo; maxBB = hi; center = (lo + hi) * 0.5f;
+    maxDim = glm::length(hi - lo);
+    if (maxDim < 0.0001f || !std::isfinite(maxDim)) maxDim = 1.0f;
     g_voxelData.clear();
     g_distanceField.clear();
     buildVoxelGrid(v, res);
@@ -328,6 +332,30 @@ void ref_sdf_sample(const float* pts, long long n, float* dist, float* normal) {
         const glm::vec3 nn = sdfNormalCPU(p);
         normal[3 * i] = nn.x; normal[3 * i + 1] = nn.y; normal[3 * i + 2] = nn.z;
     }
+}
+
+// stlformat::detect (stl_format.h:86-140): out4 = format (0 unknown, 1
+// binary, 2 ascii), declared triangles, payload bytes, trailing bytes.
+void ref_stl_detect(const unsigned char* data, unsigned long long size, unsigned long long* out4) {
+    const stlformat::Detection d = stlformat::detect(data, (std::size_t)size);
+    out4[0] = d.format == stlformat::Format::Binary ? 1 : (d.format == stlformat::Format::Ascii ? 2 : 0);
+    out4[1] = d.declaredTriangles;
+    out4[2] = d.payloadBytes;
+    out4[3] = d.trailingBytes;
+}
+
+// loadSTL (stl_loader.cpp:30-223): returns the triangle count (-1 when it
+// returned false); ref_stl_get copies the arrays of the last load.
+static std::vector<float> s_stl_v, s_stl_n;
+long long ref_stl_load(const char* path) {
+    s_stl_v.clear();
+    s_stl_n.clear();
+    if (!loadSTL(path, s_stl_v, s_stl_n)) return -1;
+    return (long long)(s_stl_v.size() / 9);
+}
+void ref_stl_get(float* v, float* n) {
+    std::memcpy(v, s_stl_v.data(), s_stl_v.size() * sizeof(float));
+    std::memcpy(n, s_stl_n.data(), s_stl_n.size() * sizeof(float));
 }
 
 // Solver mask: 0 fluid, 1 solid, 2 ground.

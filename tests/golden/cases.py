@@ -172,13 +172,25 @@ SDF_CASES = {
     "torus_res80": dict(mesh=("torus", 1.0, 0.3, 48, 24), res=80),
     "box_res48": dict(mesh=("box", (1.0, 0.4, 0.6)), res=48),
     "perturbed_l4_res96": dict(mesh=("perturbed_icosphere", 4, 1.0, (0.0, 0.0, 0.0), 11), res=96),
+    # the "binary_exact" STL file of stl_files() as the reference's loadSTL reads it
+    "stl_binary_exact_res40": dict(mesh=("stl", "binary_exact"), res=40),
 }
 SDF_NPTS = 400
 
 
-def sdf_mesh(case) -> np.ndarray:
+def sdf_mesh(case, R=None) -> np.ndarray:
+    """The case's triangles; STL cases are read by the reference harness R."""
     from aeros_gb300 import geometry
     kind, *args = case["mesh"]
+    if kind == "stl":
+        import os
+        import tempfile
+        with tempfile.TemporaryDirectory() as tmp:
+            path = os.path.join(tmp, args[0] + ".stl")
+            with open(path, "wb") as fh:
+                fh.write(stl_files()[args[0]])
+            n, v, _ = R.stl_load(path)
+        return v.reshape(n, 9)
     return getattr(geometry, kind)(*args)
 
 
@@ -201,3 +213,76 @@ def unpack_mask(s: str, n: int) -> np.ndarray:
     import base64
     import zlib
     return np.unpackbits(np.frombuffer(zlib.decompress(base64.b64decode(s)), np.uint8))[:n].astype(np.uint8)
+
+
+# ---- STL ingest fixtures -------------------------------------------------------
+# Synthetic STL files (bytes built here from seeded meshes); tests/golden/stl.json
+# keeps what the reference's loadSTL and stlformat::detect make of each.
+
+def _stl_binary(tris, normals, header=b"aeros-gb300 binary STL", count=None, tail=b""):
+    import struct
+    tris = np.asarray(tris, np.float32).reshape(-1, 9)
+    normals = np.asarray(normals, np.float32).reshape(-1, 3)
+    n = tris.shape[0] if count is None else count
+    rec = np.zeros(tris.shape[0], dtype=[("n", "<f4", 3), ("v", "<f4", 9), ("a", "<u2")])
+    rec["n"] = normals
+    rec["v"] = tris
+    return header.ljust(80, b" ")[:80] + struct.pack("<I", n) + rec.tobytes() + tail
+
+
+def _face_normals(tris):
+    t = np.asarray(tris, np.float32).reshape(-1, 3, 3)
+    n = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+    return (n / np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-30)).astype(np.float32)
+
+
+def _stl_ascii(tris, fmt="%.9g", kw=("facet normal", "outer loop", "vertex", "endloop", "endfacet"),
+               newline="\n", indent="  ", solid=True, extra_vertices=()):
+    tris = np.asarray(tris, np.float32).reshape(-1, 3, 3)
+    nrm = _face_normals(tris)
+    out = ["solid synthetic"] if solid else []
+    for t, n in zip(tris, nrm):
+        out.append(f"{indent}{kw[0]} " + " ".join(fmt % v for v in n))
+        out.append(f"{indent * 2}{kw[1]}")
+        for v in t:
+            out.append(f"{indent * 3}{kw[2]} " + " ".join(fmt % c for c in v))
+        out.append(f"{indent * 2}{kw[3]}")
+        out.append(f"{indent}{kw[4]}")
+        out.append("")
+    for v in extra_vertices:
+        out.append(f"{indent}{kw[2]} " + " ".join(fmt % c for c in v))
+    if solid:
+        out.append("endsolid synthetic")
+    return newline.join(out).encode()
+
+
+def stl_files() -> dict:
+    """name -> file bytes."""
+    from aeros_gb300 import geometry
+    ico3 = geometry.icosphere(3, 1.5, (0.25, -0.5, 2.0))
+    ico2 = geometry.icosphere(2, 0.75)
+    files = {}
+    files["binary_exact"] = _stl_binary(ico3, _face_normals(ico3))
+    # "solid" header on a binary file, a tail, normals to fix, a triangle with a NaN vertex
+    t = geometry.perturbed_icosphere(2, 1.0, (0.0, 0.0, 0.0), 5).copy()
+    n = _face_normals(t) * np.float32(3.5)
+    n[0] = np.nan
+    n[1] = 0.0
+    n[2] = [np.inf, 0.0, 1.0]
+    n[3] = [1e-8, 0.0, 0.0]
+    t[4, 2] = np.nan
+    t[5, 7] = -np.inf
+    files["binary_solid_header_tail_fixups"] = _stl_binary(t, n, header=b"solid exported by a CAD tool", tail=b"\0" * 137)
+    files["ascii_plain"] = _stl_ascii(ico2)
+    files["ascii_mixed_case_crlf"] = _stl_ascii(
+        ico2, fmt="%.6e", kw=("Facet Normal", "OUTER LOOP", "VERTEX", "EndLoop", "ENDFACET"), newline="\r\n",
+        indent="\t", extra_vertices=[(1.0, 2.0, 3.0), (4.0, 5.0, 6.0)])
+    deg = np.array([[0, 0, 0, 1, 1, 1, 2, 2, 2], [0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    files["ascii_no_solid_degenerate"] = _stl_ascii(deg, fmt="%.3f", solid=False)
+    nums = "solid n\nfacet normal 0 0 1\nouter loop\nvertex 1.5e-3 -0 +2.25\nvertex .5 7. 1E2\n" \
+           "vertex -3.25e+1 0.1 0.2\nendloop\nendfacet\nendsolid n\n"
+    files["ascii_number_forms"] = nums.encode()
+    files["binary_truncated"] = _stl_binary(ico2[:50], _face_normals(ico2[:50]), count=100)
+    files["text_without_keywords"] = b"this is a plain text file\nwith two lines of words\n"
+    files["too_small"] = b"solid x"
+    return files

@@ -138,7 +138,7 @@ def sdf_fixtures(R) -> dict:
     from cases import SDF_CASES, fdigest, pack_mask, sdf_mesh, sdf_points
     out = {}
     for name, case in SDF_CASES.items():
-        g = R.build_voxel_grid(sdf_mesh(case), case["res"])
+        g = R.build_voxel_grid(sdf_mesh(case, R), case["res"])
         nx, ny, nz = g["dims"]
         hi = g["min"] + g["cs"] * np.array([nx, ny, nz], np.float32)
         pts = sdf_points(g["min"], hi)
@@ -151,9 +151,32 @@ def sdf_fixtures(R) -> dict:
     return out
 
 
+def stl_fixtures(R) -> dict:
+    """stlformat::detect and loadSTL (stl_format.h:86-140, stl_loader.cpp:30-223)
+    of the synthetic files of cases.stl_files()."""
+    import tempfile
+    from cases import fdigest, stl_files
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, data in stl_files().items():
+            path = os.path.join(tmp, name + ".stl")
+            with open(path, "wb") as fh:
+                fh.write(data)
+            det = R.stl_detect(data)
+            n, v, nrm = R.stl_load(path)
+            out[name] = dict(detect=det, triangles=n, vertices=fdigest(v) if n > 0 else None,
+                             normals=fdigest(nrm) if n > 0 else None)
+            print(f"  {name}: detect {det}, triangles {n}")
+    return out
+
+
 def main():
     O.build()
     R = O.RefHarness()
+    if "--stl" in sys.argv:   # only the STL fixtures
+        with open(os.path.join(HERE, "stl.json"), "w") as fh:
+            json.dump(stl_fixtures(R), fh, indent=1, sort_keys=True)
+        return
     if "--sdf" in sys.argv:   # only the distance-field fixtures
         with open(os.path.join(HERE, "sdf.json"), "w") as fh:
             json.dump(sdf_fixtures(R), fh, indent=1, sort_keys=True)

@@ -25,8 +25,17 @@ def driver(tmp_path_factory):
     return exe
 
 
-def test_facade_builds_and_links(driver):
-    assert os.path.exists(driver)
+@pytest.fixture(scope="module")
+def voxel_driver(driver, tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("facade_voxel") / "voxel_driver")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", "-Werror",
+                           "-I", os.path.join(PKG, "facade"), os.path.join(ROOT, "tests", "facade", "voxel_driver.cpp"),
+                           "-o", exe, "-L" + LIB, "-laeros_facade", "-laeros_gb300", "-Wl,-rpath," + LIB])
+    return exe
+
+
+def test_facade_builds_and_links(driver, voxel_driver):
+    assert os.path.exists(driver) and os.path.exists(voxel_driver)
 
 
 NPTS = 64   # tests/facade/channel_driver.cpp
@@ -108,3 +117,43 @@ def test_facade_channel_equals_c_abi(driver, tmp_path):
     assert len(eq) == len(EQ_MOMENT_CASES)
     for row, ref in zip(eq, GOLD["eq_moments"]):
         assert row[0] == "1" and [np.float32(v) for v in row[1:]] == list(np.float32(ref))
+
+
+@pytest.mark.gpu
+def test_facade_stl_to_voxel_grid_equals_reference(voxel_driver, tmp_path):
+    """loadSTL + buildVoxelGrid + sampleSDFCPU / sdfNormalCPU through the
+    facade: the reference's grid and mask bit for bit, the distance field
+    bit for bit the least-fixed-point oracle (and within the distance-field
+    tolerance of the reference), the samplers the oracle's on that field."""
+    import json
+    import oracle
+    from golden.cases import fdigest, sdf_points, stl_files, unpack_mask
+    g = json.load(open(os.path.join(ROOT, "tests", "golden", "sdf.json")))["stl_binary_exact_res40"]
+    stl = tmp_path / "model.stl"
+    stl.write_bytes(stl_files()["binary_exact"])
+    dims = tuple(g["dims"])
+    mn = np.asarray(g["min"], np.float32)
+    cs = np.asarray(g["cs"], np.float32)
+    pts = sdf_points(mn, mn + cs * np.array(dims, np.float32))
+    ptf = tmp_path / "pts.bin"
+    pts.tofile(ptf)
+    out = tmp_path / "grid.bin"
+    r = subprocess.run([voxel_driver, str(stl), "40", str(out), str(ptf)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = out.read_bytes()
+    got_dims = tuple(np.frombuffer(raw[:12], np.int32))
+    box = np.frombuffer(raw[12:36], np.float32)
+    n = dims[0] * dims[1] * dims[2]
+    mask = np.frombuffer(raw[36:36 + n], np.uint8)
+    field = np.frombuffer(raw[36 + n:36 + 5 * n], np.float32)
+    samples = np.frombuffer(raw[36 + 5 * n:], np.float32).reshape(-1, 4)
+    assert got_dims == dims and np.array_equal(box[:3], mn)
+    assert np.array_equal(mask, unpack_mask(g["mask"], n))
+    ex = oracle.sdf(mask, dims, cs, exact=True)
+    assert np.array_equal(field, ex)
+    ref = oracle.sdf(mask, dims, cs)
+    assert fdigest(ref) == g["sdf"]
+    d = np.abs(field - ref)
+    assert np.array_equal(np.sign(field), np.sign(ref)) and np.mean(d <= 1e-4) >= 0.9999 and d.max() <= 2e-3
+    dist, nrm = oracle.sdf_sample(ex, dims, mn, cs, pts)
+    assert np.array_equal(samples[:, 0], dist) and np.array_equal(samples[:, 1:], nrm)

