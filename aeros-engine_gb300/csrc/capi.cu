@@ -93,6 +93,7 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->force_counter);
     cudaFree(h->area_count);
     if (h->ctl_host) cudaFreeHost(h->ctl_host);
+    if (h->force_host) cudaFreeHost(h->force_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     delete h;
@@ -390,9 +391,10 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     ALLOC(h->force_counter, sizeof(unsigned int));
     ALLOC(h->area_count, sizeof(unsigned long long));
 #undef ALLOC
-    if (cudaMallocHost((void**)&h->ctl_host, sizeof(Control)) != cudaSuccess) {
+    if (cudaMallocHost((void**)&h->ctl_host, sizeof(Control)) != cudaSuccess ||
+        cudaMallocHost((void**)&h->force_host, 4 * sizeof(double)) != cudaSuccess) {
         free_handle(h);
-        return set_error(AEROS_ERR_ALLOC, "pinned control block allocation failed");
+        return set_error(AEROS_ERR_ALLOC, "pinned readback allocation failed");
     }
     auto fail = [&](cudaError_t e, const char* what) {
         free_handle(h);
@@ -1060,7 +1062,6 @@ extern "C" int aeros_lbm_thermal_read(aeros_lbm* h, float* T, float* buoyancy) {
 // ---------------------------------------------------------------------------
 extern "C" int aeros_lbm_cv_force_box(aeros_lbm* h, const int32_t box[6], double out[3]) {
     if (!h || !box || !out) return set_error(AEROS_ERR_INVALID, "NULL argument");
-    if (int rc = finish_batch(h)) return rc;
     if (box[0] < 0 || box[1] >= h->nx || box[0] > box[1] || box[2] < 0 || box[3] >= h->ny || box[2] > box[3] ||
         box[4] < 0 || box[5] >= h->nz || box[4] > box[5])
         return set_error(AEROS_ERR_INVALID, "box [%d,%d]x[%d,%d]x[%d,%d] outside the grid", box[0], box[1], box[2],
@@ -1074,10 +1075,22 @@ extern "C" int aeros_lbm_cv_force_box(aeros_lbm* h, const int32_t box[6], double
     a.partials = h->force_partials;
     a.out = h->force_out;
     a.counter = h->force_counter;
-    CUDA_TRY(launch_cv_force(a, cv_force_blocks(a.box, h->max_grid), h->stream));
-    double sums[3];
-    CUDA_TRY(cudaMemcpyAsync(sums, h->force_out, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));
-    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    // Queued behind steps still in flight (stream order), so that one wait
+    // covers the steps, their statistics and the force; the destination is
+    // pinned (a plain DMA).
+    const bool pending = h->stats_dirty;
+    auto enqueue = [&]() -> cudaError_t {
+        a.u = h->u[h->ubuf];
+        cudaError_t e = launch_cv_force(a, cv_force_blocks(a.box, h->max_grid), h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h->force_host, h->force_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        return e;
+    };
+    CUDA_TRY(enqueue());
+    if (int rc = finish_batch(h)) return rc;   // waits for the stream when steps were pending
+    if (pending && h->last_diverged) CUDA_TRY(enqueue());   // the guard reset the state: take the force again
+    if (!pending || h->last_diverged) CUDA_TRY(cudaStreamSynchronize(h->stream));
+    const double* sums = h->force_host;
     // force on the body = minus the momentum flux through the box (lbm.cpp:2231)
     out[0] = -sums[0]; out[1] = -sums[1]; out[2] = -sums[2];
     return AEROS_OK;

@@ -59,6 +59,7 @@ struct aeros_lbm {
     aeros::Control* ctl_host = nullptr;   // pinned
     double* force_partials = nullptr;
     double* force_out = nullptr;
+    double* force_host = nullptr;     // pinned: the force sums read back (3 doubles) and the area count
     unsigned int* force_counter = nullptr;
     unsigned long long* area_count = nullptr;
     uint64_t dev_bytes = 0;

@@ -151,11 +151,12 @@ def run_gb300(args):
             s.close()
         # end to end through the C ABI with host buffers, the way a frame
         # loop drives the solver: the domain is created from the host mask
-        # first (setup, not timed); then per step one aeros_lbm_step(1), whose
-        # call reads the step's statistics back (the control block, D2H), and
-        # the control-volume drag of that step read back (D2H); the fields
-        # are read back to host memory at the end. A step has no host input:
-        # nothing goes host to device inside the timed region.
+        # first (setup, not timed); then per step one aeros_lbm_step_async(1)
+        # and the control-volume drag of that step (aeros_lbm_cv_force), which
+        # waits for the step and reads back its statistics (the control
+        # block, D2H) and the force (D2H); the fields are read back to host
+        # memory at the end. A step has no host input: nothing goes host to
+        # device inside the timed region.
         return_early = args.only != "both" or args.no_e2e
         e2e_steps = 0 if return_early else args.steps
         if not return_early:
@@ -166,8 +167,9 @@ def run_gb300(args):
             t1 = time.perf_counter()
             forces = []
             for _ in range(e2e_steps):
-                s.step(1)
+                s.step_async(1)
                 forces.append(s.cv_force(0.3, 0.3, 0.3))
+                stats = s.stats()   # the step's statistics, read back with the force
             s.fields()
             e2e_s = time.perf_counter() - t1
             s.close()
@@ -220,7 +222,8 @@ def run_gb300(args):
             "fp16_over_fp32": round(results["fp16"]["mlups"] / results["fp32"]["mlups"], 3),
             "e2e": {"value": round(e2e_value, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // max(1, e2e_steps)),
                     "d2h_bytes_per_step": int(d2h // max(1, e2e_steps)),
-                    "what": "per step aeros_lbm_step(1) (statistics read back) + CV-force read back; final fields "
+                    "what": "per step aeros_lbm_step_async(1) + aeros_lbm_cv_force (one wait: the step's statistics and the "
+                            "force read back) + aeros_lbm_get_stats; final fields "
                             "to host; domain created before the timed region"},
             "gpu_launches": int(head["launches"]),
             "clocks": clk.summary(),
