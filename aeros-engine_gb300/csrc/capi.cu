@@ -72,7 +72,7 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->shell_gth);
     cudaFree(h->shell_sct);
     cudaFree(h->zg_src);
-    for (float* b : {h->uxw, h->uyw, h->uzw, h->pressure, h->vort, h->qcrit, h->prev_rho}) cudaFree(b);
+    for (float* b : {h->uxw, h->uyw, h->uzw, h->pressure, h->vort, h->qcrit, h->prev_rho, h->u_split}) cudaFree(b);
     cudaFree(h->post_parts);
     cudaFree(h->post_out);
     cudaFree(h->post_counter);
@@ -796,6 +796,19 @@ extern "C" int aeros_lbm_device_bytes(aeros_lbm* h, uint64_t* b) {
 // ---------------------------------------------------------------------------
 // state I/O
 // ---------------------------------------------------------------------------
+namespace {
+// the velocity (x, y, z, pad per cell) as three planes, for a direct copy
+// into the caller's arrays
+__global__ void k_split_u(const float4* __restrict__ u, float* ux, float* uy, float* uz, long long n) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const float4 v = u[c];
+        ux[c] = v.x;
+        uy[c] = v.y;
+        uz[c] = v.z;
+    }
+}
+}  // namespace
+
 extern "C" int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float* uy, float* uz, float* strain,
                                      float* tke) {
     if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
@@ -806,14 +819,14 @@ extern "C" int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float*
     if (strain) CUDA_TRY(cudaMemcpyAsync(strain, h->strain, b, cudaMemcpyDeviceToHost, h->stream));
     if (tke) CUDA_TRY(cudaMemcpyAsync(tke, h->tke, b, cudaMemcpyDeviceToHost, h->stream));
     if (ux || uy || uz) {
-        std::vector<float4> u(n);
-        CUDA_TRY(cudaMemcpyAsync(u.data(), h->u[h->ubuf], n * 16, cudaMemcpyDeviceToHost, h->stream));
-        CUDA_TRY(cudaStreamSynchronize(h->stream));
-        for (size_t c = 0; c < n; ++c) {
-            if (ux) ux[c] = u[c].x;
-            if (uy) uy[c] = u[c].y;
-            if (uz) uz[c] = u[c].z;
-        }
+        if (!h->u_split) CUDA_TRY(cudaMalloc((void**)&h->u_split, 3 * b));
+        const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, (long long)std::max(1, h->sm_count) * 8);
+        k_split_u<<<blocks, 256, 0, h->stream>>>(h->u[h->ubuf], h->u_split, h->u_split + n, h->u_split + 2 * n,
+                                                 (long long)n);
+        CUDA_TRY(cudaGetLastError());
+        float* dst[3] = {ux, uy, uz};
+        for (int k = 0; k < 3; ++k)
+            if (dst[k]) CUDA_TRY(cudaMemcpyAsync(dst[k], h->u_split + k * n, b, cudaMemcpyDeviceToHost, h->stream));
     }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return AEROS_OK;

@@ -38,6 +38,7 @@ struct aeros_lbm {
     // post-processing (allocated on first use)
     float *uxw = nullptr, *uyw = nullptr, *uzw = nullptr, *pressure = nullptr, *vort = nullptr, *qcrit = nullptr;
     float* prev_rho = nullptr;
+    float* u_split = nullptr;         // readback scratch: ux, uy, uz planes (allocated on first use)
     void* post_parts = nullptr;
     void* post_out = nullptr;
     unsigned int* post_counter = nullptr;
