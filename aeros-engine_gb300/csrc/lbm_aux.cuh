@@ -139,7 +139,7 @@ struct Launchers {
     cudaError_t (*thermal_fill)(const StepArgs& A, float tref, cudaStream_t s);
     cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s);
     int (*batch_occupancy)();
-    int (*fused_occupancy)();
+    int (*fused_occupancy)(bool odd);
 };
 
 const Launchers& launchers_fp32();
@@ -151,7 +151,7 @@ const Launchers& launchers_bf16();
     template <bool O, bool T, bool M>                                                                                 \
     cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
         if (!M && !T && A.fused) {                                                                                    \
-            k_lbm_fused<STORE, O><<<A.fused_grid + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V);                         \
+            k_lbm_fused<STORE, O><<<(O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V); \
         } else if (!M && A.split) {                                                                                   \
             StepArgs B = A;                                                                                           \
             B.shell_part_base = grid;                                                                                 \
@@ -220,11 +220,10 @@ const Launchers& launchers_bf16();
         }                                                                                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    int fused_occ_() {                                                                                                \
-        int n = 0, m = 0;                                                                                             \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false>, STEP_BLOCK, 0);                  \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_lbm_fused<STORE, true>, STEP_BLOCK, 0);                   \
-        n = n < m ? n : m;                                                                                            \
+    int fused_occ_(bool odd) {                                                                                        \
+        int n = 0;                                                                                                    \
+        if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true>, STEP_BLOCK, 0);          \
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false>, STEP_BLOCK, 0);             \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \
     int batch_occ_() {                                                                                                \

@@ -103,7 +103,8 @@ struct StepArgs {
     int split;                  // shell and interior as two launches
     int fused;                  // one launch: shell blocks beside dynamic interior blocks (non-thermal)
     int shell_blocks;           // fused: blocks given to the boundary shell
-    int fused_grid;             // fused: interior blocks (resident blocks per SM x SMs)
+    int fused_grid;             // fused even steps: interior blocks (resident blocks per SM x SMs)
+    int fused_grid_odd;         // fused odd steps (own register budget, own occupancy)
     int inlet_pos;              // inlet plane coordinate along the flow axis
     const int* zg_src;          // zero-gradient outlet: plane index each unknown q of outlet-plane
                                 // cell pi reads, at [q * out_plane + pi] (NULL: computed)
@@ -1234,8 +1235,13 @@ __device__ __forceinline__ int warp_allsum(int v) {
 #define AEROS_BATCH_MIN_BLOCKS 4
 #endif
 
+#ifndef AEROS_FUSED_ODD_MIN_BLOCKS
+#define AEROS_FUSED_ODD_MIN_BLOCKS AEROS_FUSED_MIN_BLOCKS
+#endif
+
 template <class S, bool ODD>
-__global__ void __launch_bounds__(STEP_BLOCK, AEROS_FUSED_MIN_BLOCKS) k_lbm_fused(const StepArgs A, const StepVar V) {
+__global__ void __launch_bounds__(STEP_BLOCK, ODD ? AEROS_FUSED_ODD_MIN_BLOCKS : AEROS_FUSED_MIN_BLOCKS)
+    k_lbm_fused(const StepArgs A, const StepVar V) {
     if (A.ctl->halt) return;   // uniform: every thread reads the same flag
     __shared__ WarpSums s_sums[STEP_BLOCK / 32];
     __shared__ int s_tile[2];
