@@ -49,6 +49,36 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def rank_barrier(world: int) -> None:
+    """Under torchrun: every rank's device work done, then a barrier (both
+    sides of a timed region)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+        dist.barrier()
+
+
+def gather_max(values, world: int) -> list:
+    """Element-wise maximum over the ranks of a list of floats (times): the
+    replicas' job ends with the slowest rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def replica_rate(cells: int, steps: int, seconds: float, world: int) -> float:
+    """Whole-job MLUPS of `world` replicas, each updating `cells` cells
+    `steps` times, when the slowest took `seconds`."""
+    return world * cells * steps / seconds / 1e6
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -108,13 +138,16 @@ def sphere_case(storage, mask=None):
     return geometry.sphere_config(storage=storage, mask=mask)
 
 
-def time_steps(solver, steps, warmup):
+def time_steps(solver, steps, warmup, world=1):
     """Device time of `steps` lattice steps (CUDA events around the launches on
-    the solver's stream), after `warmup` untimed steps."""
+    the solver's stream), after `warmup` untimed steps; under torchrun the
+    timed region is bracketed by a barrier on both sides."""
     solver.step(warmup)
     solver.synchronize()
+    rank_barrier(world)
     solver.step_async(steps)
     ms = solver.last_step_ms()
+    rank_barrier(world)
     launches = solver.last_launch_count()
     st = solver.stats()
     return ms, launches, st
@@ -143,7 +176,7 @@ def run_gb300(args):
         for storage in (("fp32", "fp16") if args.only == "both" else (args.only,)):
             p, _, _ = sphere_case(storage, mask=mask)
             s = solver.Solver(p, mask)
-            ms, launches, st = time_steps(s, args.steps, args.warmup)
+            ms, launches, st = time_steps(s, args.steps, args.warmup, world)
             mlups = cells * args.steps / (ms * 1e-3) / 1e6
             gbs = BYTES_PER_CELL[storage] * cells * args.steps / (ms * 1e-3) / 1e9
             results[storage] = dict(ms_per_step=ms / args.steps, mlups=mlups, achieved_gbs=gbs, launches=launches,
@@ -164,6 +197,7 @@ def run_gb300(args):
             s = solver.Solver(p, mask)
             s.step(2)
             s.synchronize()
+            rank_barrier(world)
             t1 = time.perf_counter()
             forces = []
             for _ in range(e2e_steps):
@@ -172,30 +206,21 @@ def run_gb300(args):
                 stats = s.stats()   # the step's statistics, read back with the force
             s.fields()
             e2e_s = time.perf_counter() - t1
+            rank_barrier(world)
             s.close()
     if return_early:
         print(json.dumps({k: {kk: round(vv, 4) if isinstance(vv, float) else vv for kk, vv in v.items()}
                           for k, v in results.items()}), flush=True)
         return
-    e2e_mlups = cells * e2e_steps / e2e_s / 1e6
     h2d = 0
     # per step: the solver's control block (CONTROL_BYTES) + three doubles of
     # force; at the end six float fields
     d2h = (CONTROL_BYTES + 24) * e2e_steps + 4 * cells * 6
     head = results["fp16"]
-    value = head["mlups"]
-    e2e_value = e2e_mlups
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([value, e2e_value, head["ms_per_step"]], dtype=torch.float64, device="cuda")
-        vals = [torch.zeros_like(t) for _ in range(world)]
-        dist.all_gather(vals, t)
-        value = sum(float(v[0]) for v in vals)
-        e2e_value = sum(float(v[1]) for v in vals)
-        ms_step = max(float(v[2]) for v in vals)
-    else:
-        ms_step = head["ms_per_step"]
+    # the slowest rank's times; value = the cells all ranks updated / that time
+    ms_step, e2e_s = gather_max([head["ms_per_step"], e2e_s], world)
+    value = replica_rate(cells, 1, ms_step * 1e-3, world)
+    e2e_value = replica_rate(cells, e2e_steps, e2e_s, world)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(mask, args.cpu_steps)
