@@ -573,6 +573,67 @@ bool lbmEquilibriumMoments(float rho, float ux, float uy, float uz, float* sumFe
     return true;
 }
 
+bool lbmValidateInitialization() {   // lbm.cpp:2263-2270
+    if (!lbmInitialized || lbmNx <= 0 || lbmNy <= 0 || lbmNz <= 0) return false;
+    if (lbmRho.size() != cells()) return false;
+    for (float r : lbmRho)
+        if (!std::isfinite(r) || r < 0.5f || r > 1.5f) return false;
+    return true;
+}
+
+bool lbmValidateConservation() {   // lbm.cpp:2272-2279
+    if (!lbmInitialized) return true;
+    double sum = 0.0;
+    long long n = 0;
+    for (float r : lbmRho)
+        if (std::isfinite(r)) {
+            sum += r;
+            ++n;
+        }
+    if (n == 0) return false;
+    return std::fabs(sum / (double)n - 1.0f) <= 0.1f;
+}
+
+bool lbmValidateBoundaryConditions() {   // lbm.cpp:2281-2286
+    if (!lbmInitialized) return true;
+    const float mag = std::sqrt(g_uin[0] * g_uin[0] + g_uin[1] * g_uin[1] + g_uin[2] * g_uin[2]);
+    return std::isfinite(mag) && mag >= 1e-6f && mag <= 0.2f;
+}
+
+bool lbmValidateSolidHandling() {   // lbm.cpp:2288-2295
+    if (!lbmInitialized) return true;
+    const size_t n = std::min(lbmIsSolid.size(), lbmUx.size());
+    for (size_t i = 0; i < n; ++i)
+        if (lbmIsSolid[i] && (std::fabs(lbmUx[i]) > 1e-4f || std::fabs(lbmUy[i]) > 1e-4f || std::fabs(lbmUz[i]) > 1e-4f))
+            return false;
+    return true;
+}
+
+bool lbmValidateRealisticAero() {   // lbm.cpp:2297-2309
+    if (!lbmInitialized) return true;
+    float maxP = -1e9f, minP = 1e9f;
+    for (float p : lbmPressure) {
+        if (!std::isfinite(p)) return false;
+        maxP = std::max(maxP, p);
+        minP = std::min(minP, p);
+    }
+    const float q = 0.5f * lbmFacadeAirDensity * lbmFacadeFlowSpeed * lbmFacadeFlowSpeed;
+    if (std::fabs(maxP) > q * 1.5f || std::fabs(minP) > q * 1.5f) return false;
+    for (float t : lbmTKEField)
+        if (t < -1e-3f || !std::isfinite(t) || t > 10.0f) return false;
+    for (float v : lbmVorticityMag)
+        if (v < -1e-3f || !std::isfinite(v) || v > 1e4f) return false;
+    return true;
+}
+
+bool lbmValidateStability() {   // lbm.cpp:2311-2317
+    if (!lbmInitialized) return true;
+    if (!std::isfinite(lbmAvgRho) || lbmAvgRho < 0.8f || lbmAvgRho > 1.2f) return false;
+    if (!std::isfinite(lbmMaxVelocityLB) || lbmMaxVelocityLB > 0.35f) return false;
+    if (!std::isfinite(lbmAvgKineticEnergy) || lbmAvgKineticEnergy > 0.1f) return false;
+    return true;
+}
+
 LbmVec3 lbmControlVolumeForce(float boxHalfX, float boxHalfY, float boxHalfZ) {
     LbmVec3 r;
     double f[3] = {0.0, 0.0, 0.0};

@@ -157,6 +157,18 @@ float getLBMTotalPressureWorld(const LbmVec3& worldPos);
 // AEROS_FIELD_*; out gets n values (3n for the velocity), valid n flags.
 bool lbmFacadeSample(int field, const float* points, long long n, float* out, uint8_t* valid);
 
+// The reference's self-checks (lbm.cpp:2263-2317) over the globals above
+// (initialisation: density in [0.5, 1.5]; conservation: mean density within
+// 10 %; inlet speed in (1e-6, 0.2]; solid cells at rest; pressure within
+// 1.5 dynamic pressures, TKE and vorticity bounded; mean density, maximum
+// velocity and kinetic energy in range).
+bool lbmValidateInitialization();
+bool lbmValidateConservation();
+bool lbmValidateBoundaryConditions();
+bool lbmValidateSolidHandling();
+bool lbmValidateRealisticAero();
+bool lbmValidateStability();
+
 // ---- thermal (aeros/src/thermal_lbm.h:33-72) --------------------------------
 struct ThermalParams {
     bool enabled = false;

@@ -89,6 +89,9 @@ int main(int argc, char** argv) {
         const bool good = lbmEquilibriumMoments(c[0], c[1], c[2], c[3], &m, &px, &py, &pz);
         std::printf("eq %d %.9g %.9g %.9g %.9g\n", (int)good, m, px, py, pz);
     }
+    std::printf("validate %d %d %d %d %d %d\n", (int)lbmValidateInitialization(), (int)lbmValidateConservation(),
+                (int)lbmValidateBoundaryConditions(), (int)lbmValidateSolidHandling(), (int)lbmValidateRealisticAero(),
+                (int)lbmValidateStability());
     if (argc > 2) {
         FILE* fh = std::fopen(argv[2], "wb");
         if (!fh) return 2;

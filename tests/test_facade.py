@@ -111,6 +111,11 @@ def test_facade_channel_equals_c_abi(driver, tmp_path):
     assert np.float32(world[3]) == np.float32(uv[0, 1] * scale)
     assert np.float32(world[9]) == np.float32(np.float32(0.1) / scale)   # lbmLatticeDtWorld
     assert np.float32(world[11]) == np.float32(10.0)   # outside the grid: the freestream
+    # the self-checks: the channel is initialised and stable, conserves mass, its solid rows are at
+    # rest and its fields are bounded; its inlet velocity is zero (a forced channel), which the
+    # inlet check rejects as the reference's does
+    val = r.stdout.split("validate ")[1].splitlines()[0].split()
+    assert val == ["1", "1", "0", "1", "1", "1"], val
     from golden.cases import EQ_MOMENT_CASES
     from post_common import GOLD
     eq = [ln.split()[1:] for ln in r.stdout.splitlines() if ln.startswith("eq ")]
