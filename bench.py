@@ -394,6 +394,39 @@ def sdf_bench(res=256, reps=5, cpu=True):
     return line
 
 
+def rb_bench(steps=50000, ras=(1700.0, 2500.0, 1e4)):
+    """Rayleigh-Benard convection, 128 x 128 x 32 fluid rows (+ 2 wall rows,
+    the reference's y axis up), D3Q19 BGK + D3Q7 thermal with Boussinesq
+    feedback, Pr = 0.71, hot bottom / cold top (T = +-0.5), linear initial
+    profile + seeded U(-1e-3, 1e-3) noise, `steps` steps, FP32 plain and FP16
+    shifted storage for both lattices: MLUPS and the FP64-reduced Nusselt
+    number of each run."""
+    from aeros_gb300 import geometry, solver
+    runs = []
+    for ra in ras:
+        nus = {}
+        for storage in ("fp32", "fp16"):
+            p, mask, tp = geometry.rb_config(ra, storage=storage)
+            s = solver.Solver(p, mask)
+            s.thermal_init(tp)
+            s.thermal_upload(geometry.rb_initial_T(p.nx, p.ny, p.nz, ra))
+            s.step(steps)
+            ms = s.last_step_ms()
+            st = s.stats()
+            cells = p.nx * p.ny * p.nz
+            bpc = (BYTES_PER_CELL[storage] + (56 if storage == "fp32" else 28) + 8)
+            runs.append({"ra": ra, "storage": storage, "steps": steps, "ms_per_step": round(ms / steps, 4),
+                         "mlups": round(cells * steps / (ms * 1e-3) / 1e6, 1),
+                         "achieved_gbs": round(bpc * cells * steps / (ms * 1e-3) / 1e9, 1), "bytes_per_cell": bpc,
+                         "nusselt": round(float(st["nusselt"]), 6), "diverged": int(st["diverged"])})
+            nus[storage] = float(st["nusselt"])
+            s.close()
+        runs[-1]["nusselt_fp16_minus_fp32"] = round(nus["fp16"] - nus["fp32"], 6)
+    peak, _ = measured_peak()
+    return {"metric": "Rayleigh-Benard MLUPS (D3Q19 BGK + D3Q7, 128x34x128) and Nusselt number", "unit": "MLUPS",
+            "peak_gbs": peak, "runs": runs, "data": "synthetic"}
+
+
 def cpu_baseline(mask, steps):
     """The oracle (C restatement of the reference solver, OpenMP) on the same
     grid, `steps` lattice steps (a bounded sample)."""
@@ -463,7 +496,8 @@ def main():
     ap.add_argument("--only", default="both", choices=["both", "fp32", "fp16", "bf16"],
                     help="time one storage form only (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "serve", "sdf"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "serve", "sdf", "rb"])
+    ap.add_argument("--rb-steps", type=int, default=50000)
     ap.add_argument("--sdf-res", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-rate", type=float, default=2.0)
@@ -481,6 +515,8 @@ def main():
     elif args.workload == "serve":
         r = serve_session(args.serve_requests, args.serve_rate, args.serve_max_steps)
         print(json.dumps(r), flush=True)
+    elif args.workload == "rb":
+        print(json.dumps(rb_bench(args.rb_steps)), flush=True)
     elif args.workload == "sdf":
         print(json.dumps(sdf_bench(args.sdf_res, reps=max(1, min(args.steps, 20)), cpu=not args.no_cpu)), flush=True)
     elif args.workload == "batch":
