@@ -30,7 +30,9 @@ STAGED_MIN_BLOCKS = os.environ.get("AEROS_STAGED_MIN_BLOCKS", "3")
 FUSED_MIN_BLOCKS = os.environ.get("AEROS_FUSED_MIN_BLOCKS", "4")
 BATCH_MIN_BLOCKS = os.environ.get("AEROS_BATCH_MIN_BLOCKS", "4")
 FUSED_ODD_MIN_BLOCKS = os.environ.get("AEROS_FUSED_ODD_MIN_BLOCKS", FUSED_MIN_BLOCKS)
-TAG = f"mb{MIN_BLOCKS}s{STAGED_MIN_BLOCKS}f{FUSED_MIN_BLOCKS}o{FUSED_ODD_MIN_BLOCKS}b{BATCH_MIN_BLOCKS}"
+FUSED_TH_MIN_BLOCKS = os.environ.get("AEROS_FUSED_TH_MIN_BLOCKS", "3")
+TAG = (f"mb{MIN_BLOCKS}s{STAGED_MIN_BLOCKS}f{FUSED_MIN_BLOCKS}o{FUSED_ODD_MIN_BLOCKS}t{FUSED_TH_MIN_BLOCKS}"
+       f"b{BATCH_MIN_BLOCKS}")
 UNITS = {
     "lbm_fp32.cu": ["--fmad=false"],
     "lbm_half.cu": ["--fmad=true"],
@@ -68,6 +70,7 @@ def _compile(unit: str, flags: list[str], verbose: bool) -> str:
         cmd = [nvcc(), *ARCH, *COMMON, f"-DAEROS_STEP_MIN_BLOCKS={MIN_BLOCKS}",
                f"-DAEROS_STAGED_MIN_BLOCKS={STAGED_MIN_BLOCKS}", f"-DAEROS_FUSED_MIN_BLOCKS={FUSED_MIN_BLOCKS}",
                f"-DAEROS_BATCH_MIN_BLOCKS={BATCH_MIN_BLOCKS}", f"-DAEROS_FUSED_ODD_MIN_BLOCKS={FUSED_ODD_MIN_BLOCKS}",
+               f"-DAEROS_FUSED_TH_MIN_BLOCKS={FUSED_TH_MIN_BLOCKS}",
                *flags, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

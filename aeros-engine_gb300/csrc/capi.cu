@@ -492,8 +492,8 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     if ((e = cudaStreamSynchronize(nullptr)) != cudaSuccess) return fail(e, "init");
     for (int o = 0; o < 2; ++o)
         for (int t = 0; t < 2; ++t) h->grid[o][t] = std::min(h->max_grid, std::max(1, h->sm_count) * h->L->occupancy(o, t));
-    h->fused_grid = std::max(1, h->sm_count) * h->L->fused_occupancy(false);
-    h->fused_grid_odd = std::max(1, h->sm_count) * h->L->fused_occupancy(true);
+    for (int o = 0; o < 2; ++o)
+        for (int t = 0; t < 2; ++t) h->fused_grid[o][t] = std::max(1, h->sm_count) * h->L->fused_occupancy(o, t);
     h->stats.avg_rho = 1.0f;
     h->stats.fluid_cells = h->fluid_cells;
     *out = h;
@@ -574,10 +574,10 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     A.staged = h->staged;
     {
         const int nsh = A.ntiles - A.ntiles_interior;
-        A.fused = h->fused && !h->th_on && !h->staged;
+        A.fused = h->fused && !h->staged;
         A.shell_blocks = A.fused ? std::min(nsh, std::max(1, h->sm_count) * h->shell_blocks_per_sm) : 0;
-        A.fused_grid = h->fused_grid;
-        A.fused_grid_odd = h->fused_grid_odd;
+        A.fused_grid = h->fused_grid[0][h->th_on ? 1 : 0];
+        A.fused_grid_odd = h->fused_grid[1][h->th_on ? 1 : 0];
         A.split = h->split && nsh > 0 && !h->staged && !A.fused;
         A.shell_grid = A.split ? std::min(nsh, std::max(1, h->sm_count) * 4) : 0;
         A.shell_part_base = 0;   // set by the launcher (after the interior grid's slots)

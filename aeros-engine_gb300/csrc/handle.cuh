@@ -97,8 +97,7 @@ struct aeros_lbm {
     int split = 1;                // shell and interior as two launches per step (AEROS_SPLIT=0: one)
     int fused = 1;                // non-thermal: one launch, dynamic warp items (AEROS_FUSED=0: off)
     int shell_blocks_per_sm = 1;  // fused: shell blocks per SM (AEROS_SHELL_BLOCKS)
-    int fused_grid = 0;           // fused: interior blocks of even steps
-    int fused_grid_odd = 0;       // ... of odd steps
+    int fused_grid[2][2] = {{0, 0}, {0, 0}};   // fused: interior blocks [odd][thermal]
     long long last_kernels = 0;   // kernel launches of the last step call
     aeros_batch* batch = nullptr; // batch this domain is a member of
 };

@@ -139,7 +139,7 @@ struct Launchers {
     cudaError_t (*thermal_fill)(const StepArgs& A, float tref, cudaStream_t s);
     cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s);
     int (*batch_occupancy)();
-    int (*fused_occupancy)(bool odd);
+    int (*fused_occupancy)(bool odd, bool thermal);
 };
 
 const Launchers& launchers_fp32();
@@ -150,8 +150,8 @@ const Launchers& launchers_bf16();
     namespace NAME##_detail {                                                                                         \
     template <bool O, bool T, bool M>                                                                                 \
     cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
-        if (!M && !T && A.fused) {                                                                                    \
-            k_lbm_fused<STORE, O><<<(O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V); \
+        if (!M && A.fused) {                                                                                          \
+            k_lbm_fused<STORE, O, T><<<(O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V); \
         } else if (!M && A.split) {                                                                                   \
             StepArgs B = A;                                                                                           \
             B.shell_part_base = grid;                                                                                 \
@@ -220,10 +220,15 @@ const Launchers& launchers_bf16();
         }                                                                                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    int fused_occ_(bool odd) {                                                                                        \
+    int fused_occ_(bool odd, bool thermal) {                                                                          \
         int n = 0;                                                                                                    \
-        if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true>, STEP_BLOCK, 0);          \
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false>, STEP_BLOCK, 0);             \
+        if (thermal) {                                                                                                \
+            if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true, true>, STEP_BLOCK, 0); \
+            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false, true>, STEP_BLOCK, 0);   \
+        } else {                                                                                                      \
+            if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true, false>, STEP_BLOCK, 0); \
+            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false, false>, STEP_BLOCK, 0);  \
+        }                                                                                                             \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \
     int batch_occ_() {                                                                                                \

@@ -60,6 +60,7 @@ struct Control {
     unsigned int shell_next, warps_done;
     unsigned long long fx_drho, fx_ke, fx_tke;
     unsigned long long fx_cnt[7];   // NaN, negative, bad, rho range, rho finite, u limited, cells
+    unsigned long long fx_nu, fx_tsum, fx_nun;   // thermal: Nusselt row sum, sum of T, Nusselt row cells
     unsigned int fx_maxu2, pad2;
 };
 
@@ -1203,10 +1204,13 @@ __global__ void __launch_bounds__(STEP_BLOCK, STEP_MIN_BLOCKS) k_lbm_interior(co
 struct WarpSums {               // one warp's sums over the slices of a work item
     long long drho, ke, tke;    // fixed point
     long long cnt[7];           // NaN, negative, bad, rho range, rho finite, u limited, cells
+    long long nu, tsum, nun;    // thermal: fixed point, fixed point, count
 };
 
 constexpr float FX_SUM = 1099511627776.0f;   // 2^40: sums of rho - 1 and |u|^2 per slice
 constexpr float FX_TKE = 1048576.0f;         // 2^20: TKE per slice (up to 32 x 1e6)
+constexpr double FX_NU = 4294967296.0;       // 2^32: Nusselt row terms per slice (|term| <= 4)
+constexpr float FX_T = 16777216.0f;          // 2^24: temperatures per slice (|T| <= 1.5)
 
 __device__ __forceinline__ float warp_allsum(float v) {
 #pragma unroll
@@ -1239,8 +1243,17 @@ __device__ __forceinline__ int warp_allsum(int v) {
 #define AEROS_FUSED_ODD_MIN_BLOCKS AEROS_FUSED_MIN_BLOCKS
 #endif
 
-template <class S, bool ODD>
-__global__ void __launch_bounds__(STEP_BLOCK, ODD ? AEROS_FUSED_ODD_MIN_BLOCKS : AEROS_FUSED_MIN_BLOCKS)
+#ifndef AEROS_FUSED_TH_MIN_BLOCKS
+#define AEROS_FUSED_TH_MIN_BLOCKS 3
+#endif
+
+// The single-launch step: the first shell_blocks blocks take the boundary
+// shell's tiles, the others take interior tiles from a counter. THERMAL: the
+// D3Q7 lattice stepped in the same thread (its Nusselt row sum and mean
+// temperature summed like the other statistics, in fixed point).
+template <class S, bool ODD, bool THERMAL>
+__global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCKS
+                                                      : (ODD ? AEROS_FUSED_ODD_MIN_BLOCKS : AEROS_FUSED_MIN_BLOCKS))
     k_lbm_fused(const StepArgs A, const StepVar V) {
     if (A.ctl->halt) return;   // uniform: every thread reads the same flag
     __shared__ WarpSums s_sums[STEP_BLOCK / 32];
@@ -1250,6 +1263,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, ODD ? AEROS_FUSED_ODD_MIN_BLOCKS :
     if (lane == 0) {
         W.drho = W.ke = W.tke = 0;
         for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
+        W.nu = W.tsum = W.nun = 0;
     }
     __syncwarp();
     float mx = 0.0f;
@@ -1272,13 +1286,25 @@ __global__ void __launch_bounds__(STEP_BLOCK, ODD ? AEROS_FUSED_ODD_MIN_BLOCKS :
             if (rare)
                 for (int j = 0; j < 6; ++j) W.cnt[j] += c6[j];
         }
+        if constexpr (THERMAL) {
+            double nu = acc.nu;   // a fixed shuffle tree over the slice's cells
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) nu += __shfl_xor_sync(0xffffffffu, nu, o);
+            const float ts = warp_allsum(acc.tsum);
+            const int nun = (int)__reduce_add_sync(0xffffffffu, (unsigned)acc.nun);
+            if (lane == 0) {
+                W.nu += __double2ll_rn(nu * FX_NU);
+                W.tsum += __float2ll_rn(ts * FX_T);
+                W.nun += nun;
+            }
+        }
     };
     const int nsh = A.ntiles - A.ntiles_interior;
     if ((int)blockIdx.x < A.shell_blocks) {
         for (int st = blockIdx.x; st < nsh; st += A.shell_blocks) {
             Acc acc;
             acc.zero();
-            shell_tile<S, ODD, false, false>(A, V, st, acc);
+            shell_tile<S, ODD, THERMAL, false>(A, V, st, acc);
             add_slice(acc);
         }
     } else {
@@ -1291,7 +1317,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, ODD ? AEROS_FUSED_ODD_MIN_BLOCKS :
             if (it >= A.ntiles_interior) break;
             Acc acc;
             acc.zero();
-            interior_tile<S, ODD, false, false>(A, V, it, acc);
+            interior_tile<S, ODD, THERMAL, false>(A, V, it, acc);
             add_slice(acc);
         }
     }
@@ -1303,6 +1329,9 @@ __global__ void __launch_bounds__(STEP_BLOCK, ODD ? AEROS_FUSED_ODD_MIN_BLOCKS :
     else if (lane == 2) atomicAdd(&ctl->fx_tke, (unsigned long long)W.tke);
     else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ctl->fx_cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
     else if (lane == 10 && mx > 0.0f) atomicMax(&ctl->fx_maxu2, __float_as_uint(mx));
+    else if (THERMAL && lane == 11) atomicAdd(&ctl->fx_nu, (unsigned long long)W.nu);
+    else if (THERMAL && lane == 12) atomicAdd(&ctl->fx_tsum, (unsigned long long)W.tsum);
+    else if (THERMAL && lane == 13) atomicAdd(&ctl->fx_nun, (unsigned long long)W.nun);
     __threadfence();
     __syncwarp();
     int last = 0;
@@ -1311,13 +1340,16 @@ __global__ void __launch_bounds__(STEP_BLOCK, ODD ? AEROS_FUSED_ODD_MIN_BLOCKS :
         __threadfence();
         volatile Control* vc = ctl;
         const double t[5] = {(double)(long long)vc->fx_drho / (double)FX_SUM, (double)(long long)vc->fx_ke / (double)FX_SUM,
-                             (double)(long long)vc->fx_tke / (double)FX_TKE, 0.0, 0.0};
+                             (double)(long long)vc->fx_tke / (double)FX_TKE,
+                             THERMAL ? (double)(long long)vc->fx_nu / FX_NU : 0.0,
+                             THERMAL ? (double)(long long)vc->fx_tsum / (double)FX_T : 0.0};
         const long long c[8] = {(long long)vc->fx_cnt[0], (long long)vc->fx_cnt[1], (long long)vc->fx_cnt[2],
-                                (long long)vc->fx_cnt[3], (long long)vc->fx_cnt[4], (long long)vc->fx_cnt[5], 0,
-                                (long long)vc->fx_cnt[6]};
+                                (long long)vc->fx_cnt[3], (long long)vc->fx_cnt[4], (long long)vc->fx_cnt[5],
+                                THERMAL ? (long long)vc->fx_nun : 0, (long long)vc->fx_cnt[6]};
         const float m = __uint_as_float(vc->fx_maxu2);
         vc->fx_drho = 0; vc->fx_ke = 0; vc->fx_tke = 0;
         for (int j = 0; j < 7; ++j) vc->fx_cnt[j] = 0;
+        vc->fx_nu = 0; vc->fx_tsum = 0; vc->fx_nun = 0;
         vc->fx_maxu2 = 0;
         vc->warps_done = 0;
         apply_totals(A, t, m, c);   // also rewinds tile_next

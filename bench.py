@@ -42,7 +42,7 @@ NCU_TRAFFIC = {"fp16": (232045056 + 150228736 + 218615552 + 189820928) / 2,
                "fp32": (365174272 + 277384704 + 354234112 + 316235264) / 2}
 # bytes of the solver's device control block that every aeros_lbm_step call
 # reads back (struct Control in aeros-engine_gb300/csrc/lbm_step.cuh)
-CONTROL_BYTES = 248
+CONTROL_BYTES = 272
 
 
 def dist_env():
