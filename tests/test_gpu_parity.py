@@ -330,3 +330,29 @@ def test_staged_interior_tiles_match_direct_loads(gpu, monkeypatch, name, storag
     for k in va:
         assert np.array_equal(va[k], vb[k]), k
     assert sa["sum_rho"] == sb["sum_rho"] and sa["step"] == sb["step"]
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("name", ["rb_small", "rb_pm", "thermal_body", "thermal_diffusion"])
+def test_thermal_single_launch_matches_two_launches(gpu, monkeypatch, name, storage):
+    """Thermal domains step in one launch (shell and interior blocks side by
+    side); the two-launch form (AEROS_FUSED=0: shell, then interior) gives the
+    same populations, fields and temperatures bit for bit, and the same
+    statistics up to the order of their sums."""
+    out = []
+    for fused in ("0", "1"):
+        monkeypatch.setenv("AEROS_FUSED", fused)
+        s, _, _ = run_gpu(gpu, name, storage)
+        st = s.stats()
+        out.append((s.populations(), s.fields(), s.thermal(), st, s.last_launch_count()))
+        s.close()
+    (fa, va, ta, sa, la), (fb, vb, tb, sb, lb) = out
+    assert la == 2 * lb > 0   # kernels of the last call: shell + interior per step, then one
+    assert np.array_equal(fa, fb)
+    for k in va:
+        assert np.array_equal(va[k], vb[k]), k
+    assert np.array_equal(ta[0], tb[0]) and np.array_equal(ta[1], tb[1])
+    assert sa["step"] == sb["step"]
+    assert abs(sa["sum_rho"] - sb["sum_rho"]) <= 1e-12 * abs(sa["sum_rho"])
+    assert abs(sa["nusselt"] - sb["nusselt"]) <= 1e-6 * max(1.0, abs(sa["nusselt"]))
+    assert abs(sa["mean_t"] - sb["mean_t"]) <= 1e-6
