@@ -155,6 +155,31 @@ def test_divergence_guard_reequilibrates(gpu, oracle_built):
     assert max_rel(s.fields()["ux"], o.fields()["ux"]) <= FIELD_TOL
 
 
+def test_force_queued_behind_a_diverging_step(gpu, oracle_built):
+    """aeros_lbm_cv_force queued behind a pending step whose divergence guard
+    trips: the force is taken again on the re-equilibrated state, so it equals
+    the force read after the step has been finished on its own."""
+    name = "sphere_bgk_conv"
+    forces = []
+    for queued in (True, False):
+        s, mask, p = run_gpu(gpu, name, chunks=[20])
+        f = s.populations()
+        bad = np.random.default_rng(7).random(f.shape[1]) < 0.2
+        f[:, bad] = np.nan
+        s.write_populations(f)
+        if queued:
+            s.step_async(5)
+            forces.append(s.cv_force(0.3, 0.3, 0.3))   # one wait: the steps, the guard, the force
+        else:
+            s.step(5)
+            s.stats()
+            forces.append(s.cv_force(0.3, 0.3, 0.3))
+        assert s.stats()["diverged"] == 1
+        s.close()
+    assert np.array_equal(forces[0], forces[1])
+    assert np.all(np.isfinite(forces[0]))
+
+
 def test_run_twice_bitwise_deterministic(gpu):
     a, _, _ = run_gpu(gpu, "sphere_trt_les_conv")
     b, _, _ = run_gpu(gpu, "sphere_trt_les_conv")
