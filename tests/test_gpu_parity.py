@@ -381,3 +381,42 @@ def test_thermal_single_launch_matches_two_launches(gpu, monkeypatch, name, stor
     assert abs(sa["sum_rho"] - sb["sum_rho"]) <= 1e-12 * abs(sa["sum_rho"])
     assert abs(sa["nusselt"] - sb["nusselt"]) <= 1e-6 * max(1.0, abs(sa["nusselt"]))
     assert abs(sa["mean_t"] - sb["mean_t"]) <= 1e-6
+
+
+FREESLIP_CASES = {   # name: (golden case whose mask and flow it reuses, LES, TRT, lateral, outlet)
+    "sphere_freeslip_zerograd_trt_les": ("sphere_trt_les_conv", True, True, "freeslip", "zerograd"),
+    "sphere_freeslip_zerograd_bgk": ("sphere_bgk_conv", False, False, "freeslip", "zerograd"),
+    "sphere_copy_zerograd_les": ("sphere_les_ground_copy", True, False, "copy", "zerograd"),
+    "sphere_freeslip_reference_outlet": ("sphere_trt_les_conv", True, True, "freeslip", "reference"),
+    "sphere_plus_y_freeslip_zerograd": ("sphere_plus_y", True, True, "freeslip", "zerograd"),
+    "sphere_minus_z_freeslip_zerograd": ("sphere_minus_z_perx", True, False, "freeslip", "zerograd"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FREESLIP_CASES))
+def test_freeslip_and_zero_gradient_equal_restatement(gpu, oracle_built, name):
+    """Boundary modes the reference does not have (free-slip lateral walls,
+    zero-gradient outlet: the headline sphere's) against their C restatement:
+    FP32 populations and fields bit for bit."""
+    from aeros_gb300 import capi
+    base, les, trt, lateral, outlet = FREESLIP_CASES[name]
+    case = CASES[base]
+    g = GOLD["cases"][base]
+    mask = solver_mask(case)
+    p = params_for(case, g["u_in"])
+    p.use_les, p.use_trt = int(les), int(trt)
+    p.lateral_bc = capi.AEROS_LATERAL_FREESLIP if lateral == "freeslip" else capi.AEROS_LATERAL_COPY
+    p.outlet_bc = capi.AEROS_OUTLET_ZEROGRAD if outlet == "zerograd" else capi.AEROS_OUTLET_REFERENCE
+    p.convective_outlet = 0 if outlet == "zerograd" else p.convective_outlet
+    s = gpu.Solver(p, mask)
+    o = oracle_built.OracleLBM(p, mask)
+    for n in (case["steps"] // 2, case["steps"] - case["steps"] // 2):
+        s.step(n)
+        o.step(n)
+    fl = mask.reshape(-1) == 0
+    assert np.array_equal(s.populations()[:, fl], o.populations()[:, fl])
+    a, b = s.fields(), o.fields()
+    for k in ("rho", "ux", "uy", "uz", "strain", "tke"):
+        assert np.array_equal(a[k], b[k]), k
+    assert s.stats()["step"] == o.stats()["step"]
+    assert np.array_equal(s.cv_force(0.3, 0.3, 0.3).astype(np.float32), o.cv_force(0.3, 0.3, 0.3).astype(np.float32))
