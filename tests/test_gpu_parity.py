@@ -446,3 +446,67 @@ def test_full_size_sphere_keeps_its_mirror_symmetry(gpu, storage, tol):
     assert np.abs(uy + uy[:, ::-1, :]).max() <= tol * umax
     assert np.abs(uz + uz[::-1, :, :]).max() <= tol * umax
     assert s.stats()["diverged"] == 0
+
+
+def test_voxelizer_half_million_triangles_no_holes_no_extras(gpu):
+    """voxel_headless.cpp's large-mesh checks on a 512,000-triangle mesh (four
+    disjoint icospheres, levels 7, 6, 6, 5) at 128^3: built and voxelized in
+    under 5 s; no cell whose centre lies inside a sphere by more than the
+    polyhedron's inscribed gap is fluid, no cell outside by more than that is
+    solid; the solid volume is within 2 % of the spheres' volume."""
+    import time
+
+    from aeros_gb300 import geometry
+    from aeros_gb300.solver import voxel_grid, voxelize
+    spheres = [(7, 0.30, (-0.40, 0.0, 0.0)), (6, 0.20, (0.35, 0.25, 0.0)), (6, 0.20, (0.35, -0.25, 0.0)),
+               (5, 0.10, (0.0, 0.45, 0.35))]
+    tris = np.concatenate([geometry.icosphere(lv, r, c) for lv, r, c in spheres])
+    assert tris.shape[0] == 512000
+    n = 128
+    g = voxel_grid((n, n, n), (-0.8, -0.8, -0.8), (1.6 / n,) * 3)
+    t = time.perf_counter()
+    m = voxelize(tris, g).reshape(n, n, n)
+    assert time.perf_counter() - t < 5.0
+    c = (np.arange(n, dtype=np.float64) + 0.5) * (1.6 / n) - 0.8
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    inside = np.zeros(m.shape, bool)
+    outside = np.ones(m.shape, bool)
+    for lv, r, (cx, cy, cz) in spheres:
+        d = np.sqrt((x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2)
+        gap = r * (1.0 - np.cos(1.2 / 2 ** lv)) + 1e-6   # faces lie within this of the sphere
+        inside |= d < r - gap
+        outside &= d > r + 1e-6
+    assert not np.any(inside & (m == 0)), "holes"
+    assert not np.any(outside & (m != 0)), "extras"
+    vol = sum(4.0 / 3.0 * np.pi * r ** 3 for _, r, _ in spheres)
+    assert abs(m.sum() * (1.6 / n) ** 3 - vol) <= 0.02 * vol
+
+
+def test_mass_conserved_in_a_closed_periodic_domain(gpu, oracle_built):
+    """lbm_physics_headless.cpp's conservation check: a periodic channel with
+    a body and walls conserves its mass. Without a force the sum of rho over
+    the fluid moves by rounding only (< 1e-6 of it in 2000 steps). With the
+    Guo force the reference's FP32 arithmetic drifts by about 4e-5 (its FP64
+    run by 1.6e-13): the GPU's FP32 sum equals the FP32 restatement's to the
+    last bit, and FP16 storage stays within 1e-4."""
+    from aeros_gb300 import capi, geometry
+    nx, ny, nz = 64, 34, 24
+    mask = geometry.channel_mask(nx, ny, nz).reshape(nz, ny, nx).copy()
+    mask[8:16, 12:22, 20:30] = 1
+    for force in (0.0, 2e-6):
+        for storage in ("fp32", "fp16"):
+            p = capi.make_params(nx, ny, nz, tau=0.7, les=True, trt=True, periodic_x=True, periodic_z=True,
+                                 u_in=(0.0, 0.0, 0.0), body_force=(force, 0.0, 0.0), storage=storage)
+            s = gpu.Solver(p, mask)
+            s.step(1)
+            m0 = s.stats()["sum_rho"]
+            s.step(2000)
+            st = s.stats()
+            assert st["diverged"] == 0
+            drift = abs(st["sum_rho"] - m0) / m0
+            assert drift <= (1e-6 if force == 0.0 else 1e-4), (force, storage, drift)
+            if storage == "fp32" and force > 0.0:
+                o = oracle_built.OracleLBM(p, mask)
+                o.step(2001)
+                assert st["sum_rho"] == o.stats()["sum_rho"]
+            s.close()
