@@ -309,14 +309,12 @@ __global__ void k_sdf_sample(const SdfView g, const float* __restrict__ pts, lon
     }
 }
 
+// grid for a grid-stride kernel over `work` items on the current device
 int grid_blocks(long long work) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
     return (int)std::max<long long>(1, std::min<long long>((work + PB - 1) / PB, (long long)sms * 8));
 }
 
