@@ -735,8 +735,8 @@ __device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int
 // ---- interior cell (1 <= x,y,z <= N-2): flat neighbour offsets ---------------
 template <class S, bool ODD, bool THERMAL, bool MAT>
 __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
-                                                 Acc& acc) {
-    const uint32_t d = A.desc[cell];
+                                                 Acc& acc, const uint32_t* dpre = nullptr) {
+    const uint32_t d = dpre ? *dpre : A.desc[cell];
     constexpr bool SH = S::shifted;
     float f[Q19];
     float strainPre = 0.0f;
@@ -1131,15 +1131,17 @@ __device__ __forceinline__ void shell_cell(const StepArgs& A, const StepVar& V, 
 }
 
 // Interior cell li: the interior (x, y, z in 1 .. n-2) in x-fastest order.
+// dpre: its descriptor, already loaded (NULL: load it here).
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __forceinline__ void interior_cell(const StepArgs& A, const StepVar& V, int li, Acc& acc) {
+__device__ __forceinline__ void interior_cell(const StepArgs& A, const StepVar& V, int li, Acc& acc,
+                                              const uint32_t* dpre = nullptr) {
     if (li < A.n_interior) {
         const uint32_t r = A.div_ix.div((uint32_t)li);
         const int x = li - (int)r * (A.nx - 2) + 1;
         const uint32_t zq = A.div_iy.div(r);
         const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
         const int z = (int)zq + 1;
-        process_interior<S, ODD, THERMAL, MAT>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc);
+        process_interior<S, ODD, THERMAL, MAT>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc, dpre);
     }
 }
 
@@ -1243,6 +1245,15 @@ __device__ __forceinline__ int warp_allsum(int v) {
 #define AEROS_FUSED_ODD_MIN_BLOCKS AEROS_FUSED_MIN_BLOCKS
 #endif
 
+// Linear cell index of interior cell li (x-fastest over x, y, z in 1 .. n-2).
+__device__ __forceinline__ int interior_cell_index(const StepArgs& A, int li) {
+    const uint32_t r = A.div_ix.div((uint32_t)li);
+    const int x = li - (int)r * (A.nx - 2) + 1;
+    const uint32_t zq = A.div_iy.div(r);
+    const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
+    return (((int)zq + 1) * A.ny + y) * A.nx + x;
+}
+
 #ifndef AEROS_FUSED_TH_MIN_BLOCKS
 #define AEROS_FUSED_TH_MIN_BLOCKS 3
 #endif
@@ -1306,6 +1317,35 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             acc.zero();
             shell_tile<S, ODD, THERMAL, false>(A, V, st, acc);
             add_slice(acc);
+        }
+    } else if (ODD) {
+        // Odd steps read the descriptor before the gathers; the next tile's
+        // index is taken a tile ahead so that each thread's next descriptor
+        // is in flight while the current cell is processed.
+        if (threadIdx.x == 0) s_tile[0] = (int)atomicAdd(&ctl->tile_next, 1u);
+        __syncthreads();
+        int par = 0;
+        int it = s_tile[0];
+        uint32_t dnext = D_WALL;
+        if (it < A.ntiles_interior) {
+            const int li = it * STEP_BLOCK + (int)threadIdx.x;
+            if (li < A.n_interior) dnext = __ldg(A.desc + interior_cell_index(A, li));
+        }
+        while (it < A.ntiles_interior) {
+            if (threadIdx.x == 0) s_tile[par ^ 1] = (int)atomicAdd(&ctl->tile_next, 1u);
+            __syncthreads();
+            const int itn = s_tile[par ^ 1];
+            par ^= 1;
+            const uint32_t dcur = dnext;
+            if (itn < A.ntiles_interior) {
+                const int li = itn * STEP_BLOCK + (int)threadIdx.x;
+                if (li < A.n_interior) dnext = __ldg(A.desc + interior_cell_index(A, li));
+            }
+            Acc acc;
+            acc.zero();
+            interior_cell<S, ODD, THERMAL, false>(A, V, it * STEP_BLOCK + (int)threadIdx.x, acc, &dcur);
+            add_slice(acc);
+            it = itn;
         }
     } else {
         int par = 0;
