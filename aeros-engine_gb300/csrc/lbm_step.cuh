@@ -1327,9 +1327,13 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
         int par = 0;
         int it = s_tile[0];
         uint32_t dnext = D_WALL;
+        int cnext = 0;
         if (it < A.ntiles_interior) {
             const int li = it * STEP_BLOCK + (int)threadIdx.x;
-            if (li < A.n_interior) dnext = __ldg(A.desc + interior_cell_index(A, li));
+            if (li < A.n_interior) {
+                cnext = interior_cell_index(A, li);
+                dnext = __ldg(A.desc + cnext);
+            }
         }
         while (it < A.ntiles_interior) {
             if (threadIdx.x == 0) s_tile[par ^ 1] = (int)atomicAdd(&ctl->tile_next, 1u);
@@ -1337,13 +1341,25 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             const int itn = s_tile[par ^ 1];
             par ^= 1;
             const uint32_t dcur = dnext;
+            const int ccur = cnext;
             if (itn < A.ntiles_interior) {
                 const int li = itn * STEP_BLOCK + (int)threadIdx.x;
-                if (li < A.n_interior) dnext = __ldg(A.desc + interior_cell_index(A, li));
+                if (li < A.n_interior) {
+                    cnext = interior_cell_index(A, li);
+                    dnext = __ldg(A.desc + cnext);
+                }
             }
             Acc acc;
             acc.zero();
-            interior_cell<S, ODD, THERMAL, false>(A, V, it * STEP_BLOCK + (int)threadIdx.x, acc, &dcur);
+            if (it * STEP_BLOCK + (int)threadIdx.x < A.n_interior) {
+                // x, y, z from the cell index: only the outlet planes and the
+                // thermal sub-step use them
+                const uint32_t r = A.div_x.div((uint32_t)ccur);
+                const int x = ccur - (int)r * A.nx;
+                const uint32_t z = A.div_y.div(r);
+                const int y = (int)(r - z * (uint32_t)A.ny);
+                process_interior<S, ODD, THERMAL, false>(A, V, ccur, x, y, (int)z, acc, &dcur);
+            }
             add_slice(acc);
             it = itn;
         }
