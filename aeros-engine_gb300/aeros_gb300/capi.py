@@ -161,6 +161,58 @@ class StlInfo(C.Structure):
 
 AEROS_STL_UNKNOWN, AEROS_STL_BINARY, AEROS_STL_ASCII = 0, 1, 2
 
+
+class SurfaceParams(C.Structure):
+    _fields_ = [("velocity", C.c_float * 3), ("air_temperature", C.c_float), ("air_density", C.c_float),
+                ("use_real_density", C.c_int32), ("speed_of_sound", C.c_float), ("mach_effects", C.c_int32),
+                ("auto_ref_area", C.c_int32), ("ref_area", C.c_float), ("flow_azimuth_deg", C.c_float),
+                ("flow_elevation_deg", C.c_float), ("bb_min", C.c_float * 3), ("bb_max", C.c_float * 3),
+                ("center", C.c_float * 3), ("max_dim", C.c_float), ("reynolds", C.c_float),
+                ("ground_effect", C.c_int32), ("ground_height", C.c_float), ("vox_min_y", C.c_float),
+                ("reserved", C.c_int32 * 4)]
+
+
+AEROS_SURFACE_NOT_RUN, AEROS_SURFACE_NO_FLOW, AEROS_SURFACE_DONE = 0, 1, 2
+SURFACE_SUM_NAMES = ("force_x", "force_y", "force_z", "cp_x", "cp_y", "cp_z", "moment_x", "moment_y", "moment_z",
+                     "area", "pressure_weight", "frontal", "base_area", "base_force", "projected")
+
+
+class SurfaceForces(C.Structure):
+    _fields_ = [("status", C.c_int32), ("reserved0", C.c_int32), ("drag", C.c_float), ("lift", C.c_float),
+                ("lift_to_drag", C.c_float), ("moment_magnitude", C.c_float), ("drag_vector", C.c_float * 3),
+                ("lift_vector", C.c_float * 3), ("moment", C.c_float * 3), ("center_of_pressure", C.c_float * 3),
+                ("ref_area", C.c_float), ("ref_area_used", C.c_float), ("cp_non_finite", C.c_int64),
+                ("sums", C.c_double * 15)]
+
+    def as_dict(self) -> dict:
+        d = {}
+        for k, _ in self._fields_:
+            if k == "reserved0":
+                continue
+            v = getattr(self, k)
+            d[k] = list(v) if not isinstance(v, (int, float)) else v
+        return d
+
+
+def make_surface(*, velocity, air_temperature=288.15, air_density=1.225, use_real_density=True,
+                 speed_of_sound=340.29, mach_effects=False, auto_ref_area=True, ref_area=1.0, azimuth=0.0,
+                 elevation=0.0, bb_min, bb_max, center=None, max_dim=None, reynolds=1e5, ground_effect=False,
+                 ground_height=0.0, vox_min_y=0.0) -> SurfaceParams:
+    sp = SurfaceParams()
+    for i in range(3):
+        sp.velocity[i] = float(velocity[i])
+        sp.bb_min[i], sp.bb_max[i] = float(bb_min[i]), float(bb_max[i])
+        sp.center[i] = float(center[i]) if center is not None else 0.5 * (float(bb_min[i]) + float(bb_max[i]))
+    sp.air_temperature, sp.air_density = float(air_temperature), float(air_density)
+    sp.use_real_density, sp.speed_of_sound = int(bool(use_real_density)), float(speed_of_sound)
+    sp.mach_effects, sp.auto_ref_area, sp.ref_area = int(bool(mach_effects)), int(bool(auto_ref_area)), float(ref_area)
+    sp.flow_azimuth_deg, sp.flow_elevation_deg = float(azimuth), float(elevation)
+    if max_dim is None:
+        max_dim = sum((float(bb_max[i]) - float(bb_min[i])) ** 2 for i in range(3)) ** 0.5
+    sp.max_dim, sp.reynolds = float(max_dim), float(reynolds)
+    sp.ground_effect, sp.ground_height, sp.vox_min_y = int(bool(ground_effect)), float(ground_height), float(vox_min_y)
+    return sp
+
 _SIGS = {
     "aeros_consume_error": (C.c_int, [C.c_char_p, C.c_int]),
     "aeros_lbm_create": (C.c_int, [C.POINTER(LbmParams), _U8P, C.POINTER(_P)]),
@@ -200,6 +252,10 @@ _SIGS = {
     "aeros_stl_detect": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(StlInfo)]),
     "aeros_stl_parse": (C.c_int, [C.c_char_p, C.c_uint64, C.c_uint64, _FP, _FP, C.c_int64, C.POINTER(StlInfo)]),
     "aeros_stl_read_file": (C.c_int, [C.c_char_p, C.c_uint64, _FP, _FP, C.c_int64, C.POINTER(StlInfo)]),
+    "aeros_surface_mesh_create": (C.c_int, [_FP, _FP, C.c_int64, C.POINTER(_P)]),
+    "aeros_surface_mesh_destroy": (C.c_int, [_P]),
+    "aeros_lbm_surface_forces": (C.c_int, [_P, C.POINTER(WorldParams), C.POINTER(SurfaceParams), _P, _P,
+                                           C.POINTER(VoxelGrid), C.POINTER(SurfaceForces), _FP]),
     "aeros_batch_create": (C.c_int, [C.c_int, C.POINTER(_P)]),
     "aeros_batch_destroy": (C.c_int, [_P]),
     "aeros_batch_add": (C.c_int, [_P, _P]),

@@ -182,6 +182,45 @@ class Solver:
         check(lib().aeros_lbm_projected_area(self.h, int(axis), C.byref(v)), "projected_area")
         return float(v.value)
 
+    def surface_forces(self, world: capi.WorldParams, sp: capi.SurfaceParams, mesh: "SurfaceMesh",
+                       d_sdf: int = 0, sdf_grid: VoxelGrid | None = None, want_cp: bool = True):
+        """computeLiftDrag (aeros/src/forces.cpp:401-688) on the pressure of
+        the last world_fields call: (SurfaceForces, per-triangle Cp or None).
+        d_sdf: device address of the voxel grid's distance field (0: none)."""
+        out = capi.SurfaceForces()
+        cp = np.empty(max(mesh.ntri, 1), np.float32) if want_cp else None
+        check(lib().aeros_lbm_surface_forces(self.h, C.byref(world), C.byref(sp), mesh.h, C.c_void_p(d_sdf or None),
+                                             C.byref(sdf_grid) if sdf_grid is not None else None, C.byref(out),
+                                             _f(cp) if cp is not None else None), "surface_forces")
+        return out, (cp[:mesh.ntri] if cp is not None else None)
+
+
+class SurfaceMesh:
+    """A triangle soup resident on the device for the surface-force pass:
+    vertices and per-vertex normals, 9 floats per triangle each (the
+    reference's g_vertices / g_normals)."""
+
+    def __init__(self, vertices: np.ndarray, normals: np.ndarray):
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1)
+        n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1)
+        if v.size % 9 or n.size != v.size:
+            raise ValueError("vertices and normals need 9 floats per triangle each")
+        self.ntri = v.size // 9
+        h = C.c_void_p()
+        check(lib().aeros_surface_mesh_create(_f(v), _f(n), self.ntri, C.byref(h)), "surface_mesh_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().aeros_surface_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 def equilibrium_moments(states) -> tuple[np.ndarray, np.ndarray]:
     """lbmEquilibriumMoments (aeros/src/lbm.cpp:249-267) on the device for

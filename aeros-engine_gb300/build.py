@@ -9,6 +9,7 @@ Translation units and their floating-point contraction:
   batch.cu     --fmad=false  host side of the many-domain batch
   post.cu      --fmad=false  world fields, vorticity / Q, samplers as the reference rounds them
   sdf.cu       --fmad=false  distance field: weights, smoothing and samplers as the reference
+  surface.cu   --fmad=false  surface-pressure lift and drag: per-triangle terms as the reference
   stl.cpp      host only     STL detection and parse (-ffp-contract=off like all host code)
 """
 from __future__ import annotations
@@ -42,6 +43,7 @@ UNITS = {
     "batch.cu": ["--fmad=false"],
     "post.cu": ["--fmad=false"],
     "sdf.cu": ["--fmad=false"],
+    "surface.cu": ["--fmad=false"],
     "stl.cpp": [],
     "setup.cu": [],
 }

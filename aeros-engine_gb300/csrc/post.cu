@@ -12,6 +12,7 @@
 
 #include "../../include/aeros_lbm.h"
 #include "handle.cuh"
+#include "samplers.cuh"
 
 using namespace aeros;
 
@@ -236,32 +237,9 @@ __global__ void k_sample(const SampleArgs a, const float* pts, long long n, floa
             out[i] = r;
         } else {
             // sampleFieldTrilinear(field, pos, skipSolid = true), lbm.cpp:1881-1933
+            const smp::FieldView v{a.nx, a.ny, a.nz, {a.minx, a.miny, a.minz}, {a.csx, a.csy, a.csz}, a.desc};
             float r = 0.0f;
-            if (isfinite(wx) && isfinite(wy) && isfinite(wz) && !(a.csx < 1e-9f || a.csy < 1e-9f || a.csz < 1e-9f) &&
-                !(a.nx < 2 || a.ny < 2 || a.nz < 2)) {
-                const float fx = (wx - a.minx) / a.csx, fy = (wy - a.miny) / a.csy, fz = (wz - a.minz) / a.csz;
-                const int ix = (int)floorf(fx), iy = (int)floorf(fy), iz = (int)floorf(fz);
-                if (!(ix < 0 || iy < 0 || iz < 0) && !(ix > a.nx - 2 || iy > a.ny - 2 || iz > a.nz - 2)) {
-                    const float tx = clamp01(fx - (float)ix), ty = clamp01(fy - (float)iy), tz = clamp01(fz - (float)iz);
-                    const float wxs[2] = {1.0f - tx, tx}, wys[2] = {1.0f - ty, ty}, wzs[2] = {1.0f - tz, tz};
-                    float acc = 0.0f, wsum = 0.0f;
-                    for (int dz = 0; dz <= 1; ++dz)
-                        for (int dy = 0; dy <= 1; ++dy)
-                            for (int dx = 0; dx <= 1; ++dx) {
-                                const int cell = ((iz + dz) * a.ny + (iy + dy)) * a.nx + (ix + dx);
-                                if (a.desc[cell] & D_WALL) continue;
-                                const float v = a.field[cell];
-                                if (!isfinite(v)) continue;
-                                const float w = wxs[dx] * wys[dy] * wzs[dz];
-                                acc += v * w;
-                                wsum += w;
-                            }
-                    if (!(wsum < 1e-6f)) {
-                        acc /= wsum;
-                        if (isfinite(acc)) { r = acc; ok = 1; }
-                    }
-                }
-            }
+            ok = smp::field_trilinear(v, a.field, wx, wy, wz, &r) ? 1 : 0;
             out[i] = r;
         }
         if (valid) valid[i] = ok;

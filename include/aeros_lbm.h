@@ -382,6 +382,78 @@ enum {
 int aeros_lbm_sample(aeros_lbm* h, const aeros_world_params* wp, int field, const float* points, int64_t n,
                      float* out, uint8_t* valid);
 
+/* ---- surface-pressure lift and drag ------------------------------------------------
+ * Replaces computeLiftDrag (aeros/src/forces.cpp:401-688) with the LBM branch
+ * of its per-triangle pass (the analytic-flow branch is not on the solver
+ * path): the pressure of the last aeros_lbm_world_fields call is sampled per
+ * triangle 0.6 LBM cells out along the triangle's normal (wallSamplePoint,
+ * forces.cpp:75-90), Cp with the Karman-Tsien correction, pressure force,
+ * Blasius / Schlichting skin friction, moment about the quarter chord and the
+ * pressure-weighted centre; then base, induced and wave drag, ground effect
+ * and the frontal reference area as the reference. The per-triangle pass runs
+ * on the device (sums in FP64, a fixed reduction order); the scalar set-up and
+ * the closing formulas run on the host in FP32 as the reference's. */
+typedef struct aeros_surface_mesh aeros_surface_mesh;
+/* Uploads a triangle soup: vertices 9 floats per triangle (g_vertices) and
+ * per-vertex normals 9 floats per triangle (g_normals; the pass reads the
+ * first vertex's normal of each triangle, as the reference). ntri may be 0
+ * (no model: the pass returns AEROS_SURFACE_NOT_RUN). */
+int aeros_surface_mesh_create(const float* vertices, const float* normals, int64_t ntri,
+                              aeros_surface_mesh** out);
+int aeros_surface_mesh_destroy(aeros_surface_mesh* mesh);
+
+typedef struct aeros_surface_params {
+    float velocity[3];          /* flowParams.vx, vy, vz (m/s)                              */
+    float air_temperature;      /* flowParams.airTemperature (K), Sutherland viscosity       */
+    float air_density;          /* flowParams.airDensity (kg/m^3)                            */
+    int32_t use_real_density;   /* useRealDensity: else 1.225                                */
+    float speed_of_sound;       /* speedOfSound (m/s)                                        */
+    int32_t mach_effects;       /* aeroMachEffects: Karman-Tsien for 0.3 < M < 0.85, wave drag */
+    int32_t auto_ref_area;      /* aeroAutoRefArea: projected area from the flow angles       */
+    float ref_area;             /* aeroRefArea when auto_ref_area is 0                        */
+    float flow_azimuth_deg;     /* flowAzimuth (computeLBMRefArea's direction, lbm.cpp:2111)  */
+    float flow_elevation_deg;   /* flowElevation                                              */
+    float bb_min[3], bb_max[3]; /* minBB, maxBB: model bounds (span and chord estimates)      */
+    float center[3];            /* center: model centre                                       */
+    float max_dim;              /* maxDim                                                     */
+    float reynolds;             /* aeroReNumber (open-base correction above 1e6)              */
+    int32_t ground_effect;      /* aeroGroundEffect                                           */
+    float ground_height;        /* aeroGroundHeight, above vox_min_y                          */
+    float vox_min_y;            /* g_voxMinY                                                  */
+    int32_t reserved[4];
+} aeros_surface_params;
+
+enum {
+    AEROS_SURFACE_NOT_RUN = 0,   /* the reference returns before writing (no usable mesh)  */
+    AEROS_SURFACE_NO_FLOW = 1,   /* flow direction undefined: lift, drag and L/D are 0     */
+    AEROS_SURFACE_DONE = 2
+};
+
+typedef struct aeros_surface_forces {
+    int32_t status;             /* AEROS_SURFACE_*                                          */
+    int32_t reserved0;
+    float drag, lift;           /* dragMagnitude, liftMagnitude (N)                         */
+    float lift_to_drag;         /* liftToDragRatio                                          */
+    float moment_magnitude;     /* momentMagnitude (N m)                                    */
+    float drag_vector[3], lift_vector[3], moment[3];
+    float center_of_pressure[3];
+    float ref_area;             /* aeroRefArea after the call                               */
+    float ref_area_used;        /* the area the coefficients used                           */
+    int64_t cp_non_finite;      /* aeroCpNonFinite                                          */
+    /* per-triangle sums of the pass (FP64): force xyz, pressure-weighted centre
+     * xyz, moment xyz, area, pressure weight, frontal, base area, base force,
+     * projected area of computeLBMRefArea */
+    double sums[15];
+} aeros_surface_forces;
+
+/* cp: optional host array, one value per triangle (the Cp the pass used;
+ * 0 for skipped triangles). d_sdf / sdf_grid: the voxel grid's distance
+ * field on the device (both NULL: no field, the sample point is never held
+ * back). */
+int aeros_lbm_surface_forces(aeros_lbm* h, const aeros_world_params* wp, const aeros_surface_params* sp,
+                             const aeros_surface_mesh* mesh, const float* d_sdf, const aeros_voxel_grid* sdf_grid,
+                             aeros_surface_forces* out, float* cp);
+
 /* ---- timing helper for benches ------------------------------------------------ */
 /* Milliseconds of the step kernels enqueued by the last aeros_lbm_step*/
 /* call, measured with CUDA events on the handle's stream. */

@@ -82,6 +82,19 @@ int     ao_sdf_exact(const uint8_t* mask, int nx, int ny, int nz, const float cs
 int     ao_sdf_sample(const float* sdf, int nx, int ny, int nz, const float mn[3], const float cs[3],
                       const float* pts, int64_t n, float* dist, float* normal);
 
+/* surface_oracle.c: computeLiftDrag (forces.cpp:401-688) on the state's world
+ * pressure (ao_lbm_world_fields first); f32_sums: FP32 sums in triangle order
+ * (the reference on one thread), else FP64 sums (the device's form). */
+int     ao_surface_forces(const ao_lbm* s, const aeros_world_params* wp, const aeros_surface_params* sp,
+                          const float* sdf, const aeros_voxel_grid* sdf_grid, const float* vert, const float* nrm,
+                          int64_t ntri, int f32_sums, aeros_surface_forces* out, float* cp_out);
+/* The same over a world pressure array and its wall cells (1 = solid or
+ * ground: the sampler skips them), nx*ny*nz each. */
+int     ao_surface_forces_field(const float* pressure, const uint8_t* wall, int nx, int ny, int nz,
+                                const aeros_world_params* wp, const aeros_surface_params* sp, const float* sdf,
+                                const aeros_voxel_grid* sdf_grid, const float* vert, const float* nrm, int64_t ntri,
+                                int f32_sums, aeros_surface_forces* out, float* cp_out);
+
 #ifdef __cplusplus
 }
 #endif

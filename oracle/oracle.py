@@ -18,8 +18,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "aeros-engine_gb300"))
-from aeros_gb300.capi import (AEROS_FIELD_VELOCITY_LB, LbmParams, LbmStats, ThermalParams, VoxelGrid,  # noqa: E402
-                              VoxelPlan, WorldParams, WorldStats)
+from aeros_gb300.capi import (AEROS_FIELD_VELOCITY_LB, LbmParams, LbmStats, SurfaceForces,  # noqa: E402
+                              SurfaceParams, ThermalParams, VoxelGrid, VoxelPlan, WorldParams, WorldStats)
 
 _FP = C.POINTER(C.c_float)
 _U8P = C.POINTER(C.c_uint8)
@@ -82,6 +82,12 @@ def oracle_lib(precision: str = "f32") -> C.CDLL:
                                           C.POINTER(WorldStats)]
         L.ao_lbm_vorticity_q.argtypes = [C.c_void_p, C.POINTER(WorldParams), _FP, _FP, _FP]
         L.ao_lbm_sample.argtypes = [C.c_void_p, C.POINTER(WorldParams), C.c_int, _FP, C.c_int64, _FP, _U8P]
+        L.ao_surface_forces.argtypes = [C.c_void_p, C.POINTER(WorldParams), C.POINTER(SurfaceParams), _FP,
+                                        C.POINTER(VoxelGrid), _FP, _FP, C.c_int64, C.c_int, C.POINTER(SurfaceForces),
+                                        _FP]
+        L.ao_surface_forces_field.argtypes = [_FP, _U8P, C.c_int, C.c_int, C.c_int, C.POINTER(WorldParams),
+                                              C.POINTER(SurfaceParams), _FP, C.POINTER(VoxelGrid), _FP, _FP,
+                                              C.c_int64, C.c_int, C.POINTER(SurfaceForces), _FP]
         _libs[precision] = L
     return _libs[precision]
 
@@ -201,6 +207,43 @@ class OracleLBM:
         return (out.reshape(n, 3) if per == 3 else out), valid
 
 
+    def surface_forces(self, world: WorldParams, sp: SurfaceParams, verts: np.ndarray, normals: np.ndarray,
+                       sdf_field: np.ndarray | None = None, sdf_grid: VoxelGrid | None = None, f32_sums: bool = False):
+        """computeLiftDrag restated on this state's world pressure (call
+        world_fields first). Returns (SurfaceForces, per-triangle Cp)."""
+        v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1)
+        nn = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1)
+        ntri = v.size // 9
+        out = SurfaceForces()
+        cp = np.empty(max(ntri, 1), np.float32)
+        f = None if sdf_field is None else np.ascontiguousarray(sdf_field, dtype=np.float32)
+        self.L.ao_surface_forces(self.h, C.byref(world), C.byref(sp), fptr(f) if f is not None else None,
+                                 C.byref(sdf_grid) if sdf_grid is not None else None, fptr(v), fptr(nn), ntri,
+                                 int(bool(f32_sums)), C.byref(out), fptr(cp))
+        return out, cp[:ntri]
+
+
+def surface_forces_field(pressure: np.ndarray, wall: np.ndarray, dims, world: WorldParams, sp: SurfaceParams,
+                         verts: np.ndarray, normals: np.ndarray, sdf_field: np.ndarray | None = None,
+                         sdf_grid: VoxelGrid | None = None, f32_sums: bool = False):
+    """computeLiftDrag restated over a world pressure array and its wall
+    cells (1 = solid or ground). Returns (SurfaceForces, per-triangle Cp)."""
+    L = oracle_lib("f32")
+    nx, ny, nz = dims
+    p = np.ascontiguousarray(pressure, dtype=np.float32).reshape(-1)
+    w = np.ascontiguousarray(wall, dtype=np.uint8).reshape(-1)
+    v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1)
+    nn = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1)
+    ntri = v.size // 9
+    out = SurfaceForces()
+    cp = np.empty(max(ntri, 1), np.float32)
+    f = None if sdf_field is None else np.ascontiguousarray(sdf_field, dtype=np.float32)
+    L.ao_surface_forces_field(fptr(p), u8ptr(w), nx, ny, nz, C.byref(world), C.byref(sp),
+                              fptr(f) if f is not None else None, C.byref(sdf_grid) if sdf_grid is not None else None,
+                              fptr(v), fptr(nn), ntri, int(bool(f32_sums)), C.byref(out), fptr(cp))
+    return out, cp[:ntri]
+
+
 def equilibrium_moments(rho, ux, uy, uz):
     L = oracle_lib("f32")
     out = np.zeros(4, np.float32)
@@ -260,6 +303,22 @@ def voxel_plan(size, res: int, budget: int = 0) -> VoxelPlan:
     return p
 
 
+class RefAeroIn(C.Structure):
+    _fields_ = [("flow_speed", C.c_float), ("azimuth", C.c_float), ("elevation", C.c_float), ("altitude", C.c_float),
+                ("use_real_density", C.c_int), ("auto_ref_area", C.c_int), ("ref_area", C.c_float),
+                ("mach_effects", C.c_int), ("ground_effect", C.c_int), ("ground_height", C.c_float),
+                ("re_number", C.c_float), ("bb_min", C.c_float * 3), ("bb_max", C.c_float * 3),
+                ("center", C.c_float * 3), ("max_dim", C.c_float)]
+
+
+class RefAeroOut(C.Structure):
+    _fields_ = [("drag", C.c_float), ("lift", C.c_float), ("ld", C.c_float), ("moment_mag", C.c_float),
+                ("drag_vec", C.c_float * 3), ("lift_vec", C.c_float * 3), ("moment", C.c_float * 3),
+                ("cop", C.c_float * 3), ("ref_area", C.c_float), ("cp_bad", C.c_longlong), ("vel", C.c_float * 3),
+                ("air_temperature", C.c_float), ("air_density", C.c_float), ("speed_of_sound", C.c_float),
+                ("vox_min_y", C.c_float), ("re_number", C.c_float)]
+
+
 class RefHarness:
     """The reference's own solver sources (oracle/_ref/libaeros_ref.so)."""
 
@@ -305,6 +364,8 @@ class RefHarness:
         L.ref_stl_load.restype = C.c_longlong
         L.ref_stl_load.argtypes = [C.c_char_p]
         L.ref_stl_get.argtypes = [_FP, _FP]
+        L.ref_set_air_density.argtypes = [C.c_float]
+        L.ref_lift_drag.argtypes = [_FP, _FP, C.c_longlong, _FP, C.POINTER(RefAeroIn), C.POINTER(RefAeroOut)]
         self.L = L
         self.n = 0
 
@@ -470,6 +531,23 @@ class RefHarness:
     def vorticity_q(self) -> dict:
         out = {k: np.empty(self.n, np.float32) for k in ("vorticity", "q", "strain")}
         self.L.ref_vorticity_q(fptr(out["vorticity"]), fptr(out["q"]), fptr(out["strain"]))
+        return out
+
+    def lift_drag(self, verts: np.ndarray, normals: np.ndarray, sdf_field: np.ndarray | None = None, **kw):
+        """computeLiftDrag on the last step's state. kw: RefAeroIn fields."""
+        v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1)
+        nn = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1)
+        a = RefAeroIn()
+        for k, val in kw.items():
+            if k in ("bb_min", "bb_max", "center"):
+                for i in range(3):
+                    getattr(a, k)[i] = float(val[i])
+            else:
+                setattr(a, k, val)
+        out = RefAeroOut()
+        f = None if sdf_field is None else np.ascontiguousarray(sdf_field, dtype=np.float32)
+        self.L.ref_lift_drag(fptr(v), fptr(nn), v.size // 9, fptr(f) if f is not None else None, C.byref(a),
+                             C.byref(out))
         return out
 
     def sample(self, field: int, points: np.ndarray):

@@ -11,8 +11,10 @@
 // for GL/GLFW/CUDA (aeros/tests/physics_ref_headless.cpp:40-45).
 #include "lbm.cpp"
 #include "thermal_lbm.cpp"
+#include "forces.cpp"
 
 #include <cstdint>
+#include <omp.h>
 #include <cstring>
 
 #include "mesh_bvh.h"
@@ -22,9 +24,23 @@
 extern "C" double glfwGetTime(void) { static double t = 0.0; return (t += 1.0 / 60.0); }
 extern "C" void setVoxelData(const int*, const float*, int, int, int, float, float, float, float, float, float) {}
 extern "C" int cudaConsumeError(char* buf, int sz) { if (buf && sz > 0) buf[0] = 0; return 0; }
-void updateVertexColors() {}
-void computeLiftDrag() {}
 void drawModel() {}
+extern "C" void computeVertexPressureCUDA(const std::vector<float>&, const std::vector<float>&, std::vector<float>&, int,
+                                          const FlowParams&) {}
+
+// forces.cpp (computeLiftDrag) is included as well. Its vertex-colour and
+// arrow uploads are GL calls behind glBackendActive(); reporting the Vulkan
+// backend keeps them off, and the function pointers it names are null
+// stubs, as in the reference's headless test builds.
+bool isRendererVulkan() { return true; }
+PFNGLBINDBUFFERPROC glad_glBindBuffer = nullptr;
+PFNGLBINDVERTEXARRAYPROC glad_glBindVertexArray = nullptr;
+PFNGLBUFFERDATAPROC glad_glBufferData = nullptr;
+PFNGLBUFFERSUBDATAPROC glad_glBufferSubData = nullptr;
+PFNGLENABLEVERTEXATTRIBARRAYPROC glad_glEnableVertexAttribArray = nullptr;
+PFNGLGENBUFFERSPROC glad_glGenBuffers = nullptr;
+PFNGLGENVERTEXARRAYSPROC glad_glGenVertexArrays = nullptr;
+PFNGLVERTEXATTRIBPOINTERPROC glad_glVertexAttribPointer = nullptr;
 
 extern "C" {
 
@@ -408,6 +424,69 @@ void ref_sample(int field, const float* pts, long long n, float* out, uint8_t* v
             out[i] = v;
         }
     }
+}
+
+// The atmosphere global the readback's pressure scale uses; computeLiftDrag's
+// updateFlowParams rewrites it from the altitude (atmosphere.cpp:175-190).
+void ref_set_air_density(float rho) { airDensity = rho; }
+
+// computeLiftDrag (forces.cpp:401-688) on the LBM state of the last step,
+// with the world pressure of that step. One OpenMP thread, so that the
+// per-triangle sums run in triangle order. sdf: a field on the solver's voxel
+// grid (NULL: no field). Globals the call leaves unchanged keep the
+// sentinel 7.
+struct RefAeroIn {
+    float flow_speed, azimuth, elevation, altitude;
+    int use_real_density, auto_ref_area;
+    float ref_area;
+    int mach_effects, ground_effect;
+    float ground_height, re_number;
+    float bb_min[3], bb_max[3], center[3], max_dim;
+};
+struct RefAeroOut {
+    float drag, lift, ld, moment_mag, drag_vec[3], lift_vec[3], moment[3], cop[3], ref_area;
+    long long cp_bad;
+    float vel[3], air_temperature, air_density, speed_of_sound, vox_min_y, re_number;
+};
+void ref_lift_drag(const float* v, const float* n, long long ntri, const float* sdf, const RefAeroIn* in,
+                   RefAeroOut* out) {
+    g_vertices.assign(v, v + 9 * ntri);
+    g_normals.assign(n, n + 9 * ntri);
+    if (sdf) g_distanceField.assign(sdf, sdf + (size_t)g_voxNx * g_voxNy * g_voxNz);
+    else g_distanceField.clear();
+    flowSpeed = in->flow_speed; flowAzimuth = in->azimuth; flowElevation = in->elevation; altitude = in->altitude;
+    useRealDensity = in->use_real_density != 0;
+    aeroAutoRefArea = in->auto_ref_area != 0;
+    aeroRefArea = in->ref_area;
+    aeroMachEffects = in->mach_effects != 0;
+    aeroGroundEffect = in->ground_effect != 0;
+    aeroGroundHeight = in->ground_height;
+    aeroReNumber = in->re_number;
+    minBB = glm::vec3(in->bb_min[0], in->bb_min[1], in->bb_min[2]);
+    maxBB = glm::vec3(in->bb_max[0], in->bb_max[1], in->bb_max[2]);
+    center = glm::vec3(in->center[0], in->center[1], in->center[2]);
+    maxDim = in->max_dim;
+    const glm::vec3 s7(7.0f);
+    dragMagnitude = liftMagnitude = liftToDragRatio = momentMagnitude = 7.0f;
+    dragVector = liftVector = momentVector = centerOfPressure = s7;
+    aeroCpNonFinite = 7;
+    const int prev = omp_get_max_threads();
+    omp_set_num_threads(1);
+    computeLiftDrag();
+    omp_set_num_threads(prev);
+    out->drag = dragMagnitude; out->lift = liftMagnitude; out->ld = liftToDragRatio; out->moment_mag = momentMagnitude;
+    for (int k = 0; k < 3; ++k) {
+        out->drag_vec[k] = dragVector[k]; out->lift_vec[k] = liftVector[k];
+        out->moment[k] = momentVector[k]; out->cop[k] = centerOfPressure[k];
+    }
+    out->ref_area = aeroRefArea;
+    out->cp_bad = aeroCpNonFinite;
+    out->vel[0] = flowParams.vx; out->vel[1] = flowParams.vy; out->vel[2] = flowParams.vz;
+    out->air_temperature = flowParams.airTemperature;
+    out->air_density = flowParams.airDensity;
+    out->speed_of_sound = speedOfSound;
+    out->vox_min_y = g_voxMinY;
+    out->re_number = aeroReNumber;   // updateFlowParams recomputes it
 }
 
 }  // extern "C"

@@ -286,3 +286,75 @@ def stl_files() -> dict:
     files["text_without_keywords"] = b"this is a plain text file\nwith two lines of words\n"
     files["too_small"] = b"solid x"
     return files
+
+
+# ---- surface-pressure lift and drag fixtures ----------------------------------
+# computeLiftDrag (forces.cpp:401-688) of the reference on the post cases'
+# stepped states: a level-3 icosphere on the solver's sphere (radius 4 cells
+# around (12, 12, 12)) with radial vertex normals, optionally the solver
+# mask's distance field, and the aerodynamic options of the reference's globals.
+SURFACE_CENTER = (12.0, 12.0, 12.0)
+SURFACE_RADIUS = 4.0
+
+
+def surface_mesh(kind: str = "sphere") -> tuple[np.ndarray, np.ndarray]:
+    """(vertices, normals), 9 floats per triangle each. kinds: "sphere";
+    "degenerate" adds triangles the pass skips (zero area, NaN first vertex,
+    zero normal, NaN second vertex, a 1e-11 sliver) and one whose sample point
+    lies outside the grid; "huge" adds a triangle above the 1e6 area limit
+    (still counted by the projected area, which then falls back to the box);
+    "empty" has none."""
+    from aeros_gb300 import geometry
+    if kind == "empty":
+        z = np.zeros((0, 9), np.float32)
+        return z, z
+    t = geometry.icosphere(3, SURFACE_RADIUS, SURFACE_CENTER).astype(np.float64).reshape(-1, 9)
+    extra = []
+    if kind == "degenerate":
+        extra = [[12, 12, 17, 12, 12, 17, 12, 12, 17],
+                 [np.nan, 1, 1, 1, 2, 1, 1, 1, 2],
+                 [12, 17, 12, 13, 17, 12, 12, 17, 13],
+                 [12, 12, 20, np.nan, 12, 20, 12, 13, 20],
+                 [12, 7, 12, 12 + 1e-6, 7, 12, 12, 7, 12 + 1e-5],
+                 [-5, -5, -5, -4, -5, -5, -5, -4, -5]]
+    elif kind == "huge":
+        extra = [[0, 0, 30, 2000, 0, 30, 0, 2000, 30]]
+    if extra:
+        t = np.concatenate([t, np.asarray(extra, np.float64)])
+    v = t.reshape(-1, 3, 3)
+    c = np.asarray(SURFACE_CENTER, np.float64)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        n = v - c
+        n = n / np.linalg.norm(n, axis=2, keepdims=True)
+    n = np.nan_to_num(n, nan=0.0)
+    if kind == "degenerate":
+        n[-4] = 0.0                       # the zero-normal triangle
+        n[-1] = (0.0, 0.0, -1.0)          # the outside one
+    return v.astype(np.float32).reshape(-1, 9), n.astype(np.float32).reshape(-1, 9)
+
+
+SURFACE_DEFAULTS = dict(flow_speed=12.5, azimuth=0.0, elevation=0.0, altitude=0.0, use_real_density=1,
+                        auto_ref_area=1, ref_area=1.0, mach_effects=0, ground_effect=0, ground_height=0.0,
+                        re_number=1e5, bb_min=(8.0, 8.0, 8.0), bb_max=(16.0, 16.0, 16.0), center=SURFACE_CENTER,
+                        max_dim=13.856406)
+SURFACE_CASES = {
+    "plain": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=False, aero={}),
+    "sdf": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=True, aero={}),
+    "karman_tsien_m044": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=True,
+                              aero=dict(mach_effects=1, flow_speed=150.0)),
+    "karman_tsien_wave_m082": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=True,
+                                   aero=dict(mach_effects=1, flow_speed=280.0)),
+    "wave_m097": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=True, aero=dict(mach_effects=1, flow_speed=330.0)),
+    "fixed_area_ground_angles": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=True,
+                                     aero=dict(auto_ref_area=0, ref_area=30.0, ground_effect=1, ground_height=3.0,
+                                               azimuth=20.0, elevation=10.0)),
+    "degenerate": dict(case="sphere_trt_les_conv", mesh="degenerate", sdf=True, aero=dict(azimuth=-35.0)),
+    "huge_box_area": dict(case="sphere_trt_les_conv", mesh="huge", sdf=False, aero={}),
+    "ground_altitude": dict(case="sphere_les_ground_copy", mesh="sphere", sdf=True,
+                            aero=dict(ground_effect=1, ground_height=1.5, altitude=3000.0, use_real_density=0,
+                                      elevation=-20.0)),
+    "plus_y_low_density": dict(case="sphere_plus_y", mesh="sphere", sdf=True,
+                               aero=dict(altitude=11000.0, azimuth=90.0, elevation=60.0, flow_speed=40.0)),
+    "no_flow": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=False, aero=dict(flow_speed=0.0)),
+    "empty_mesh": dict(case="sphere_trt_les_conv", mesh="empty", sdf=False, aero={}),
+}

@@ -132,6 +132,38 @@ def post_fixtures(R) -> dict:
     return out
 
 
+def surface_fixtures(R) -> dict:
+    """computeLiftDrag (forces.cpp:401-688) of the reference after the post
+    cases' steps, for SURFACE_CASES: its outputs and the flow parameters its
+    updateFlowParams resolved (velocity, temperature, density, speed of
+    sound, Reynolds number), which the tests feed to the oracle and device."""
+    from cases import (POST_FLOW_SPEED, SURFACE_CASES, SURFACE_DEFAULTS, digest, solver_mask, surface_mesh)
+    import oracle as O
+    out = {}
+    for name, sc in SURFACE_CASES.items():
+        case = CASES[sc["case"]]
+        nx, ny, nz = case["grid"]
+        solid = case["solid"]().astype(np.uint8).reshape(-1)
+        kw = dict(case["kw"])
+        kw["flow_speed"] = POST_FLOW_SPEED
+        R.setup(nx, ny, nz, solid, ground_rows=case.get("ground_rows", 0), **kw)
+        R.step(case["steps"])
+        wp = R.world()[2]   # the step's world parameters (an earlier call's atmosphere update changes airDensity)
+        v, n = surface_mesh(sc["mesh"])
+        sdf = None
+        if sc["sdf"]:
+            m = (solver_mask(case).reshape(-1) == 1).astype(np.uint8)
+            sdf = O.sdf(m, (nx, ny, nz), (1.0, 1.0, 1.0))
+        aero = dict(SURFACE_DEFAULTS, **sc["aero"])
+        r = R.lift_drag(v, n, sdf, **aero)
+        res = {k: (list(getattr(r, k)) if k in ("drag_vec", "lift_vec", "moment", "cop", "vel")
+                   else (int(r.cp_bad) if k == "cp_bad" else float(getattr(r, k)))) for k, _ in r._fields_}
+        out[name] = dict(result=res, world=wp, mesh=digest(np.concatenate([v.reshape(-1), n.reshape(-1)])),
+                         sdf=digest(sdf) if sdf is not None else None)
+        print(f"  {name}: drag {r.drag:.6g} lift {r.lift:.6g} area {r.ref_area:.6g}")
+    return out
+
+
 def sdf_fixtures(R) -> dict:
     """buildVoxelGrid's mask and distance field (voxel_grid.cpp:224-553) and
     sampleSDFCPU / sdfNormalCPU (:32-123) of the reference, for SDF_CASES."""
@@ -180,6 +212,10 @@ def main():
     if "--sdf" in sys.argv:   # only the distance-field fixtures
         with open(os.path.join(HERE, "sdf.json"), "w") as fh:
             json.dump(sdf_fixtures(R), fh, indent=1, sort_keys=True)
+        return
+    if "--surface" in sys.argv:   # only the surface-force fixtures
+        with open(os.path.join(HERE, "surface.json"), "w") as fh:
+            json.dump(surface_fixtures(R), fh, indent=1, sort_keys=True)
         return
     if "--post" in sys.argv:   # only the post-processing fixtures
         with open(os.path.join(HERE, "post.json"), "w") as fh:
@@ -246,6 +282,9 @@ def main():
     print("post-processing ...")
     with open(os.path.join(HERE, "post.json"), "w") as fh:
         json.dump(post_fixtures(R), fh, indent=1, sort_keys=True)
+    print("surface forces ...")
+    with open(os.path.join(HERE, "surface.json"), "w") as fh:
+        json.dump(surface_fixtures(R), fh, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(HERE, "masks.npz"), **masks)
     print(f"done in {time.time() - t0:.0f} s")
 
