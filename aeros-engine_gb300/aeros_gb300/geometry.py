@@ -79,6 +79,19 @@ def icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.nda
     return v[f].reshape(-1, 9).astype(np.float32)
 
 
+def face_normals(tris: np.ndarray, center=None) -> np.ndarray:
+    """Per-vertex normals as an STL file carries them: each triangle's unit
+    face normal (FP64 cross product of its FP32 vertices) on its three
+    vertices, 9 floats per triangle. With `center`, oriented away from it."""
+    t = np.asarray(tris, np.float32).reshape(-1, 3, 3).astype(np.float64)
+    n = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    if center is not None:
+        out = np.einsum("ij,ij->i", n, t.mean(axis=1) - np.asarray(center, np.float64)) < 0
+        n[out] = -n[out]
+    return np.repeat(n[:, None, :], 3, axis=1).astype(np.float32).reshape(-1, 9)
+
+
 @functools.lru_cache(maxsize=8)
 def _unit_icosphere_vertices(level: int):
     """Distinct vertices of the unit icosphere and each triangle corner's index."""

@@ -136,6 +136,7 @@ bool read_world() {
 
 namespace {
 aeros_sdf_field* g_sdf = nullptr;   // the device copy of g_distanceField
+aeros_voxel_grid g_sdf_grid{};      // its grid
 }  // namespace
 
 bool loadSTL(const std::string& filename, std::vector<float>& vertices, std::vector<float>& normals) {
@@ -227,6 +228,7 @@ void buildVoxelGrid(const std::vector<float>& verts, int res) {
     }
     aeros_sdf_field_destroy(g_sdf);
     g_sdf = f;
+    g_sdf_grid = grid;
     g_voxNx = grid.nx;
     g_voxNy = grid.ny;
     g_voxNz = grid.nz;
@@ -379,6 +381,70 @@ void computeLBMVorticityAndQ() {
     lbmStrainMag.resize(n);
     if (!g_world_read && !read_world()) return;
     ok(aeros_lbm_vorticity_q(g_handle, lbmVorticityMag.data(), lbmQCriterion.data(), lbmStrainMag.data()));
+}
+
+std::vector<float> g_vertices, g_normals;
+float lbmFacadeAirTemperature = 288.15f;
+bool useRealDensity = true;
+float flowAzimuth = 0.0f, flowElevation = 0.0f;
+LbmVec3 minBB, maxBB, center;
+float maxDim = 1.0f;
+float aeroRefArea = 1.0f;
+bool aeroAutoRefArea = true, aeroMachEffects = false, aeroGroundEffect = false;
+float aeroGroundHeight = 0.0f, aeroReNumber = 0.0f;
+float liftMagnitude = 0.0f, dragMagnitude = 0.0f, liftToDragRatio = 0.0f, momentMagnitude = 0.0f;
+LbmVec3 liftVector, dragVector, momentVector, centerOfPressure;
+long long aeroCpNonFinite = 0;
+
+void computeLiftDrag() {
+    if (!g_handle || g_vertices.size() < 9 || g_normals.size() != g_vertices.size()) return;   // forces.cpp:403-406
+    if (!g_world_read && !read_world()) return;
+    aeros_surface_params sp{};
+    for (int a = 0; a < 3; ++a) sp.velocity[a] = lbmFacadeFreestream[a];
+    sp.air_temperature = lbmFacadeAirTemperature;
+    sp.air_density = lbmFacadeAirDensity;
+    sp.use_real_density = useRealDensity;
+    sp.speed_of_sound = lbmFacadeSpeedOfSound;
+    sp.mach_effects = aeroMachEffects;
+    sp.auto_ref_area = aeroAutoRefArea;
+    sp.ref_area = aeroRefArea;
+    sp.flow_azimuth_deg = flowAzimuth;
+    sp.flow_elevation_deg = flowElevation;
+    const LbmVec3* bv[3] = {&minBB, &maxBB, &center};
+    float* dv[3] = {sp.bb_min, sp.bb_max, sp.center};
+    for (int i = 0; i < 3; ++i) {
+        dv[i][0] = bv[i]->x;
+        dv[i][1] = bv[i]->y;
+        dv[i][2] = bv[i]->z;
+    }
+    sp.max_dim = maxDim;
+    sp.reynolds = aeroReNumber;
+    sp.ground_effect = aeroGroundEffect;
+    sp.ground_height = aeroGroundHeight;
+    sp.vox_min_y = g_voxMinY;
+    aeros_surface_mesh* mesh = nullptr;
+    if (!ok(aeros_surface_mesh_create(g_vertices.data(), g_normals.data(), (int64_t)(g_vertices.size() / 9), &mesh)))
+        return;
+    const aeros_world_params w = world_params();
+    aeros_surface_forces out{};
+    const bool done = ok(aeros_lbm_surface_forces(g_handle, &w, &sp, mesh, g_sdf ? aeros_sdf_field_device(g_sdf) : nullptr,
+                                                  g_sdf ? &g_sdf_grid : nullptr, &out, nullptr));
+    aeros_surface_mesh_destroy(mesh);
+    if (!done || out.status == AEROS_SURFACE_NOT_RUN) return;
+    liftMagnitude = out.lift;
+    dragMagnitude = out.drag;
+    liftToDragRatio = out.lift_to_drag;
+    if (out.status == AEROS_SURFACE_NO_FLOW) return;   // forces.cpp:412: only these three
+    momentMagnitude = out.moment_magnitude;
+    LbmVec3* vs[4] = {&dragVector, &liftVector, &momentVector, &centerOfPressure};
+    const float* src[4] = {out.drag_vector, out.lift_vector, out.moment, out.center_of_pressure};
+    for (int i = 0; i < 4; ++i) {
+        vs[i]->x = src[i][0];
+        vs[i]->y = src[i][1];
+        vs[i]->z = src[i][2];
+    }
+    aeroRefArea = out.ref_area;
+    aeroCpNonFinite = out.cp_non_finite;
 }
 
 bool lbmFacadeSample(int field, const float* points, long long n, float* out, uint8_t* valid) {

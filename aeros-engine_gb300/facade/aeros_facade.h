@@ -215,6 +215,28 @@ extern std::string g_voxelBuildError;
 extern long long g_voxelSolidCells;
 extern int g_voxelUsedRes;
 
+// ---- lift and drag from the surface pressure (aeros/src/forces.h, globals.h) -------
+// computeLiftDrag (forces.cpp:401-688), LBM branch: the per-triangle pass on the
+// device over the pressure of the last step, the closing formulas on the host.
+// Inputs: the model (g_vertices / g_normals, 9 floats per triangle each), the
+// flow (lbmFacadeFreestream, lbmFacadeAirTemperature, lbmFacadeAirDensity,
+// lbmFacadeSpeedOfSound), the aero options and model bounds below, and the
+// distance field of the last buildVoxelGrid. Outputs: the globals below, as
+// the reference sets them (unchanged when it returns early).
+extern std::vector<float> g_vertices, g_normals;
+extern float lbmFacadeAirTemperature;   // flowParams.airTemperature, K
+extern bool useRealDensity;
+extern float flowAzimuth, flowElevation;   // degrees (computeLBMRefArea's direction)
+extern LbmVec3 minBB, maxBB, center;
+extern float maxDim;
+extern float aeroRefArea;
+extern bool aeroAutoRefArea, aeroMachEffects, aeroGroundEffect;
+extern float aeroGroundHeight, aeroReNumber;
+extern float liftMagnitude, dragMagnitude, liftToDragRatio, momentMagnitude;
+extern LbmVec3 liftVector, dragVector, momentVector, centerOfPressure;
+extern long long aeroCpNonFinite;
+void computeLiftDrag();
+
 // ---- extras of this layer ----------------------------------------------------
 // The C-ABI handle (NULL before initLBM): for callers that also use the batch
 // or the device field pointers.

@@ -394,6 +394,69 @@ def sdf_bench(res=256, reps=5, cpu=True):
     return line
 
 
+def surface_bench(reps=20, warm_steps=300, cpu=True):
+    """Surface-pressure lift and drag (computeLiftDrag) of the level-6
+    icosphere (81,920 triangles, radial vertex normals) on the Re = 100
+    sphere, 240 x 120 x 115 FP32, after `warm_steps` steps, with the device
+    distance field of its mask: `reps` timed calls through the C ABI (the
+    three kernels, the 144-byte readback and the host closing formulas; no
+    per-triangle Cp copy). CPU baseline: the restatement over the same
+    pressure field, FP32 as the reference runs its OpenMP loop on one thread."""
+    import torch
+    from aeros_gb300 import capi, geometry, solver
+    p, mask, tris = geometry.sphere_config("fp32")
+    nx, ny, nz = geometry.SPHERE_GRID
+    s = solver.Solver(p, mask)
+    s.step(warm_steps)
+    # the reference's sampler puts cell i's value at min + i * cell (lbm.cpp:1881-1933), the mask's
+    # cell centres sit at i + 0.5: min = 0.5 centres the pressure on the mesh
+    w = capi.make_world(12.5, 1.225, (0.5, 0.5, 0.5), (1.0, 1.0, 1.0))
+    fields, _ = s.world_fields(w)
+    v = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    c = np.asarray(geometry.SPHERE_CENTER, np.float64)
+    nrm = geometry.face_normals(v, c)
+    grid = solver.voxel_grid((nx, ny, nz), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    sdf = solver.sdf((mask.reshape(-1) == 1).astype(np.uint8), grid)
+    d = torch.from_numpy(sdf).cuda()
+    torch.cuda.synchronize()
+    r = geometry.SPHERE_RADIUS
+    sp = capi.make_surface(velocity=(12.5, 0.0, 0.0), bb_min=c - r, bb_max=c + r, center=c, reynolds=1e7)
+    mesh = solver.SurfaceMesh(v, nrm)
+    ntri = v.shape[0]
+    s.surface_forces(w, sp, mesh, d.data_ptr(), grid, want_cp=False)   # warm-up
+    ms = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        o, _ = s.surface_forces(w, sp, mesh, d.data_ptr(), grid, want_cp=False)
+        ms.append(1000 * (time.perf_counter() - t0))
+    dev_ms = float(np.median(ms))
+    line = {"metric": "surface-pressure lift and drag rate (computeLiftDrag, level-6 icosphere)",
+            "value": round(ntri / (dev_ms * 1e-3) / 1e6, 2), "unit": "Mtriangles/s", "higher_is_better": True,
+            "ms_per_call": round(dev_ms, 4), "calls": reps, "dtype": "f32 (sums f64)", "data": "synthetic",
+            "config": {"workload": f"icosphere L6 ({ntri} triangles) on the Re=100 sphere 240x120x115 FP32 after "
+                                   f"{warm_steps} steps, distance field of the mask", "what": "aeros_lbm_surface_forces, "
+                                   "host to host (params in, 144 B result out)"},
+            "drag_N": float(o.drag), "lift_N": float(o.lift), "ref_area": float(o.ref_area)}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        wall = (mask.reshape(-1) != 0).astype(np.uint8)
+        t0 = time.perf_counter()
+        k = 0
+        while True:
+            oracle.surface_forces_field(fields["pressure"], wall, (nx, ny, nz), w, sp, v, nrm, sdf, grid,
+                                        f32_sums=True)
+            k += 1
+            if time.perf_counter() - t0 > 2.0:
+                break
+        cpu_s = (time.perf_counter() - t0) / k
+        line["cpu_baseline"] = {"value": round(ntri / cpu_s / 1e6, 3), "unit": "Mtriangles/s", "cores": 1,
+                                "kind": "port", "sample": f"{k} full passes over the same {ntri} triangles and "
+                                                          "pressure field (the restatement, one thread)"}
+    return line
+
+
 def rb_bench(steps=50000, ras=(1700.0, 2500.0, 1e4)):
     """Rayleigh-Benard convection, 128 x 128 x 32 fluid rows (+ 2 wall rows,
     the reference's y axis up), D3Q19 BGK + D3Q7 thermal with Boussinesq
@@ -496,7 +559,7 @@ def main():
     ap.add_argument("--only", default="both", choices=["both", "fp32", "fp16", "bf16"],
                     help="time one storage form only (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "serve", "sdf", "rb"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "serve", "sdf", "rb", "surface"])
     ap.add_argument("--rb-steps", type=int, default=50000)
     ap.add_argument("--sdf-res", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=16)
@@ -517,6 +580,8 @@ def main():
         print(json.dumps(r), flush=True)
     elif args.workload == "rb":
         print(json.dumps(rb_bench(args.rb_steps)), flush=True)
+    elif args.workload == "surface":
+        print(json.dumps(surface_bench(reps=max(1, min(args.steps, 200)), cpu=not args.no_cpu)), flush=True)
     elif args.workload == "sdf":
         print(json.dumps(sdf_bench(args.sdf_res, reps=max(1, min(args.steps, 20)), cpu=not args.no_cpu)), flush=True)
     elif args.workload == "batch":

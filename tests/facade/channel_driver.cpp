@@ -6,7 +6,8 @@
 // lbmUx, lbmUxWorld, lbmUyWorld, lbmPressure, lbmVorticityMag, lbmQCriterion,
 // lbmStrainMag (cells each), then NPTS sample points (xyz) and, for each field
 // 0..7 of lbmFacadeSample, its values (3 per point for the velocity) and
-// validity flags (as floats).
+// validity flags (as floats); then the box mesh of the lift / drag call
+// (vertices, normals: 108 floats each).
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -92,6 +93,34 @@ int main(int argc, char** argv) {
     std::printf("validate %d %d %d %d %d %d\n", (int)lbmValidateInitialization(), (int)lbmValidateConservation(),
                 (int)lbmValidateBoundaryConditions(), (int)lbmValidateSolidHandling(), (int)lbmValidateRealisticAero(),
                 (int)lbmValidateStability());
+    // lift and drag on a 1 m box around the origin (12 triangles, face normals)
+    g_vertices.clear();
+    g_normals.clear();
+    for (int a = 0; a < 3; ++a)
+        for (int sgn = -1; sgn <= 1; sgn += 2) {
+            const int b = (a + 1) % 3, c = (a + 2) % 3;
+            const float q[4][2] = {{-0.5f, -0.5f}, {0.5f, -0.5f}, {0.5f, 0.5f}, {-0.5f, 0.5f}};
+            const int tri[2][3] = {{0, 1, 2}, {0, 2, 3}};
+            for (const auto& t : tri)
+                for (int k = 0; k < 3; ++k) {
+                    float v[3], n[3] = {0.0f, 0.0f, 0.0f};
+                    v[a] = 0.5f * (float)sgn;
+                    v[b] = q[t[k]][0];
+                    v[c] = q[t[k]][1];
+                    n[a] = (float)sgn;
+                    g_vertices.insert(g_vertices.end(), v, v + 3);
+                    g_normals.insert(g_normals.end(), n, n + 3);
+                }
+        }
+    minBB = LbmVec3{-0.5f, -0.5f, -0.5f};
+    maxBB = LbmVec3{0.5f, 0.5f, 0.5f};
+    center = LbmVec3{0.0f, 0.0f, 0.0f};
+    maxDim = 1.7320508f;
+    aeroReNumber = 3e5f;
+    computeLiftDrag();
+    std::printf("forces drag %.9g lift %.9g ld %.9g moment %.9g cop %.9g %.9g %.9g area %.9g bad %lld\n",
+                dragMagnitude, liftMagnitude, liftToDragRatio, momentMagnitude, centerOfPressure.x, centerOfPressure.y,
+                centerOfPressure.z, aeroRefArea, aeroCpNonFinite);
     if (argc > 2) {
         FILE* fh = std::fopen(argv[2], "wb");
         if (!fh) return 2;
@@ -106,6 +135,8 @@ int main(int argc, char** argv) {
             put(fh, out);
             put(fh, std::vector<float>(valid.begin(), valid.end()));
         }
+        put(fh, g_vertices);
+        put(fh, g_normals);
         std::fclose(fh);
     }
     shutdownLBM();

@@ -116,6 +116,19 @@ def test_facade_channel_equals_c_abi(driver, tmp_path):
     # inlet check rejects as the reference's does
     val = r.stdout.split("validate ")[1].splitlines()[0].split()
     assert val == ["1", "1", "0", "1", "1", "1"], val
+    # computeLiftDrag through the facade: the C ABI's surface pass on the same state and mesh
+    verts = blob[pos:pos + 108]
+    nrms = blob[pos + 108:pos + 216]
+    assert pos + 216 == blob.size
+    sp = capi.make_surface(velocity=(10.0, 0.0, 0.0), air_temperature=288.15, air_density=1.225,
+                           speed_of_sound=340.0, bb_min=(-0.5, -0.5, -0.5), bb_max=(0.5, 0.5, 0.5),
+                           center=(0.0, 0.0, 0.0), max_dim=1.7320508, reynolds=3e5)
+    so, _ = s.surface_forces(wp, sp, solver.SurfaceMesh(verts, nrms))
+    fl = r.stdout.split("forces ")[1].splitlines()[0].split()
+    want = [so.drag, so.lift, so.lift_to_drag, so.moment_magnitude, *so.center_of_pressure, so.ref_area]
+    got_f = [np.float32(fl[i]) for i in (1, 3, 5, 7, 9, 10, 11, 13)]
+    assert got_f == [np.float32(v) for v in want], (got_f, want)
+    assert so.drag > 0 and fl[15] == "0"
     from golden.cases import EQ_MOMENT_CASES
     from post_common import GOLD
     eq = [ln.split()[1:] for ln in r.stdout.splitlines() if ln.startswith("eq ")]
