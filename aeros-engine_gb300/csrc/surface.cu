@@ -12,20 +12,27 @@
 //                     pressure weight; plus the projected area of
 //                     computeLBMRefArea (lbm.cpp:2128-2139). FP32 in the
 //                     reference's operation order (--fmad=false); the 15
-//                     per-triangle terms are summed in FP64 per block
-//   k_surface_fold    the block partials summed in block order (one thread
-//                     per term): the result does not depend on scheduling
+//                     per-triangle terms are summed over the warp in FP32
+//                     (a fixed xor tree over 32 triangles), then over the
+//                     block's warps in FP64
+//   k_surface_fold    the block partials summed in a fixed tree (16 lanes per
+//                     term, each in block order, then the lanes in order):
+//                     the result does not depend on scheduling
 // then one small device-to-host copy, and the closing formulas on the host
 // in FP32 as the reference's (forces.cpp:615-687).
 //
-// The reference sums the terms in FP32 (in thread order under OpenMP); the
-// FP64 sums here differ from its one-thread order by the FP32 rounding of
-// that order. The skin-friction power law uses log10 / pow in FP64 rounded to
-// FP32 (the reference calls log10f / powf); every other operation is a
-// correctly rounded FP32 operation, so the per-triangle Cp is the
-// reference's bit for bit.
+// The reference sums the terms in FP32 in triangle order (in thread order
+// under OpenMP); the tree here (FP32 over 32 triangles, FP64 above) differs
+// from that order by the rounding of the reference's long FP32 running sums.
+// The skin-friction power law calls CUDA's log10f / powf where the reference
+// calls the host library's (a few units in the last place apart); every
+// other operation is a correctly rounded FP32 operation, so the per-triangle
+// Cp is the reference's bit for bit. (FP64 log10 / pow and FP64 per-thread
+// sums kept the FP64 pipe 72 % busy on GB300 and took 68 us for 81,920
+// triangles.)
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -37,9 +44,11 @@
 using namespace aeros;
 
 struct aeros_surface_mesh {
-    float* tri = nullptr;   // 9 floats per triangle
-    float* nrm = nullptr;   // the first vertex's normal, 3 floats per triangle
+    float* tri = nullptr;        // 9 floats per triangle
+    float* nrm = nullptr;        // the first vertex's normal, 3 floats per triangle
     int64_t ntri = 0;
+    char* scratch = nullptr;     // leading-edge keys | sums | block partials (sized at creation)
+    unsigned char* host = nullptr;   // pinned copy of keys and sums
 };
 
 namespace {
@@ -164,9 +173,9 @@ __device__ inline V3 wall_sample_point(const TriArgs& a, V3 p, V3 n) {
 
 __global__ void __launch_bounds__(SB) k_surface_tri(const TriArgs a) {
     __shared__ double red[SB / 32][NS];
-    double acc[NS];
+    float acc[NS];
 #pragma unroll
-    for (int k = 0; k < NS; ++k) acc[k] = 0.0;
+    for (int k = 0; k < NS; ++k) acc[k] = 0.0f;
     const Chord ch = quarter_chord(a.ext[0], a.ext[1], a.fd, a.ctr, a.max_dim);
     for (long long t = blockIdx.x * (long long)SB + threadIdx.x; t < a.ntri; t += (long long)gridDim.x * SB) {
         const float* p = a.tri + 9 * t;
@@ -177,7 +186,7 @@ __global__ void __launch_bounds__(SB) k_surface_tri(const TriArgs a) {
             const float area = 0.5f * length(cr);
             if (isfinite(area) && !(area < 1e-12f)) {
                 const V3 n = cr * (1.0f / sqrtf(dot(cr, cr)));
-                acc[S_PROJ] += (double)(area * fabsf(dot(n, a.adir)));
+                acc[S_PROJ] += area * fabsf(dot(n, a.adir));
             }
         }
         // computeTri, forces.cpp:486-582
@@ -199,15 +208,15 @@ __global__ void __launch_bounds__(SB) k_surface_tri(const TriArgs a) {
                     else cp /= a.beta;
                 }
                 if (!isfinite(cp)) {
-                    acc[NT] += 1.0;
+                    acc[NT] += 1.0f;
                     cp = 0.0f;
                 }
                 const V3 pf = n * (-cp * a.q) * area;
                 const float fdn = dot(a.fd, n);
-                acc[S_FRONT] += (double)(area * fabsf(fdn));
+                acc[S_FRONT] += area * fabsf(fdn);
                 if (fdn > 0.7f) {
-                    acc[S_BASEA] += (double)area;
-                    acc[S_BASEF] += (double)(cp * a.q * area);
+                    acc[S_BASEA] += area;
+                    acc[S_BASEF] += cp * a.q * area;
                 }
                 float xa = dot(tc, a.fd) - ch.min_al;
                 if (xa < 0.001f) xa = 0.001f;
@@ -218,9 +227,9 @@ __global__ void __launch_bounds__(SB) k_surface_tri(const TriArgs a) {
                 if (re < 5e5f) {
                     cf = 0.664f / sqrtf(re);
                 } else {
-                    float lr = (float)log10((double)re);
+                    float lr = log10f(re);
                     if (lr < 1.0f) lr = 1.0f;
-                    cf = 0.455f / (float)pow((double)lr, (double)2.58f);
+                    cf = 0.455f / powf(lr, 2.58f);
                     if (re < 1e9f) {
                         cf -= 1700.0f / re;
                         if (cf < 0.0005f) cf = 0.0005f;
@@ -236,22 +245,23 @@ __global__ void __launch_bounds__(SB) k_surface_tri(const TriArgs a) {
                 if (cp < 0) pw *= 0.8f;
                 const V3 cw = tc * pw;
                 const V3 m = cross(tc - ch.ac, force);
-                acc[S_FX] += (double)force.x; acc[S_FY] += (double)force.y; acc[S_FZ] += (double)force.z;
-                acc[S_CX] += (double)cw.x; acc[S_CY] += (double)cw.y; acc[S_CZ] += (double)cw.z;
-                acc[S_MX] += (double)m.x; acc[S_MY] += (double)m.y; acc[S_MZ] += (double)m.z;
-                acc[S_AREA] += (double)area;
-                acc[S_PRESS] += (double)pw;
+                acc[S_FX] += force.x; acc[S_FY] += force.y; acc[S_FZ] += force.z;
+                acc[S_CX] += cw.x; acc[S_CY] += cw.y; acc[S_CZ] += cw.z;
+                acc[S_MX] += m.x; acc[S_MY] += m.y; acc[S_MZ] += m.z;
+                acc[S_AREA] += area;
+                acc[S_PRESS] += pw;
             }
         }
         if (a.cp) a.cp[t] = cp;
     }
-    // block sum: xor tree in each warp, then the warps in order
+    // block sum: xor tree in each warp (FP32: 32 triangles), then the warps
+    // in order in FP64
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-        double v = acc[k];
+        float v = acc[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[warp][k] = v;
+        if (lane == 0) red[warp][k] = (double)v;
     }
     __syncthreads();
     if (threadIdx.x < NS) {
@@ -261,14 +271,31 @@ __global__ void __launch_bounds__(SB) k_surface_tri(const TriArgs a) {
     }
 }
 
-// one thread per term: the block partials in block order
-__global__ void k_surface_fold(const double* __restrict__ part, int nblk, double* out) {
-    const int k = threadIdx.x;
-    if (k >= NS) return;
+// FOLD_LANES threads per term, each summing the partials of blocks
+// j, j + FOLD_LANES, ... in order, then the lanes' sums in lane order: a
+// fixed tree whose dependent chains are FOLD_LANES times shorter than a
+// single running sum.
+constexpr int FOLD_LANES = 16;
+__global__ void __launch_bounds__(NS * FOLD_LANES) k_surface_fold(const double* __restrict__ part, int nblk,
+                                                                  double* out) {
+    __shared__ double lane_sum[FOLD_LANES][NS];
+    const int k = threadIdx.x % NS, j = threadIdx.x / NS;
     double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += part[(long long)b * NS + k];
-    out[k] = s;
+    for (int b = j; b < nblk; b += FOLD_LANES) s += part[(long long)b * NS + k];
+    lane_sum[j][k] = s;
+    __syncthreads();
+    if (threadIdx.x < NS) {
+        double t = 0.0;
+        for (int l = 0; l < FOLD_LANES; ++l) t += lane_sum[l][threadIdx.x];
+        out[threadIdx.x] = t;
+    }
 }
+
+constexpr size_t RES_OFF = 16;                              // after the two keys (padded)
+constexpr size_t PART_OFF = RES_OFF + NS * sizeof(double);  // then the block partials
+constexpr size_t HOST_BYTES = PART_OFF;                     // what comes back per call
+
+int blocks_for(int64_t ntri) { return (int)std::min<long long>(MAX_BLOCKS, (ntri + SB - 1) / SB); }
 
 // computeLBMRefArea's direction (lbm.cpp:2114-2121), on the host with the
 // host's cosf / sinf as the reference's
@@ -423,6 +450,8 @@ extern "C" int aeros_surface_mesh_create(const float* vertices, const float* nor
         for (int64_t t = 0; t < ntri; ++t) std::memcpy(first + 3 * t, normals + 9 * t, 12);
     if (e == cudaSuccess) e = cudaMalloc((void**)&m->tri, (size_t)ntri * 36);
     if (e == cudaSuccess) e = cudaMalloc((void**)&m->nrm, (size_t)ntri * 12);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->scratch, PART_OFF + (size_t)blocks_for(ntri) * NS * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&m->host, HOST_BYTES);
     if (e == cudaSuccess) e = cudaMemcpy(m->tri, vertices, (size_t)ntri * 36, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(m->nrm, first, (size_t)ntri * 12, cudaMemcpyHostToDevice);
     delete[] first;
@@ -438,6 +467,8 @@ extern "C" int aeros_surface_mesh_destroy(aeros_surface_mesh* mesh) {
     if (!mesh) return AEROS_OK;
     if (mesh->tri) cudaFree(mesh->tri);
     if (mesh->nrm) cudaFree(mesh->nrm);
+    if (mesh->scratch) cudaFree(mesh->scratch);
+    if (mesh->host) cudaFreeHost(mesh->host);
     delete mesh;
     return AEROS_OK;
 }
@@ -508,36 +539,31 @@ extern "C" int aeros_lbm_surface_forces(aeros_lbm* h, const aeros_world_params* 
     a.nrm = mesh->nrm;
     a.ntri = ntri;
 
-    const int nblk = (int)std::min<long long>(MAX_BLOCKS, (ntri + SB - 1) / SB);
-    // scratch: ext (2 x u32, padded to 16 B) | result (NS doubles) | partials (nblk x NS doubles)
-    const size_t res_off = 16, part_off = res_off + NS * sizeof(double);
-    const size_t bytes = part_off + (size_t)nblk * NS * sizeof(double);
-    char* scratch = nullptr;
+    const int nblk = blocks_for(ntri);
+    char* scratch = mesh->scratch;   // the mesh's own: one pass per mesh at a time
     float* dcp = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&scratch, bytes, h->stream);
-    if (e == cudaSuccess && cp) e = cudaMallocAsync((void**)&dcp, (size_t)ntri * 4, h->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, 16, h->stream);
-    unsigned char host[16 + NS * sizeof(double)];
+    cudaError_t e = cudaSuccess;
+    if (cp) e = cudaMallocAsync((void**)&dcp, (size_t)ntri * 4, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, 8, h->stream);
     if (e == cudaSuccess) {
         a.ext = reinterpret_cast<uint32_t*>(scratch);
-        a.part = reinterpret_cast<double*>(scratch + part_off);
+        a.part = reinterpret_cast<double*>(scratch + PART_OFF);
         a.cp = dcp;
         k_surface_extent<<<nblk, SB, 0, h->stream>>>(a.tri, ntri, a.fd, reinterpret_cast<uint32_t*>(scratch));
         k_surface_tri<<<nblk, SB, 0, h->stream>>>(a);
-        k_surface_fold<<<1, 32, 0, h->stream>>>(a.part, nblk, reinterpret_cast<double*>(scratch + res_off));
+        k_surface_fold<<<1, NS * FOLD_LANES, 0, h->stream>>>(a.part, nblk, reinterpret_cast<double*>(scratch + RES_OFF));
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(host, scratch, sizeof(host), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mesh->host, scratch, HOST_BYTES, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess && cp) e = cudaMemcpyAsync(cp, dcp, (size_t)ntri * 4, cudaMemcpyDeviceToHost, h->stream);
-    if (scratch) cudaFreeAsync(scratch, h->stream);
     if (dcp) cudaFreeAsync(dcp, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "surface forces: %s", cudaGetErrorString(e));
 
     uint32_t ext[2];
     double sums[NS];
-    std::memcpy(ext, host, 8);
-    std::memcpy(sums, host + res_off, sizeof(sums));
+    std::memcpy(ext, mesh->host, 8);
+    std::memcpy(sums, mesh->host + RES_OFF, sizeof(sums));
     float tot[NT];
     for (int k = 0; k < NT; ++k) {
         out->sums[k] = sums[k];

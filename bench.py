@@ -432,7 +432,7 @@ def surface_bench(reps=20, warm_steps=300, cpu=True):
     dev_ms = float(np.median(ms))
     line = {"metric": "surface-pressure lift and drag rate (computeLiftDrag, level-6 icosphere)",
             "value": round(ntri / (dev_ms * 1e-3) / 1e6, 2), "unit": "Mtriangles/s", "higher_is_better": True,
-            "ms_per_call": round(dev_ms, 4), "calls": reps, "dtype": "f32 (sums f64)", "data": "synthetic",
+            "ms_per_call": round(dev_ms, 4), "calls": reps, "dtype": "f32 (warp sums f32, block and grid sums f64)", "data": "synthetic",
             "config": {"workload": f"icosphere L6 ({ntri} triangles) on the Re=100 sphere 240x120x115 FP32 after "
                                    f"{warm_steps} steps, distance field of the mask", "what": "aeros_lbm_surface_forces, "
                                    "host to host (params in, 144 B result out)"},
