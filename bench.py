@@ -38,8 +38,8 @@ BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 16 + 16 + 4, "fp16": 2 * 19 * 2 + 16 + 16
 # DRAM bytes per launch of the step kernel (read + write, mean of an odd and
 # an even step) from the ncu capture summarised in
 # profiles/k_lbm_fused_sphere_240x120x115.md
-NCU_TRAFFIC = {"fp16": (232045056 + 150228736 + 218615552 + 189820928) / 2,
-               "fp32": (365174272 + 277384704 + 354234112 + 316235264) / 2}
+NCU_TRAFFIC = {"fp16": (232081408 + 149953536 + 218365952 + 189753344) / 2,
+               "fp32": (364544768 + 275870208 + 354004992 + 316344064) / 2}
 # bytes of the solver's device control block that every aeros_lbm_step call
 # reads back (struct Control in aeros-engine_gb300/csrc/lbm_step.cuh)
 CONTROL_BYTES = 272
