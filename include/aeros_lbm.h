@@ -449,7 +449,9 @@ typedef struct aeros_surface_forces {
 /* cp: optional host array, one value per triangle (the Cp the pass used;
  * 0 for skipped triangles). d_sdf / sdf_grid: the voxel grid's distance
  * field on the device (both NULL: no field, the sample point is never held
- * back). */
+ * back). A mesh holds the pass's scratch: passes that share a mesh must not
+ * run at the same time (one host thread, or one mesh per thread). Returns
+ * after the pass, on the handle's stream. */
 int aeros_lbm_surface_forces(aeros_lbm* h, const aeros_world_params* wp, const aeros_surface_params* sp,
                              const aeros_surface_mesh* mesh, const float* d_sdf, const aeros_voxel_grid* sdf_grid,
                              aeros_surface_forces* out, float* cp);
