@@ -38,10 +38,11 @@ def test_struct_layout_matches_c(lib):
 #include "aeros_lbm.h"
 #include "aeros_batch.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(aeros_lbm_params), sizeof(aeros_thermal_params),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(aeros_lbm_params), sizeof(aeros_thermal_params),
          sizeof(aeros_lbm_stats), sizeof(aeros_voxel_grid), sizeof(aeros_voxel_plan_t),
          offsetof(aeros_lbm_params, storage), offsetof(aeros_lbm_stats, sum_rho), offsetof(aeros_lbm_stats, nusselt),
-         sizeof(aeros_batch_tuning));
+         sizeof(aeros_batch_tuning), sizeof(aeros_surface_params), sizeof(aeros_surface_forces),
+         offsetof(aeros_surface_forces, cp_non_finite), offsetof(aeros_surface_forces, sums));
   return 0; }
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -52,7 +53,8 @@ int main(void) {
         got = [int(v) for v in subprocess.check_output([exe]).split()]
     want = [C.sizeof(lib.LbmParams), C.sizeof(lib.ThermalParams), C.sizeof(lib.LbmStats), C.sizeof(lib.VoxelGrid),
             C.sizeof(lib.VoxelPlan), lib.LbmParams.storage.offset, lib.LbmStats.sum_rho.offset,
-            lib.LbmStats.nusselt.offset, C.sizeof(lib.BatchTuning)]
+            lib.LbmStats.nusselt.offset, C.sizeof(lib.BatchTuning), C.sizeof(lib.SurfaceParams),
+            C.sizeof(lib.SurfaceForces), lib.SurfaceForces.cp_non_finite.offset, lib.SurfaceForces.sums.offset]
     assert got == want
 
 
@@ -80,6 +82,16 @@ def test_invalid_arguments_are_reported(lib):
     assert L.aeros_batch_set_tuning(None, None) == -1
     assert L.aeros_batch_autotune(None, 4, None) == -1
     L.aeros_consume_error(buf, 512)
+    # surface forces: argument checks come before any device work
+    mesh = C.c_void_p()
+    assert L.aeros_surface_mesh_create(None, None, 12, C.byref(mesh)) == -1 and not mesh.value
+    assert L.aeros_consume_error(buf, 512) == -1 and b"NULL" in buf.value
+    assert L.aeros_surface_mesh_create(None, None, -1, C.byref(mesh)) == -1
+    assert L.aeros_consume_error(buf, 512) == -1 and b"triangles" in buf.value
+    assert L.aeros_surface_mesh_destroy(None) == 0
+    out = lib.SurfaceForces()
+    assert L.aeros_lbm_surface_forces(None, None, None, None, None, None, C.byref(out), None) == -1
+    assert L.aeros_consume_error(buf, 512) == -1 and b"NULL" in buf.value
 
 
 def test_voxel_plan_matches_oracle(lib, oracle_built):
