@@ -212,11 +212,11 @@ const Launchers& launchers_bf16();
     }                                                                                                                 \
     cudaError_t batch_(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s) {                          \
         if (kind == 0) {                                                                                              \
-            if (odd) k_batch_step<STORE, true, 0><<<grid, STEP_BLOCK, 0, s>>>(B);                                     \
-            else k_batch_step<STORE, false, 0><<<grid, STEP_BLOCK, 0, s>>>(B);                                        \
+            if (odd) k_batch_step<STORE, true, 0><<<grid, BATCH_BLOCK, 0, s>>>(B);                                     \
+            else k_batch_step<STORE, false, 0><<<grid, BATCH_BLOCK, 0, s>>>(B);                                        \
         } else {                                                                                                      \
-            if (odd) k_batch_step<STORE, true, 1><<<grid, STEP_BLOCK, 0, s>>>(B);                                     \
-            else k_batch_step<STORE, false, 1><<<grid, STEP_BLOCK, 0, s>>>(B);                                        \
+            if (odd) k_batch_step<STORE, true, 1><<<grid, BATCH_BLOCK, 0, s>>>(B);                                     \
+            else k_batch_step<STORE, false, 1><<<grid, BATCH_BLOCK, 0, s>>>(B);                                        \
         }                                                                                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
@@ -233,8 +233,8 @@ const Launchers& launchers_bf16();
     }                                                                                                                 \
     int batch_occ_() {                                                                                                \
         int n = 0, m = 0;                                                                                             \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<STORE, false, 1>, STEP_BLOCK, 0);              \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_batch_step<STORE, true, 1>, STEP_BLOCK, 0);               \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<STORE, false, 1>, BATCH_BLOCK, 0);              \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_batch_step<STORE, true, 1>, BATCH_BLOCK, 0);               \
         n = n < m ? n : m;                                                                                            \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \

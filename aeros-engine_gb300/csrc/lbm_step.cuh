@@ -26,9 +26,13 @@
 
 namespace aeros {
 
-constexpr int STEP_BLOCK = 256;
+#ifndef AEROS_STEP_BLOCK
+#define AEROS_STEP_BLOCK 128
+#endif
+constexpr int STEP_BLOCK = AEROS_STEP_BLOCK;   // threads per block = cells per tile (a multiple of 32)
+constexpr int BATCH_BLOCK = 256;               // threads per block of the many-domain kernel
 #ifndef AEROS_STEP_MIN_BLOCKS
-#define AEROS_STEP_MIN_BLOCKS 3
+#define AEROS_STEP_MIN_BLOCKS 6
 #endif
 constexpr int STEP_MIN_BLOCKS = AEROS_STEP_MIN_BLOCKS;   // resident blocks per SM the register budget targets
 
@@ -1235,7 +1239,7 @@ __device__ __forceinline__ int warp_allsum(int v) {
 // point and accumulated exactly, so the statistics do not depend on which
 // block took which tile.
 #ifndef AEROS_FUSED_MIN_BLOCKS
-#define AEROS_FUSED_MIN_BLOCKS 4
+#define AEROS_FUSED_MIN_BLOCKS 8
 #endif
 #ifndef AEROS_BATCH_MIN_BLOCKS
 #define AEROS_BATCH_MIN_BLOCKS 4
@@ -1255,7 +1259,7 @@ __device__ __forceinline__ int interior_cell_index(const StepArgs& A, int li) {
 }
 
 #ifndef AEROS_FUSED_TH_MIN_BLOCKS
-#define AEROS_FUSED_TH_MIN_BLOCKS 3
+#define AEROS_FUSED_TH_MIN_BLOCKS 6
 #endif
 
 // The single-launch step: the first shell_blocks blocks take the boundary
@@ -1462,7 +1466,7 @@ struct BatchArgs {
 // KIND 0: the shell slices of every domain; KIND 1: the interior slices (one
 // launch each per step, so each launch's code is only its own path).
 template <class S, bool ODD, int KIND>
-__global__ void __launch_bounds__(STEP_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_step(const BatchArgs B) {
+__global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_step(const BatchArgs B) {
     // Blocks take items; warp w of the block takes slice w of every group of
     // eight, so a block covers 256 consecutive cells at a time (the rows the
     // velocity stencil shares stay in L1). The current domain's arguments are
@@ -1471,7 +1475,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_st
     // count) to the domain's accumulators when the block moves to another
     // domain or runs out of items.
     __shared__ __align__(16) unsigned char s_args[sizeof(StepArgs)];
-    __shared__ WarpSums s_sums[STEP_BLOCK / 32];
+    __shared__ WarpSums s_sums[BATCH_BLOCK / 32];
     __shared__ int s_item[2];
     const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
     StepArgs& A = *reinterpret_cast<StepArgs*>(s_args);   // StepArgs is not trivially constructible
@@ -1538,7 +1542,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_st
             __syncthreads();   // every warp is done with the previous arguments
             const int* src = reinterpret_cast<const int*>(&D.A);
             int* dst = reinterpret_cast<int*>(s_args);
-            for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / 4); i += STEP_BLOCK) dst[i] = src[i];
+            for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / 4); i += BATCH_BLOCK) dst[i] = src[i];
             __syncthreads();
             cur = dom;
         }
@@ -1553,7 +1557,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_st
         V.apply_overrides = D.overrides0 || k > 0;
         V.write_obs = write_obs;
         V.write_u = D.les || write_obs;
-        for (int base = 0; base < wk.nslices; base += STEP_BLOCK / 32) {
+        for (int base = 0; base < wk.nslices; base += BATCH_BLOCK / 32) {
             const int sl = base + wid;
             if (sl >= wk.nslices) break;   // warp-uniform
             Acc acc;
@@ -1603,7 +1607,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_st
 // continues with direct loads.
 constexpr int STAGE_SLOT = 288;   // elements per staged range
 #ifndef AEROS_STAGED_MIN_BLOCKS
-#define AEROS_STAGED_MIN_BLOCKS 3
+#define AEROS_STAGED_MIN_BLOCKS 6
 #endif
 constexpr int STAGED_MIN_BLOCKS = AEROS_STAGED_MIN_BLOCKS;
 constexpr int STAGE_WAIT_LIMIT = 1 << 20;   // try_wait polls before a staged tile is given up
