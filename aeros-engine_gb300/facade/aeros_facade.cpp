@@ -396,6 +396,46 @@ float liftMagnitude = 0.0f, dragMagnitude = 0.0f, liftToDragRatio = 0.0f, moment
 LbmVec3 liftVector, dragVector, momentVector, centerOfPressure;
 long long aeroCpNonFinite = 0;
 
+float computeLBMRefArea() {
+    if (!aeroAutoRefArea) return (!std::isfinite(aeroRefArea) || aeroRefArea < 1e-6f) ? 1.0f : aeroRefArea;
+    const float az = flowAzimuth * 0.01745329251994329576923690768489f;
+    const float el = flowElevation * 0.01745329251994329576923690768489f;
+    const float ce = cosf(el), se = sinf(el), ca = cosf(az), sa = sinf(az);
+    float fd[3] = {ce * ca, se, ce * sa};
+    const float fl = sqrtf((fd[0] * fd[0] + fd[1] * fd[1]) + fd[2] * fd[2]);
+    if (fl > 1e-6f) {
+        fd[0] /= fl; fd[1] /= fl; fd[2] /= fl;
+    } else {
+        fd[0] = 1.0f; fd[1] = 0.0f; fd[2] = 0.0f;
+    }
+    if (g_vertices.size() >= 9) {
+        float proj = 0.0f;
+        const size_t ntri = g_vertices.size() / 9;
+        for (size_t t = 0; t < ntri; ++t) {
+            const float* v = g_vertices.data() + 9 * t;
+            const float e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+            const float e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+            const float c[3] = {e1[1] * e2[2] - e2[1] * e1[2], e1[2] * e2[0] - e2[2] * e1[0],
+                                e1[0] * e2[1] - e2[0] * e1[1]};
+            const float d = (c[0] * c[0] + c[1] * c[1]) + c[2] * c[2];
+            const float area = 0.5f * sqrtf(d);
+            if (!std::isfinite(area) || area < 1e-12f) continue;
+            const float inv = 1.0f / sqrtf(d);   // glm::normalize: v * inversesqrt(dot(v, v))
+            const float n[3] = {c[0] * inv, c[1] * inv, c[2] * inv};
+            proj += area * fabsf((n[0] * fd[0] + n[1] * fd[1]) + n[2] * fd[2]);
+        }
+        const float frontal = proj * 0.5f;
+        if (std::isfinite(frontal) && frontal > 1e-6f && frontal < 1e6f) return frontal;
+    }
+    float sy = maxBB.y - minBB.y, sz = maxBB.z - minBB.z, sx = maxBB.x - minBB.x;
+    if (!std::isfinite(sy) || sy < 0.01f) sy = maxDim;
+    if (!std::isfinite(sz) || sz < 0.01f) sz = maxDim;
+    if (!std::isfinite(sx) || sx < 0.01f) sx = maxDim;
+    float area = (fabsf(fd[0]) * sy * sz + fabsf(fd[1]) * sx * sz + fabsf(fd[2]) * sx * sy);
+    if (!std::isfinite(area) || area < 1e-6f) area = maxDim * maxDim * 0.5f;
+    return area;
+}
+
 void computeLiftDrag() {
     if (!g_handle || g_vertices.size() < 9 || g_normals.size() != g_vertices.size()) return;   // forces.cpp:403-406
     if (!g_world_read && !read_world()) return;

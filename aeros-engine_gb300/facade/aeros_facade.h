@@ -236,6 +236,11 @@ extern float liftMagnitude, dragMagnitude, liftToDragRatio, momentMagnitude;
 extern LbmVec3 liftVector, dragVector, momentVector, centerOfPressure;
 extern long long aeroCpNonFinite;
 void computeLiftDrag();
+// computeLBMRefArea (lbm.cpp:2111-2160): with aeroAutoRefArea, the frontal area of g_vertices
+// along the flowAzimuth / flowElevation direction (half the sum of area x |cos|), else the
+// bounding-box projection; without it, aeroRefArea (1 when not positive). Host FP32, in the
+// reference's order.
+float computeLBMRefArea();
 
 // ---- extras of this layer ----------------------------------------------------
 // The C-ABI handle (NULL before initLBM): for callers that also use the batch

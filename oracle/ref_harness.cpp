@@ -426,6 +426,20 @@ void ref_sample(int field, const float* pts, long long n, float* out, uint8_t* v
     }
 }
 
+// computeLBMRefArea (lbm.cpp:2111-2160) of a triangle soup and settings.
+float ref_ref_area(const float* v, long long ntri, float az, float el, int auto_area, float area_in, const float* bbmin,
+                   const float* bbmax, float max_dim) {
+    g_vertices.assign(v, v + 9 * ntri);
+    flowAzimuth = az;
+    flowElevation = el;
+    aeroAutoRefArea = auto_area != 0;
+    aeroRefArea = area_in;
+    minBB = glm::vec3(bbmin[0], bbmin[1], bbmin[2]);
+    maxBB = glm::vec3(bbmax[0], bbmax[1], bbmax[2]);
+    maxDim = max_dim;
+    return computeLBMRefArea();
+}
+
 // The atmosphere global the readback's pressure scale uses; computeLiftDrag's
 // updateFlowParams rewrites it from the altitude (atmosphere.cpp:175-190).
 void ref_set_air_density(float rho) { airDensity = rho; }

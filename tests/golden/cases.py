@@ -358,3 +358,9 @@ SURFACE_CASES = {
     "no_flow": dict(case="sphere_trt_les_conv", mesh="sphere", sdf=False, aero=dict(flow_speed=0.0)),
     "empty_mesh": dict(case="sphere_trt_les_conv", mesh="empty", sdf=False, aero={}),
 }
+
+
+# computeLBMRefArea (lbm.cpp:2111-2160) settings: (mesh kind, azimuth, elevation, automatic, fixed area)
+REF_AREA_CASES = [("sphere", 0.0, 0.0, 1, 1.0), ("sphere", 37.0, -20.0, 1, 1.0), ("degenerate", 90.0, 45.0, 1, 1.0),
+                  ("huge", 90.0, 0.0, 1, 1.0), ("empty", 15.0, 5.0, 1, 1.0), ("sphere", 0.0, 0.0, 0, 30.0),
+                  ("sphere", 0.0, 0.0, 0, -1.0)]

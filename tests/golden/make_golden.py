@@ -161,6 +161,16 @@ def surface_fixtures(R) -> dict:
         out[name] = dict(result=res, world=wp, mesh=digest(np.concatenate([v.reshape(-1), n.reshape(-1)])),
                          sdf=digest(sdf) if sdf is not None else None)
         print(f"  {name}: drag {r.drag:.6g} lift {r.lift:.6g} area {r.ref_area:.6g}")
+    from cases import REF_AREA_CASES
+    areas = []
+    for kind, az, el, auto, area in REF_AREA_CASES:
+        v, _ = surface_mesh(kind)
+        d = SURFACE_DEFAULTS
+        bmin, bmax = np.asarray(d["bb_min"], np.float32), np.asarray(d["bb_max"], np.float32)
+        areas.append(float(R.L.ref_ref_area(O.fptr(np.ascontiguousarray(v, np.float32).reshape(-1)), v.shape[0], az, el,
+                                            auto, area, O.fptr(bmin), O.fptr(bmax), d["max_dim"])))
+    out["ref_area_cases"] = areas
+    print(f"  computeLBMRefArea: {areas}")
     return out
 
 

@@ -38,6 +38,28 @@ def test_facade_builds_and_links(driver, voxel_driver):
     assert os.path.exists(driver) and os.path.exists(voxel_driver)
 
 
+def test_facade_ref_area_equals_reference(driver, tmp_path):
+    """computeLBMRefArea through the facade (host FP32) equals the reference's
+    own (tests/golden/surface.json) on every setting: frontal areas along
+    oblique directions, skipped triangles, the box fallback, the fixed area."""
+    import json
+    from golden.cases import REF_AREA_CASES, SURFACE_DEFAULTS, surface_mesh
+    exe = str(tmp_path / "refarea_driver")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", "-Werror",
+                           "-I", os.path.join(PKG, "facade"), os.path.join(ROOT, "tests", "facade", "refarea_driver.cpp"),
+                           "-o", exe, "-L" + LIB, "-laeros_facade", "-laeros_gb300", "-Wl,-rpath," + LIB])
+    want = json.load(open(os.path.join(ROOT, "tests", "golden", "surface.json")))["ref_area_cases"]
+    d = SURFACE_DEFAULTS
+    for (kind, az, el, auto, area), w in zip(REF_AREA_CASES, want):
+        v, _ = surface_mesh(kind)
+        f = tmp_path / f"{kind}.bin"
+        np.ascontiguousarray(v, np.float32).tofile(f)
+        args = [exe, str(f), repr(az), repr(el), str(auto), repr(area), *[repr(x) for x in d["bb_min"]],
+                *[repr(x) for x in d["bb_max"]], repr(d["max_dim"])]
+        got = np.float32(subprocess.check_output(args, text=True).strip())
+        assert got == np.float32(w), (kind, az, el, got, w)
+
+
 NPTS = 64   # tests/facade/channel_driver.cpp
 
 

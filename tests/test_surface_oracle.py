@@ -61,7 +61,7 @@ def test_surface_cases_cover_the_branches():
     """The fixtures reach every branch the pass has: Karman-Tsien only, with
     wave drag, wave drag only, ground effect on a downforce, the box fallback
     of the reference area, skipped triangles, and both early returns."""
-    res = {k: SURF[k]["result"] for k in SURF}
+    res = {k: SURF[k]["result"] for k in SURFACE_CASES}
     assert res["karman_tsien_wave_m082"]["drag"] > 3 * res["karman_tsien_m044"]["drag"]
     assert res["fixed_area_ground_angles"]["lift"] < 0 and res["fixed_area_ground_angles"]["ref_area"] == 30.0
     assert res["huge_box_area"]["drag"] != res["plain"]["drag"]
