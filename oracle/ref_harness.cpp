@@ -440,6 +440,9 @@ float ref_ref_area(const float* v, long long ntri, float az, float el, int auto_
     return computeLBMRefArea();
 }
 
+// Overwrites one cell of the last step's world pressure (lbmPressure).
+void ref_poke_pressure(long long cell, float value) { lbmPressure[(size_t)cell] = value; }
+
 // The atmosphere global the readback's pressure scale uses; computeLiftDrag's
 // updateFlowParams rewrites it from the altitude (atmosphere.cpp:175-190).
 void ref_set_air_density(float rho) { airDensity = rho; }

@@ -104,3 +104,51 @@ def test_surface_oracle_field_form_equals_state_form():
         assert np.array_equal(cpa.view(np.int32), cpb.view(np.int32))
         assert np.array_equal(out_vector(a).view(np.int32), out_vector(b).view(np.int32))
         assert list(a.sums) == list(b.sums)
+
+
+@pytest.mark.skipif(not O.RefHarness.available(), reason="reference build not present")
+def test_surface_non_finite_cp_counted_as_reference():
+    """A Cp that overflows FP32 (a huge finite pressure in front of the body
+    at a low freestream speed): the reference zeroes that Cp and counts it in
+    aeroCpNonFinite; the restatement over the same poked field does the same,
+    bit for bit."""
+    from aeros_gb300 import capi
+    from golden.cases import CASES, POST_FLOW_SPEED, SURFACE_DEFAULTS, surface_mesh
+    name = "plain"
+    sc = SURFACE_CASES[name]
+    case = CASES[sc["case"]]
+    nx, ny, nz = case["grid"]
+    R = O.RefHarness()
+    R.L.ref_set_air_density(SURF[name]["world"][1])
+    R.setup(nx, ny, nz, case["solid"]().astype(np.uint8).reshape(-1), **dict(case["kw"], flow_speed=POST_FLOW_SPEED))
+    R.step(case["steps"])
+    fields, _, wp8 = R.world()
+    # a block of cells just upstream of the sphere (centre 12, 12, 12, radius 4), where the front
+    # triangles sample
+    p = fields["pressure"].copy()
+    for z in range(11, 14):
+        for y in range(11, 14):
+            for x in (6, 7):
+                c = (z * ny + y) * nx + x
+                R.L.ref_poke_pressure(c, 3e38)
+                p[c] = np.float32(3e38)
+    v, n = surface_mesh(sc["mesh"])
+    aero = dict(SURFACE_DEFAULTS, flow_speed=0.1)   # q = 0.006 Pa: 3e38 / q overflows
+    r = R.lift_drag(v, n, None, **aero)
+    assert r.cp_bad > 0
+    sp = capi.make_surface(velocity=list(r.vel), air_temperature=r.air_temperature, air_density=r.air_density,
+                           use_real_density=aero["use_real_density"], speed_of_sound=r.speed_of_sound,
+                           mach_effects=aero["mach_effects"], auto_ref_area=aero["auto_ref_area"],
+                           ref_area=aero["ref_area"], azimuth=aero["azimuth"], elevation=aero["elevation"],
+                           bb_min=aero["bb_min"], bb_max=aero["bb_max"], center=aero["center"],
+                           max_dim=aero["max_dim"], reynolds=r.re_number, ground_effect=aero["ground_effect"],
+                           ground_height=aero["ground_height"], vox_min_y=r.vox_min_y)
+    w = capi.make_world(wp8[0], wp8[1], wp8[2:5], wp8[5:8])
+    wall = (R.mask().reshape(-1) != 0).astype(np.uint8)
+    o, cp = O.surface_forces_field(p, wall, (nx, ny, nz), w, sp, v, n, f32_sums=True)
+    assert o.cp_non_finite == r.cp_bad
+    print(f"non-finite Cp: {r.cp_bad} triangles")
+    got = out_vector(o)
+    want = np.array([r.drag, r.lift, r.ld, r.moment_mag, *r.drag_vec, *r.lift_vec, *r.moment, *r.cop, r.ref_area],
+                    np.float32)
+    assert np.array_equal(got.view(np.int32), want.view(np.int32)), (got, want)
