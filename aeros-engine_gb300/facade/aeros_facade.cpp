@@ -436,6 +436,21 @@ float computeLBMRefArea() {
     return area;
 }
 
+float computeLBMRe() {
+    float T = lbmFacadeAirTemperature;   // airSutherlandViscosity, flow_field.h:46-54
+    if (!std::isfinite(T) || T < 50.0f) T = 288.15f;
+    if (T > 2000.0f) T = 2000.0f;
+    const float T0 = 273.15f, S = 110.4f, mu0 = 1.716e-5f;
+    float mu = mu0 * powf(T / T0, 1.5f) * (T0 + S) / (T + S);
+    if (!std::isfinite(mu) || mu < 1e-7f) mu = 1.81e-5f;
+    float L = maxDim;
+    if (L < 1e-6f) L = 1.0f;
+    float re = lbmFacadeAirDensity * lbmFacadeFlowSpeed * L / mu;
+    if (!std::isfinite(re)) re = aeroReNumber;
+    if (re > 1e9f) re = 1e9f;
+    return re;
+}
+
 void computeLiftDrag() {
     if (!g_handle || g_vertices.size() < 9 || g_normals.size() != g_vertices.size()) return;   // forces.cpp:403-406
     if (!g_world_read && !read_world()) return;

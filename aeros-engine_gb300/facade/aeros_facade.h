@@ -241,6 +241,9 @@ void computeLiftDrag();
 // bounding-box projection; without it, aeroRefArea (1 when not positive). Host FP32, in the
 // reference's order.
 float computeLBMRefArea();
+// computeLBMRe (lbm.cpp:2094-2108): air density x flow speed x maxDim / the Sutherland viscosity
+// at lbmFacadeAirTemperature (flow_field.h:46-54); aeroReNumber when not finite; at most 1e9.
+float computeLBMRe();
 
 // ---- extras of this layer ----------------------------------------------------
 // The C-ABI handle (NULL before initLBM): for callers that also use the batch

@@ -366,6 +366,8 @@ class RefHarness:
         L.ref_stl_get.argtypes = [_FP, _FP]
         L.ref_set_air_density.argtypes = [C.c_float]
         L.ref_poke_pressure.argtypes = [C.c_longlong, C.c_float]
+        L.ref_lbm_re.restype = C.c_float
+        L.ref_lbm_re.argtypes = [C.c_float] * 5
         L.ref_ref_area.restype = C.c_float
         L.ref_ref_area.argtypes = [_FP, C.c_longlong, C.c_float, C.c_float, C.c_int, C.c_float, _FP, _FP, C.c_float]
         L.ref_lift_drag.argtypes = [_FP, _FP, C.c_longlong, _FP, C.POINTER(RefAeroIn), C.POINTER(RefAeroOut)]

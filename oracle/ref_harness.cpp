@@ -440,6 +440,16 @@ float ref_ref_area(const float* v, long long ntri, float az, float el, int auto_
     return computeLBMRefArea();
 }
 
+// computeLBMRe (lbm.cpp:2094-2108) with the globals it reads.
+float ref_lbm_re(float T, float rho, float speed, float max_dim, float re_prev) {
+    airTemperature = T;
+    airDensity = rho;
+    flowSpeed = speed;
+    maxDim = max_dim;
+    aeroReNumber = re_prev;
+    return computeLBMRe();
+}
+
 // Overwrites one cell of the last step's world pressure (lbmPressure).
 void ref_poke_pressure(long long cell, float value) { lbmPressure[(size_t)cell] = value; }
 

@@ -364,3 +364,7 @@ SURFACE_CASES = {
 REF_AREA_CASES = [("sphere", 0.0, 0.0, 1, 1.0), ("sphere", 37.0, -20.0, 1, 1.0), ("degenerate", 90.0, 45.0, 1, 1.0),
                   ("huge", 90.0, 0.0, 1, 1.0), ("empty", 15.0, 5.0, 1, 1.0), ("sphere", 0.0, 0.0, 0, 30.0),
                   ("sphere", 0.0, 0.0, 0, -1.0)]
+
+# computeLBMRe (lbm.cpp:2094-2108) inputs: (air temperature K, air density, flow speed, maxDim, previous aeroReNumber)
+RE_CASES = [(288.15, 1.225, 12.5, 13.856406, 0.0), (216.65, 0.3639, 250.0, 40.0, 0.0), (30.0, 1.0, 5.0, 1e-9, 0.0),
+            (3000.0, 0.5, 20.0, 2.0, 0.0), (300.0, 1.2, 1e9, 10.0, 0.0), (300.0, 1.2, float("inf"), 10.0, 123.0)]

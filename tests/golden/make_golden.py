@@ -170,6 +170,9 @@ def surface_fixtures(R) -> dict:
         areas.append(float(R.L.ref_ref_area(O.fptr(np.ascontiguousarray(v, np.float32).reshape(-1)), v.shape[0], az, el,
                                             auto, area, O.fptr(bmin), O.fptr(bmax), d["max_dim"])))
     out["ref_area_cases"] = areas
+    from cases import RE_CASES
+    out["re_cases"] = [float(R.L.ref_lbm_re(*c)) for c in RE_CASES]
+    print(f"  computeLBMRe: {out['re_cases']}")
     print(f"  computeLBMRefArea: {areas}")
     return out
 

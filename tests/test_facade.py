@@ -60,6 +60,23 @@ def test_facade_ref_area_equals_reference(driver, tmp_path):
         assert got == np.float32(w), (kind, az, el, got, w)
 
 
+def test_facade_reynolds_equals_reference(driver, tmp_path):
+    """computeLBMRe through the facade equals the reference's own
+    (tests/golden/surface.json): sea level, the stratosphere, the clamps of
+    the Sutherland viscosity and of the length, the 1e9 cap, a non-finite
+    result falling back to the previous number."""
+    import json
+    from golden.cases import RE_CASES
+    exe = str(tmp_path / "re_driver")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", "-Werror",
+                           "-I", os.path.join(PKG, "facade"), os.path.join(ROOT, "tests", "facade", "re_driver.cpp"),
+                           "-o", exe, "-L" + LIB, "-laeros_facade", "-laeros_gb300", "-Wl,-rpath," + LIB])
+    want = json.load(open(os.path.join(ROOT, "tests", "golden", "surface.json")))["re_cases"]
+    for c, w in zip(RE_CASES, want):
+        got = np.float32(subprocess.check_output([exe, *[repr(float(x)) for x in c]], text=True).strip())
+        assert got == np.float32(w), (c, got, w)
+
+
 NPTS = 64   # tests/facade/channel_driver.cpp
 
 
