@@ -451,6 +451,13 @@ float computeLBMRe() {
     return re;
 }
 
+float lbmReynolds = 0.0f;
+
+void computeLBMForcesFromLBM() {
+    lbmReynolds = computeLBMRe();
+    aeroReNumber = lbmReynolds;
+}
+
 void computeLiftDrag() {
     if (!g_handle || g_vertices.size() < 9 || g_normals.size() != g_vertices.size()) return;   // forces.cpp:403-406
     if (!g_world_read && !read_world()) return;

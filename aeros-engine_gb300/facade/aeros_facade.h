@@ -244,6 +244,9 @@ float computeLBMRefArea();
 // computeLBMRe (lbm.cpp:2094-2108): air density x flow speed x maxDim / the Sutherland viscosity
 // at lbmFacadeAirTemperature (flow_field.h:46-54); aeroReNumber when not finite; at most 1e9.
 float computeLBMRe();
+// computeLBMForcesFromLBM (lbm.cpp:2258-2261): lbmReynolds = aeroReNumber = computeLBMRe().
+extern float lbmReynolds;
+void computeLBMForcesFromLBM();
 
 // ---- extras of this layer ----------------------------------------------------
 // The C-ABI handle (NULL before initLBM): for callers that also use the batch

@@ -1,5 +1,6 @@
 // computeLBMRe through the C++17 facade: argv = air temperature (K), air
-// density, flow speed, maxDim, previous aeroReNumber; prints the number.
+// density, flow speed, maxDim, previous aeroReNumber; prints the number, then
+// lbmReynolds and aeroReNumber after computeLBMForcesFromLBM.
 #include <cstdio>
 #include <cstdlib>
 
@@ -12,6 +13,8 @@ int main(int argc, char** argv) {
     lbmFacadeFlowSpeed = std::strtof(argv[3], nullptr);
     maxDim = std::strtof(argv[4], nullptr);
     aeroReNumber = std::strtof(argv[5], nullptr);
-    std::printf("%.9g\n", computeLBMRe());
+    const float re = computeLBMRe();
+    computeLBMForcesFromLBM();
+    std::printf("%.9g %.9g %.9g\n", re, lbmReynolds, aeroReNumber);
     return 0;
 }
