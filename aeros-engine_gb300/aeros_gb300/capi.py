@@ -248,6 +248,11 @@ _SIGS = {
     "aeros_sdf_device": (C.c_int, [_P, C.POINTER(VoxelGrid), _P, _P]),
     "aeros_sdf": (C.c_int, [_U8P, C.POINTER(VoxelGrid), _FP]),
     "aeros_sdf_sample": (C.c_int, [_P, C.POINTER(VoxelGrid), _FP, C.c_int64, _FP, _FP]),
+    "aeros_sdf_field_create": (C.c_int, [_U8P, C.POINTER(VoxelGrid), C.POINTER(_P)]),
+    "aeros_sdf_field_destroy": (C.c_int, [_P]),
+    "aeros_sdf_field_device": (_P, [_P]),
+    "aeros_sdf_field_read": (C.c_int, [_P, _FP]),
+    "aeros_sdf_field_sample": (C.c_int, [_P, _FP, C.c_int64, _FP, _FP]),
     "aeros_sdf_last_stats": (C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "aeros_stl_detect": (C.c_int, [C.c_char_p, C.c_uint64, C.POINTER(StlInfo)]),
     "aeros_stl_parse": (C.c_int, [C.c_char_p, C.c_uint64, C.c_uint64, _FP, _FP, C.c_int64, C.POINTER(StlInfo)]),

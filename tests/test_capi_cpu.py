@@ -31,6 +31,11 @@ def test_library_exports_every_declared_symbol(lib):
     assert not missing, missing
 
 
+def test_ctypes_table_covers_every_declared_symbol(lib):
+    """The Python host binds every entry point the headers declare."""
+    assert sorted(set(lib.header_symbols()) - set(lib._SIGS)) == []
+
+
 def test_struct_layout_matches_c(lib):
     src = r'''
 #include <stdio.h>
