@@ -18,6 +18,7 @@ AEROS_CELL_FLUID, AEROS_CELL_SOLID, AEROS_CELL_GROUND = 0, 1, 2
 AEROS_STORE_FP32, AEROS_STORE_FP16, AEROS_STORE_BF16 = 0, 1, 2
 AEROS_LATERAL_COPY, AEROS_LATERAL_FREESLIP = 0, 1
 AEROS_OUTLET_REFERENCE, AEROS_OUTLET_ZEROGRAD = 0, 1
+AEROS_SHIFT_FREESTREAM, AEROS_SHIFT_WEIGHTS = 0, 1
 STORAGE_NAMES = {"fp32": AEROS_STORE_FP32, "fp16": AEROS_STORE_FP16, "bf16": AEROS_STORE_BF16}
 
 
@@ -32,7 +33,7 @@ class LbmParams(C.Structure):
         ("u_in", C.c_float * 3), ("u_init", C.c_float * 3), ("body_force", C.c_float * 3),
         ("vel_scale", C.c_float), ("convergence_threshold", C.c_float),
         ("storage", C.c_int32), ("lateral_bc", C.c_int32), ("outlet_bc", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("storage_shift", C.c_int32), ("reserved", C.c_int32 * 7),
     ]
 
 
@@ -111,7 +112,8 @@ def make_params(nx, ny, nz, *, tau=0.6, smagorinsky_c=0.12, les=False, trt=False
                 periodic_x=False, periodic_z=False, convective_outlet=False,
                 flow_axis=0, flow_sign=1, u_in=(0.08, 0.0, 0.0), u_init=None,
                 body_force=(0.0, 0.0, 0.0), vel_scale=1.0, convergence_threshold=1e-5,
-                storage="fp32", lateral_bc=AEROS_LATERAL_COPY, outlet_bc=AEROS_OUTLET_REFERENCE) -> LbmParams:
+                storage="fp32", lateral_bc=AEROS_LATERAL_COPY, outlet_bc=AEROS_OUTLET_REFERENCE,
+                storage_shift=AEROS_SHIFT_FREESTREAM) -> LbmParams:
     """Builds an LbmParams with the reference's LBMParams defaults where not given."""
     p = LbmParams()
     p.nx, p.ny, p.nz = int(nx), int(ny), int(nz)
@@ -129,6 +131,7 @@ def make_params(nx, ny, nz, *, tau=0.6, smagorinsky_c=0.12, les=False, trt=False
     p.convergence_threshold = float(convergence_threshold)
     p.storage = STORAGE_NAMES[storage] if isinstance(storage, str) else int(storage)
     p.lateral_bc, p.outlet_bc = int(lateral_bc), int(outlet_bc)
+    p.storage_shift = int(storage_shift)
     return p
 
 
@@ -236,7 +239,7 @@ _SIGS = {
     "aeros_lbm_projected_area": (C.c_int, [_P, C.c_int, _DP]),
     "aeros_voxelize": (C.c_int, [_FP, C.c_int64, C.POINTER(VoxelGrid), _U8P]),
     "aeros_voxelize_device": (C.c_int, [_FP, C.c_int64, C.POINTER(VoxelGrid), _P]),
-    "aeros_voxelize_device_noalloc": (C.c_int, [_FP, C.c_int64, C.POINTER(VoxelGrid), _P]),
+    "aeros_voxelize_device_noalloc": (C.c_int, [_FP, C.c_int64, C.POINTER(VoxelGrid), _P, _P]),
     "aeros_voxel_plan": (C.c_int, [_FP, C.c_int, C.c_uint64, C.POINTER(VoxelPlan)]),
     "aeros_lbm_last_step_ms": (C.c_int, [_P, _FP]),
     "aeros_lbm_last_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),

@@ -103,6 +103,11 @@ def domain_for(req: Request, storage="fp16", u_in=0.05, smag=0.1):
     return s, box, area, len(tris), u_in
 
 
+# Device memory the library holds in every context that loads it, whether or
+# not it is used: the fixed 24 MiB array of the no-allocation voxelizer.
+LIBRARY_STATIC_BYTES = 24 << 20
+
+
 def footprint_estimate(req: Request, storage="fp16") -> int:
     """Device bytes of a request before it is created: per cell populations
     (19 x 2 or 4 B), descriptor, two velocity buffers, rho / |S| / TKE and the
@@ -128,7 +133,7 @@ class Server:
         if check_every % chunk or chunk % 2:
             raise ValueError("chunk must be even and divide check_every")
         self.storage = storage
-        self.budget = int(budget_bytes)
+        self.budget = int(budget_bytes) - LIBRARY_STATIC_BYTES
         self.slots = int(slots)
         self.check_every = int(check_every)
         self.tol = float(tol)

@@ -27,13 +27,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-warn-spills"]
 # resident blocks per SM the step kernel's register budget targets (tuning knob)
 MIN_BLOCKS = os.environ.get("AEROS_STEP_MIN_BLOCKS", "6")
-STAGED_MIN_BLOCKS = os.environ.get("AEROS_STAGED_MIN_BLOCKS", "6")
 FUSED_MIN_BLOCKS = os.environ.get("AEROS_FUSED_MIN_BLOCKS", "8")
 BATCH_MIN_BLOCKS = os.environ.get("AEROS_BATCH_MIN_BLOCKS", "4")
 FUSED_ODD_MIN_BLOCKS = os.environ.get("AEROS_FUSED_ODD_MIN_BLOCKS", FUSED_MIN_BLOCKS)
 FUSED_TH_MIN_BLOCKS = os.environ.get("AEROS_FUSED_TH_MIN_BLOCKS", "6")
 STEP_BLOCK = os.environ.get("AEROS_STEP_BLOCK", "128")
-TAG = (f"mb{MIN_BLOCKS}s{STAGED_MIN_BLOCKS}f{FUSED_MIN_BLOCKS}o{FUSED_ODD_MIN_BLOCKS}t{FUSED_TH_MIN_BLOCKS}"
+TAG = (f"mb{MIN_BLOCKS}f{FUSED_MIN_BLOCKS}o{FUSED_ODD_MIN_BLOCKS}t{FUSED_TH_MIN_BLOCKS}"
        f"b{BATCH_MIN_BLOCKS}" + f"k{STEP_BLOCK}")
 UNITS = {
     "lbm_fp32.cu": ["--fmad=false"],
@@ -71,7 +70,7 @@ def _compile(unit: str, flags: list[str], verbose: bool) -> str:
     obj = os.path.join(BUILD_DIR, f"{os.path.splitext(unit)[0]}.{TAG}.o")
     if _stale(obj, src):
         cmd = [nvcc(), *ARCH, *COMMON, f"-DAEROS_STEP_MIN_BLOCKS={MIN_BLOCKS}",
-               f"-DAEROS_STAGED_MIN_BLOCKS={STAGED_MIN_BLOCKS}", f"-DAEROS_FUSED_MIN_BLOCKS={FUSED_MIN_BLOCKS}",
+               f"-DAEROS_FUSED_MIN_BLOCKS={FUSED_MIN_BLOCKS}",
                f"-DAEROS_BATCH_MIN_BLOCKS={BATCH_MIN_BLOCKS}", f"-DAEROS_FUSED_ODD_MIN_BLOCKS={FUSED_ODD_MIN_BLOCKS}",
                f"-DAEROS_FUSED_TH_MIN_BLOCKS={FUSED_TH_MIN_BLOCKS}", f"-DAEROS_STEP_BLOCK={STEP_BLOCK}",
                *flags, "-c", src, "-o", obj]

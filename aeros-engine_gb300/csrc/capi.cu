@@ -305,6 +305,7 @@ static void fill_args(const aeros_lbm* h, FillArgs& fa, const float u[3]) {
     for (int q = 0; q < Q19; ++q) {
         fa.fluid[q] = eq_checked(q, 1.0f, vx, vy, vz, usqr);
         fa.wall[q] = eq_checked(q, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f);
+        fa.dq[q] = h->shift.d[q];
     }
 }
 
@@ -322,6 +323,8 @@ static int check_params(const aeros_lbm_params* p) {
         return set_error(AEROS_ERR_INVALID, "unknown lateral_bc %d", p->lateral_bc);
     if (p->outlet_bc != AEROS_OUTLET_REFERENCE && p->outlet_bc != AEROS_OUTLET_ZEROGRAD)
         return set_error(AEROS_ERR_INVALID, "unknown outlet_bc %d", p->outlet_bc);
+    if (p->storage_shift != AEROS_SHIFT_FREESTREAM && p->storage_shift != AEROS_SHIFT_WEIGHTS)
+        return set_error(AEROS_ERR_INVALID, "unknown storage_shift %d", p->storage_shift);
     if (p->lateral_bc == AEROS_LATERAL_FREESLIP && !p->periodic_x && p->flow_axis != 0 &&
         p->outlet_bc == AEROS_OUTLET_REFERENCE && !p->convective_outlet)
         return set_error(AEROS_ERR_UNSUPPORTED, "free-slip lateral walls need an overriding outlet");
@@ -353,7 +356,6 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (const char* e = getenv("AEROS_STAGED")) h->staged = atoi(e) != 0;
     if (const char* e = getenv("AEROS_SPLIT")) h->split = atoi(e) != 0;
     if (const char* e = getenv("AEROS_FUSED")) h->fused = atoi(e) != 0;
     if (const char* e = getenv("AEROS_SHELL_BLOCKS")) h->shell_blocks_per_sm = std::max(1, std::min(8, atoi(e)));
@@ -367,7 +369,6 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         free_handle(h);                          \
         return rc;                               \
     }
-    // staged copies round ranges up to 16 bytes: pad the arrays they read
     ALLOC(h->f, ((size_t)h->qstride * Q19 + 64) * h->esize);
     ALLOC(h->desc, (n + 64) * 4);
     ALLOC(h->shell, (size_t)std::max(1, h->n_shell) * 4);
@@ -463,6 +464,18 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         const float v = eq_checked(q, 1.0f, ui0, ui1, ui2, usq);
         h->feq_in[q] = shifted ? v - w19(q) : v;
     }
+    if (shifted && params->storage_shift == AEROS_SHIFT_FREESTREAM) {
+        // s_q - w_q = w_q (3 c.u + 4.5 (c.u)^2 - 1.5 u^2), u = the inlet velocity
+        // (the velocity the far field relaxes to), or the initial velocity of a
+        // domain without an inlet; evaluated in double, rounded once
+        const float* us = params->periodic_x ? params->u_init : params->u_in;
+        const double sx = us[0], sy = us[1], sz = us[2];
+        const double u2 = sx * sx + sy * sy + sz * sz;
+        for (int q = 0; q < Q19; ++q) {
+            const double cu = cx19(q) * sx + cy19(q) * sy + cz19(q) * sz;
+            h->shift.d[q] = (float)((double)w19(q) * (3.0 * cu + 4.5 * cu * cu - 1.5 * u2));
+        }
+    }
     float U0mag = sqrtf(usq);
     if (!std::isfinite(U0mag) || U0mag < 1e-6f) U0mag = 0.08f;
     float conv = U0mag * 0.8f;
@@ -520,6 +533,24 @@ extern "C" int aeros_lbm_synchronize(aeros_lbm* h) {
     return AEROS_OK;
 }
 
+// Shift of the 16-bit D3Q7 storage: the conduction profile between fixed
+// wall temperatures (hot wall row 0, cold wall row ny-1, the profile the
+// walls impose: hot at y = 0.5, cold at y = ny - 1.5), else Tref.
+static ShiftT th_shift(const aeros_lbm* h) {
+    ShiftT ts;
+    ts.nx = h->nx;
+    ts.ny = h->ny;
+    const float hot = h->tp.hot_temp, cold = h->tp.cold_temp;
+    if (h->tp.fixed_wall_temps && h->ny > 2) {
+        ts.tc1 = (cold - hot) / (float)(h->ny - 2);
+        ts.tc0 = hot - 0.5f * ts.tc1;
+    } else {
+        ts.tc0 = 0.5f * (hot + cold);
+        ts.tc1 = 0.0f;
+    }
+    return ts;
+}
+
 void base_args(const aeros_lbm* h, StepArgs& A) {
     memset(&A, 0, sizeof(A));
     A.nx = h->nx; A.ny = h->ny; A.nz = h->nz; A.nxny = h->nx * h->ny; A.ncell = h->ncell;
@@ -560,6 +591,13 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     A.Fx = p.body_force[0]; A.Fy = p.body_force[1]; A.Fz = p.body_force[2];
     for (int i = 0; i < 3; ++i) A.uin[i] = p.u_in[i];
     for (int q = 0; q < Q19; ++q) A.feq_in[q] = h->feq_in[q];
+    {
+        const float sc = h->p.storage == AEROS_STORE_FP16 ? STORE_SCALE_F16 : 1.0f;
+        for (int q = 0; q < Q19; ++q) {
+            A.dq[q] = h->shift.d[q];
+            A.dqs[q] = h->shift.d[q] * sc;   // a power of two: exact
+        }
+    }
     A.conv = h->conv;
     A.flow_axis = p.flow_axis; A.flow_sign = p.flow_sign;
     {
@@ -571,14 +609,13 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     A.freeslip = p.lateral_bc == AEROS_LATERAL_FREESLIP;
     A.outlet_mode = h->outlet_mode;
     A.total_div10 = h->ncell / 10;
-    A.staged = h->staged;
     {
         const int nsh = A.ntiles - A.ntiles_interior;
-        A.fused = h->fused && !h->staged;
+        A.fused = h->fused;
         A.shell_blocks = A.fused ? std::min(nsh, std::max(1, h->sm_count) * h->shell_blocks_per_sm) : 0;
         A.fused_grid = h->fused_grid[0][h->th_on ? 1 : 0];
         A.fused_grid_odd = h->fused_grid[1][h->th_on ? 1 : 0];
-        A.split = h->split && nsh > 0 && !h->staged && !A.fused;
+        A.split = h->split && nsh > 0 && !A.fused;
         A.shell_grid = A.split ? std::min(nsh, std::max(1, h->sm_count) * 4) : 0;
         A.shell_part_base = 0;   // set by the launcher (after the interior grid's slots)
     }
@@ -599,6 +636,9 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
         A.th_hot = h->tp.hot_temp;
         A.th_cold = h->tp.cold_temp;
         A.th_tref = 0.5f * (h->tp.hot_temp + h->tp.cold_temp);
+        const ShiftT ts = th_shift(h);
+        A.th_tc0 = ts.tc0;
+        A.th_tc1 = ts.tc1;
         A.th_glb = h->glb;
         A.th_H = h->H;
         A.th_buoy_mode = h->th_buoy_mode;
@@ -644,10 +684,9 @@ static int normalize_layout(aeros_lbm* h) {
     }
     int rc = launch_materialize(h, df, dg);
     if (rc == AEROS_OK) {
-        cudaError_t e = h->L->write_pre(h->f, h->desc, h->qstride, h->ncell, df, Q19, 0.0f, h->stream);
+        cudaError_t e = h->L->write_pre(h->f, h->desc, h->qstride, h->ncell, df, Q19, th_shift(h), h->shift, h->stream);
         if (e == cudaSuccess && h->th_on)
-            e = h->L->write_pre(h->g, h->desc, h->qstride, h->ncell, dg, Q7,
-                                0.5f * (h->tp.hot_temp + h->tp.cold_temp), h->stream);
+            e = h->L->write_pre(h->g, h->desc, h->qstride, h->ncell, dg, Q7, th_shift(h), h->shift, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) rc = set_error(AEROS_ERR_CUDA, "normalize: %s", cudaGetErrorString(e));
     }
@@ -699,12 +738,6 @@ int finish_batch(aeros_lbm* h) {
     h->stats_dirty = false;
     Control& c = *h->ctl_host;
     aeros_lbm_stats& s = h->stats;
-    if (c.stage_timeout) {
-        c.stage_timeout = 0;
-        CUDA_TRY(cudaMemcpyAsync(&h->ctl->stage_timeout, &c.stage_timeout, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-        CUDA_TRY(cudaStreamSynchronize(h->stream));
-        return set_error(AEROS_ERR_TIMEOUT, "a bounded wait on a staged bulk copy gave up (results used direct loads)");
-    }
     if (c.halt) {
         const long long executed = c.kexec - h->kexec_before;
         const long long launched = h->last_launches;
@@ -877,7 +910,7 @@ extern "C" int aeros_lbm_write_populations(aeros_lbm* h, const float* f) {
     const size_t n = (size_t)h->ncell;
     if (cudaMalloc((void**)&df, n * Q19 * 4) != cudaSuccess) return set_error(AEROS_ERR_ALLOC, "upload buffer");
     cudaError_t e = cudaMemcpyAsync(df, f, n * Q19 * 4, cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess) e = h->L->write_pre(h->f, h->desc, h->qstride, h->ncell, df, Q19, 0.0f, h->stream);
+    if (e == cudaSuccess) e = h->L->write_pre(h->f, h->desc, h->qstride, h->ncell, df, Q19, th_shift(h), h->shift, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     cudaFree(df);
     if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "write populations: %s", cudaGetErrorString(e));
@@ -899,7 +932,7 @@ extern "C" int aeros_lbm_set_equilibrium(aeros_lbm* h, const float* rho, const f
     if (e == cudaSuccess) e = cudaMemcpyAsync(d + 3 * n, uz, n * 4, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess)
         e = h->L->set_equilibrium(h->f, h->desc, h->qstride, h->ncell, rho ? d : nullptr, d + n, d + 2 * n, d + 3 * n,
-                                  h->stream);
+                                  h->shift, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     cudaFree(d);
     if (e != cudaSuccess) return set_error(AEROS_ERR_CUDA, "set equilibrium: %s", cudaGetErrorString(e));
@@ -930,7 +963,7 @@ static int upload_T(aeros_lbm* h, const std::vector<float>& T) {
     CUDA_TRY(cudaMemcpyAsync(h->T, T.data(), T.size() * 4, cudaMemcpyHostToDevice, h->stream));
     StepArgs A;
     base_args(h, A);
-    CUDA_TRY(h->L->thermal_fill(A, 0.5f * (h->tp.hot_temp + h->tp.cold_temp), h->stream));
+    CUDA_TRY(h->L->thermal_fill(A, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return AEROS_OK;
 }
@@ -1194,8 +1227,8 @@ extern "C" int aeros_lbm_projected_area(aeros_lbm* h, int axis, double* area) {
 namespace aeros {
 int voxelize_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask, cudaStream_t s,
                   char* err, size_t errn);
-int voxelize_noalloc_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask, char* err,
-                          size_t errn);
+int voxelize_noalloc_impl(const float* tris, int64_t ntri, const aeros_voxel_grid* g, uint8_t* d_mask,
+                          cudaStream_t s, char* err, size_t errn);
 }
 
 static int check_grid(const float* tris, int64_t ntri, const aeros_voxel_grid* g) {
@@ -1219,11 +1252,11 @@ extern "C" int aeros_voxelize_device(const float* tris, int64_t ntri, const aero
 // Fixed-scratch variant of aeros_voxelize_device for callers that cannot
 // allocate device memory (see voxelize_noalloc_impl in voxel.cu).
 extern "C" int aeros_voxelize_device_noalloc(const float* tris, int64_t ntri, const aeros_voxel_grid* g,
-                                             uint8_t* d_mask) {
+                                             uint8_t* d_mask, void* stream) {
     if (int rc = check_grid(tris, ntri, g)) return rc;
     if (!d_mask) return set_error(AEROS_ERR_INVALID, "mask is NULL");
     char err[512] = {0};
-    const int rc = voxelize_noalloc_impl(tris, ntri, g, d_mask, err, sizeof(err));
+    const int rc = voxelize_noalloc_impl(tris, ntri, g, d_mask, (cudaStream_t)stream, err, sizeof(err));
     if (rc) return set_error(rc, "%s", err);
     return AEROS_OK;
 }

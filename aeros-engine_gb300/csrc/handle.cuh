@@ -69,6 +69,7 @@ struct aeros_lbm {
     int n_interior = 0, n_shell = 0, fluid_cells = 1;
     int outlet_mode = 0;
     float feq_in[19] = {0};
+    aeros::Shift19 shift{};      // shifted storage: s_q - w_q (zero for FP32)
     float conv = 0.08f;
     // layout state of the AA pattern
     bool next_odd = false;        // next step gathers from neighbours
@@ -93,7 +94,6 @@ struct aeros_lbm {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     long long last_launches = 0;
     int sm_count = 0;
-    int staged = 0;               // TMA-staged interior tiles (opt-in: AEROS_STAGED=1)
     int split = 1;                // shell and interior as two launches per step (AEROS_SPLIT=0: one)
     int fused = 1;                // non-thermal: one launch, dynamic warp items (AEROS_FUSED=0: off)
     int shell_blocks_per_sm = 1;  // fused: shell blocks per SM (AEROS_SHELL_BLOCKS)

@@ -61,28 +61,45 @@ constexpr uint32_t D_GROUND = 1u << 29;     // wall cell that is ground, not bod
 constexpr uint32_t D_LINKS = (1u << 19) - 2u;
 
 // ---- population storage ---------------------------------------------------
-// FP32 stores f_i. FP16 / BF16 store the shifted deviation f_i - w_i (and
-// g_i - w_i T_ref for the thermal lattice) and compute in FP32.
+// FP32 stores f_i. FP16 / BF16 store shifted deviations (f_i - s_i for the
+// fluid lattice, g_i - w_i Tc for the thermal one) and compute in FP32.
+// FP16 keeps them times 2^10 (STORE_SCALE_F16): with the freestream shift the
+// far-field deviations are 1e-7 .. 1e-5, below FP16's normal range (6.1e-5),
+// where its spacing is absolute; scaled, they keep 11 significant bits, and
+// |f - s| up to 64 stays finite (the guards treat f outside [-1, 10] as bad).
+// load / store apply the scale; raw_load / raw_store move the stored bits'
+// value and kScale / kInv let a caller fold the scale into its own FMA.
+constexpr float STORE_SCALE_F16 = 1024.0f;
+
 struct StoreF32 {
     using T = float;
     static constexpr bool shifted = false;
+    static constexpr float kScale = 1.0f, kInv = 1.0f;
     __device__ __forceinline__ static float load(const T* p) { return __ldg(p); }
     __device__ __forceinline__ static float load_rw(const T* p) { return *p; }
     __device__ __forceinline__ static void store(T* p, float v) { *p = v; }
+    __device__ __forceinline__ static float raw_load(const T* p) { return *p; }
+    __device__ __forceinline__ static void raw_store(T* p, float v) { *p = v; }
 };
 struct StoreF16 {
     using T = __half;
     static constexpr bool shifted = true;
-    __device__ __forceinline__ static float load(const T* p) { return __half2float(*p); }
-    __device__ __forceinline__ static float load_rw(const T* p) { return __half2float(*p); }
-    __device__ __forceinline__ static void store(T* p, float v) { *p = __float2half_rn(v); }
+    static constexpr float kScale = STORE_SCALE_F16, kInv = 1.0f / STORE_SCALE_F16;
+    __device__ __forceinline__ static float load(const T* p) { return __half2float(*p) * kInv; }
+    __device__ __forceinline__ static float load_rw(const T* p) { return __half2float(*p) * kInv; }
+    __device__ __forceinline__ static void store(T* p, float v) { *p = __float2half_rn(v * kScale); }
+    __device__ __forceinline__ static float raw_load(const T* p) { return __half2float(*p); }
+    __device__ __forceinline__ static void raw_store(T* p, float v) { *p = __float2half_rn(v); }
 };
 struct StoreBF16 {
     using T = __nv_bfloat16;
     static constexpr bool shifted = true;
+    static constexpr float kScale = 1.0f, kInv = 1.0f;
     __device__ __forceinline__ static float load(const T* p) { return __bfloat162float(*p); }
     __device__ __forceinline__ static float load_rw(const T* p) { return __bfloat162float(*p); }
     __device__ __forceinline__ static void store(T* p, float v) { *p = __float2bfloat16_rn(v); }
+    __device__ __forceinline__ static float raw_load(const T* p) { return __bfloat162float(*p); }
+    __device__ __forceinline__ static void raw_store(T* p, float v) { *p = __float2bfloat16_rn(v); }
 };
 
 // ---- exact unsigned division by a run-time constant -------------------------

@@ -30,6 +30,16 @@ struct FillArgs {
     int ncell;
     float fluid[19];   // plain values
     float wall[19];
+    float dq[19];      // shifted storage: s_q - w_q (stored value = f - w - dq)
+};
+
+struct Shift19 {       // s_q - w_q of the shifted storage (zero for FP32)
+    float d[Q19];
+};
+
+struct ShiftT {        // shifted D3Q7 storage: Tc(y) = tc0 + tc1 * y, the grid's nx, ny
+    float tc0, tc1;
+    int nx, ny;
 };
 
 // Uniform equilibrium (initLBM, aeros/src/lbm.cpp:686-739) in pre-collision layout.
@@ -42,14 +52,14 @@ __global__ void k_fill_uniform(const FillArgs a) {
 #pragma unroll
     for (int q = 0; q < Q19; ++q) {
         const float v = wall ? a.wall[q] : a.fluid[q];
-        S::store(f + (long long)q * a.qstride + c, S::shifted ? v - w19(q) : v);
+        S::store(f + (long long)q * a.qstride + c, S::shifted ? (v - w19(q)) - a.dq[q] : v);
     }
 }
 
 // Equilibrium from per-cell rho/u with the init limiter (lbm.cpp:720-737).
 template <class S>
 __global__ void k_set_equilibrium(void* fp, const uint32_t* desc, long long qstride, int ncell, const float* rho,
-                                  const float* ux, const float* uy, const float* uz) {
+                                  const float* ux, const float* uy, const float* uz, const Shift19 sh) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell || (desc[c] & D_WALL)) return;
     const float r = rho ? rho[c] : 1.0f;
@@ -64,22 +74,35 @@ __global__ void k_set_equilibrium(void* fp, const uint32_t* desc, long long qstr
 #pragma unroll
     for (int q = 0; q < Q19; ++q) {
         const float v = eq_checked(q, r, vx, vy, vz, usqr);
-        S::store(f + (long long)q * qstride + c, S::shifted ? v - w19(q) : v);
+        S::store(f + (long long)q * qstride + c, S::shifted ? (v - w19(q)) - sh.d[q] : v);
     }
 }
 
 // Pre-collision populations [19][ncell] (plain values) into the slots the
 // next even step gathers from. Wall cells are left untouched.
+// D3Q7 (nq = 7): the slot of direction i holds g - w_i Tc(y_w), y_w the row
+// of the cell the even step's gather takes it as stored by (y - c_iy on a
+// regular link, y otherwise; only i = 3, 4 move along y).
 template <class S>
 __global__ void k_write_pre(void* fp, const uint32_t* desc, long long qstride, int ncell, const float* src, int nq,
-                            float shift_ref) {
+                            const ShiftT ts, const Shift19 sh) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell || (desc[c] & D_WALL)) return;
     typename S::T* f = reinterpret_cast<typename S::T*>(fp);
+    const int y = (c / ts.nx) % ts.ny;
     for (int q = 0; q < nq; ++q) {
-        const float w = nq == Q19 ? w19(q) : w7(q) * shift_ref;
         const float v = src[(long long)q * ncell + c];
-        S::store(f + (long long)q * qstride + c, S::shifted ? v - w : v);
+        float st = v;
+        if (S::shifted) {
+            if (nq == Q19) {
+                st = (v - w19(q)) - sh.d[q];
+            } else {
+                const bool regular = !((desc[c] >> q) & 1u);
+                const int yw = regular ? y - cy19(q) : y;
+                st = v - w7(q) * fmaf(ts.tc1, (float)yw, ts.tc0);
+            }
+        }
+        S::store(f + (long long)q * qstride + c, st);
     }
 }
 
@@ -92,7 +115,8 @@ __global__ void k_reset(void* fp, const uint32_t* desc, long long qstride, int n
     if (c >= ncell || (desc[c] & D_WALL)) return;
     typename S::T* f = reinterpret_cast<typename S::T*>(fp);
 #pragma unroll
-    for (int q = 0; q < Q19; ++q) S::store(f + (long long)q * qstride + c, S::shifted ? fa.fluid[q] - w19(q) : fa.fluid[q]);
+    for (int q = 0; q < Q19; ++q)
+        S::store(f + (long long)q * qstride + c, S::shifted ? (fa.fluid[q] - w19(q)) - fa.dq[q] : fa.fluid[q]);
     rho[c] = 1.0f;
     u[c] = make_float4(uin0, uin1, uin2, 0.0f);
 }
@@ -103,7 +127,7 @@ __global__ void k_reset(void* fp, const uint32_t* desc, long long qstride, int n
 // post-collision state: they are streamed here once, with the step's own
 // boundary rules, into the slots the next (even) step gathers from.
 template <class S>
-__global__ void k_thermal_prestream(const StepArgs A, float tref) {
+__global__ void k_thermal_prestream(const StepArgs A) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= A.ncell) return;
     const uint32_t d = A.desc[c];
@@ -120,7 +144,7 @@ __global__ void k_thermal_prestream(const StepArgs A, float tref) {
             const float go = w7(opp19(i)) * A.T[c] * (1.0f + 4.0f * 0.0f);
             v = L.bounce == 2 ? (-go + 2.0f * w7(i) * L.Tw) : go;
         }
-        S::store(g + (long long)i * A.qstride + c, S::shifted ? v - w7(i) * tref : v);
+        S::store(g + (long long)i * A.qstride + c, S::shifted ? v - w7(i) * th_tc(A, L.bounce == 0 ? y - cy19(i) : y) : v);
     }
 }
 
@@ -131,12 +155,13 @@ struct Launchers {
     int (*occupancy)(bool odd, bool thermal);
     cudaError_t (*fill_uniform)(const FillArgs& a, cudaStream_t s);
     cudaError_t (*set_equilibrium)(void* f, const uint32_t* desc, long long qstride, int ncell, const float* rho,
-                                   const float* ux, const float* uy, const float* uz, cudaStream_t s);
+                                   const float* ux, const float* uy, const float* uz, const Shift19& sh,
+                                   cudaStream_t s);
     cudaError_t (*write_pre)(void* f, const uint32_t* desc, long long qstride, int ncell, const float* src, int nq,
-                             float shift_ref, cudaStream_t s);
+                             const ShiftT& ts, const Shift19& sh, cudaStream_t s);
     cudaError_t (*reset)(void* f, const uint32_t* desc, long long qstride, int ncell, const FillArgs& fa, float* rho,
                          float4* u, const float* uin, cudaStream_t s);
-    cudaError_t (*thermal_fill)(const StepArgs& A, float tref, cudaStream_t s);
+    cudaError_t (*thermal_fill)(const StepArgs& A, cudaStream_t s);
     cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s);
     int (*batch_occupancy)();
     int (*fused_occupancy)(bool odd, bool thermal);
@@ -157,8 +182,6 @@ const Launchers& launchers_bf16();
             B.shell_part_base = grid;                                                                                 \
             if (B.shell_grid > 0) k_lbm_shell<STORE, O, T><<<B.shell_grid, STEP_BLOCK, 0, s>>>(B, V);                 \
             k_lbm_interior<STORE, O, T><<<grid, STEP_BLOCK, 0, s>>>(B, V);                                            \
-        } else if (!T && !M && A.staged) {                                                                            \
-            k_lbm_step_staged<STORE, O><<<grid, STEP_BLOCK, 0, s>>>(A, V);                                            \
         } else {                                                                                                      \
             k_lbm_step<STORE, O, T, M><<<grid, STEP_BLOCK, 0, s>>>(A, V);                                             \
         }                                                                                                             \
@@ -175,12 +198,8 @@ const Launchers& launchers_bf16();
     }                                                                                                                 \
     template <bool O, bool T>                                                                                         \
     int occ_one() {                                                                                                   \
-        int n = 0, m = 0;                                                                                             \
+        int n = 0;                                                                                                    \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_step<STORE, O, T, false>, STEP_BLOCK, 0);             \
-        if (!T) {                                                                                                     \
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_lbm_step_staged<STORE, O>, STEP_BLOCK, 0);            \
-            n = n < m ? n : m;                                                                                        \
-        }                                                                                                             \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \
     int occupancy_(bool odd, bool thermal) {                                                                          \
@@ -192,13 +211,13 @@ const Launchers& launchers_bf16();
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
     cudaError_t seteq_(void* f, const uint32_t* desc, long long qs, int n, const float* rho, const float* ux,        \
-                       const float* uy, const float* uz, cudaStream_t s) {                                            \
-        k_set_equilibrium<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, rho, ux, uy, uz);                    \
+                       const float* uy, const float* uz, const Shift19& sh, cudaStream_t s) {                         \
+        k_set_equilibrium<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, rho, ux, uy, uz, sh);                \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    cudaError_t writepre_(void* f, const uint32_t* desc, long long qs, int n, const float* src, int nq, float sr,     \
-                          cudaStream_t s) {                                                                           \
-        k_write_pre<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, src, nq, sr);                              \
+    cudaError_t writepre_(void* f, const uint32_t* desc, long long qs, int n, const float* src, int nq,              \
+                          const ShiftT& ts, const Shift19& sh, cudaStream_t s) {                                      \
+        k_write_pre<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, src, nq, ts, sh);                          \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
     cudaError_t reset_(void* f, const uint32_t* desc, long long qs, int n, const FillArgs& fa, float* rho, float4* u,  \
@@ -206,8 +225,8 @@ const Launchers& launchers_bf16();
         k_reset<STORE><<<(n + 255) / 256, 256, 0, s>>>(f, desc, qs, n, fa, rho, u, uin[0], uin[1], uin[2]);           \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    cudaError_t thfill_(const StepArgs& A, float tref, cudaStream_t s) {                                              \
-        k_thermal_prestream<STORE><<<(A.ncell + 255) / 256, 256, 0, s>>>(A, tref);                                    \
+    cudaError_t thfill_(const StepArgs& A, cudaStream_t s) {                                                          \
+        k_thermal_prestream<STORE><<<(A.ncell + 255) / 256, 256, 0, s>>>(A);                                          \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
     cudaError_t batch_(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s) {                          \

@@ -49,7 +49,7 @@ struct Control {
     int halt;               // divergence guard tripped: later steps return at once
     int halt_kind;          // 1: NaN count before streaming, 2: mean density
     int th_valid;           // Nusselt updated at least once
-    int stage_timeout;      // a bounded wait on a bulk copy gave up (error)
+    int pad0;
     long long steps;        // counted steps (lbmCurrentStep)
     long long kexec;        // step bodies executed
     float prev_kinetic;
@@ -96,7 +96,9 @@ struct StepArgs {
     float tau0, Cs, velScale2;
     float Fx, Fy, Fz;
     float uin[3];
-    float feq_in[19];           // inlet equilibrium in storage form
+    float feq_in[19];           // inlet equilibrium in register form (h = f - w when shifted)
+    float dq[19];               // shifted storage: s_q - w_q, s = f_eq(1, u_shift) (stored value = f - s_r)
+    float dqs[19];              // dq times the storage scale (2^10 for FP16, 1 for BF16)
     float conv;
     int flow_axis, flow_sign;
     int periodic_x, periodic_z;
@@ -104,7 +106,6 @@ struct StepArgs {
     int freeslip, outlet_mode;  // outlet_mode: 0 none, 1 convective, 2 zero-gradient
     int fast_ok;                // forces bounded: clean states need no non-finite checks
     int shifted_fast;           // shifted storage, no body force, no thermal: collide19_shifted_fast
-    int staged;                 // interior tiles through TMA bulk copies (non-thermal steps)
     int split;                  // shell and interior as two launches
     int fused;                  // one launch: shell blocks beside dynamic interior blocks (non-thermal)
     int shell_blocks;           // fused: blocks given to the boundary shell
@@ -118,6 +119,7 @@ struct StepArgs {
     float conv_threshold;
     int th_on, th_fixed, th_ylo;
     float th_invtau, th_hot, th_cold, th_tref, th_glb, th_H;
+    float th_tc0, th_tc1;       // shifted D3Q7 storage: Tc(y) = th_tc0 + th_tc1 * y (conduction profile or Tref)
     int th_buoy_mode;           // 0: from the previous step's T, 1: zero (fresh
                                 // field, thermal_lbm.cpp:132), 2: from T_buoy
     const float* T_buoy;
@@ -170,6 +172,24 @@ __device__ __forceinline__ typename S::T* gplane(const StepArgs& A, int q) {
 
 __device__ __forceinline__ int nb19(const StepArgs& A, int q) { return A.nbq[q]; }
 
+// ---- shifted storage ---------------------------------------------------------
+// FP16 / BF16 slots hold f - s_r, s = f_eq(rho = 1, u_shift) (the freestream
+// equilibrium; s = w when u_shift = 0), for the direction r that the next
+// gather reads the value as. Registers hold h = f - w. A load of direction q
+// adds dq[q] = s_q - w_q; a store subtracts dq of its reader's direction, which
+// differs from the value's own direction on links that turn a population
+// (bounce-back, copy-own, free slip): s is not symmetric under c -> -c.
+template <class S>
+__device__ __forceinline__ float ldp(const StepArgs& A, int q, const typename S::T* p) {
+    if constexpr (S::shifted) return fmaf(S::raw_load(p), S::kInv, A.dq[q]);
+    else return S::load_rw(p);
+}
+template <class S>
+__device__ __forceinline__ void stp(const StepArgs& A, int r, typename S::T* p, float v) {
+    if constexpr (S::shifted) S::raw_store(p, fmaf(v, S::kScale, -A.dqs[r]));
+    else S::store(p, v);
+}
+
 __device__ __forceinline__ bool is_wall(const StepArgs& A, int c) { return (A.desc[c] & D_WALL) != 0; }
 
 // ---- boundary-shell link resolution (reference rules, lbm.cpp:1376-1406) ----
@@ -212,6 +232,21 @@ __device__ __forceinline__ Link resolve_kind(const StepArgs& A, int x, int y, in
     const int r0 = o0 ? x : s0, r1 = o1 ? y : s1, r2 = o2 ? z : s2;
     const int rq = dir19_of(o0 ? -cx19(q) : cx19(q), o1 ? -cy19(q) : cy19(q), o2 ? -cz19(q) : cz19(q));
     return {(r2 * A.ny + r1) * A.nx + r0, opp19(rq), L_FREESLIP};
+}
+
+// Direction the next gather reads post-collision population j of cell
+// (x,y,z) as, given the kind of the cell's link of direction opp(j): j on a
+// regular link, opp(j) when it comes back to the cell (bounce-back, copy-own
+// of population opp(j)), c_j reflected on the axes where x + c_j leaves the
+// domain on a free-slip link.
+__device__ __forceinline__ int reader_of(const StepArgs& A, int kind, int x, int y, int z, int j) {
+    if (kind == L_REGULAR) return j;
+    if (kind != L_FREESLIP) return opp19(j);
+    int s0 = x + cx19(j), s1 = y + cy19(j), s2 = z + cz19(j);
+    if (A.periodic_x) { s0 = s0 < 0 ? s0 + A.nx : (s0 >= A.nx ? s0 - A.nx : s0); }
+    if (A.periodic_z) { s2 = s2 < 0 ? s2 + A.nz : (s2 >= A.nz ? s2 - A.nz : s2); }
+    const bool o0 = (s0 < 0 || s0 >= A.nx), o1 = (s1 < 0 || s1 >= A.ny), o2 = (s2 < 0 || s2 >= A.nz);
+    return dir19_of(o0 ? -cx19(j) : cx19(j), o1 ? -cy19(j) : cy19(j), o2 ? -cz19(j) : cz19(j));
 }
 
 // ---- collision of one fluid cell, plain form ---------------------------------
@@ -673,23 +708,37 @@ __device__ __forceinline__ TLink th_resolve(const StepArgs& A, int x, int y, int
 // Gather (stream, with Dirichlet / adiabatic walls), BGK with this cell's new
 // velocity, scatter. INTERIOR: links from the descriptor, unrolled;
 // otherwise the shell's precomputed kinds, rolled loops.
+// Shifted D3Q7 storage: a slot holds g_i - w_i Tc(y_w), Tc the conduction
+// profile between fixed wall temperatures (Tref without fixed walls) and y_w
+// the row of the cell that stored the value: the reader's own row on links
+// that come back to it, its row - c_iy on a regular link. Far from the
+// conduction state only the perturbation is stored, which 16 bits resolve.
+// Writer and reader evaluate Tc of the same integer row: the same bits.
+__device__ __forceinline__ float th_tc(const StepArgs& A, int yw) { return fmaf(A.th_tc1, (float)yw, A.th_tc0); }
+
 template <class S, bool ODD, bool MAT, bool INTERIOR>
 __device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int x, int y, int z, uint32_t d,
                                                 unsigned long long skind, const CellResult& r, Acc& acc) {
     constexpr bool SH = S::shifted;
-    const float wshift = SH ? A.th_tref : 0.0f;   // stored value = g - w*Tref
+    // shift of a value read as direction i: the storing row is y - c_iy on a
+    // regular link (only i = 3, 4 have c_iy != 0; for them the descriptor's
+    // link bit is exactly "not regular", y never wraps)
+    auto rd_shift = [&](int i, bool regular) -> float {
+        return SH ? w7(i) * th_tc(A, regular ? y - cy19(i) : y) : 0.0f;
+    };
+    const float tc_own = SH ? th_tc(A, y) : 0.0f;   // stored by this cell: g - w Tc(y)
     float g[Q7];
 #pragma unroll
     for (int i = 0; i < Q7; ++i) {
         if (!ODD) {
-            g[i] = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;
+            g[i] = S::load_rw(gplane<S>(A, i) + cell) + rd_shift(i, !((d >> i) & 1u));
         } else {
             const TLink L = th_resolve(A, x, y, z, cell, i, INTERIOR, d,
                                        INTERIOR ? -1 : (int)((skind >> (40 + 2 * i)) & 3ull));
             if (L.bounce == 0) {
-                g[i] = S::load_rw(gplane<S>(A, opp19(i)) + L.idx) + w7(i) * wshift;
+                g[i] = S::load_rw(gplane<S>(A, opp19(i)) + L.idx) + rd_shift(i, true);
             } else {
-                const float v = S::load_rw(gplane<S>(A, i) + cell) + w7(i) * wshift;   // post_{opp i}
+                const float v = S::load_rw(gplane<S>(A, i) + cell) + rd_shift(i, false);   // post_{opp i}
                 g[i] = L.bounce == 2 ? (-v + 2.0f * w7(i) * L.Tw) : v;
             }
         }
@@ -721,16 +770,16 @@ __device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int
 #pragma unroll
     for (int j = 0; j < Q7; ++j) {
         if (!ODD) {
-            S::store(gplane<S>(A, opp19(j)) + cell, g[j] - w7(j) * wshift);
+            S::store(gplane<S>(A, opp19(j)) + cell, g[j] - w7(j) * tc_own);
         } else {
             const TLink L = th_resolve(A, x, y, z, cell, opp19(j), INTERIOR, d,
                                        INTERIOR ? -1 : (int)((skind >> (40 + 2 * opp19(j))) & 3ull));
             if (L.bounce == 0) {
-                S::store(gplane<S>(A, j) + L.idx, g[j] - w7(j) * wshift);
+                S::store(gplane<S>(A, j) + L.idx, g[j] - w7(j) * tc_own);
             } else {
                 // becomes pre-collision population opp j of this cell
                 const float val = L.bounce == 2 ? (-g[j] + 2.0f * w7(j) * L.Tw) : g[j];
-                S::store(gplane<S>(A, opp19(j)) + cell, val - w7(j) * wshift);
+                S::store(gplane<S>(A, opp19(j)) + cell, val - w7(j) * tc_own);
             }
         }
     }
@@ -750,7 +799,7 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
         // arrives (one memory round trip less on the critical path)
         const float strainAll = (!MAT && A.use_les) ? strain_prev(A, V, cell) : 0.0f;
 #pragma unroll
-        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
+        for (int q = 0; q < Q19; ++q) f[q] = ldp<S>(A, q, fplane<S>(A, q) + cell);
         if (d & D_WALL) return;
         if (d & D_LES) strainPre = strainAll;
     } else {
@@ -760,13 +809,13 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
         if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
         if ((d & D_LINKS) == 0) {
 #pragma unroll
-            for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
+            for (int q = 0; q < Q19; ++q) f[q] = ldp<S>(A, q, fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
         } else {
 #pragma unroll
             for (int q = 0; q < Q19; ++q) {
                 const bool special = (d >> q) & 1u;
                 const int src = special ? cell : cell - nb19(A, q);
-                f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
+                f[q] = ldp<S>(A, q, fplane<S>(A, special ? q : opp19(q)) + src);
             }
         }
     }
@@ -789,56 +838,31 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
             for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
         }
         if (!ODD) {
+            if (!S::shifted || plain) {
 #pragma unroll
-            for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
+                for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, opp19(j)) + cell, f[j]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < Q19; ++j) {
+                    const bool solid = (d >> opp19(j)) & 1u;   // c + c_j is a wall: read back as opp j
+                    stp<S>(A, solid ? opp19(j) : j, fplane<S>(A, opp19(j)) + cell, f[j]);
+                }
+            }
         } else if (plain) {
 #pragma unroll
-            for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
+            for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
         } else {
 #pragma unroll
             for (int j = 0; j < Q19; ++j) {
                 const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
-                if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
-                else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+                if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
+                else stp<S>(A, j, fplane<S>(A, j) + cell + nb19(A, j), f[j]);
             }
         }
         if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
         if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
     }
     if (THERMAL) thermal_substep<S, ODD, MAT, true>(A, cell, x, y, z, d, 0ull, r, acc);
-}
-
-// Collision, outlet side buffer, scatter and field writes of an interior cell
-// whose pre-collision populations are already in f (staged kernel).
-template <class S, bool ODD>
-__device__ __forceinline__ void interior_finish(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
-                                                uint32_t d, float f[Q19], float strainPre, Acc& acc) {
-    constexpr bool SH = S::shifted;
-    CellResult r;
-    collide19<SH>(f, A, d, false, false, strainPre, 0.0f, r, acc);
-    const uint32_t os = (d >> D_OUT_SHIFT) & 3u;
-    if (os) {
-        const int P = A.out_plane;
-        const int pi = plane_index(A, x, y, z);
-#pragma unroll
-        for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
-    }
-    if (!ODD) {
-#pragma unroll
-        for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
-    } else if ((d & D_LINKS) == 0) {
-#pragma unroll
-        for (int j = 0; j < Q19; ++j) S::store(fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
-    } else {
-#pragma unroll
-        for (int j = 0; j < Q19; ++j) {
-            const bool solid = (d >> opp19(j)) & 1u;
-            if (solid) S::store(fplane<S>(A, opp19(j)) + cell, f[j]);
-            else S::store(fplane<S>(A, j) + cell + nb19(A, j), f[j]);
-        }
-    }
-    if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
-    if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
 }
 
 // ---- boundary-shell cell: precomputed link kinds (kept out of line so the
@@ -865,15 +889,15 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
 #pragma unroll
         for (int q = 0; q < Q19; ++q) off[q] = __ldg(A.shell_gth + (size_t)q * A.n_shell + si);
 #pragma unroll
-        for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fb + off[q]);
+        for (int q = 0; q < Q19; ++q) f[q] = ldp<S>(A, q, fb + off[q]);
     } else {
 #pragma unroll
         for (int q = 0; q < Q19; ++q) {
             if (!ODD) {
-                f[q] = S::load_rw(fplane<S>(A, q) + cell);
+                f[q] = ldp<S>(A, q, fplane<S>(A, q) + cell);
             } else {
                 const Link L = resolve_kind(A, x, y, z, cell, q, (int)((skind >> (2 * q)) & 3ull));
-                f[q] = S::load_rw(fplane<S>(A, L.slot) + L.idx);
+                f[q] = ldp<S>(A, q, fplane<S>(A, L.slot) + L.idx);
             }
         }
     }
@@ -949,8 +973,9 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
 #pragma unroll
             for (int j = 0; j < Q19; ++j) {
                 const int oj = opp19(j);
-                const bool copy_own = ((skind >> (2 * oj)) & 3ull) == (unsigned long long)L_COPYOWN;
-                S::store(fb + off[j], copy_own ? f[oj] : f[j]);
+                const int kind = (int)((skind >> (2 * oj)) & 3ull);
+                const int r = S::shifted ? reader_of(A, kind, x, y, z, j) : j;
+                stp<S>(A, r, fb + off[j], kind == L_COPYOWN ? f[oj] : f[j]);
             }
         } else {
 #pragma unroll
@@ -958,12 +983,13 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
                 const int oj = opp19(j);
                 const int kind = (int)((skind >> (2 * oj)) & 3ull);
                 if (!ODD) {
-                    S::store(fplane<S>(A, oj) + cell, kind == L_COPYOWN ? f[oj] : f[j]);
+                    const int r = S::shifted ? reader_of(A, kind, x, y, z, j) : j;
+                    stp<S>(A, r, fplane<S>(A, oj) + cell, kind == L_COPYOWN ? f[oj] : f[j]);
                 } else {
                     const Link L = resolve_kind(A, x, y, z, cell, oj, kind);
-                    if (L.kind == L_REGULAR || L.kind == L_FREESLIP) S::store(fplane<S>(A, L.slot) + L.idx, f[j]);
-                    else if (L.kind == L_BOUNCE) S::store(fplane<S>(A, oj) + cell, f[j]);
-                    else S::store(fplane<S>(A, oj) + cell, f[oj]);
+                    if (L.kind == L_REGULAR || L.kind == L_FREESLIP) stp<S>(A, L.slot, fplane<S>(A, L.slot) + L.idx, f[j]);
+                    else if (L.kind == L_BOUNCE) stp<S>(A, oj, fplane<S>(A, oj) + cell, f[j]);
+                    else stp<S>(A, oj, fplane<S>(A, oj) + cell, f[oj]);
                 }
             }
         }
@@ -1593,223 +1619,6 @@ __global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_s
             if (KIND == 1) B.ctl->k = k + 1;
         }
     }
-}
-
-// ---- staged interior tiles: TMA bulk copies into shared memory ----------------
-// Each interior tile (STEP_BLOCK consecutive interior cells, one or a few row
-// segments) pulls 19 contiguous population ranges — the tile's own cells on
-// even steps, the tile shifted by -c_q on odd steps — plus its descriptors.
-// One elected thread issues them as cp.async.bulk copies completing on an
-// mbarrier, for the NEXT tile of the block while the current one computes;
-// threads then read shared memory. Tiles whose span (row gaps included)
-// exceeds the staging slot, shell tiles and wall-adjacent links use direct
-// loads. Waits are bounded: on timeout the kernel records an error and
-// continues with direct loads.
-constexpr int STAGE_SLOT = 288;   // elements per staged range
-#ifndef AEROS_STAGED_MIN_BLOCKS
-#define AEROS_STAGED_MIN_BLOCKS 6
-#endif
-constexpr int STAGED_MIN_BLOCKS = AEROS_STAGED_MIN_BLOCKS;
-constexpr int STAGE_WAIT_LIMIT = 1 << 20;   // try_wait polls before a staged tile is given up
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ int interior_cell_of(const StepArgs& A, int li) {
-    const uint32_t r = A.div_ix.div((uint32_t)li);
-    const int x = li - (int)r * (A.nx - 2) + 1;
-    const uint32_t zq = A.div_iy.div(r);
-    const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
-    return ((int)zq + 1) * A.nxny + y * A.nx + x;
-}
-
-// Interior tile index of a tile of the sequence, -1 for a shell tile.
-__device__ __forceinline__ int interior_tile_of(const StepArgs& A, int tile) {
-    const int nsh = A.ntiles - A.ntiles_interior;
-    const int k = A.shell_stride;
-    if (nsh > 0 && (tile % k) == 0 && tile / k < nsh) return -1;
-    return tile - min(nsh, tile / k + 1);
-}
-
-template <class S>
-struct StageBuf {
-    typename S::T pop[Q19][STAGE_SLOT];
-    uint32_t desc[STAGE_SLOT];
-    int lo[Q19 + 1];
-    unsigned long long bar;
-};
-
-// First and last cell of interior tile `it`; true when it fits the slot.
-template <class S>
-__device__ __forceinline__ bool stage_span(const StepArgs& A, int it, int& c0, int& c1) {
-    constexpr int AL = 16 / (int)sizeof(typename S::T);
-    const int li0 = it * STEP_BLOCK;
-    const int li1 = min(li0 + STEP_BLOCK, A.n_interior) - 1;
-    c0 = interior_cell_of(A, li0);
-    c1 = interior_cell_of(A, li1);
-    return (c1 - c0 + 1) + 2 * AL <= STAGE_SLOT;
-}
-
-template <class S, bool ODD>
-__device__ __forceinline__ void stage_issue(const StepArgs& A, StageBuf<S>& sb, int c0, int c1) {
-    using T = typename S::T;
-    constexpr int AL = 16 / (int)sizeof(T);
-    uint32_t bytes[Q19 + 1];
-    int lo[Q19 + 1];
-    uint32_t total = 0;
-#pragma unroll
-    for (int q = 0; q < Q19; ++q) {
-        const int a = ODD ? c0 - nb19(A, q) : c0, b = ODD ? c1 - nb19(A, q) : c1;
-        lo[q] = a & ~(AL - 1);
-        bytes[q] = (uint32_t)(((b + 1 - lo[q]) * (int)sizeof(T) + 15) & ~15);
-        total += bytes[q];
-    }
-    lo[Q19] = c0 & ~3;
-    bytes[Q19] = (uint32_t)(((c1 + 1 - lo[Q19]) * 4 + 15) & ~15);
-    total += bytes[Q19];
-#pragma unroll
-    for (int q = 0; q <= Q19; ++q) sb.lo[q] = lo[q];
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(&sb.bar, total);
-#pragma unroll
-    for (int q = 0; q < Q19; ++q)
-        bulk_g2s(sb.pop[q], fplane<S>(A, ODD ? opp19(q) : q) + lo[q], bytes[q], &sb.bar);
-    bulk_g2s(sb.desc, A.desc + lo[Q19], bytes[Q19], &sb.bar);
-}
-
-template <class S, bool ODD>
-__global__ void __launch_bounds__(STEP_BLOCK, STAGED_MIN_BLOCKS) k_lbm_step_staged(const StepArgs A, const StepVar V) {
-    if (A.ctl->halt) return;   // uniform: every thread reads the same flag
-    __shared__ __align__(128) StageBuf<S> sb;
-    Acc acc;
-    acc.zero();
-    if (threadIdx.x == 0) mbar_init(&sb.bar);
-    __syncthreads();
-    uint32_t parity = 0;
-    bool stage_ok = true, pending = false;
-    int c0n = 0, c1n = 0;
-    int tile = blockIdx.x;
-    bool cur = false;
-    if (tile < A.ntiles) {
-        const int it = interior_tile_of(A, tile);
-        if (it >= 0 && stage_span<S>(A, it, c0n, c1n)) {
-            cur = true;
-            if (threadIdx.x == 0) stage_issue<S, ODD>(A, sb, c0n, c1n);
-        }
-    }
-    for (; tile < A.ntiles; tile += gridDim.x) {
-        const int next = tile + gridDim.x;
-        const int it = interior_tile_of(A, tile);
-        int itn = -1;
-        bool nxt = false;
-        if (stage_ok && next < A.ntiles) {
-            itn = interior_tile_of(A, next);
-            nxt = itn >= 0 && stage_span<S>(A, itn, c0n, c1n);
-        }
-        if (it < 0) {   // shell tile: shared memory idle, prefetch the next tile first
-            if (nxt && threadIdx.x == 0) stage_issue<S, ODD>(A, sb, c0n, c1n);
-            const int si = (tile / A.shell_stride) * STEP_BLOCK + (int)threadIdx.x;
-            if (si < A.n_shell) {
-                const int cell = A.shell[si];
-                const uint32_t r = A.div_x.div((uint32_t)cell);
-                const int x = cell - (int)r * A.nx;
-                const uint32_t z = A.div_y.div(r);
-                const int y = (int)(r - z * (uint32_t)A.ny);
-                process_shell<S, ODD, false, false>(A, V, si, cell, x, y, (int)z, A.shell_kind[si], acc);
-            }
-            cur = nxt;
-            continue;
-        }
-        const int li = it * STEP_BLOCK + (int)threadIdx.x;
-        const bool valid = li < A.n_interior;
-        int x = 0, y = 0, z = 0, cell = 0;
-        if (valid) {
-            const uint32_t r = A.div_ix.div((uint32_t)li);
-            x = li - (int)r * (A.nx - 2) + 1;
-            const uint32_t zq = A.div_iy.div(r);
-            y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
-            z = (int)zq + 1;
-            cell = (z * A.ny + y) * A.nx + x;
-        }
-        if (cur) {
-            bool done = false;
-            for (int spin = 0; spin < STAGE_WAIT_LIMIT && !done; ++spin) done = mbar_try_wait(&sb.bar, parity);
-            if (__syncthreads_or(!done)) {   // never expected: record, stop staging, use direct loads
-                if (threadIdx.x == 0) A.ctl->stage_timeout = 1;
-                stage_ok = false;
-                cur = false;
-                nxt = false;
-                pending = true;
-            } else {
-                parity ^= 1u;
-            }
-        }
-        uint32_t d = D_WALL;
-        float f[Q19];
-        float strainPre = 0.0f;
-        if (valid) {
-            d = cur ? sb.desc[cell - sb.lo[Q19]] : A.desc[cell];
-            if (!(d & D_WALL)) {
-                if (A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
-                if (cur && (!ODD || (d & D_LINKS) == 0)) {
-#pragma unroll
-                    for (int q = 0; q < Q19; ++q) {
-                        const int src = ODD ? cell - nb19(A, q) : cell;
-                        f[q] = S::load_rw(&sb.pop[q][src - sb.lo[q]]);
-                    }
-                } else if (cur) {
-#pragma unroll
-                    for (int q = 0; q < Q19; ++q) {
-                        if ((d >> q) & 1u) f[q] = S::load_rw(fplane<S>(A, q) + cell);
-                        else f[q] = S::load_rw(&sb.pop[q][cell - nb19(A, q) - sb.lo[q]]);
-                    }
-                } else if (!ODD) {
-#pragma unroll
-                    for (int q = 0; q < Q19; ++q) f[q] = S::load_rw(fplane<S>(A, q) + cell);
-                } else {
-#pragma unroll
-                    for (int q = 0; q < Q19; ++q) {
-                        const bool special = (d >> q) & 1u;
-                        const int src = special ? cell : cell - nb19(A, q);
-                        f[q] = S::load_rw(fplane<S>(A, special ? q : opp19(q)) + src);
-                    }
-                }
-            }
-        }
-        __syncthreads();   // shared memory consumed
-        if (nxt && threadIdx.x == 0) stage_issue<S, ODD>(A, sb, c0n, c1n);
-        if (valid && !(d & D_WALL)) interior_finish<S, ODD>(A, V, cell, x, y, z, d, f, strainPre, acc);
-        cur = nxt;
-    }
-    if (pending) {   // a copy that outlived its wait: give it one more bounded wait before exiting
-        bool done = false;
-        for (int spin = 0; spin < STAGE_WAIT_LIMIT && !done; ++spin) done = mbar_try_wait(&sb.bar, parity);
-    }
-    block_reduce_store<STEP_BLOCK>(acc, A.partials + blockIdx.x);
-    finish_step<STEP_BLOCK>(A, (int)gridDim.x);
 }
 
 }  // namespace aeros

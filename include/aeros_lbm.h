@@ -36,9 +36,16 @@ extern "C" {
 enum { AEROS_CELL_FLUID = 0, AEROS_CELL_SOLID = 1, AEROS_CELL_GROUND = 2 };
 
 /* Population storage. FP32 is the drop-in form (bitwise the reference's
- * arithmetic); FP16/BF16 store shifted deviations f_i - w_i and compute in
+ * arithmetic); FP16/BF16 store shifted deviations f_i - s_i and compute in
  * FP32. */
 enum { AEROS_STORE_FP32 = 0, AEROS_STORE_FP16 = 1, AEROS_STORE_BF16 = 2 };
+
+/* What FP16/BF16 storage subtracts from each population (storage_shift).
+ * FREESTREAM: the equilibrium f_eq(rho = 1, u_s), u_s = u_in when the domain
+ * has an inlet (periodic_x == 0), else u_init; away from a body the stored
+ * deviations are then only the non-equilibrium part, which 16 bits resolve.
+ * WEIGHTS: the lattice weights w_i (f_eq at rest). */
+enum { AEROS_SHIFT_FREESTREAM = 0, AEROS_SHIFT_WEIGHTS = 1 };
 
 /* Lateral (non-flow-axis, non-periodic) faces. COPY is the reference's rule
  * (an out-of-domain source copies the cell's own post-collision population,
@@ -75,7 +82,8 @@ typedef struct aeros_lbm_params {
     int32_t storage;             /* AEROS_STORE_*                                    */
     int32_t lateral_bc;          /* AEROS_LATERAL_*                                  */
     int32_t outlet_bc;           /* AEROS_OUTLET_*                                   */
-    int32_t reserved[8];         /* zero                                             */
+    int32_t storage_shift;       /* AEROS_SHIFT_* (FP16/BF16 storage only)          */
+    int32_t reserved[7];         /* zero                                             */
 } aeros_lbm_params;
 
 /* Mirrors ThermalParams (aeros/src/thermal_lbm.h:33-41); nu_lb is the solver
@@ -209,10 +217,12 @@ typedef struct aeros_voxel_grid {
     float   cell[3];             /* cell size; centre = min + (i+0.5)*cell */
 } aeros_voxel_grid;
 
-/* Solid mask of a closed triangle mesh at the grid's cell centres: BVH
- * (median split, leaf 4, aeros/src/mesh_bvh.h:219-266) + three-ray parity vote
- * with FP64 Moller-Trumbore (mesh_bvh.h:62-96,116-185) — the mask loop of
- * buildVoxelGrid (aeros/src/voxel_grid.cpp:337-351). tris: ntri*9 floats.
+/* Solid mask of a closed triangle mesh at the grid's cell centres: the
+ * three-ray parity vote with FP64 Moller-Trumbore of the reference's inside
+ * test (aeros/src/mesh_bvh.h:62-96,168-185), the mask loop of buildVoxelGrid
+ * (aeros/src/voxel_grid.cpp:337-351); the same mask bit for bit. Rays are
+ * traced once per grid row through a Morton-code BVH; each cell evaluates the
+ * row's candidate triangles from its own origin. tris: ntri*9 floats.
  * mask_out: nx*ny*nz bytes, 1 = inside. Degenerate / non-finite triangles are
  * dropped as voxel_grid.cpp:313-325 does. */
 int aeros_voxelize(const float* tris, int64_t ntri, const aeros_voxel_grid* grid,
@@ -225,13 +235,16 @@ int aeros_voxelize_device(const float* tris, int64_t ntri,
  * HBM budget is spent on resident domains; callers whose other streams must
  * not be stalled by the device-wide synchronization of cudaFree). BVH,
  * triangles and overflow flag live in one fixed 24 MiB device array per
- * device (about 330,000 triangles); a larger mesh returns AEROS_ERR_INVALID
- * before any device work. Calls share that array: they must not overlap in
- * time (the call returns after its device work has completed). The first
- * call on a device looks the array up and must come before any stream
- * capture on that device. Same mask as aeros_voxelize_device. */
+ * device, present from the library's load on (the level-7 icosphere's
+ * 327,680 triangles fit, about 36 bytes per triangle plus 32 per BVH node); a
+ * larger mesh returns AEROS_ERR_INVALID before any device work. All work runs
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream, which
+ * synchronizes with the device's blocking streams), and the call returns
+ * after it has completed there. Calls share the array: they must not overlap
+ * in time. The array's address is looked up on every call, before any work is
+ * queued. Same mask as aeros_voxelize_device. */
 int aeros_voxelize_device_noalloc(const float* tris, int64_t ntri,
-                                  const aeros_voxel_grid* grid, uint8_t* d_mask);
+                                  const aeros_voxel_grid* grid, uint8_t* d_mask, void* stream);
 
 /* ---- signed distance field -------------------------------------------------------- */
 /* The voxel grid's signed distance field (the distance-field part of

@@ -31,7 +31,9 @@ def build(quiet: bool = True) -> None:
     reference tree is present)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-s", "-C", HERE, "all"], stdout=out)
-    if os.path.isdir("/root/reference/aeros/src"):
+    present = subprocess.call(["make", "-s", "-C", HERE, "has-ref"], stdout=subprocess.DEVNULL,
+                              stderr=subprocess.DEVNULL) == 0
+    if present:
         subprocess.check_call(["make", "-s", "-C", HERE, "ref"], stdout=out)
 
 

@@ -274,10 +274,9 @@ def _validation_cd(make, storage="fp32"):
 def test_shifted_storage_cd_vs_plain_and_fp64(gpu, oracle_built):
     """Precision form on the Re = 100 validation sphere (649 k cells, 550
     steps), against the plain FP32 path (1.127719, the reference's 1.128) and
-    the FP64 oracle (1.128573). Measured: FP16 1.134937 (+0.64 % / +0.56 %),
-    BF16 1.174430 (+4.1 % / +4.1 %). Tolerances: FP16 1 %, BF16 5 % (the
-    0.5 % aim is not reached: 16-bit rounding of f - w, see the precision
-    section of the design notes)."""
+    the FP64 oracle (1.128573). Tolerance: 0.5 % for FP16 and BF16 storage
+    shifted by the freestream equilibrium (the w shift gave FP16 +0.64 % /
+    +0.56 %, BF16 +4.1 %)."""
     cd32 = _validation_cd(lambda p, m: gpu.Solver(p, m))
     cd16 = _validation_cd(lambda p, m: gpu.Solver(p, m), "fp16")
     cdbf = _validation_cd(lambda p, m: gpu.Solver(p, m), "bf16")
@@ -285,10 +284,10 @@ def test_shifted_storage_cd_vs_plain_and_fp64(gpu, oracle_built):
     cd64 = _validation_cd(lambda p, m: oracle_built.OracleLBM(p, m, "f64"))
     print(f"Cd: fp32 {cd32:.6f} fp16 {cd16:.6f} bf16 {cdbf:.6f} fp64 {cd64:.6f}")
     assert abs(cd32 - cd64) <= 0.001 * abs(cd64)
-    assert abs(cd16 - cd32) <= 0.01 * abs(cd32)
-    assert abs(cd16 - cd64) <= 0.01 * abs(cd64)
-    assert abs(cdbf - cd32) <= 0.05 * abs(cd32)
-    assert abs(cdbf - cd64) <= 0.05 * abs(cd64)
+    assert abs(cd16 - cd32) <= 0.005 * abs(cd32)
+    assert abs(cd16 - cd64) <= 0.005 * abs(cd64)
+    assert abs(cdbf - cd32) <= 0.005 * abs(cd32)
+    assert abs(cdbf - cd64) <= 0.005 * abs(cd64)
 
 
 def test_voxelizer_bit_exact(gpu):
@@ -332,29 +331,6 @@ def test_shifted_storage_error_vs_fp64(gpu, oracle_built, storage):
     for k in ("ux", "uy", "uz"):
         assert np.max(np.abs(a[k] - b[k])) <= tol * np.max(np.abs(b["ux"])), (k, storage)
     assert np.max(np.abs(a["rho"] - b["rho"])) <= tol
-
-
-@pytest.mark.parametrize("storage", ["fp32", "fp16"])
-@pytest.mark.parametrize("name", ["sphere_trt_les_conv", "channel_force3"])
-def test_staged_interior_tiles_match_direct_loads(gpu, monkeypatch, name, storage):
-    """Interior tiles staged in shared memory by bulk copies (opt-in kernel)
-    produce the same state, bit for bit, as the direct-load kernel."""
-    case = CASES[name]
-    g = GOLD["cases"][name]
-    mask = solver_mask(case)
-    p = params_for(case, g["u_in"], storage)
-    out = []
-    for staged in ("0", "1"):
-        monkeypatch.setenv("AEROS_STAGED", staged)
-        s = gpu.Solver(p, mask)
-        s.step(case["steps"])
-        out.append((s.populations(), s.fields(), s.stats()))
-        s.close()
-    (fa, va, sa), (fb, vb, sb) = out
-    assert np.array_equal(fa, fb)
-    for k in va:
-        assert np.array_equal(va[k], vb[k]), k
-    assert sa["sum_rho"] == sb["sum_rho"] and sa["step"] == sb["step"]
 
 
 @pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
