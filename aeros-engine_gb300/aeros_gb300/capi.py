@@ -227,6 +227,8 @@ _SIGS = {
     "aeros_lbm_step_async": (C.c_int, [_P, C.c_int]),
     "aeros_lbm_get_stats": (C.c_int, [_P, C.POINTER(LbmStats)]),
     "aeros_lbm_read_fields": (C.c_int, [_P, _FP, _FP, _FP, _FP, _FP, _FP]),
+    "aeros_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
+    "aeros_host_free": (C.c_int, [_P]),
     "aeros_lbm_device_fields": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "aeros_lbm_read_populations": (C.c_int, [_P, _FP]),
     "aeros_lbm_write_populations": (C.c_int, [_P, _FP]),

@@ -91,8 +91,11 @@ class Solver:
         return int(v.value)
 
     # ---- state I/O -------------------------------------------------------
-    def fields(self) -> dict:
-        out = {k: np.empty(self.n, np.float32) for k in ("rho", "ux", "uy", "uz", "strain", "tke")}
+    def fields(self, out: dict | None = None) -> dict:
+        """rho, ux, uy, uz, strain, tke as float32 arrays of nx*ny*nz cells;
+        `out` (e.g. from pinned_fields) receives them without a new allocation."""
+        if out is None:
+            out = {k: np.empty(self.n, np.float32) for k in ("rho", "ux", "uy", "uz", "strain", "tke")}
         check(lib().aeros_lbm_read_fields(self.h, *(_f(out[k]) for k in ("rho", "ux", "uy", "uz", "strain", "tke"))),
               "read_fields")
         return out
@@ -220,6 +223,39 @@ class SurfaceMesh:
             self.close()
         except Exception:
             pass
+
+
+class PinnedArray(np.ndarray):
+    """A numpy array over page-locked host memory (aeros_host_alloc): device
+    readbacks into it are single direct copies. The memory is released when
+    the array (and every view of it) is gone."""
+
+    class _Owner:
+        def __init__(self, ptr):
+            self.ptr = ptr
+
+        def __del__(self):
+            try:
+                lib().aeros_host_free(C.c_void_p(self.ptr))
+            except Exception:
+                pass
+
+    def __new__(cls, n: int, dtype=np.float32):
+        dt = np.dtype(dtype)
+        ptr = C.c_void_p()
+        check(lib().aeros_host_alloc(max(1, n) * dt.itemsize, C.byref(ptr)), "aeros_host_alloc")
+        buf = (C.c_char * (max(1, n) * dt.itemsize)).from_address(ptr.value)
+        a = np.frombuffer(buf, dtype=dt, count=n).view(cls)
+        a._owner = PinnedArray._Owner(ptr.value)
+        return a
+
+    def __array_finalize__(self, obj):
+        self._owner = getattr(obj, "_owner", None)
+
+
+def pinned_fields(n: int) -> dict:
+    """Page-locked host arrays for Solver.fields(out=...)."""
+    return {k: PinnedArray(n) for k in ("rho", "ux", "uy", "uz", "strain", "tke")}
 
 
 def equilibrium_moments(states) -> tuple[np.ndarray, np.ndarray]:

@@ -867,6 +867,22 @@ extern "C" int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float*
     return AEROS_OK;
 }
 
+extern "C" int aeros_host_alloc(size_t bytes, void** out) {
+    if (!out) return set_error(AEROS_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    if (cudaHostAlloc(out, bytes ? bytes : 16, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return set_error(AEROS_ERR_ALLOC, "page-locked host buffer of %zu bytes", bytes);
+    }
+    return AEROS_OK;
+}
+
+extern "C" int aeros_host_free(void* p) {
+    if (p) CUDA_TRY(cudaFreeHost(p));
+    return AEROS_OK;
+}
+
 extern "C" int aeros_lbm_device_fields(aeros_lbm* h, const float** rho, const float** u4) {
     if (!h) return set_error(AEROS_ERR_INVALID, "handle is NULL");
     if (int rc = finish_batch(h)) return rc;

@@ -40,6 +40,11 @@ BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 16 + 16 + 4, "fp16": 2 * 19 * 2 + 16 + 16
 # profiles/k_lbm_fused_sphere_240x120x115.md
 NCU_TRAFFIC = {"fp16": (232081408 + 149953536 + 218365952 + 189753344) / 2,
                "fp32": (364544768 + 275870208 + 354004992 + 316344064) / 2}
+# the workload both arms run (the reference arm in its own FP32 form)
+WORKLOAD_CONFIG = {"workload": "sphere Re=100, 240x120x115 (3.31 M cells), icosphere L6 (81,920 triangles), "
+                               "TRT+Smagorinsky, zero-gradient outlet, free-slip lateral walls",
+                   "storage": "fp16 shifted by the freestream equilibrium (fp32 plain measured beside it)",
+                   "l2": "working set > 129 MB L2, no flush"}
 # bytes of the solver's device control block that every aeros_lbm_step call
 # reads back (struct Control in aeros-engine_gb300/csrc/lbm_step.cuh)
 CONTROL_BYTES = 272
@@ -195,7 +200,10 @@ def run_gb300(args):
         if not return_early:
             p, _, _ = sphere_case("fp16", mask=mask)
             s = solver.Solver(p, mask)
+            # the frame loop's host mirrors of the fields: page-locked, allocated once
+            host = solver.pinned_fields(cells)
             s.step(2)
+            s.fields(out=host)
             s.synchronize()
             rank_barrier(world)
             t1 = time.perf_counter()
@@ -204,10 +212,13 @@ def run_gb300(args):
                 s.step_async(1)
                 forces.append(s.cv_force(0.3, 0.3, 0.3))
                 stats = s.stats()   # the step's statistics, read back with the force
-            s.fields()
+            t2 = time.perf_counter()
+            s.fields(out=host)
             e2e_s = time.perf_counter() - t1
+            readback_ms = 1000 * (time.perf_counter() - t2)
             rank_barrier(world)
             s.close()
+            del host
     if return_early:
         print(json.dumps({k: {kk: round(vv, 4) if isinstance(vv, float) else vv for kk, vv in v.items()}
                           for k, v in results.items()}), flush=True)
@@ -231,10 +242,7 @@ def run_gb300(args):
             "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp16-storage/fp32-math", "data": "synthetic",
-            "config": {"workload": "sphere Re=100, 240x120x115 (3.31 M cells), icosphere L6 voxelized on GPU, "
-                                   "TRT+Smagorinsky, zero-gradient outlet, free-slip lateral walls",
-                       "storage": "fp16 shifted (f - w)", "l2": "working set > 129 MB L2, no flush",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": dict(WORKLOAD_CONFIG, parallelism="replicas" if world > 1 else "single device"),
             "roofline": {"bound": "hbm", "achieved": round(head["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
                          "frac": round(frac, 4), "traffic": round(NCU_TRAFFIC["fp16"]),
                          "traffic_unit": "bytes per launch (ncu)", "algorithmic_bytes": BYTES_PER_CELL["fp16"] * cells,
@@ -247,9 +255,12 @@ def run_gb300(args):
             "fp16_over_fp32": round(results["fp16"]["mlups"] / results["fp32"]["mlups"], 3),
             "e2e": {"value": round(e2e_value, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // max(1, e2e_steps)),
                     "d2h_bytes_per_step": int(d2h // max(1, e2e_steps)),
+                    "readback_ms": round(readback_ms, 3),
                     "what": "per step aeros_lbm_step_async(1) + aeros_lbm_cv_force (one wait: the step's statistics and the "
-                            "force read back) + aeros_lbm_get_stats; final fields "
-                            "to host; domain created before the timed region"},
+                            "force read back) + aeros_lbm_get_stats; then the six final fields (rho, u, |S|, TKE: "
+                            f"{4 * cells * 6} B) into page-locked host mirrors allocated before the timed region "
+                            "(readback_ms of the total); domain created before the timed region; a step has no host "
+                            "input, so nothing goes host to device"},
             "gpu_launches": int(head["launches"]),
             "clocks": clk.summary(),
             "voxelize_s": round(vox_s, 3),
@@ -505,8 +516,17 @@ def cpu_baseline(mask, steps):
     o.step(steps)
     dt = time.perf_counter() - t
     cells = p.nx * p.ny * p.nz
+    # one thread (the reference's loop without OpenMP), a shorter sample
+    oracle.set_threads(1)
+    steps1 = max(1, steps // 10)
+    t = time.perf_counter()
+    o.step(steps1)
+    dt1 = time.perf_counter() - t
+    oracle.set_threads(cores)
     return {"value": round(cells * steps / dt / 1e6, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
-            "sample": f"{steps} lattice steps of the full 240x120x115 sphere grid (FP32, OpenMP {cores} threads)"}
+            "value_1thread": round(cells * steps1 / dt1 / 1e6, 2),
+            "sample": f"{steps} lattice steps of the full 240x120x115 sphere grid (FP32, OpenMP {cores} threads); "
+                      f"value_1thread: {steps1} steps on one thread"}
 
 
 def run_reference(args):
@@ -540,10 +560,10 @@ def run_reference(args):
             "value": round(v, 2), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1000 * dt / args.steps, 2), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-            "config": {"workload": "sphere Re=100, 240x120x115 (3.31 M cells), TRT+Smagorinsky, zero-gradient outlet, "
-                                   "free-slip lateral walls", "parallelism": f"OpenMP {cores} threads"},
+            "config": dict(WORKLOAD_CONFIG, parallelism="single device"),
             "cpu_baseline": {"value": round(v, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} full-grid lattice steps per timed run"},
+                             "sample": f"{args.steps} full-grid lattice steps per timed run, FP32 (the reference "
+                                       f"solver's own arithmetic), OpenMP {cores} threads"},
             "e2e": {"value": round(v, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

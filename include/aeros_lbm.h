@@ -168,6 +168,13 @@ int aeros_lbm_get_stats(aeros_lbm* h, aeros_lbm_stats* out);
  * Any pointer may be NULL. */
 int aeros_lbm_read_fields(aeros_lbm* h, float* rho, float* ux, float* uy,
                           float* uz, float* strain, float* tke);
+/* Page-locked host memory for readback targets (no reference counterpart:
+ * the reference's fields are std::vector mirrors). A copy into pageable
+ * memory goes through the driver's staging buffer at a fraction of the link
+ * speed; into these buffers aeros_lbm_read_fields copies each field with one
+ * direct DMA. aeros_host_free releases a buffer from aeros_host_alloc. */
+int aeros_host_alloc(size_t bytes, void** out);
+int aeros_host_free(void* p);
 /* Device pointers of the density and of the velocity, interleaved as
  * (ux, uy, uz, 0) per cell (valid until the next step call). Either may be
  * NULL. */

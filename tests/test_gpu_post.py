@@ -58,3 +58,24 @@ def test_gpu_equilibrium_moments_equal_reference():
     # above the limiter: the momentum is that of |u| = 0.3 along u, the mass is kept
     out, ok = solver.equilibrium_moments(np.array([[1.0, 0.5, 0.0, 0.0]], np.float32))
     assert ok[0] and abs(out[0, 0] - 1.0) <= 3e-5 and abs(out[0, 1] - 0.3) <= 3e-5
+
+
+def test_pinned_readback_equals_pageable():
+    """Fields read into page-locked mirrors (aeros_host_alloc) equal the ones
+    read into ordinary numpy arrays, twice in a row into the same mirrors."""
+    import json
+    import os
+    from aeros_gb300 import solver
+    from golden.cases import CASES, params_for, solver_mask
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+    case = CASES["sphere_trt_les_conv"]
+    mask = solver_mask(case)
+    s = solver.Solver(params_for(case, gold["cases"]["sphere_trt_les_conv"]["u_in"]), mask)
+    host = solver.pinned_fields(s.n)
+    for _ in range(2):
+        s.step(7)
+        a = s.fields()
+        b = s.fields(out=host)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
+    s.close()

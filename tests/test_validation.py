@@ -1,0 +1,150 @@
+"""The reference's published validation values, reproduced.
+
+tests/golden/validation.json holds the reference solver's own runs of its
+validation programs (physics_ref_headless.cpp: viscosity decay, grid order;
+thermal_headless.cpp: diffusion, advection, conduction, Rayleigh-Benard
+onset, buoyancy sign), generated by tests/golden/validation.py. The plain
+FP32 form is bitwise the reference's arithmetic, so the GPU (and the C
+oracle) must give the same field digests and therefore every printed number
+to the digits the reference prints it with.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from golden import validation as V
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIX = json.load(open(os.path.join(HERE, "golden", "validation.json")))
+GOLD = json.load(open(os.path.join(HERE, "golden", "golden.json")))
+
+# the reference's printed values and the formats it prints them with
+PRINTED = {
+    "decay_lambda": ("%.3e", "4.823e-04"),        # physics_ref_headless.cpp:220
+    "alpha_diffusion": ("%.6f", "0.048906"),      # thermal_headless.cpp:181
+    "advection_phase_speed": ("%.6f", "0.050008"),   # thermal_headless.cpp:228
+    "conduction_nusselt": ("%.4f", "1.0000"),     # thermal_headless.cpp:273
+    "rb_2500_amp_6000": ("%.5f", "0.14034"),      # thermal_headless.cpp:307
+    "rb_2500_amp_24000": ("%.5f", "0.14028"),
+    "rb_2500_nusselt": ("%.3f", "1.457"),
+    "rb_1000_nusselt": ("%.3f", "1.000"),
+    "rb_1700_nusselt": ("%.3f", "1.000"),
+}
+
+
+def _check_printed(summary):
+    for k, (fmt, want) in PRINTED.items():
+        assert fmt % summary[k] == want, (k, summary[k], want)
+    # the reference's own pass criteria (thermal_headless.cpp:182-334, physics_ref_headless.cpp:222-225)
+    assert abs(summary["decay_lambda"] - summary["decay_lambda_exact"]) / summary["decay_lambda_exact"] < 0.03
+    assert abs(summary["advection_phase_residual"]) < 0.05
+    assert summary["conduction_max_err"] < 0.01
+    assert summary["rb_1000_amp_24000"] <= 1e-4
+    assert summary["rb_1700_amp_24000"] < summary["rb_1700_amp_6000"]
+    assert summary["rb_2500_amp_24000"] > 0.9 * summary["rb_2500_amp_6000"]
+    assert summary["rb_2500_nusselt"] > 1.2
+    assert summary["buoyancy_hot"] > 0.0 > summary["buoyancy_cold"]
+
+
+def _check_runs(res, names):
+    for n in names:
+        assert res[n]["digest"] == FIX["runs"][n]["digest"], n
+        if "T_digest" in FIX["runs"][n]:
+            assert res[n]["T_digest"] == FIX["runs"][n]["T_digest"], n
+
+
+def test_fixture_carries_the_printed_values():
+    """The reference's own runs give the numbers its programs print."""
+    _check_printed(FIX["summary"])
+
+
+def test_grid_order_fixture():
+    """physics_ref_headless.cpp:227-243: L2 on H = 8, 16, 32 and the observed
+    order p = log(d12 / d23) / log 2, printed with 3 decimals."""
+    pr = GOLD["physref"]
+    p = math.log(abs(pr["h16_15k"]["l2"] - pr["h8_4k"]["l2"]) / abs(pr["bgk_40k"]["l2"] - pr["h16_15k"]["l2"])) / math.log(2)
+    assert "%.3f" % p == "1.796"
+
+
+def test_oracle_reproduces_validation_runs(oracle_built):
+    """The C restatement on the same runs: the reference's field digests
+    (u, rho and T after the last read) and so every printed number."""
+    O = oracle_built
+    res = V.solver_results(lambda p, m: O.OracleLBM(p, m), FIX)
+    _check_runs(res, V.RUNS)
+    _check_printed(V.summarise(res))
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_validation_runs():
+    """The GPU (FP32, the drop-in) on the reference's validation runs: the
+    reference's field digests, and the printed values to their digits:
+    viscosity 4.823e-4, diffusivity 0.048906, phase speed 0.050008,
+    conduction Nu 1.0000, Rayleigh-Benard Ra 2500 amplitude 0.140 and
+    Nu 1.457, no convection at Ra 1000 / 1700, buoyancy upward."""
+    from aeros_gb300 import solver
+    res = V.solver_results(lambda p, m: solver.Solver(p, m), FIX)
+    _check_runs(res, V.RUNS)
+    s = V.summarise(res)
+    print({k: s[k] for k in PRINTED})
+    _check_printed(s)
+
+
+@pytest.mark.gpu
+def test_gpu_grid_order():
+    """physics_ref_headless.cpp:227-243 on the GPU: the three channels
+    (H = 8, 16, 32; force scaled by 1 / H^2; 4000, 15000, 40000 steps), their
+    L2 errors equal the reference's, and the observed order is 1.796."""
+    from aeros_gb300 import capi, geometry, solver
+    l2 = {}
+    for key, ny, force, steps in (("h8_4k", 10, 7.8e-6 * 16.0, 4000), ("h16_15k", 18, 7.8e-6 * 4.0, 15000),
+                                  ("bgk_40k", 34, 7.8e-6, 40000)):
+        p = capi.make_params(8, ny, 8, tau=0.65, periodic_x=True, periodic_z=True, u_in=(0.08, 0, 0),
+                             u_init=(0.08, 0, 0), body_force=(force, 0, 0), vel_scale=12.5)
+        s = solver.Solver(p, geometry.channel_mask(8, ny, 8))
+        s.step(steps)
+        ux = s.fields()["ux"].reshape(8, ny, 8)
+        s.close()
+        prof = ux[4, 1:ny - 1, :].astype(np.float64).mean(axis=1)
+        exact = geometry.poiseuille_exact(ny, 0.65, force)
+        l2[key] = float(np.sqrt(np.sum((prof - exact) ** 2) / np.sum(exact ** 2)))
+        assert abs(l2[key] - GOLD["physref"][key]["l2"]) <= 1e-6 * GOLD["physref"][key]["l2"], key
+    p = math.log(abs(l2["h16_15k"] - l2["h8_4k"]) / abs(l2["bgk_40k"] - l2["h16_15k"])) / math.log(2)
+    print(f"grid order p = {p:.3f}")
+    assert "%.3f" % p == "1.796"
+
+
+CONFIGS = json.load(open(os.path.join(HERE, "golden", "configs.json")))["configs"]
+
+
+def _max_rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-30))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_gpu_full_size_config_equals_oracle(name):
+    """The full-size configurations in FP32 after their stated step counts:
+    the 240 x 120 x 115 sphere (free-slip walls, zero-gradient outlet, 200
+    steps) and the 128 x 34 x 128 Rayleigh-Benard domain at Ra 1e4 (2000
+    steps, both lattices). Fixture: the C restatement's field digests; on a
+    digest mismatch the restatement runs here and rho, u (and T) must agree
+    within 1e-5 max-relative, with the Nusselt number to 1e-5."""
+    from aeros_gb300 import solver
+    got = V.run_config(lambda p, m: solver.Solver(p, m), name)
+    want = CONFIGS[name]
+    same = got["digest"] == want["digest"] and got.get("T_digest") == want.get("T_digest")
+    if not same:
+        import oracle as O
+        O.build()
+        O.set_threads(os.cpu_count() or 1, "f32")
+        ref = V.run_config(lambda p, m: O.OracleLBM(p, m), name)
+        for k, v in ref["fields"].items():
+            assert _max_rel(got["fields"][k], v) <= 1e-5, (name, k, _max_rel(got["fields"][k], v))
+    if "nusselt" in want:
+        assert abs(got["nusselt"] - want["nusselt"]) <= 1e-5 * abs(want["nusselt"])
