@@ -358,6 +358,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (const char* e = getenv("AEROS_SPLIT")) h->split = atoi(e) != 0;
     if (const char* e = getenv("AEROS_FUSED")) h->fused = atoi(e) != 0;
+    if (const char* e = getenv("AEROS_STAGED")) h->staged = atoi(e) != 0;
     if (const char* e = getenv("AEROS_SHELL_BLOCKS")) h->shell_blocks_per_sm = std::max(1, std::min(8, atoi(e)));
 
     std::vector<int> shell;
@@ -369,8 +370,10 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         free_handle(h);                          \
         return rc;                               \
     }
-    ALLOC(h->f, ((size_t)h->qstride * Q19 + 64) * h->esize);
-    ALLOC(h->desc, (n + 64) * 4);
+    // tail padding: the staged kernel's rows may run up to STEP_BLOCK + 8
+    // elements past the last plane's end, its descriptor copies past ncell
+    ALLOC(h->f, ((size_t)h->qstride * Q19 + 64 + 4 * STEP_BLOCK) * h->esize);
+    ALLOC(h->desc, (n + 64 + 2 * STEP_BLOCK) * 4);
     ALLOC(h->shell, (size_t)std::max(1, h->n_shell) * 4);
     ALLOC(h->shell_kind, (size_t)std::max(1, h->n_shell) * 8);
     ALLOC(h->u[0], n * 16);
@@ -507,6 +510,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         for (int t = 0; t < 2; ++t) h->grid[o][t] = std::min(h->max_grid, std::max(1, h->sm_count) * h->L->occupancy(o, t));
     for (int o = 0; o < 2; ++o)
         for (int t = 0; t < 2; ++t) h->fused_grid[o][t] = std::max(1, h->sm_count) * h->L->fused_occupancy(o, t);
+    for (int o = 0; o < 2; ++o) h->stg_grid[o] = std::max(1, h->sm_count) * h->L->staged_occupancy(o);
     h->stats.avg_rho = 1.0f;
     h->stats.fluid_cells = h->fluid_cells;
     *out = h;
@@ -612,10 +616,21 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     {
         const int nsh = A.ntiles - A.ntiles_interior;
         A.fused = h->fused;
-        A.shell_blocks = A.fused ? std::min(nsh, std::max(1, h->sm_count) * h->shell_blocks_per_sm) : 0;
+        // staged interior (non-thermal): rows of 16-byte multiples need nx a
+        // multiple of 16 bytes of storage; tiles are linear runs of
+        // STEP_BLOCK cells from the first to the last interior cell
+        A.staged = h->staged && !h->th_on && h->n_interior > 0 && h->nx % h->L->staged_pad == 0;
+        if (A.staged) {
+            const int first = h->nx * h->ny + h->nx + 1, last = h->ncell - h->nx * h->ny - h->nx - 2;
+            A.stg_first = first / STEP_BLOCK;
+            A.stg_last = last / STEP_BLOCK;
+            A.stg_grid = h->stg_grid[0];
+            A.stg_grid_odd = h->stg_grid[1];
+        }
+        A.shell_blocks = (A.fused || A.staged) ? std::min(nsh, std::max(1, h->sm_count) * h->shell_blocks_per_sm) : 0;
         A.fused_grid = h->fused_grid[0][h->th_on ? 1 : 0];
         A.fused_grid_odd = h->fused_grid[1][h->th_on ? 1 : 0];
-        A.split = h->split && nsh > 0 && !A.fused;
+        A.split = h->split && nsh > 0 && !A.fused && !A.staged;
         A.shell_grid = A.split ? std::min(nsh, std::max(1, h->sm_count) * 4) : 0;
         A.shell_part_base = 0;   // set by the launcher (after the interior grid's slots)
     }
@@ -738,6 +753,15 @@ int finish_batch(aeros_lbm* h) {
     h->stats_dirty = false;
     Control& c = *h->ctl_host;
     aeros_lbm_stats& s = h->stats;
+    if (c.stage_timeout) {
+        // a bounded wait of the staged ring gave up: the step did not complete
+        c.stage_timeout = 0;
+        static const int zero = 0;
+        CUDA_TRY(cudaMemcpyAsync(&h->ctl->stage_timeout, &zero, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        return set_error(AEROS_ERR_TIMEOUT, "staged step: a shared-memory ring wait gave up; the populations of "
+                                            "this call are not valid");
+    }
     if (c.halt) {
         const long long executed = c.kexec - h->kexec_before;
         const long long launched = h->last_launches;

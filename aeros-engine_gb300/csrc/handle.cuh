@@ -98,6 +98,8 @@ struct aeros_lbm {
     int fused = 1;                // non-thermal: one launch, dynamic warp items (AEROS_FUSED=0: off)
     int shell_blocks_per_sm = 1;  // fused: shell blocks per SM (AEROS_SHELL_BLOCKS)
     int fused_grid[2][2] = {{0, 0}, {0, 0}};   // fused: interior blocks [odd][thermal]
+    bool staged = true;           // non-thermal steps through k_lbm_staged where nx allows (AEROS_STAGED)
+    int stg_grid[2] = {0, 0};     // staged: interior blocks [odd]
     long long last_kernels = 0;   // kernel launches of the last step call
     aeros_batch* batch = nullptr; // batch this domain is a member of
 };

@@ -165,6 +165,8 @@ struct Launchers {
     cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s);
     int (*batch_occupancy)();
     int (*fused_occupancy)(bool odd, bool thermal);
+    int (*staged_occupancy)(bool odd);
+    int staged_pad;             // nx must be a multiple of this for the staged kernel (16 bytes of storage)
 };
 
 const Launchers& launchers_fp32();
@@ -175,7 +177,9 @@ const Launchers& launchers_bf16();
     namespace NAME##_detail {                                                                                         \
     template <bool O, bool T, bool M>                                                                                 \
     cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
-        if (!M && A.fused) {                                                                                          \
+        if (!M && !T && A.staged) {                                                                                   \
+            k_lbm_staged<STORE, O><<<(O ? A.stg_grid_odd : A.stg_grid) + A.shell_blocks, STG_THREADS, StgLayout<STORE>::BYTES, s>>>(A, V);     \
+        } else if (!M && A.fused) {                                                                                   \
             k_lbm_fused<STORE, O, T><<<(O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V); \
         } else if (!M && A.split) {                                                                                   \
             StepArgs B = A;                                                                                           \
@@ -250,6 +254,21 @@ const Launchers& launchers_bf16();
         }                                                                                                             \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \
+    int staged_occ_(bool odd) {                                                                                       \
+        int n = 0;                                                                                                    \
+        if (odd) {                                                                                                    \
+            cudaFuncSetAttribute(k_lbm_staged<STORE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,              \
+                                 StgLayout<STORE>::BYTES);                                                            \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_staged<STORE, true>, STG_THREADS,                 \
+                                                          StgLayout<STORE>::BYTES);                                   \
+        } else {                                                                                                      \
+            cudaFuncSetAttribute(k_lbm_staged<STORE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
+                                 StgLayout<STORE>::BYTES);                                                            \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_staged<STORE, false>, STG_THREADS,                \
+                                                          StgLayout<STORE>::BYTES);                                   \
+        }                                                                                                             \
+        return n > 0 ? n : 1;                                                                                         \
+    }                                                                                                                 \
     int batch_occ_() {                                                                                                \
         int n = 0, m = 0;                                                                                             \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_step<STORE, false, 1>, BATCH_BLOCK, 0);              \
@@ -260,7 +279,9 @@ const Launchers& launchers_bf16();
     }                                                                                                                 \
     const Launchers& NAME() {                                                                                         \
         using namespace NAME##_detail;                                                                                \
-        static const Launchers L = {step_, occupancy_, fill_, seteq_, writepre_, reset_, thfill_, batch_, batch_occ_, fused_occ_};                    \
+        static const Launchers L = {step_,      occupancy_, fill_,      seteq_,      writepre_,                     \
+                                    reset_,     thfill_,    batch_,     batch_occ_,  fused_occ_,                    \
+                                    staged_occ_, StgLayout<STORE>::PAD};                                              \
         return L;                                                                                                     \
     }
 

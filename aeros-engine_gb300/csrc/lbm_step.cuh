@@ -49,7 +49,7 @@ struct Control {
     int halt;               // divergence guard tripped: later steps return at once
     int halt_kind;          // 1: NaN count before streaming, 2: mean density
     int th_valid;           // Nusselt updated at least once
-    int pad0;
+    int stage_timeout;      // a staged-ring wait gave up (k_lbm_staged): the step's result is not valid
     long long steps;        // counted steps (lbmCurrentStep)
     long long kexec;        // step bodies executed
     float prev_kinetic;
@@ -111,6 +111,9 @@ struct StepArgs {
     int shell_blocks;           // fused: blocks given to the boundary shell
     int fused_grid;             // fused even steps: interior blocks (resident blocks per SM x SMs)
     int fused_grid_odd;         // fused odd steps (own register budget, own occupancy)
+    int staged;                 // interior tiles staged through a shared-memory ring (k_lbm_staged)
+    int stg_first, stg_last;    // staged: first and last linear tile of STEP_BLOCK cells holding interior cells
+    int stg_grid, stg_grid_odd; // staged: interior blocks of even / odd steps (resident blocks per SM x SMs)
     int inlet_pos;              // inlet plane coordinate along the flow axis
     const int* zg_src;          // zero-gradient outlet: plane index each unknown q of outlet-plane
                                 // cell pi reads, at [q * out_plane + pi] (NULL: computed)
@@ -1239,10 +1242,25 @@ struct WarpSums {               // one warp's sums over the slices of a work ite
     long long nu, tsum, nun;    // thermal: fixed point, fixed point, count
 };
 
-constexpr float FX_SUM = 1099511627776.0f;   // 2^40: sums of rho - 1 and |u|^2 per slice
-constexpr float FX_TKE = 1048576.0f;         // 2^20: TKE per slice (up to 32 x 1e6)
+// Fixed-point units of the per-cell statistics. Each cell's value is rounded
+// to its unit once and the integers are summed exactly (warp redux, then
+// 64-bit atomics), so the totals do not depend on how cells are grouped into
+// slices, blocks or launches.
+constexpr float FX_DRHO = 16777216.0f;         // 2^24: rho - 1 (|rho - 1| <= 0.5; exact for the plain form)
+constexpr float FX_KE = 1099511627776.0f;      // 2^40: |u|^2 (<= 0.09 after the limiter)
+constexpr float FX_TKE = 1073741824.0f;        // 2^30: TKE (0 .. 1e6)
 constexpr double FX_NU = 4294967296.0;       // 2^32: Nusselt row terms per slice (|term| <= 4)
 constexpr float FX_T = 16777216.0f;          // 2^24: temperatures per slice (|T| <= 1.5)
+
+// Exact warp sum of a non-negative value in units of 1/scale (x * scale <
+// 2^50): high and low 24-bit parts are summed by redux separately.
+__device__ __forceinline__ long long warp_fixed_sum(float x, float scale) {
+    const float y = x * scale;
+    const float hi = floorf(y * 0x1p-24f);
+    const unsigned h = (unsigned)hi;
+    const unsigned l = (unsigned)(y - hi * 0x1p24f);
+    return ((long long)__reduce_add_sync(0xffffffffu, h) << 24) + (long long)__reduce_add_sync(0xffffffffu, l);
+}
 
 __device__ __forceinline__ float warp_allsum(float v) {
 #pragma unroll
@@ -1288,6 +1306,85 @@ __device__ __forceinline__ int interior_cell_index(const StepArgs& A, int li) {
 #define AEROS_FUSED_TH_MIN_BLOCKS 6
 #endif
 
+// One 32-cell slice's statistics into the warp's running sums: FP32 warp sums
+// (a fixed shuffle tree over a fixed set of cells) converted to 64-bit fixed
+// point, so that the totals do not depend on which block took which slice.
+template <bool THERMAL>
+__device__ __forceinline__ void add_slice_sums(WarpSums& W, const Acc& acc, float& mx, int lane) {
+    const long long sd = (int)__reduce_add_sync(0xffffffffu, (unsigned)__float2int_rn(acc.drho * FX_DRHO));
+    const long long sk = warp_fixed_sum(acc.ke, FX_KE), st = warp_fixed_sum(acc.tke, FX_TKE);
+    mx = fmaxf(mx, acc.maxu2);
+    const int cells = __popc(__ballot_sync(0xffffffffu, acc.cells != 0));
+    const bool rare = __any_sync(0xffffffffu, (acc.nan | acc.neg | acc.bad | acc.rout | acc.rnf | acc.ulim) != 0);
+    int c6[6] = {0, 0, 0, 0, 0, 0};
+    if (rare) {
+        c6[0] = warp_allsum(acc.nan); c6[1] = warp_allsum(acc.neg); c6[2] = warp_allsum(acc.bad);
+        c6[3] = warp_allsum(acc.rout); c6[4] = warp_allsum(acc.rnf); c6[5] = warp_allsum(acc.ulim);
+    }
+    if (lane == 0) {
+        W.drho += sd;
+        W.ke += sk;
+        W.tke += st;
+        W.cnt[6] += cells;
+        if (rare)
+            for (int j = 0; j < 6; ++j) W.cnt[j] += c6[j];
+    }
+    if constexpr (THERMAL) {
+        double nu = acc.nu;   // a fixed shuffle tree over the slice's cells
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nu += __shfl_xor_sync(0xffffffffu, nu, o);
+        const float ts = warp_allsum(acc.tsum);
+        const int nun = (int)__reduce_add_sync(0xffffffffu, (unsigned)acc.nun);
+        if (lane == 0) {
+            W.nu += __double2ll_rn(nu * FX_NU);
+            W.tsum += __float2ll_rn(ts * FX_T);
+            W.nun += nun;
+        }
+    }
+}
+
+// A warp's sums of the step into the domain's fixed-point accumulators; the
+// last of the step's `nwarps` warps applies the totals (statistics, divergence
+// guard, Nusselt number) and rewinds the accumulators for the next step.
+template <bool THERMAL>
+__device__ __forceinline__ void finish_warp_sums(const StepArgs& A, const WarpSums& W, float mx, int lane,
+                                                 unsigned int nwarps) {
+    Control* ctl = A.ctl;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __syncwarp();
+    if (lane == 0) atomicAdd(&ctl->fx_drho, (unsigned long long)W.drho);
+    else if (lane == 1) atomicAdd(&ctl->fx_ke, (unsigned long long)W.ke);
+    else if (lane == 2) atomicAdd(&ctl->fx_tke, (unsigned long long)W.tke);
+    else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ctl->fx_cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
+    else if (lane == 10 && mx > 0.0f) atomicMax(&ctl->fx_maxu2, __float_as_uint(mx));
+    else if (THERMAL && lane == 11) atomicAdd(&ctl->fx_nu, (unsigned long long)W.nu);
+    else if (THERMAL && lane == 12) atomicAdd(&ctl->fx_tsum, (unsigned long long)W.tsum);
+    else if (THERMAL && lane == 13) atomicAdd(&ctl->fx_nun, (unsigned long long)W.nun);
+    __threadfence();
+    __syncwarp();
+    int last = 0;
+    if (lane == 0) last = atomicAdd(&ctl->warps_done, 1u) == nwarps - 1;
+    if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
+        __threadfence();
+        volatile Control* vc = ctl;
+        const double t[5] = {(double)(long long)vc->fx_drho / (double)FX_DRHO, (double)(long long)vc->fx_ke / (double)FX_KE,
+                             (double)(long long)vc->fx_tke / (double)FX_TKE,
+                             THERMAL ? (double)(long long)vc->fx_nu / FX_NU : 0.0,
+                             THERMAL ? (double)(long long)vc->fx_tsum / (double)FX_T : 0.0};
+        const long long c[8] = {(long long)vc->fx_cnt[0], (long long)vc->fx_cnt[1], (long long)vc->fx_cnt[2],
+                                (long long)vc->fx_cnt[3], (long long)vc->fx_cnt[4], (long long)vc->fx_cnt[5],
+                                THERMAL ? (long long)vc->fx_nun : 0, (long long)vc->fx_cnt[6]};
+        const float m = __uint_as_float(vc->fx_maxu2);
+        vc->fx_drho = 0; vc->fx_ke = 0; vc->fx_tke = 0;
+        for (int j = 0; j < 7; ++j) vc->fx_cnt[j] = 0;
+        vc->fx_nu = 0; vc->fx_tsum = 0; vc->fx_nun = 0;
+        vc->fx_maxu2 = 0;
+        vc->warps_done = 0;
+        apply_totals(A, t, m, c);   // also rewinds tile_next
+    }
+}
+
 // The single-launch step: the first shell_blocks blocks take the boundary
 // shell's tiles, the others take interior tiles from a counter. THERMAL: the
 // D3Q7 lattice stepped in the same thread (its Nusselt row sum and mean
@@ -1309,37 +1406,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
     __syncwarp();
     float mx = 0.0f;
     Control* ctl = A.ctl;
-    auto add_slice = [&](const Acc& acc) {
-        const float sd = warp_allsum(acc.drho), sk = warp_allsum(acc.ke), st = warp_allsum(acc.tke);
-        mx = fmaxf(mx, acc.maxu2);
-        const int cells = __popc(__ballot_sync(0xffffffffu, acc.cells != 0));
-        const bool rare = __any_sync(0xffffffffu, (acc.nan | acc.neg | acc.bad | acc.rout | acc.rnf | acc.ulim) != 0);
-        int c6[6] = {0, 0, 0, 0, 0, 0};
-        if (rare) {
-            c6[0] = warp_allsum(acc.nan); c6[1] = warp_allsum(acc.neg); c6[2] = warp_allsum(acc.bad);
-            c6[3] = warp_allsum(acc.rout); c6[4] = warp_allsum(acc.rnf); c6[5] = warp_allsum(acc.ulim);
-        }
-        if (lane == 0) {
-            W.drho += __float2ll_rn(sd * FX_SUM);
-            W.ke += __float2ll_rn(sk * FX_SUM);
-            W.tke += __float2ll_rn(st * FX_TKE);
-            W.cnt[6] += cells;
-            if (rare)
-                for (int j = 0; j < 6; ++j) W.cnt[j] += c6[j];
-        }
-        if constexpr (THERMAL) {
-            double nu = acc.nu;   // a fixed shuffle tree over the slice's cells
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) nu += __shfl_xor_sync(0xffffffffu, nu, o);
-            const float ts = warp_allsum(acc.tsum);
-            const int nun = (int)__reduce_add_sync(0xffffffffu, (unsigned)acc.nun);
-            if (lane == 0) {
-                W.nu += __double2ll_rn(nu * FX_NU);
-                W.tsum += __float2ll_rn(ts * FX_T);
-                W.nun += nun;
-            }
-        }
-    };
+    auto add_slice = [&](const Acc& acc) { add_slice_sums<THERMAL>(W, acc, mx, lane); };
     const int nsh = A.ntiles - A.ntiles_interior;
     if ((int)blockIdx.x < A.shell_blocks) {
         for (int st = blockIdx.x; st < nsh; st += A.shell_blocks) {
@@ -1407,39 +1474,237 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             add_slice(acc);
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    __syncwarp();
-    if (lane == 0) atomicAdd(&ctl->fx_drho, (unsigned long long)W.drho);
-    else if (lane == 1) atomicAdd(&ctl->fx_ke, (unsigned long long)W.ke);
-    else if (lane == 2) atomicAdd(&ctl->fx_tke, (unsigned long long)W.tke);
-    else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ctl->fx_cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
-    else if (lane == 10 && mx > 0.0f) atomicMax(&ctl->fx_maxu2, __float_as_uint(mx));
-    else if (THERMAL && lane == 11) atomicAdd(&ctl->fx_nu, (unsigned long long)W.nu);
-    else if (THERMAL && lane == 12) atomicAdd(&ctl->fx_tsum, (unsigned long long)W.tsum);
-    else if (THERMAL && lane == 13) atomicAdd(&ctl->fx_nun, (unsigned long long)W.nun);
-    __threadfence();
-    __syncwarp();
-    int last = 0;
-    if (lane == 0) last = atomicAdd(&ctl->warps_done, 1u) == gridDim.x * (STEP_BLOCK / 32) - 1;
-    if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
-        __threadfence();
-        volatile Control* vc = ctl;
-        const double t[5] = {(double)(long long)vc->fx_drho / (double)FX_SUM, (double)(long long)vc->fx_ke / (double)FX_SUM,
-                             (double)(long long)vc->fx_tke / (double)FX_TKE,
-                             THERMAL ? (double)(long long)vc->fx_nu / FX_NU : 0.0,
-                             THERMAL ? (double)(long long)vc->fx_tsum / (double)FX_T : 0.0};
-        const long long c[8] = {(long long)vc->fx_cnt[0], (long long)vc->fx_cnt[1], (long long)vc->fx_cnt[2],
-                                (long long)vc->fx_cnt[3], (long long)vc->fx_cnt[4], (long long)vc->fx_cnt[5],
-                                THERMAL ? (long long)vc->fx_nun : 0, (long long)vc->fx_cnt[6]};
-        const float m = __uint_as_float(vc->fx_maxu2);
-        vc->fx_drho = 0; vc->fx_ke = 0; vc->fx_tke = 0;
-        for (int j = 0; j < 7; ++j) vc->fx_cnt[j] = 0;
-        vc->fx_nu = 0; vc->fx_tsum = 0; vc->fx_nun = 0;
-        vc->fx_maxu2 = 0;
-        vc->warps_done = 0;
-        apply_totals(A, t, m, c);   // also rewinds tile_next
+    finish_warp_sums<THERMAL>(A, W, mx, lane, gridDim.x * (STEP_BLOCK / 32));
+}
+
+// ---- staged interior: bulk copies into a shared-memory ring -----------------------
+// The interior's populations reach the threads through shared memory. A block
+// is STEP_BLOCK consumer threads (one cell each) plus one producer warp. Its
+// tiles are linear runs of STEP_BLOCK cells (tile t = cells t*T .. t*T+T-1,
+// shell and wall lanes idle), taken statically: block b gets tiles
+// stg_first + b, + G, + 2G, ... For each tile the producer's lane 0 issues
+// 19 bulk copies (cp.async.bulk, one row of T + PAD elements per plane: the
+// plane the step gathers direction q from, shifted by the neighbour offset
+// and rounded down to 16 bytes) and one of the tile's descriptors into the
+// next free stage of a STG_STAGES-deep ring; a stage's "full" mbarrier
+// completes on the copies' bytes, its "empty" mbarrier on the consumer warps'
+// release. No block-wide barrier after set-up: consumers wait on full,
+// producer on empty, both with bounded waits (a wait that gives up sets
+// Control::stage_timeout and stops the block's work; the host reports it).
+// The copies keep STG_STAGES tiles of populations in flight per block without
+// holding them in registers. Requires nx to be a multiple of 16 bytes of
+// storage (8 cells FP16/BF16, 4 FP32), so that every row starts on a 16-byte
+// boundary at a fixed element offset per direction.
+constexpr int STG_STAGES = 4;
+constexpr int STG_THREADS = STEP_BLOCK + 32;
+constexpr uint32_t STG_WAIT_LIMIT = 1u << 22;   // try_wait rounds before a wait gives up
+#ifndef AEROS_STG_MIN_BLOCKS
+#define AEROS_STG_MIN_BLOCKS 6
+#endif
+
+template <class S>
+struct StgLayout {
+    static constexpr int ESZ = (int)sizeof(typename S::T);
+    static constexpr int PAD = 16 / ESZ;                    // elements of alignment slack per row
+    static constexpr int ROW = (STEP_BLOCK + PAD) * ESZ;   // bytes per staged row (a multiple of 16)
+    static constexpr int DESC = STEP_BLOCK * 4;
+    static constexpr int STAGE = Q19 * ROW + DESC;
+    static constexpr int BYTES = STG_STAGES * STAGE;       // dynamic shared memory of a block
+    // element offset of a cell's value in the odd-step row of direction q:
+    // the row starts at c0 - nb_q rounded down to PAD elements, and nb_q = c_x
+    // modulo PAD when nx is a multiple of PAD
+    __host__ __device__ static constexpr int moff(int q) {
+        return cx19(q) > 0 ? PAD - 1 : (cx19(q) < 0 ? 1 : 0);
     }
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// true once the barrier's phase of the given parity has completed; false when
+// STG_WAIT_LIMIT rounds of try_wait (each may suspend briefly) did not see it
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < STG_WAIT_LIMIT; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// bulk copy global -> shared completing on an mbarrier (16-byte aligned
+// addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// One interior cell of a staged tile (non-thermal). rows: this thread's
+// element in the stage's plane rows (stage + t * ESZ).
+template <class S, bool ODD>
+__device__ __forceinline__ void staged_cell(const StepArgs& A, const StepVar& V, int cell, uint32_t d,
+                                            const unsigned char* rows, Acc& acc) {
+    using L = StgLayout<S>;
+    using T = typename S::T;
+    constexpr bool SH = S::shifted;
+    float f[Q19];
+    float strainPre = 0.0f;
+    if (A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
+    auto staged = [&](int q) {
+        const T* p = reinterpret_cast<const T*>(rows + q * L::ROW + (ODD ? L::moff(q) * L::ESZ : 0));
+        if constexpr (SH) return fmaf(S::raw_load(p), S::kInv, A.dq[q]);
+        else return S::raw_load(p);
+    };
+    const bool plain = (d & D_LINKS) == 0;   // no wall next to the cell
+    if (!ODD || plain) {
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) f[q] = staged(q);
+    } else {
+        // links to walls read the cell's own slot (bounce-back), the others the stage
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) f[q] = ((d >> q) & 1u) ? ldp<S>(A, q, fplane<S>(A, q) + cell) : staged(q);
+    }
+    CellResult r;
+    collide19<SH>(f, A, d, false, false, strainPre, 0.0f, r, acc);
+    const uint32_t os = (d >> D_OUT_SHIFT) & 3u;   // planes Nx-2 / Nx-3 feed the outlet
+    if (os) {
+        const uint32_t rr = A.div_x.div((uint32_t)cell);
+        const int x = cell - (int)rr * A.nx;
+        const uint32_t z = A.div_y.div(rr);
+        const int y = (int)(rr - z * (uint32_t)A.ny);
+        const int P = A.out_plane;
+        const int pi = plane_index(A, x, y, (int)z);
+#pragma unroll
+        for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
+    }
+    if (!ODD) {
+        if (!SH || plain) {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, opp19(j)) + cell, f[j]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) {
+                const bool solid = (d >> opp19(j)) & 1u;   // c + c_j is a wall: read back as opp j
+                stp<S>(A, solid ? opp19(j) : j, fplane<S>(A, opp19(j)) + cell, f[j]);
+            }
+        }
+    } else if (plain) {
+#pragma unroll
+        for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < Q19; ++j) {
+            const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
+            if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
+            else stp<S>(A, j, fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+        }
+    }
+    if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
+    if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
+}
+
+// One lattice step (non-thermal) in one launch: shell blocks as in
+// k_lbm_fused, interior blocks through the staged ring.
+template <class S, bool ODD>
+__global__ void __launch_bounds__(STG_THREADS, AEROS_STG_MIN_BLOCKS) k_lbm_staged(const StepArgs A, const StepVar V) {
+    using L = StgLayout<S>;
+    if (A.ctl->halt) return;   // uniform: every thread reads the same flag
+    extern __shared__ __align__(128) unsigned char stg_smem[];
+    __shared__ __align__(8) unsigned long long bar_full[STG_STAGES], bar_empty[STG_STAGES];
+    __shared__ WarpSums s_sums[STEP_BLOCK / 32];
+    const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
+    constexpr int PRODUCER = STEP_BLOCK / 32;   // warp index of the producer
+    const bool shell_block = (int)blockIdx.x < A.shell_blocks;
+    if (!shell_block && threadIdx.x == 0) {
+        for (int s = 0; s < STG_STAGES; ++s) {
+            mbar_init(smem_u32(&bar_full[s]), 1u);
+            mbar_init(smem_u32(&bar_empty[s]), (uint32_t)PRODUCER);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int b = (int)blockIdx.x - A.shell_blocks;
+    const int G = (int)gridDim.x - A.shell_blocks;
+    if (wid == PRODUCER) {
+        if (shell_block || lane != 0) return;
+        const uint32_t row_bytes = (uint32_t)((ODD ? STEP_BLOCK + L::PAD : STEP_BLOCK) * L::ESZ);
+        const uint32_t tx = Q19 * row_bytes + (uint32_t)L::DESC;
+        for (int k = 0;; ++k) {
+            const int tile = A.stg_first + b + k * G;
+            if (tile > A.stg_last) break;
+            const int s = k % STG_STAGES;
+            if (k >= STG_STAGES && !mbar_wait(smem_u32(&bar_empty[s]), (uint32_t)(((k / STG_STAGES) & 1) ^ 1))) {
+                atomicExch(&A.ctl->stage_timeout, 1);
+                break;
+            }
+            if (*(volatile int*)&A.ctl->stage_timeout) break;
+            const uint32_t full = smem_u32(&bar_full[s]);
+            mbar_expect_tx(full, tx);
+            const uint32_t st = smem_u32(stg_smem + s * L::STAGE);
+            const long long c0 = (long long)tile * STEP_BLOCK;
+#pragma unroll
+            for (int q = 0; q < Q19; ++q) {
+                const char* plane = static_cast<const char*>(A.fq[ODD ? opp19(q) : q]);
+                const long long x0 = ODD ? c0 - nb19(A, q) - L::moff(q) : c0;
+                bulk_g2s(st + q * L::ROW, plane + x0 * L::ESZ, row_bytes, full);
+            }
+            bulk_g2s(st + Q19 * L::ROW, A.desc + c0, (uint32_t)L::DESC, full);
+        }
+        return;
+    }
+    WarpSums& W = s_sums[wid];
+    if (lane == 0) {
+        W.drho = W.ke = W.tke = 0;
+        for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
+        W.nu = W.tsum = W.nun = 0;
+    }
+    __syncwarp();
+    float mx = 0.0f;
+    if (shell_block) {
+        const int nsh = A.ntiles - A.ntiles_interior;
+        for (int st = blockIdx.x; st < nsh; st += A.shell_blocks) {
+            Acc acc;
+            acc.zero();
+            shell_tile<S, ODD, false, false>(A, V, st, acc);
+            add_slice_sums<false>(W, acc, mx, lane);
+        }
+    } else {
+        const int t = (int)threadIdx.x;
+        for (int k = 0;; ++k) {
+            const int tile = A.stg_first + b + k * G;
+            if (tile > A.stg_last) break;
+            const int s = k % STG_STAGES;
+            if (!mbar_wait(smem_u32(&bar_full[s]), (uint32_t)((k / STG_STAGES) & 1))) {
+                atomicExch(&A.ctl->stage_timeout, 1);
+                break;
+            }
+            const unsigned char* stage = stg_smem + s * L::STAGE;
+            const uint32_t d = reinterpret_cast<const uint32_t*>(stage + Q19 * L::ROW)[t];
+            const int cell = tile * STEP_BLOCK + t;
+            Acc acc;
+            acc.zero();
+            if (cell < A.ncell && !(d & (D_WALL | D_SHELL))) staged_cell<S, ODD>(A, V, cell, d, stage + t * L::ESZ, acc);
+            add_slice_sums<false>(W, acc, mx, lane);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bar_empty[s]));
+        }
+    }
+    finish_warp_sums<false>(A, W, mx, lane, gridDim.x * (STEP_BLOCK / 32));
 }
 
 // ---- many domains in one persistent kernel -----------------------------------
@@ -1533,7 +1798,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_s
         if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
             __threadfence();
             volatile BatchAcc* va = ac;
-            const double t[5] = {(double)(long long)va->drho / (double)FX_SUM, (double)(long long)va->ke / (double)FX_SUM,
+            const double t[5] = {(double)(long long)va->drho / (double)FX_DRHO, (double)(long long)va->ke / (double)FX_KE,
                                  (double)(long long)va->tke / (double)FX_TKE, 0.0, 0.0};
             const long long c[8] = {(long long)va->cnt[0], (long long)va->cnt[1], (long long)va->cnt[2],
                                     (long long)va->cnt[3], (long long)va->cnt[4], (long long)va->cnt[5], 0,
@@ -1591,23 +1856,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_s
             const int idx = (wk.slice0 + sl) * 32 + lane;
             if (KIND == 0) shell_cell<S, ODD, false, false>(A, V, idx, acc);
             else interior_cell<S, ODD, false, false>(A, V, idx, acc);
-            const float sd = warp_allsum(acc.drho), sk = warp_allsum(acc.ke), st = warp_allsum(acc.tke);
-            mx = fmaxf(mx, acc.maxu2);
-            const int cells = __popc(__ballot_sync(0xffffffffu, acc.cells != 0));
-            const bool rare = __any_sync(0xffffffffu, (acc.nan | acc.neg | acc.bad | acc.rout | acc.rnf | acc.ulim) != 0);
-            int c6[6] = {0, 0, 0, 0, 0, 0};
-            if (rare) {
-                c6[0] = warp_allsum(acc.nan); c6[1] = warp_allsum(acc.neg); c6[2] = warp_allsum(acc.bad);
-                c6[3] = warp_allsum(acc.rout); c6[4] = warp_allsum(acc.rnf); c6[5] = warp_allsum(acc.ulim);
-            }
-            if (lane == 0) {
-                W.drho += __float2ll_rn(sd * FX_SUM);
-                W.ke += __float2ll_rn(sk * FX_SUM);
-                W.tke += __float2ll_rn(st * FX_TKE);
-                W.cnt[6] += cells;
-                if (rare)
-                    for (int j = 0; j < 6; ++j) W.cnt[j] += c6[j];
-            }
+            add_slice_sums<false>(W, acc, mx, lane);
             ++w_slices;
         }
     }

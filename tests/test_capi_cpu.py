@@ -130,6 +130,6 @@ def test_bench_control_block_size_matches_device_struct(tmp_path):
     src.write_text('#include <cstdio>\n#include "lbm_step.cuh"\n'
                    'int main() { printf("%zu\\n", sizeof(aeros::Control)); return 0; }\n')
     exe = tmp_path / "t"
-    subprocess.check_call(["nvcc", "-std=c++17", "-I", os.path.join(ROOT, "aeros-engine_gb300", "csrc"), str(src),
-                           "-o", str(exe)])
+    subprocess.check_call(["nvcc", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-I",
+                           os.path.join(ROOT, "aeros-engine_gb300", "csrc"), str(src), "-o", str(exe)])
     assert int(subprocess.check_output([str(exe)]).decode().strip()) == bench.CONTROL_BYTES
