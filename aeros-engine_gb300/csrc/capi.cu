@@ -76,8 +76,8 @@ static void free_handle(aeros_lbm* h) {
     cudaFree(h->post_parts);
     cudaFree(h->post_out);
     cudaFree(h->post_counter);
-    cudaFree(h->u[0]);
-    cudaFree(h->u[1]);
+    cudaFree(h->u_alloc[0]);
+    cudaFree(h->u_alloc[1]);
     cudaFree(h->rho);
     cudaFree(h->strain);
     cudaFree(h->tke);
@@ -358,8 +358,11 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (const char* e = getenv("AEROS_SPLIT")) h->split = atoi(e) != 0;
     if (const char* e = getenv("AEROS_FUSED")) h->fused = atoi(e) != 0;
-    if (const char* e = getenv("AEROS_STAGED")) h->staged = atoi(e) != 0;
-    if (const char* e = getenv("AEROS_SHELL_BLOCKS")) h->shell_blocks_per_sm = std::max(1, std::min(8, atoi(e)));
+    if (const char* e = getenv("AEROS_WARP")) h->warp = atoi(e) != 0;
+    // measured on the sphere workload: 16-bit storage steps fastest with the
+    // shell's tiles first in the interior queue, FP32 with one shell block per SM
+    h->shell_blocks_per_sm = h->esize == 2 ? 0 : 1;
+    if (const char* e = getenv("AEROS_SHELL_BLOCKS")) h->shell_blocks_per_sm = std::max(0, std::min(8, atoi(e)));
 
     std::vector<int> shell;
     host_geometry(h, shell);
@@ -370,14 +373,18 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         free_handle(h);                          \
         return rc;                               \
     }
-    // tail padding: the staged kernel's rows may run up to STEP_BLOCK + 8
-    // elements past the last plane's end, its descriptor copies past ncell
+    // tail padding: the warp tiles' odd-step rows may run up to a tile + 16
+    // bytes past the last plane's end, their descriptor copies past ncell
     ALLOC(h->f, ((size_t)h->qstride * Q19 + 64 + 4 * STEP_BLOCK) * h->esize);
     ALLOC(h->desc, (n + 64 + 2 * STEP_BLOCK) * 4);
     ALLOC(h->shell, (size_t)std::max(1, h->n_shell) * 4);
     ALLOC(h->shell_kind, (size_t)std::max(1, h->n_shell) * 8);
-    ALLOC(h->u[0], n * 16);
-    ALLOC(h->u[1], n * 16);
+    // velocity buffers with VEL_GUARD cells of slack on both sides (the warp
+    // tiles' stencil rows of the first and last tiles reach past the domain)
+    for (int i = 0; i < 2; ++i) {
+        ALLOC(h->u_alloc[i], (n + 2 * (size_t)VEL_GUARD) * 16);
+        h->u[i] = h->u_alloc[i] + VEL_GUARD;
+    }
     ALLOC(h->rho, n * 4);
     ALLOC(h->strain, n * 4);
     ALLOC(h->tke, n * 4);
@@ -510,7 +517,7 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
         for (int t = 0; t < 2; ++t) h->grid[o][t] = std::min(h->max_grid, std::max(1, h->sm_count) * h->L->occupancy(o, t));
     for (int o = 0; o < 2; ++o)
         for (int t = 0; t < 2; ++t) h->fused_grid[o][t] = std::max(1, h->sm_count) * h->L->fused_occupancy(o, t);
-    for (int o = 0; o < 2; ++o) h->stg_grid[o] = std::max(1, h->sm_count) * h->L->staged_occupancy(o);
+    for (int o = 0; o < 2; ++o) h->warp_grid[o] = std::max(1, h->sm_count) * h->L->warp_occupancy(o);
     h->stats.avg_rho = 1.0f;
     h->stats.fluid_cells = h->fluid_cells;
     *out = h;
@@ -616,21 +623,28 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     {
         const int nsh = A.ntiles - A.ntiles_interior;
         A.fused = h->fused;
-        // staged interior (non-thermal): rows of 16-byte multiples need nx a
-        // multiple of 16 bytes of storage; tiles are linear runs of
-        // STEP_BLOCK cells from the first to the last interior cell
-        A.staged = h->staged && !h->th_on && h->n_interior > 0 && h->nx % h->L->staged_pad == 0;
-        if (A.staged) {
+        // warp tiles (non-thermal): rows start on 16-byte boundaries when nx is
+        // a multiple of 16 bytes of storage; tiles are linear runs of WT cells
+        // from the first to the last interior cell, inside the domain when
+        // nx*ny >= WT; chunk offsets are 32-bit
+        const int WT = h->L->warp_tile;
+        const bool small = (double)h->qstride * Q19 * h->esize + 64.0 * WT < 2147483647.0;
+        A.warp = h->warp && !h->th_on && h->n_interior > 0 && h->nx % h->L->warp_pad == 0 &&
+                 h->nx * h->ny >= WT && small;
+        if (A.warp) {
             const int first = h->nx * h->ny + h->nx + 1, last = h->ncell - h->nx * h->ny - h->nx - 2;
-            A.stg_first = first / STEP_BLOCK;
-            A.stg_last = last / STEP_BLOCK;
-            A.stg_grid = h->stg_grid[0];
-            A.stg_grid_odd = h->stg_grid[1];
+            A.wt_first = first / WT;
+            A.wt_last = last / WT;
+            A.warp_grid = h->warp_grid[0];
+            A.warp_grid_odd = h->warp_grid[1];
         }
-        A.shell_blocks = (A.fused || A.staged) ? std::min(nsh, std::max(1, h->sm_count) * h->shell_blocks_per_sm) : 0;
+        // the warp tiles need shell blocks; the fused kernel without them takes
+        // the shell's tiles first from its queue
+        const int per_sm = A.warp ? std::max(1, h->shell_blocks_per_sm) : h->shell_blocks_per_sm;
+        A.shell_blocks = (A.fused || A.warp) ? std::min(nsh, std::max(1, h->sm_count) * per_sm) : 0;
         A.fused_grid = h->fused_grid[0][h->th_on ? 1 : 0];
         A.fused_grid_odd = h->fused_grid[1][h->th_on ? 1 : 0];
-        A.split = h->split && nsh > 0 && !A.fused && !A.staged;
+        A.split = h->split && nsh > 0 && !A.fused && !A.warp;
         A.shell_grid = A.split ? std::min(nsh, std::max(1, h->sm_count) * 4) : 0;
         A.shell_part_base = 0;   // set by the launcher (after the interior grid's slots)
     }
@@ -753,15 +767,6 @@ int finish_batch(aeros_lbm* h) {
     h->stats_dirty = false;
     Control& c = *h->ctl_host;
     aeros_lbm_stats& s = h->stats;
-    if (c.stage_timeout) {
-        // a bounded wait of the staged ring gave up: the step did not complete
-        c.stage_timeout = 0;
-        static const int zero = 0;
-        CUDA_TRY(cudaMemcpyAsync(&h->ctl->stage_timeout, &zero, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-        CUDA_TRY(cudaStreamSynchronize(h->stream));
-        return set_error(AEROS_ERR_TIMEOUT, "staged step: a shared-memory ring wait gave up; the populations of "
-                                            "this call are not valid");
-    }
     if (c.halt) {
         const long long executed = c.kexec - h->kexec_before;
         const long long launched = h->last_launches;

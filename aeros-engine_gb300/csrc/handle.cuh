@@ -48,6 +48,7 @@ struct aeros_lbm {
     std::vector<int> shell_host;
     std::vector<unsigned long long> shell_kind_host;
     float4* u[2] = {nullptr, nullptr};   // velocity (ux, uy, uz, 0), double buffered
+    float4* u_alloc[2] = {nullptr, nullptr};   // their allocations: VEL_GUARD cells of slack on both sides
     float *rho = nullptr, *strain = nullptr, *tke = nullptr;
     float* out[2] = {nullptr, nullptr};
     int out_plane = 0;
@@ -96,10 +97,10 @@ struct aeros_lbm {
     int sm_count = 0;
     int split = 1;                // shell and interior as two launches per step (AEROS_SPLIT=0: one)
     int fused = 1;                // non-thermal: one launch, dynamic warp items (AEROS_FUSED=0: off)
-    int shell_blocks_per_sm = 1;  // fused: shell blocks per SM (AEROS_SHELL_BLOCKS)
+    int shell_blocks_per_sm = 1;  // fused: shell blocks per SM, 0: shell tiles first in the queue (AEROS_SHELL_BLOCKS)
     int fused_grid[2][2] = {{0, 0}, {0, 0}};   // fused: interior blocks [odd][thermal]
-    bool staged = true;           // non-thermal steps through k_lbm_staged where nx allows (AEROS_STAGED)
-    int stg_grid[2] = {0, 0};     // staged: interior blocks [odd]
+    bool warp = false;            // non-thermal steps through k_lbm_warp where the shape allows (AEROS_WARP=1)
+    int warp_grid[2] = {0, 0};    // warp tiles: interior blocks [odd]
     long long last_kernels = 0;   // kernel launches of the last step call
     aeros_batch* batch = nullptr; // batch this domain is a member of
 };

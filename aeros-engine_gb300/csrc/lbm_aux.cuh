@@ -165,8 +165,9 @@ struct Launchers {
     cudaError_t (*batch_step)(const BatchArgs& B, bool odd, int kind, int grid, cudaStream_t s);
     int (*batch_occupancy)();
     int (*fused_occupancy)(bool odd, bool thermal);
-    int (*staged_occupancy)(bool odd);
-    int staged_pad;             // nx must be a multiple of this for the staged kernel (16 bytes of storage)
+    int (*warp_occupancy)(bool odd);
+    int warp_pad;               // nx must be a multiple of this for warp tiles (16 bytes of storage)
+    int warp_tile;              // cells per warp tile
 };
 
 const Launchers& launchers_fp32();
@@ -177,8 +178,12 @@ const Launchers& launchers_bf16();
     namespace NAME##_detail {                                                                                         \
     template <bool O, bool T, bool M>                                                                                 \
     cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
-        if (!M && !T && A.staged) {                                                                                   \
-            k_lbm_staged<STORE, O><<<(O ? A.stg_grid_odd : A.stg_grid) + A.shell_blocks, STG_THREADS, StgLayout<STORE>::BYTES, s>>>(A, V);     \
+        if (!M && !T && A.warp) {                                                                                     \
+            const int g = (O ? A.warp_grid_odd : A.warp_grid) + A.shell_blocks;                                       \
+            if (A.Fx != 0.0f || A.Fy != 0.0f || A.Fz != 0.0f)                                                         \
+                k_lbm_warp<STORE, O, true><<<g, STEP_BLOCK, WarpLayout<STORE>::BYTES, s>>>(A, V);                     \
+            else                                                                                                      \
+                k_lbm_warp<STORE, O, false><<<g, STEP_BLOCK, WarpLayout<STORE>::BYTES, s>>>(A, V);                    \
         } else if (!M && A.fused) {                                                                                   \
             k_lbm_fused<STORE, O, T><<<(O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V); \
         } else if (!M && A.split) {                                                                                   \
@@ -254,20 +259,19 @@ const Launchers& launchers_bf16();
         }                                                                                                             \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \
-    int staged_occ_(bool odd) {                                                                                       \
+    template <bool O, bool F>                                                                                         \
+    int warp_occ_one() {                                                                                              \
         int n = 0;                                                                                                    \
-        if (odd) {                                                                                                    \
-            cudaFuncSetAttribute(k_lbm_staged<STORE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,              \
-                                 StgLayout<STORE>::BYTES);                                                            \
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_staged<STORE, true>, STG_THREADS,                 \
-                                                          StgLayout<STORE>::BYTES);                                   \
-        } else {                                                                                                      \
-            cudaFuncSetAttribute(k_lbm_staged<STORE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
-                                 StgLayout<STORE>::BYTES);                                                            \
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_staged<STORE, false>, STG_THREADS,                \
-                                                          StgLayout<STORE>::BYTES);                                   \
-        }                                                                                                             \
+        cudaFuncSetAttribute(k_lbm_warp<STORE, O, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,                    \
+                             WarpLayout<STORE>::BYTES);                                                               \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_warp<STORE, O, F>, STEP_BLOCK,                        \
+                                                      WarpLayout<STORE>::BYTES);                                      \
         return n > 0 ? n : 1;                                                                                         \
+    }                                                                                                                 \
+    int warp_occ_(bool odd) {                                                                                         \
+        const int a = odd ? warp_occ_one<true, false>() : warp_occ_one<false, false>();                               \
+        const int b = odd ? warp_occ_one<true, true>() : warp_occ_one<false, true>();                                 \
+        return a < b ? a : b;                                                                                         \
     }                                                                                                                 \
     int batch_occ_() {                                                                                                \
         int n = 0, m = 0;                                                                                             \
@@ -281,7 +285,7 @@ const Launchers& launchers_bf16();
         using namespace NAME##_detail;                                                                                \
         static const Launchers L = {step_,      occupancy_, fill_,      seteq_,      writepre_,                     \
                                     reset_,     thfill_,    batch_,     batch_occ_,  fused_occ_,                    \
-                                    staged_occ_, StgLayout<STORE>::PAD};                                              \
+                                    warp_occ_,  WarpLayout<STORE>::PAD, WarpLayout<STORE>::WT};                       \
         return L;                                                                                                     \
     }
 

@@ -49,7 +49,7 @@ struct Control {
     int halt;               // divergence guard tripped: later steps return at once
     int halt_kind;          // 1: NaN count before streaming, 2: mean density
     int th_valid;           // Nusselt updated at least once
-    int stage_timeout;      // a staged-ring wait gave up (k_lbm_staged): the step's result is not valid
+    int pad0;
     long long steps;        // counted steps (lbmCurrentStep)
     long long kexec;        // step bodies executed
     float prev_kinetic;
@@ -111,9 +111,9 @@ struct StepArgs {
     int shell_blocks;           // fused: blocks given to the boundary shell
     int fused_grid;             // fused even steps: interior blocks (resident blocks per SM x SMs)
     int fused_grid_odd;         // fused odd steps (own register budget, own occupancy)
-    int staged;                 // interior tiles staged through a shared-memory ring (k_lbm_staged)
-    int stg_first, stg_last;    // staged: first and last linear tile of STEP_BLOCK cells holding interior cells
-    int stg_grid, stg_grid_odd; // staged: interior blocks of even / odd steps (resident blocks per SM x SMs)
+    int warp;                   // interior through warp tiles (k_lbm_warp)
+    int wt_first, wt_last;      // warp tiles: first and last linear tile (WarpLayout::WT cells) holding interior cells
+    int warp_grid, warp_grid_odd;   // warp tiles: interior blocks of even / odd steps (resident blocks per SM x SMs)
     int inlet_pos;              // inlet plane coordinate along the flow axis
     const int* zg_src;          // zero-gradient outlet: plane index each unknown q of outlet-plane
                                 // cell pi reads, at [q * out_plane + pi] (NULL: computed)
@@ -480,7 +480,9 @@ __device__ __forceinline__ bool collide19_shifted_fast(float f[Q19], const StepA
     return true;
 }
 
-template <bool SHIFTED>
+// NOFORCE: the domain has no body force and no buoyancy (the force terms are
+// compiled out; the results are the same as with zero forces).
+template <bool SHIFTED, bool NOFORCE = false>
 __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint32_t d, bool isInlet, bool isOutlet,
                                           float strainPre, float buoy, CellResult& o, Acc& acc) {
     if (SHIFTED && A.shifted_fast && !isInlet && !isOutlet && collide19_shifted_fast(f, A, d, strainPre, o, acc)) return;
@@ -561,7 +563,7 @@ __device__ __forceinline__ void collide19(float f[Q19], const StepArgs& A, uint3
     const float invTau = __frcp_rn(tauEff);
     const float Fx = A.Fx, Fz = A.Fz;
     const float Fy = A.th_on ? A.Fy + buoy : A.Fy;
-    const bool hasForce = (Fx != 0.0f || Fy != 0.0f || Fz != 0.0f);
+    const bool hasForce = !NOFORCE && (Fx != 0.0f || Fy != 0.0f || Fz != 0.0f);
     float ueX = ux, ueY = uy, ueZ = uz, ueSqr = usqr;
     float halfInvRho = 0.0f;
     if (hasForce) {
@@ -1408,6 +1410,9 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
     Control* ctl = A.ctl;
     auto add_slice = [&](const Acc& acc) { add_slice_sums<THERMAL>(W, acc, mx, lane); };
     const int nsh = A.ntiles - A.ntiles_interior;
+    // without dedicated shell blocks the shell's tiles come first in the queue
+    const int nq = A.shell_blocks > 0 ? 0 : nsh;
+    const int nall = nq + A.ntiles_interior;
     if ((int)blockIdx.x < A.shell_blocks) {
         for (int st = blockIdx.x; st < nsh; st += A.shell_blocks) {
             Acc acc;
@@ -1417,30 +1422,30 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
         }
     } else if (ODD) {
         // Odd steps read the descriptor before the gathers; the next tile's
-        // index is taken a tile ahead so that each thread's next descriptor
-        // is in flight while the current cell is processed.
+        // index is taken a tile ahead so that each thread's next interior
+        // descriptor is in flight while the current cell is processed.
         if (threadIdx.x == 0) s_tile[0] = (int)atomicAdd(&ctl->tile_next, 1u);
         __syncthreads();
         int par = 0;
         int it = s_tile[0];
         uint32_t dnext = D_WALL;
         int cnext = 0;
-        if (it < A.ntiles_interior) {
-            const int li = it * STEP_BLOCK + (int)threadIdx.x;
+        if (it >= nq && it < nall) {
+            const int li = (it - nq) * STEP_BLOCK + (int)threadIdx.x;
             if (li < A.n_interior) {
                 cnext = interior_cell_index(A, li);
                 dnext = __ldg(A.desc + cnext);
             }
         }
-        while (it < A.ntiles_interior) {
+        while (it < nall) {
             if (threadIdx.x == 0) s_tile[par ^ 1] = (int)atomicAdd(&ctl->tile_next, 1u);
             __syncthreads();
             const int itn = s_tile[par ^ 1];
             par ^= 1;
             const uint32_t dcur = dnext;
             const int ccur = cnext;
-            if (itn < A.ntiles_interior) {
-                const int li = itn * STEP_BLOCK + (int)threadIdx.x;
+            if (itn >= nq && itn < nall) {
+                const int li = (itn - nq) * STEP_BLOCK + (int)threadIdx.x;
                 if (li < A.n_interior) {
                     cnext = interior_cell_index(A, li);
                     dnext = __ldg(A.desc + cnext);
@@ -1448,7 +1453,9 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             }
             Acc acc;
             acc.zero();
-            if (it * STEP_BLOCK + (int)threadIdx.x < A.n_interior) {
+            if (it < nq) {
+                shell_tile<S, ODD, THERMAL, false>(A, V, it, acc);
+            } else if ((it - nq) * STEP_BLOCK + (int)threadIdx.x < A.n_interior) {
                 // x, y, z from the cell index: only the outlet planes and the
                 // thermal sub-step use them
                 const uint32_t r = A.div_x.div((uint32_t)ccur);
@@ -1467,52 +1474,87 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             __syncthreads();
             const int it = s_tile[par];
             par ^= 1;
-            if (it >= A.ntiles_interior) break;
+            if (it >= nall) break;
             Acc acc;
             acc.zero();
-            interior_tile<S, ODD, THERMAL, false>(A, V, it, acc);
+            if (it < nq) shell_tile<S, ODD, THERMAL, false>(A, V, it, acc);
+            else interior_tile<S, ODD, THERMAL, false>(A, V, it - nq, acc);
             add_slice(acc);
         }
     }
     finish_warp_sums<THERMAL>(A, W, mx, lane, gridDim.x * (STEP_BLOCK / 32));
 }
 
-// ---- staged interior: bulk copies into a shared-memory ring -----------------------
-// The interior's populations reach the threads through shared memory. A block
-// is STEP_BLOCK consumer threads (one cell each) plus one producer warp. Its
-// tiles are linear runs of STEP_BLOCK cells (tile t = cells t*T .. t*T+T-1,
-// shell and wall lanes idle), taken statically: block b gets tiles
-// stg_first + b, + G, + 2G, ... For each tile the producer's lane 0 issues
-// 19 bulk copies (cp.async.bulk, one row of T + PAD elements per plane: the
-// plane the step gathers direction q from, shifted by the neighbour offset
-// and rounded down to 16 bytes) and one of the tile's descriptors into the
-// next free stage of a STG_STAGES-deep ring; a stage's "full" mbarrier
-// completes on the copies' bytes, its "empty" mbarrier on the consumer warps'
-// release. No block-wide barrier after set-up: consumers wait on full,
-// producer on empty, both with bounded waits (a wait that gives up sets
-// Control::stage_timeout and stops the block's work; the host reports it).
-// The copies keep STG_STAGES tiles of populations in flight per block without
-// holding them in registers. Requires nx to be a multiple of 16 bytes of
-// storage (8 cells FP16/BF16, 4 FP32), so that every row starts on a 16-byte
-// boundary at a fixed element offset per direction.
-constexpr int STG_STAGES = 4;
-constexpr int STG_THREADS = STEP_BLOCK + 32;
-constexpr uint32_t STG_WAIT_LIMIT = 1u << 22;   // try_wait rounds before a wait gives up
-#ifndef AEROS_STG_MIN_BLOCKS
-#define AEROS_STG_MIN_BLOCKS 6
+// ---- warp-tiled interior: 16-byte async copies into per-warp shared memory ------
+// Each warp of an interior block steps tiles of WT = 32 * M consecutive cells
+// (tile t holds cells t*WT .. t*WT + WT - 1, lane l the cells l + 32 m; lanes
+// of shell and wall cells idle) from wt_first to wt_last, taken from a global
+// counter two tiles ahead. What a tile reads reaches the warp's shared
+// memory by cp.async 16-byte copies, which hold no registers while in flight,
+// and no barrier wider than the warp is taken:
+//   populations and descriptors, double buffered: the next tile's copies fly
+//   while the warp steps the current one. Rows:
+//     even step: plane q at cells c0 .. c0 + WT - 1 (the slots the cells read);
+//     odd step : the plane direction q gathers from (opp q) at c0 - nb_q,
+//                moved back to a 16-byte boundary (moff(q)), WT + PAD long;
+//   the previous step's velocity rows for the |S| stencil (LES), one buffer:
+//     the x-row c0 - 16 .. c0 + WT + 15 and the rows at -nx, +nx, -nx*ny,
+//     +nx*ny. The strains of a tile are taken first, then the next tile's rows
+//     are requested, so they arrive while this tile collides.
+// A cell reads exactly the slots it writes (AA pattern), so results go back
+// into the rows in place. Even steps then write the rows out as 16-byte
+// stores (a chunk holding a shell cell, whose slots the shell blocks write,
+// goes out element by element); odd steps scatter from registers. Wall cells
+// of an even tile are written back unchanged: no thread writes a wall slot.
+// Requires nx a multiple of PAD (every row starts on a 16-byte boundary at a
+// fixed offset per direction), nx*ny >= WT (tiles stay inside the domain),
+// the population array below 2 GiB (32-bit chunk offsets) and velocity
+// buffers with VEL_GUARD cells of slack on both sides.
+#ifndef AEROS_WARP_M16
+#define AEROS_WARP_M16 1   // cells per lane of a tile, 16-bit storage
 #endif
+#ifndef AEROS_WARP_M32
+#define AEROS_WARP_M32 1   // cells per lane of a tile, FP32 storage
+#endif
+constexpr int VEL_GUARD = 512;   // velocity cells of slack before and after each buffer
+
+// Per-lane exact sums of a warp's cells, in the warp's shared memory (no
+// registers held across tiles).
+struct LaneSums {
+    long long drho[32], ke[32], tke[32];
+    int cells[32];
+};
 
 template <class S>
-struct StgLayout {
-    static constexpr int ESZ = (int)sizeof(typename S::T);
-    static constexpr int PAD = 16 / ESZ;                    // elements of alignment slack per row
-    static constexpr int ROW = (STEP_BLOCK + PAD) * ESZ;   // bytes per staged row (a multiple of 16)
-    static constexpr int DESC = STEP_BLOCK * 4;
-    static constexpr int STAGE = Q19 * ROW + DESC;
-    static constexpr int BYTES = STG_STAGES * STAGE;       // dynamic shared memory of a block
-    // element offset of a cell's value in the odd-step row of direction q:
-    // the row starts at c0 - nb_q rounded down to PAD elements, and nb_q = c_x
-    // modulo PAD when nx is a multiple of PAD
+struct WarpLayout {
+    using T = typename S::T;
+    static constexpr int ESZ = (int)sizeof(T);
+    static constexpr int M = ESZ == 4 ? AEROS_WARP_M32 : AEROS_WARP_M16;
+    static constexpr int PAD = 16 / ESZ;                 // elements per 16-byte chunk
+    static constexpr int WT = 32 * M;                    // cells per tile
+    static constexpr int CH_E = WT / PAD, CH_O = CH_E + 1;   // chunks per row (even / odd step)
+    static constexpr int ROW_E = CH_E * 16, ROW_O = CH_O * 16;
+    static constexpr int NCH_E = Q19 * CH_E, NCH_O = Q19 * CH_O;
+    static constexpr int K_E = (NCH_E + 31) / 32, K_O = (NCH_O + 31) / 32;   // chunks per lane
+    static constexpr int DESC = WT * 4;                  // descriptor bytes of a tile
+    static constexpr int OFF_DESC = NCH_O * 16;          // descriptors after the rows
+    static constexpr int BUF = OFF_DESC + DESC;          // one tile's populations and descriptors
+    static constexpr int VX = WT + 32;                   // x-row of velocities: c0 - 16 .. c0 + WT + 15
+    static constexpr int VEL = (VX + 4 * WT) * 16;       // velocity rows of a tile (float4)
+    static constexpr int TAB = K_O * 32 * 4;             // per-lane chunk offsets
+    static constexpr int SUMS = (int)((sizeof(LaneSums) + 15) / 16 * 16);
+    static constexpr int OFF_VEL = 2 * BUF, OFF_TAB = OFF_VEL + VEL, OFF_SUMS = OFF_TAB + TAB;
+    static constexpr int WARP = OFF_SUMS + SUMS;         // shared memory of one warp
+    static constexpr int BYTES = (STEP_BLOCK / 32) * WARP;   // dynamic shared memory of a block
+    // blocks that fit an SM's 228 KB of shared memory (1 KB reserved per
+    // block): the register budget of the launch bounds follows
+    static constexpr int MIN_BLOCKS = 233472 / (BYTES + 1024) < 8 ? 233472 / (BYTES + 1024) : 8;
+    static_assert(M >= 1 && M <= 4 && DESC / 16 <= 32, "tile shape");
+    static_assert(BUF % 16 == 0 && WARP % 16 == 0, "16-byte chunks");
+    static_assert(WT + 32 <= VEL_GUARD, "velocity guard: rows reach WT + 16 cells past the domain");
+    // odd-step element offset of a cell in the row of direction q: the row
+    // starts at c0 - nb_q - moff(q), and nb_q = c_x modulo PAD when nx is a
+    // multiple of PAD
     __host__ __device__ static constexpr int moff(int q) {
         return cx19(q) > 0 ? PAD - 1 : (cx19(q) < 0 ? 1 : 0);
     }
@@ -1521,66 +1563,120 @@ struct StgLayout {
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+// 16-byte global -> shared copy, cached in L2 only (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Exact statistics of the lanes' cells (LaneSums): each cell's values are
+// rounded once to the fixed-point units of WarpSums and added as integers,
+// the same integers the slice sums of the other kernels add, so the totals do
+// not depend on which warp stepped which cell.
+// x * scale (non-negative, < 2^50) as the integer warp_fixed_sum adds for it
+__device__ __forceinline__ long long fixed_units(float x, float scale) {
+    const float y = x * scale;
+    const float hi = floorf(y * 0x1p-24f);
+    return ((long long)(unsigned)hi << 24) + (long long)(unsigned)(y - hi * 0x1p24f);
 }
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+__device__ __forceinline__ void lane_zero(LaneSums& L, int lane) {
+    L.drho[lane] = L.ke[lane] = L.tke[lane] = 0;
+    L.cells[lane] = 0;
 }
-// true once the barrier's phase of the given parity has completed; false when
-// STG_WAIT_LIMIT rounds of try_wait (each may suspend briefly) did not see it
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (uint32_t i = 0; i < STG_WAIT_LIMIT; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
+// The rare counters (NaN, negative, bad, rho range, rho finite, u limited)
+// go straight to the step's integer accumulators.
+__device__ __forceinline__ void lane_add(const StepArgs& A, LaneSums& L, int lane, const Acc& a, float& mx) {
+    if (!a.cells) return;
+    L.drho[lane] += __float2int_rn(a.drho * FX_DRHO);
+    L.ke[lane] += fixed_units(a.ke, FX_KE);
+    L.tke[lane] += fixed_units(a.tke, FX_TKE);
+    L.cells[lane] += 1;
+    if (a.nan | a.neg | a.bad | a.rout | a.rnf | a.ulim) {
+        const int c[6] = {a.nan, a.neg, a.bad, a.rout, a.rnf, a.ulim};
+        for (int j = 0; j < 6; ++j)
+            if (c[j]) atomicAdd(&A.ctl->fx_cnt[j], (unsigned long long)c[j]);
     }
-    return false;
+    mx = fmaxf(mx, a.maxu2);
 }
-// bulk copy global -> shared completing on an mbarrier (16-byte aligned
-// addresses, size a multiple of 16)
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                 "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
+__device__ __forceinline__ long long warp_allsum64(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// The warp's totals into the step's accumulators (finish_warp_sums).
+__device__ __forceinline__ void finish_lane_sums(const StepArgs& A, const LaneSums& L, float mx, int lane,
+                                                 unsigned int nwarps) {
+    __syncwarp();
+    WarpSums W;
+    W.drho = warp_allsum64(L.drho[lane]);
+    W.ke = warp_allsum64(L.ke[lane]);
+    W.tke = warp_allsum64(L.tke[lane]);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) W.cnt[j] = 0;
+    W.cnt[6] = warp_allsum(L.cells[lane]);
+    W.nu = W.tsum = W.nun = 0;
+    finish_warp_sums<false>(A, W, mx, lane, nwarps);
 }
 
-// One interior cell of a staged tile (non-thermal). rows: this thread's
-// element in the stage's plane rows (stage + t * ESZ).
-template <class S, bool ODD>
-__device__ __forceinline__ void staged_cell(const StepArgs& A, const StepVar& V, int cell, uint32_t d,
-                                            const unsigned char* rows, Acc& acc) {
-    using L = StgLayout<S>;
+// Shared-memory population slot of a tile cell, in register form.
+template <class S>
+__device__ __forceinline__ float lds_pop(const StepArgs& A, int q, const typename S::T* p) {
+    if constexpr (S::shifted) return fmaf(S::raw_load(p), S::kInv, A.dq[q]);
+    else return *p;
+}
+
+// Two-pass |S| (aeros/src/lbm.cpp:1012-1031) of tile cell t from the staged
+// previous-step velocity rows: the expression tree of strain_prev.
+template <int WT>
+__device__ __forceinline__ float strain_rows(const float4* vel, int t) {
+    constexpr int VX = WT + 32;
+    const float4 xm = vel[t + 15], xp = vel[t + 17];
+    const float4 ym = vel[VX + t], yp = vel[VX + WT + t];
+    const float4 zm = vel[VX + 2 * WT + t], zp = vel[VX + 3 * WT + t];
+    const float dux_dx = (xp.x - xm.x) * 0.5f;
+    const float duy_dy = (yp.y - ym.y) * 0.5f;
+    const float duz_dz = (zp.z - zm.z) * 0.5f;
+    const float dux_dy = (yp.x - ym.x) * 0.5f;
+    const float dux_dz = (zp.x - zm.x) * 0.5f;
+    const float duy_dx = (xp.y - xm.y) * 0.5f;
+    const float duy_dz = (zp.y - zm.y) * 0.5f;
+    const float duz_dx = (xp.z - xm.z) * 0.5f;
+    const float duz_dy = (yp.z - ym.z) * 0.5f;
+    const float Sxx = dux_dx, Syy = duy_dy, Szz = duz_dz;
+    const float Sxy = 0.5f * (dux_dy + duy_dx);
+    const float Sxz = 0.5f * (dux_dz + duz_dx);
+    const float Syz = 0.5f * (duy_dz + duz_dy);
+    const float S2 = Sxx * Sxx + Syy * Syy + Szz * Szz + 2.0f * (Sxy * Sxy + Sxz * Sxz + Syz * Syz);
+    return sqrtf(2.0f * S2);
+}
+
+// One interior cell of a warp tile (non-thermal). buf: the tile's buffer;
+// t: the cell's position in the tile; strainPre: its previous-step |S|.
+template <class S, bool ODD, bool FORCE>
+__device__ __forceinline__ void warp_cell(const StepArgs& A, const StepVar& V, int cell, uint32_t d,
+                                          unsigned char* buf, int t, float strainPre, Acc& acc) {
+    using L = WarpLayout<S>;
     using T = typename S::T;
     constexpr bool SH = S::shifted;
-    float f[Q19];
-    float strainPre = 0.0f;
-    if (A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
-    auto staged = [&](int q) {
-        const T* p = reinterpret_cast<const T*>(rows + q * L::ROW + (ODD ? L::moff(q) * L::ESZ : 0));
-        if constexpr (SH) return fmaf(S::raw_load(p), S::kInv, A.dq[q]);
-        else return S::raw_load(p);
+    constexpr int ROW = ODD ? L::ROW_O : L::ROW_E;
+    auto slot = [&](int q) -> T* {
+        return reinterpret_cast<T*>(buf + q * ROW) + t + (ODD ? L::moff(q) : 0);
     };
-    const bool plain = (d & D_LINKS) == 0;   // no wall next to the cell
-    if (!ODD || plain) {
+    float f[Q19];
+    if (!ODD || (d & D_LINKS) == 0) {
 #pragma unroll
-        for (int q = 0; q < Q19; ++q) f[q] = staged(q);
+        for (int q = 0; q < Q19; ++q) f[q] = lds_pop<S>(A, q, slot(q));
     } else {
-        // links to walls read the cell's own slot (bounce-back), the others the stage
+        // a link to a wall or out of the domain: the population comes back to
+        // the cell's own slot (bounce-back), which is not in the row
 #pragma unroll
-        for (int q = 0; q < Q19; ++q) f[q] = ((d >> q) & 1u) ? ldp<S>(A, q, fplane<S>(A, q) + cell) : staged(q);
+        for (int q = 0; q < Q19; ++q)
+            f[q] = ((d >> q) & 1u) ? ldp<S>(A, q, fplane<S>(A, q) + cell) : lds_pop<S>(A, q, slot(q));
     }
     CellResult r;
-    collide19<SH>(f, A, d, false, false, strainPre, 0.0f, r, acc);
+    collide19<SH, !FORCE>(f, A, d, false, false, strainPre, 0.0f, r, acc);
     const uint32_t os = (d >> D_OUT_SHIFT) & 3u;   // planes Nx-2 / Nx-3 feed the outlet
     if (os) {
         const uint32_t rr = A.div_x.div((uint32_t)cell);
@@ -1593,17 +1689,15 @@ __device__ __forceinline__ void staged_cell(const StepArgs& A, const StepVar& V,
         for (int q = 0; q < Q19; ++q) V.out_w[((int)(os - 1) * Q19 + q) * P + pi] = f[q];
     }
     if (!ODD) {
-        if (!SH || plain) {
+        // post_j goes to the slot (cell, opp j): row opp j, in place; read back
+        // as opp j when c + c_j is a wall (the shift of the reader)
 #pragma unroll
-            for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, opp19(j)) + cell, f[j]);
-        } else {
-#pragma unroll
-            for (int j = 0; j < Q19; ++j) {
-                const bool solid = (d >> opp19(j)) & 1u;   // c + c_j is a wall: read back as opp j
-                stp<S>(A, solid ? opp19(j) : j, fplane<S>(A, opp19(j)) + cell, f[j]);
-            }
+        for (int j = 0; j < Q19; ++j) {
+            const int rd = (SH && ((d >> opp19(j)) & 1u)) ? opp19(j) : j;
+            if constexpr (SH) S::raw_store(slot(opp19(j)), fmaf(f[j], S::kScale, -A.dqs[rd]));
+            else *slot(opp19(j)) = f[j];
         }
-    } else if (plain) {
+    } else if ((d & D_LINKS) == 0) {
 #pragma unroll
         for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
     } else {
@@ -1618,93 +1712,168 @@ __device__ __forceinline__ void staged_cell(const StepArgs& A, const StepVar& V,
     if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
 }
 
-// One lattice step (non-thermal) in one launch: shell blocks as in
-// k_lbm_fused, interior blocks through the staged ring.
+// Issues a tile's population and descriptor copies into buf: population
+// chunks from the lane's offset table (bytes from A.f before the tile's own
+// offset), then the descriptors.
 template <class S, bool ODD>
-__global__ void __launch_bounds__(STG_THREADS, AEROS_STG_MIN_BLOCKS) k_lbm_staged(const StepArgs A, const StepVar V) {
-    using L = StgLayout<S>;
-    if (A.ctl->halt) return;   // uniform: every thread reads the same flag
-    extern __shared__ __align__(128) unsigned char stg_smem[];
-    __shared__ __align__(8) unsigned long long bar_full[STG_STAGES], bar_empty[STG_STAGES];
-    __shared__ WarpSums s_sums[STEP_BLOCK / 32];
-    const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
-    constexpr int PRODUCER = STEP_BLOCK / 32;   // warp index of the producer
-    const bool shell_block = (int)blockIdx.x < A.shell_blocks;
-    if (!shell_block && threadIdx.x == 0) {
-        for (int s = 0; s < STG_STAGES; ++s) {
-            mbar_init(smem_u32(&bar_full[s]), 1u);
-            mbar_init(smem_u32(&bar_empty[s]), (uint32_t)PRODUCER);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    const int b = (int)blockIdx.x - A.shell_blocks;
-    const int G = (int)gridDim.x - A.shell_blocks;
-    if (wid == PRODUCER) {
-        if (shell_block || lane != 0) return;
-        const uint32_t row_bytes = (uint32_t)((ODD ? STEP_BLOCK + L::PAD : STEP_BLOCK) * L::ESZ);
-        const uint32_t tx = Q19 * row_bytes + (uint32_t)L::DESC;
-        for (int k = 0;; ++k) {
-            const int tile = A.stg_first + b + k * G;
-            if (tile > A.stg_last) break;
-            const int s = k % STG_STAGES;
-            if (k >= STG_STAGES && !mbar_wait(smem_u32(&bar_empty[s]), (uint32_t)(((k / STG_STAGES) & 1) ^ 1))) {
-                atomicExch(&A.ctl->stage_timeout, 1);
-                break;
-            }
-            if (*(volatile int*)&A.ctl->stage_timeout) break;
-            const uint32_t full = smem_u32(&bar_full[s]);
-            mbar_expect_tx(full, tx);
-            const uint32_t st = smem_u32(stg_smem + s * L::STAGE);
-            const long long c0 = (long long)tile * STEP_BLOCK;
+__device__ __forceinline__ void warp_issue_pops(const StepArgs& A, int c0, uint32_t buf, const int* tab, int lane) {
+    using L = WarpLayout<S>;
+    constexpr int NCH = ODD ? L::NCH_O : L::NCH_E;
+    constexpr int K = ODD ? L::K_O : L::K_E;
+    const char* fb = static_cast<const char*>(A.f) + (long long)c0 * L::ESZ;
 #pragma unroll
-            for (int q = 0; q < Q19; ++q) {
-                const char* plane = static_cast<const char*>(A.fq[ODD ? opp19(q) : q]);
-                const long long x0 = ODD ? c0 - nb19(A, q) - L::moff(q) : c0;
-                bulk_g2s(st + q * L::ROW, plane + x0 * L::ESZ, row_bytes, full);
-            }
-            bulk_g2s(st + Q19 * L::ROW, A.desc + c0, (uint32_t)L::DESC, full);
-        }
-        return;
+    for (int k = 0; k < K; ++k) {
+        const int i = lane + 32 * k;
+        if (k < K - 1 || i < NCH) cp_async16(buf + (uint32_t)i * 16u, fb + tab[k * 32 + lane]);
     }
-    WarpSums& W = s_sums[wid];
-    if (lane == 0) {
-        W.drho = W.ke = W.tke = 0;
-        for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
-        W.nu = W.tsum = W.nun = 0;
-    }
-    __syncwarp();
+    if (lane < L::DESC / 16)
+        cp_async16(buf + (uint32_t)(L::OFF_DESC + lane * 16), reinterpret_cast<const char*>(A.desc + c0) + lane * 16);
+}
+// ... and the tile's previous-step velocity rows into vbuf.
+template <class S>
+__device__ __forceinline__ void warp_issue_vel(const StepArgs& A, const StepVar& V, int c0, uint32_t vbuf, int lane) {
+    using L = WarpLayout<S>;
+    const float4* u = V.up + c0 + lane;
+#pragma unroll
+    for (int k = 0; k <= L::M; ++k) cp_async16(vbuf + (uint32_t)((lane + 32 * k) * 16), u - 16 + 32 * k);
+    const int off[4] = {-A.nx, A.nx, -A.nxny, A.nxny};
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int k = 0; k < L::M; ++k)
+            cp_async16(vbuf + (uint32_t)((L::VX + r * L::WT + lane + 32 * k) * 16), u + off[r] + 32 * k);
+}
+
+// One lattice step (non-thermal) in one launch: shell blocks as in
+// k_lbm_fused, interior warps over warp tiles.
+template <class S, bool ODD, bool FORCE>
+__global__ void __launch_bounds__(STEP_BLOCK, WarpLayout<S>::MIN_BLOCKS) k_lbm_warp(const StepArgs A, const StepVar V) {
+    using L = WarpLayout<S>;
+    using T = typename S::T;
+    if (A.ctl->halt) return;   // uniform: every thread reads the same flag
+    extern __shared__ __align__(128) unsigned char wsm[];
+    const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
+    unsigned char* ws = wsm + wid * L::WARP;
+    LaneSums& sums = *reinterpret_cast<LaneSums*>(ws + L::OFF_SUMS);
+    lane_zero(sums, lane);
     float mx = 0.0f;
-    if (shell_block) {
+    if ((int)blockIdx.x < A.shell_blocks) {
         const int nsh = A.ntiles - A.ntiles_interior;
         for (int st = blockIdx.x; st < nsh; st += A.shell_blocks) {
             Acc acc;
             acc.zero();
             shell_tile<S, ODD, false, false>(A, V, st, acc);
-            add_slice_sums<false>(W, acc, mx, lane);
+            lane_add(A, sums, lane, acc, mx);
         }
     } else {
-        const int t = (int)threadIdx.x;
-        for (int k = 0;; ++k) {
-            const int tile = A.stg_first + b + k * G;
-            if (tile > A.stg_last) break;
-            const int s = k % STG_STAGES;
-            if (!mbar_wait(smem_u32(&bar_full[s]), (uint32_t)((k / STG_STAGES) & 1))) {
-                atomicExch(&A.ctl->stage_timeout, 1);
-                break;
+        constexpr int NCH = ODD ? L::NCH_O : L::NCH_E;
+        constexpr int CH = ODD ? L::CH_O : L::CH_E;
+        constexpr int K = ODD ? L::K_O : L::K_E;
+        int* tab = reinterpret_cast<int*>(ws + L::OFF_TAB);
+        const float4* vel = reinterpret_cast<const float4*>(ws + L::OFF_VEL);
+        // chunk i = lane + 32 k of a tile: row i / CH, chunk i % CH of the row
+        for (int k = 0; k < K; ++k) {
+            const int i = lane + 32 * k;
+            long long e = 0;
+            if (i < NCH) {
+                const int q = i / CH, ch = i - q * CH;
+                e = ODD ? (long long)opp19(q) * A.qstride - A.nbq[q] - L::moff(q) : (long long)q * A.qstride;
+                e += (long long)ch * L::PAD;
             }
-            const unsigned char* stage = stg_smem + s * L::STAGE;
-            const uint32_t d = reinterpret_cast<const uint32_t*>(stage + Q19 * L::ROW)[t];
-            const int cell = tile * STEP_BLOCK + t;
-            Acc acc;
-            acc.zero();
-            if (cell < A.ncell && !(d & (D_WALL | D_SHELL))) staged_cell<S, ODD>(A, V, cell, d, stage + t * L::ESZ, acc);
-            add_slice_sums<false>(W, acc, mx, lane);
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&bar_empty[s]));
+            tab[k * 32 + lane] = (int)(e * L::ESZ);
         }
+        __syncwarp();
+        const bool les = A.use_les != 0;
+        const int ntiles = A.wt_last - A.wt_first + 1;
+        const uint32_t b0 = smem_u32(ws), vb = b0 + (uint32_t)L::OFF_VEL;
+        int cur = 0, nxt = 0;
+        if (lane == 0) {
+            cur = (int)atomicAdd(&A.ctl->tile_next, 1u);
+            nxt = (int)atomicAdd(&A.ctl->tile_next, 1u);
+        }
+        cur = __shfl_sync(0xffffffffu, cur, 0);
+        nxt = __shfl_sync(0xffffffffu, nxt, 0);
+        if (cur < ntiles) warp_issue_pops<S, ODD>(A, (A.wt_first + cur) * L::WT, b0, tab, lane);
+        cp_async_commit();
+        if (les && cur < ntiles) warp_issue_vel<S>(A, V, (A.wt_first + cur) * L::WT, vb, lane);
+        cp_async_commit();
+        int b = 0;
+        while (cur < ntiles) {
+            const int cn = (A.wt_first + nxt) * L::WT;
+            if (nxt < ntiles) warp_issue_pops<S, ODD>(A, cn, b0 + (uint32_t)((b ^ 1) * L::BUF), tab, lane);
+            cp_async_commit();
+            int nn = 0;   // the tile after next: its index arrives while this one is stepped
+            if (lane == 0 && nxt < ntiles) nn = (int)atomicAdd(&A.ctl->tile_next, 1u);
+            cp_async_wait<1>();   // this tile's rows (only the newest group may still be in flight)
+            __syncwarp();
+            unsigned char* buf = ws + b * L::BUF;
+            const uint32_t* dsc = reinterpret_cast<const uint32_t*>(buf + L::OFF_DESC);
+            const int c0 = (A.wt_first + cur) * L::WT;
+            // the tile's strains first: the velocity rows are then free for the
+            // next tile's, which arrive while this tile collides
+            float sp[L::M];
+            uint32_t own[L::M];   // even step: cells whose slots this warp writes back
+#pragma unroll
+            for (int m = 0; m < L::M; ++m) {
+                const int t = lane + 32 * m;
+                const uint32_t d = dsc[t];
+                const bool in = c0 + t < A.ncell;
+                sp[m] = (les && in && !(d & (D_WALL | D_SHELL)) && (d & D_LES)) ? strain_rows<L::WT>(vel, t) : 0.0f;
+                own[m] = ODD ? 0u : __ballot_sync(0xffffffffu, in && !(d & D_SHELL));
+            }
+            __syncwarp();
+            if (les && nxt < ntiles) warp_issue_vel<S>(A, V, cn, vb, lane);
+            cp_async_commit();
+#pragma unroll 1
+            for (int m = 0; m < L::M; ++m) {
+                const int t = lane + 32 * m;
+                const int cell = c0 + t;
+                const uint32_t d = dsc[t];
+                float s = sp[0];
+#pragma unroll
+                for (int k = 1; k < L::M; ++k)
+                    if (m == k) s = sp[k];
+                Acc acc;
+                acc.zero();
+                if (cell < A.ncell && !(d & (D_WALL | D_SHELL))) warp_cell<S, ODD, FORCE>(A, V, cell, d, buf, t, s, acc);
+                lane_add(A, sums, lane, acc, mx);
+            }
+            __syncwarp();
+            if (!ODD) {
+                // the rows back to their planes: whole 16-byte chunks where every
+                // cell is the warp's, element by element where a shell cell is in
+                char* fb = static_cast<char*>(A.f) + (long long)c0 * L::ESZ;
+#pragma unroll
+                for (int k = 0; k < L::K_E; ++k) {
+                    const int i = lane + 32 * k;
+                    if (k < L::K_E - 1 || i < L::NCH_E) {
+                        const int e0 = (i % L::CH_E) * L::PAD;   // first cell of the chunk
+                        uint32_t word = own[0];
+#pragma unroll
+                        for (int m = 1; m < L::M; ++m)
+                            if ((e0 >> 5) == m) word = own[m];
+                        const uint32_t bits = (word >> (e0 & 31)) & ((1u << L::PAD) - 1u);
+                        char* g = fb + tab[k * 32 + lane];
+                        const unsigned char* sp16 = buf + i * 16;
+                        if (bits == (1u << L::PAD) - 1u) {
+                            *reinterpret_cast<uint4*>(g) = *reinterpret_cast<const uint4*>(sp16);
+                        } else if (bits) {
+                            for (int e = 0; e < L::PAD; ++e)
+                                if ((bits >> e) & 1u)
+                                    reinterpret_cast<T*>(g)[e] = reinterpret_cast<const T*>(sp16)[e];
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            cur = nxt;
+            nxt = __shfl_sync(0xffffffffu, nn, 0);
+            if (cur >= ntiles) nxt = ntiles;
+            b ^= 1;
+        }
+        cp_async_wait<0>();
     }
-    finish_warp_sums<false>(A, W, mx, lane, gridDim.x * (STEP_BLOCK / 32));
+    finish_lane_sums(A, sums, mx, lane, gridDim.x * (STEP_BLOCK / 32));
 }
 
 // ---- many domains in one persistent kernel -----------------------------------

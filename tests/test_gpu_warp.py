@@ -1,9 +1,12 @@
-"""GPU: the staged interior step (populations brought into a shared-memory
-ring by bulk copies, k_lbm_staged) against the direct single-launch step
-(k_lbm_fused). Same arithmetic, so populations and fields must be bit for bit
-equal, in every storage form and on every boundary kind; the statistics are
-exact fixed-point sums of per-cell values, so they are equal too although the
-two kernels group cells differently."""
+"""GPU: the schedules of the single-launch step against each other, bit for
+bit. The warp-tiled interior (each warp's tiles brought into shared memory by
+16-byte cp.async copies, double buffered, k_lbm_warp; AEROS_WARP=1) and the
+direct step (k_lbm_fused) with the boundary shell on dedicated blocks
+(AEROS_SHELL_BLOCKS=1) or first in the tile queue (AEROS_SHELL_BLOCKS=0) do
+the same arithmetic, so populations and fields must be equal in every storage
+form and on every boundary kind; the statistics are exact fixed-point sums of
+per-cell values, so they are equal too although the schedules group cells
+differently."""
 import json
 import os
 
@@ -17,9 +20,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = json.load(open(os.path.join(HERE, "golden", "golden.json")))
 
 
-def _run(monkeypatch, staged, name, storage, steps, **mod):
+def _run(monkeypatch, env, name, storage, steps, **mod):
     from aeros_gb300 import solver
-    monkeypatch.setenv("AEROS_STAGED", "1" if staged else "0")
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
     case = CASES[name]
     mask = solver_mask(case)
     p = params_for(case, GOLD["cases"][name]["u_in"], storage)
@@ -44,10 +48,12 @@ def _run(monkeypatch, staged, name, storage, steps, **mod):
     ("channel_force3", {}),
     ("sphere_trt_les_conv", {"lateral_bc": 1, "outlet_bc": 1, "convective_outlet": 0}),
 ])
-def test_staged_equals_direct(monkeypatch, name, mod, storage):
+@pytest.mark.parametrize("env", [{"AEROS_WARP": "1", "AEROS_SHELL_BLOCKS": "1"},
+                                 {"AEROS_WARP": "0", "AEROS_SHELL_BLOCKS": "0"}], ids=["warp", "shell_queue"])
+def test_schedules_equal_direct(monkeypatch, env, name, mod, storage):
     steps = [CASES[name]["steps"] // 2 + 1, 6, 7]
-    a = _run(monkeypatch, True, name, storage, steps, **mod)
-    b = _run(monkeypatch, False, name, storage, steps, **mod)
+    a = _run(monkeypatch, env, name, storage, steps, **mod)
+    b = _run(monkeypatch, {"AEROS_WARP": "0", "AEROS_SHELL_BLOCKS": "1"}, name, storage, steps, **mod)
     for (fa, va, sa), (fb, vb, sb) in zip(a, b):
         assert np.array_equal(fa, fb)
         for k in va:
