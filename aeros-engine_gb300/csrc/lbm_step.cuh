@@ -182,14 +182,26 @@ __device__ __forceinline__ int nb19(const StepArgs& A, int q) { return A.nbq[q];
 // adds dq[q] = s_q - w_q; a store subtracts dq of its reader's direction, which
 // differs from the value's own direction on links that turn a population
 // (bounce-back, copy-own, free slip): s is not symmetric under c -> -c.
+// The shift is applied as an add of the scaled constant dqs (a kernel
+// parameter operand) and an exact power-of-two scale: the same bits as
+// raw * kInv + dq rounded once (dq = dqs * kInv exactly), without moving the
+// constant into a register first.
+template <class S>
+__device__ __forceinline__ float ld_shift(const StepArgs& A, int q, float raw) {
+    return __fmul_rn(__fadd_rn(raw, A.dqs[q]), S::kInv);
+}
+template <class S>
+__device__ __forceinline__ float st_shift(const StepArgs& A, int r, float v) {
+    return __fsub_rn(__fmul_rn(v, S::kScale), A.dqs[r]);
+}
 template <class S>
 __device__ __forceinline__ float ldp(const StepArgs& A, int q, const typename S::T* p) {
-    if constexpr (S::shifted) return fmaf(S::raw_load(p), S::kInv, A.dq[q]);
+    if constexpr (S::shifted) return ld_shift<S>(A, q, S::raw_load(p));
     else return S::load_rw(p);
 }
 template <class S>
 __device__ __forceinline__ void stp(const StepArgs& A, int r, typename S::T* p, float v) {
-    if constexpr (S::shifted) S::raw_store(p, fmaf(v, S::kScale, -A.dqs[r]));
+    if constexpr (S::shifted) S::raw_store(p, st_shift<S>(A, r, v));
     else S::store(p, v);
 }
 
@@ -1623,7 +1635,7 @@ __device__ __forceinline__ void finish_lane_sums(const StepArgs& A, const LaneSu
 // Shared-memory population slot of a tile cell, in register form.
 template <class S>
 __device__ __forceinline__ float lds_pop(const StepArgs& A, int q, const typename S::T* p) {
-    if constexpr (S::shifted) return fmaf(S::raw_load(p), S::kInv, A.dq[q]);
+    if constexpr (S::shifted) return ld_shift<S>(A, q, S::raw_load(p));
     else return *p;
 }
 
@@ -1694,7 +1706,7 @@ __device__ __forceinline__ void warp_cell(const StepArgs& A, const StepVar& V, i
 #pragma unroll
         for (int j = 0; j < Q19; ++j) {
             const int rd = (SH && ((d >> opp19(j)) & 1u)) ? opp19(j) : j;
-            if constexpr (SH) S::raw_store(slot(opp19(j)), fmaf(f[j], S::kScale, -A.dqs[rd]));
+            if constexpr (SH) S::raw_store(slot(opp19(j)), st_shift<S>(A, rd, f[j]));
             else *slot(opp19(j)) = f[j];
         }
     } else if ((d & D_LINKS) == 0) {

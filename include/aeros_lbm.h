@@ -41,9 +41,11 @@ enum { AEROS_CELL_FLUID = 0, AEROS_CELL_SOLID = 1, AEROS_CELL_GROUND = 2 };
 enum { AEROS_STORE_FP32 = 0, AEROS_STORE_FP16 = 1, AEROS_STORE_BF16 = 2 };
 
 /* What FP16/BF16 storage subtracts from each population (storage_shift).
- * FREESTREAM: the equilibrium f_eq(rho = 1, u_s), u_s = u_in when the domain
- * has an inlet (periodic_x == 0), else u_init; away from a body the stored
- * deviations are then only the non-equilibrium part, which 16 bits resolve.
+ * FREESTREAM: the equilibrium f_eq(rho = 1, u_in) when the domain has an
+ * inlet (periodic_x == 0); away from a body the stored deviations are then
+ * only the non-equilibrium part, which 16 bits resolve. A domain without an
+ * inlet keeps the rest state (as WEIGHTS): its flow is not held at any
+ * velocity.
  * WEIGHTS: the lattice weights w_i (f_eq at rest). */
 enum { AEROS_SHIFT_FREESTREAM = 0, AEROS_SHIFT_WEIGHTS = 1 };
 

@@ -21,6 +21,7 @@ plus the step counts at which it is read. Drivers:
 Generate the fixtures (validation.json) where the reference tree exists:
 
     python tests/golden/validation.py
+    python tests/golden/validation.py --f64    # the FP64 summary (C restatement)
 """
 from __future__ import annotations
 
@@ -298,6 +299,21 @@ def main():
                            "reference's own solver", "runs": res, "summary": s}, fh, indent=1, sort_keys=True)
 
 
+def make_f64_summary():
+    """The same runs stepped by the C restatement in FP64: the yardstick the
+    16-bit storage forms state their errors against. Added to validation.json
+    as "summary_f64" (python tests/golden/validation.py --f64)."""
+    import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1, "f64")
+    fx = json.load(open(FIXTURE))
+    res = solver_results(lambda p, m: O.OracleLBM(p, m, "f64"), fx)
+    fx["summary_f64"] = summarise(res)
+    for k, v in fx["summary_f64"].items():
+        print(f"  {k}: {v}")
+    with open(FIXTURE, "w") as fh:
+        json.dump(fx, fh, indent=1, sort_keys=True)
+
 
 
 # ---- the full-size configurations (C restatement as the checker) -----------------
@@ -362,5 +378,7 @@ def make_config_fixture():
 if __name__ == "__main__":
     if "--configs" in sys.argv:
         make_config_fixture()
+    elif "--f64" in sys.argv:
+        make_f64_summary()
     else:
         main()
