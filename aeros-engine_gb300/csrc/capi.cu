@@ -360,9 +360,13 @@ extern "C" int aeros_lbm_create(const aeros_lbm_params* params, const uint8_t* m
     if (const char* e = getenv("AEROS_FUSED")) h->fused = atoi(e) != 0;
     if (const char* e = getenv("AEROS_WARP")) h->warp = atoi(e) != 0;
     // measured on the sphere workload: 16-bit storage steps fastest with the
-    // shell's tiles first in the interior queue, FP32 with one shell block per SM
+    // shell's tiles first in the interior queue, FP32 with one shell block per
+    // SM (a domain with the thermal lattice keeps one shell block per SM)
     h->shell_blocks_per_sm = h->esize == 2 ? 0 : 1;
-    if (const char* e = getenv("AEROS_SHELL_BLOCKS")) h->shell_blocks_per_sm = std::max(0, std::min(8, atoi(e)));
+    if (const char* e = getenv("AEROS_SHELL_BLOCKS")) {
+        h->shell_blocks_per_sm = std::max(0, std::min(8, atoi(e)));
+        h->shell_blocks_set = true;
+    }
 
     std::vector<int> shell;
     host_geometry(h, shell);
@@ -643,7 +647,8 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
         }
         // the warp tiles need shell blocks; the fused kernel without them takes
         // the shell's tiles first from its queue
-        const int per_sm = A.warp ? std::max(1, h->shell_blocks_per_sm) : h->shell_blocks_per_sm;
+        const int per_sm = (A.warp || (h->th_on && !h->shell_blocks_set)) ? std::max(1, h->shell_blocks_per_sm)
+                                                                            : h->shell_blocks_per_sm;
         A.shell_blocks = (A.fused || A.warp) ? std::min(nsh, std::max(1, h->sm_count) * per_sm) : 0;
         A.fused_grid = h->fused_grid[0][h->th_on ? 1 : 0];
         A.fused_grid_odd = h->fused_grid[1][h->th_on ? 1 : 0];

@@ -98,6 +98,7 @@ struct aeros_lbm {
     int split = 1;                // shell and interior as two launches per step (AEROS_SPLIT=0: one)
     int fused = 1;                // non-thermal: one launch, dynamic warp items (AEROS_FUSED=0: off)
     int shell_blocks_per_sm = 1;  // fused: shell blocks per SM, 0: shell tiles first in the queue (AEROS_SHELL_BLOCKS)
+    bool shell_blocks_set = false;   // AEROS_SHELL_BLOCKS given
     int fused_grid[2][2] = {{0, 0}, {0, 0}};   // fused: interior blocks [odd][thermal]
     bool warp = false;            // non-thermal steps through k_lbm_warp where the shape allows (AEROS_WARP=1)
     int warp_grid[2] = {0, 0};    // warp tiles: interior blocks [odd]

@@ -185,7 +185,9 @@ const Launchers& launchers_bf16();
             else                                                                                                      \
                 k_lbm_warp<STORE, O, false><<<g, STEP_BLOCK, WarpLayout<STORE>::BYTES, s>>>(A, V);                    \
         } else if (!M && A.fused) {                                                                                   \
-            k_lbm_fused<STORE, O, T><<<(O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks, STEP_BLOCK, 0, s>>>(A, V); \
+            const int g = (O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks;                                      \
+            if (A.shell_blocks > 0) k_lbm_fused<STORE, O, T, false><<<g, STEP_BLOCK, 0, s>>>(A, V);                    \
+            else k_lbm_fused<STORE, O, T, true><<<g, STEP_BLOCK, 0, s>>>(A, V);                                        \
         } else if (!M && A.split) {                                                                                   \
             StepArgs B = A;                                                                                           \
             B.shell_part_base = grid;                                                                                 \
@@ -251,11 +253,11 @@ const Launchers& launchers_bf16();
     int fused_occ_(bool odd, bool thermal) {                                                                          \
         int n = 0;                                                                                                    \
         if (thermal) {                                                                                                \
-            if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true, true>, STEP_BLOCK, 0); \
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false, true>, STEP_BLOCK, 0);   \
+            if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true, true, false>, STEP_BLOCK, 0); \
+            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false, true, false>, STEP_BLOCK, 0);   \
         } else {                                                                                                      \
-            if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true, false>, STEP_BLOCK, 0); \
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false, false>, STEP_BLOCK, 0);  \
+            if (odd) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, true, false, false>, STEP_BLOCK, 0); \
+            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_fused<STORE, false, false, false>, STEP_BLOCK, 0);  \
         }                                                                                                             \
         return n > 0 ? n : 1;                                                                                         \
     }                                                                                                                 \

@@ -182,17 +182,16 @@ __device__ __forceinline__ int nb19(const StepArgs& A, int q) { return A.nbq[q];
 // adds dq[q] = s_q - w_q; a store subtracts dq of its reader's direction, which
 // differs from the value's own direction on links that turn a population
 // (bounce-back, copy-own, free slip): s is not symmetric under c -> -c.
-// The shift is applied as an add of the scaled constant dqs (a kernel
-// parameter operand) and an exact power-of-two scale: the same bits as
-// raw * kInv + dq rounded once (dq = dqs * kInv exactly), without moving the
-// constant into a register first.
+// One FMA each way (an add of the parameter constant and a separate
+// power-of-two scale gives the same bits but measured 20 % slower on even
+// steps).
 template <class S>
 __device__ __forceinline__ float ld_shift(const StepArgs& A, int q, float raw) {
-    return __fmul_rn(__fadd_rn(raw, A.dqs[q]), S::kInv);
+    return fmaf(raw, S::kInv, A.dq[q]);
 }
 template <class S>
 __device__ __forceinline__ float st_shift(const StepArgs& A, int r, float v) {
-    return __fsub_rn(__fmul_rn(v, S::kScale), A.dqs[r]);
+    return fmaf(v, S::kScale, -A.dqs[r]);
 }
 template <class S>
 __device__ __forceinline__ float ldp(const StepArgs& A, int q, const typename S::T* p) {
@@ -1400,10 +1399,11 @@ __device__ __forceinline__ void finish_warp_sums(const StepArgs& A, const WarpSu
 }
 
 // The single-launch step: the first shell_blocks blocks take the boundary
-// shell's tiles, the others take interior tiles from a counter. THERMAL: the
+// shell's tiles, the others take interior tiles from a counter (QUEUE: no
+// shell blocks, the counter hands out the shell's tiles first). THERMAL: the
 // D3Q7 lattice stepped in the same thread (its Nusselt row sum and mean
 // temperature summed like the other statistics, in fixed point).
-template <class S, bool ODD, bool THERMAL>
+template <class S, bool ODD, bool THERMAL, bool QUEUE>
 __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCKS
                                                       : (ODD ? AEROS_FUSED_ODD_MIN_BLOCKS : AEROS_FUSED_MIN_BLOCKS))
     k_lbm_fused(const StepArgs A, const StepVar V) {
@@ -1422,27 +1422,46 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
     Control* ctl = A.ctl;
     auto add_slice = [&](const Acc& acc) { add_slice_sums<THERMAL>(W, acc, mx, lane); };
     const int nsh = A.ntiles - A.ntiles_interior;
-    // without dedicated shell blocks the shell's tiles come first in the queue
-    const int nq = A.shell_blocks > 0 ? 0 : nsh;
+    const int nq = QUEUE ? nsh : 0;   // shell tiles handed out by the counter
     const int nall = nq + A.ntiles_interior;
-    if ((int)blockIdx.x < A.shell_blocks) {
+    int par = 0;
+    int it = 0;
+    if (!QUEUE && (int)blockIdx.x < A.shell_blocks) {
         for (int st = blockIdx.x; st < nsh; st += A.shell_blocks) {
             Acc acc;
             acc.zero();
             shell_tile<S, ODD, THERMAL, false>(A, V, st, acc);
             add_slice(acc);
         }
-    } else if (ODD) {
+        it = nall;
+    } else if (QUEUE) {
+        // The counter only grows: a block that has drawn an interior tile
+        // never draws a shell tile again, and the interior loops below hold
+        // no call to the out-of-line shell path.
+        for (;;) {
+            if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
+            __syncthreads();
+            it = s_tile[par];
+            par ^= 1;
+            if (it >= nq) break;
+            Acc acc;
+            acc.zero();
+            shell_tile<S, ODD, THERMAL, false>(A, V, it, acc);
+            add_slice(acc);
+        }
+    } else {
+        if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
+        __syncthreads();
+        it = s_tile[par];
+        par ^= 1;
+    }
+    if (ODD) {
         // Odd steps read the descriptor before the gathers; the next tile's
         // index is taken a tile ahead so that each thread's next interior
         // descriptor is in flight while the current cell is processed.
-        if (threadIdx.x == 0) s_tile[0] = (int)atomicAdd(&ctl->tile_next, 1u);
-        __syncthreads();
-        int par = 0;
-        int it = s_tile[0];
         uint32_t dnext = D_WALL;
         int cnext = 0;
-        if (it >= nq && it < nall) {
+        if (it < nall) {
             const int li = (it - nq) * STEP_BLOCK + (int)threadIdx.x;
             if (li < A.n_interior) {
                 cnext = interior_cell_index(A, li);
@@ -1450,13 +1469,13 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             }
         }
         while (it < nall) {
-            if (threadIdx.x == 0) s_tile[par ^ 1] = (int)atomicAdd(&ctl->tile_next, 1u);
+            if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
             __syncthreads();
-            const int itn = s_tile[par ^ 1];
+            const int itn = s_tile[par];
             par ^= 1;
             const uint32_t dcur = dnext;
             const int ccur = cnext;
-            if (itn >= nq && itn < nall) {
+            if (itn < nall) {
                 const int li = (itn - nq) * STEP_BLOCK + (int)threadIdx.x;
                 if (li < A.n_interior) {
                     cnext = interior_cell_index(A, li);
@@ -1465,9 +1484,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             }
             Acc acc;
             acc.zero();
-            if (it < nq) {
-                shell_tile<S, ODD, THERMAL, false>(A, V, it, acc);
-            } else if ((it - nq) * STEP_BLOCK + (int)threadIdx.x < A.n_interior) {
+            if ((it - nq) * STEP_BLOCK + (int)threadIdx.x < A.n_interior) {
                 // x, y, z from the cell index: only the outlet planes and the
                 // thermal sub-step use them
                 const uint32_t r = A.div_x.div((uint32_t)ccur);
@@ -1480,18 +1497,15 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             it = itn;
         }
     } else {
-        int par = 0;
-        for (;;) {
-            if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
-            __syncthreads();
-            const int it = s_tile[par];
-            par ^= 1;
-            if (it >= nall) break;
+        while (it < nall) {
             Acc acc;
             acc.zero();
-            if (it < nq) shell_tile<S, ODD, THERMAL, false>(A, V, it, acc);
-            else interior_tile<S, ODD, THERMAL, false>(A, V, it - nq, acc);
+            interior_tile<S, ODD, THERMAL, false>(A, V, it - nq, acc);
             add_slice(acc);
+            if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
+            __syncthreads();
+            it = s_tile[par];
+            par ^= 1;
         }
     }
     finish_warp_sums<THERMAL>(A, W, mx, lane, gridDim.x * (STEP_BLOCK / 32));

@@ -31,10 +31,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "aeros-engine_gb300"))
 
-# algorithmic bytes per cell update of the step kernel (read + write):
-#   populations 2 x 19 x bytes, previous velocity 16 (ux, uy, uz, pad),
-#   new velocity 16, descriptor 4
-BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 16 + 16 + 4, "fp16": 2 * 19 * 2 + 16 + 16 + 4, "bf16": 2 * 19 * 2 + 16 + 16 + 4}
+# algorithmic bytes per cell update of the step with LES (read + write):
+#   populations 2 x 19 x bytes, previous velocity 12 (ux, uy, uz), new
+#   velocity 12, a one-byte cell mask
+BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 12 + 12 + 1, "fp16": 2 * 19 * 2 + 12 + 12 + 1, "bf16": 2 * 19 * 2 + 12 + 12 + 1}
+# what this layout moves per cell: the velocity as float4 (16 + 16) and a
+# 4-byte descriptor in place of the mask (11 bytes more per cell)
+LAYOUT_BYTES_PER_CELL = {k: v + 8 + 3 for k, v in BYTES_PER_CELL.items()}
 # DRAM bytes per launch of the step kernel (read + write, mean of an odd and
 # an even step) from the ncu capture summarised in
 # profiles/k_lbm_fused_sphere_240x120x115.md
@@ -246,12 +249,15 @@ def run_gb300(args):
             "roofline": {"bound": "hbm", "achieved": round(head["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
                          "frac": round(frac, 4), "traffic": round(NCU_TRAFFIC["fp16"]),
                          "traffic_unit": "bytes per launch (ncu)", "algorithmic_bytes": BYTES_PER_CELL["fp16"] * cells,
-                         "peak_kind": peak_kind, "bytes_per_cell": BYTES_PER_CELL["fp16"]},
+                         "peak_kind": peak_kind, "bytes_per_cell": BYTES_PER_CELL["fp16"],
+                         "layout_bytes_per_cell": LAYOUT_BYTES_PER_CELL["fp16"],
+                         "frac_layout": round(frac * LAYOUT_BYTES_PER_CELL["fp16"] / BYTES_PER_CELL["fp16"], 4)},
             "fp32_plain": {"mlups": round(results["fp32"]["mlups"], 1),
                            "ms_per_step": round(results["fp32"]["ms_per_step"], 4),
                            "achieved_gbs": round(results["fp32"]["achieved_gbs"], 1),
                            "frac": round(results["fp32"]["achieved_gbs"] / peak, 4),
-                           "traffic": round(NCU_TRAFFIC["fp32"]), "bytes_per_cell": BYTES_PER_CELL["fp32"]},
+                           "traffic": round(NCU_TRAFFIC["fp32"]), "bytes_per_cell": BYTES_PER_CELL["fp32"],
+                           "layout_bytes_per_cell": LAYOUT_BYTES_PER_CELL["fp32"]},
             "fp16_over_fp32": round(results["fp16"]["mlups"] / results["fp32"]["mlups"], 3),
             "e2e": {"value": round(e2e_value, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // max(1, e2e_steps)),
                     "d2h_bytes_per_step": int(d2h // max(1, e2e_steps)),
