@@ -79,6 +79,86 @@ def icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)) -> np.nda
     return v[f].reshape(-1, 9).astype(np.float32)
 
 
+_ICO_FACES = ((0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+              (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+              (6, 2, 10), (8, 6, 7), (9, 8, 1))
+
+
+@functools.lru_cache(maxsize=4)
+def geodesic_unit(n: int):
+    """Class-I geodesic sphere of frequency n: every icosahedron face cut
+    into n^2 triangles, the points projected radially onto the unit sphere
+    (20 n^2 triangles; any count 20 n^2, where subdivision levels give
+    20 * 4^level). Returns (vertices [nv, 3] float64, corners [20 n^2, 3]
+    int64). A point on an edge is computed once from the edge's lower
+    vertex index, so faces share their edge vertices exactly: the mesh is
+    closed, as the voxelizer's inside test needs."""
+    n = int(n)
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    V0 = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+                   (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    V0 /= np.linalg.norm(V0, axis=1, keepdims=True)
+    pts = [V0]
+    nid = 12
+    k = np.arange(1, n, dtype=np.float64)[:, None] / n
+    edge_base = {}
+    for a, b, c in _ICO_FACES:
+        for u, v in ((a, b), (b, c), (a, c)):
+            e = (min(u, v), max(u, v))
+            if e not in edge_base and n > 1:
+                p = V0[e[0]] + (V0[e[1]] - V0[e[0]]) * k
+                pts.append(p / np.linalg.norm(p, axis=1, keepdims=True))
+                edge_base[e] = nid
+                nid += n - 1
+
+    def edge_ids(u, v, steps):
+        """Ids of the points u + (v - u) * steps / n (0 < steps < n)."""
+        base = edge_base[(min(u, v), max(u, v))]
+        return base + (steps - 1 if u < v else n - steps - 1)
+
+    tris = []
+    i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    for a, b, c in _ICO_FACES:
+        G = np.full((n + 1, n + 1), -1, np.int64)   # G[i, j]: the point A + (B-A) i/n + (C-A) j/n
+        G[0, 0], G[n, 0], G[0, n] = a, b, c
+        if n > 1:
+            s = np.arange(1, n)
+            G[s, 0] = edge_ids(a, b, s)
+            G[0, s] = edge_ids(a, c, s)
+            G[n - s, s] = edge_ids(b, c, s)
+        inner = (i >= 1) & (j >= 1) & (i + j <= n - 1)
+        m = int(inner.sum())
+        if m:
+            ii, jj = i[inner].astype(np.float64)[:, None], j[inner].astype(np.float64)[:, None]
+            p = V0[a] + (V0[b] - V0[a]) * ii / n + (V0[c] - V0[a]) * jj / n
+            pts.append(p / np.linalg.norm(p, axis=1, keepdims=True))
+            G[inner] = np.arange(nid, nid + m)
+            nid += m
+        up = i + j <= n - 1
+        ui, uj = i[up], j[up]
+        tris.append(np.stack([G[ui, uj], G[ui + 1, uj], G[ui, uj + 1]], axis=1))
+        dn = i + j <= n - 2
+        di, dj = i[dn], j[dn]
+        tris.append(np.stack([G[di + 1, dj], G[di + 1, dj + 1], G[di, dj + 1]], axis=1))
+    verts = np.concatenate(pts)
+    corners = np.concatenate(tris)
+    verts.flags.writeable = False
+    corners.flags.writeable = False
+    return verts, corners
+
+
+def perturbed_geodesic(n: int, radius: float, center, seed: int, radial: float = 0.15,
+                       axis_scale=(0.5, 1.5)) -> np.ndarray:
+    """Geodesic sphere of frequency n (20 n^2 triangles) with vertex radii
+    scaled by U(1-radial, 1+radial) and axes by U(axis_scale), as
+    perturbed_icosphere. Returns float32 [ntri, 9]."""
+    uniq, corners = geodesic_unit(n)
+    scales = uniform_array(seed, 3, axis_scale[0], axis_scale[1])
+    rad = uniform_array(seed, len(uniq), 1.0 - radial, 1.0 + radial, skip=3)
+    pts = uniq * rad[:, None] * scales[None, :] * radius + np.asarray(center, np.float64)
+    return pts[corners].reshape(-1, 9).astype(np.float32)
+
+
 def face_normals(tris: np.ndarray, center=None) -> np.ndarray:
     """Per-vertex normals as an STL file carries them: each triangle's unit
     face normal (FP64 cross product of its FP32 vertices) on its three

@@ -32,7 +32,8 @@ from .batch import Batch
 from .solver import Solver, voxel_grid, voxelize
 
 SERVE_GRIDS = ((48, 48, 48), (96, 48, 48), (128, 64, 64), (192, 96, 96), (256, 128, 128))
-SERVE_LEVELS = (5, 6, 7)   # icosphere subdivisions: 20,480 / 81,920 / 327,680 triangles
+# geodesic sphere frequencies: 20 n^2 triangles, 20,480 (n = 32) to 499,280 (n = 158)
+SERVE_FREQS = (32, 158)
 
 
 @dataclasses.dataclass
@@ -40,7 +41,7 @@ class Request:
     rid: int
     arrival: float          # seconds after the start of the session
     grid: tuple
-    level: int
+    freq: int               # mesh: perturbed geodesic sphere of 20 freq^2 triangles
     re: float
     seed: int
 
@@ -63,9 +64,11 @@ class Result:
         return self.finished - self.arrival
 
 
-def make_requests(n: int, rate: float = 2.0, seed: int = 0x5E12, grids=SERVE_GRIDS, levels=SERVE_LEVELS,
+def make_requests(n: int, rate: float = 2.0, seed: int = 0x5E12, grids=SERVE_GRIDS, freqs=SERVE_FREQS,
                   re_range=(50.0, 1000.0)) -> list[Request]:
-    """n requests with exponential inter-arrival gaps of mean 1/rate (seeded)."""
+    """n requests with exponential inter-arrival gaps of mean 1/rate (seeded);
+    grid uniform over `grids`, mesh frequency uniform over the integers of
+    `freqs` (inclusive), Re ~ U(re_range)."""
     g = geometry.splitmix64(seed)
     t = 0.0
     out = []
@@ -73,9 +76,10 @@ def make_requests(n: int, rate: float = 2.0, seed: int = 0x5E12, grids=SERVE_GRI
         u = geometry.uniform(g, 0.0, 1.0)
         t += -math.log(max(1.0 - u, 1e-300)) / rate
         grid = grids[min(len(grids) - 1, int(geometry.uniform(g, 0.0, float(len(grids)))))]
-        level = levels[min(len(levels) - 1, int(geometry.uniform(g, 0.0, float(len(levels)))))]
+        nf = freqs[1] - freqs[0] + 1
+        freq = freqs[0] + min(nf - 1, int(geometry.uniform(g, 0.0, float(nf))))
         re = geometry.uniform(g, re_range[0], re_range[1])
-        out.append(Request(i, t, grid, level, re, 0xA0000 + i))
+        out.append(Request(i, t, grid, freq, re, 0xA0000 + i))
     return out
 
 
@@ -88,7 +92,7 @@ def domain_for(req: Request, storage="fp16", u_in=0.05, smag=0.1):
     nx, ny, nz = req.grid
     r = ny / 8.0
     c = (nx / 3.0, ny / 2.0, nz / 2.0)
-    tris = geometry.perturbed_icosphere(req.level, r, c, seed=req.seed)
+    tris = geometry.perturbed_geodesic(req.freq, r, c, seed=req.seed)
     mask = voxelize(tris, voxel_grid((nx, ny, nz), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)))
     tau = 0.5 + 3.0 * u_in * ny / req.re
     p = capi.make_params(nx, ny, nz, tau=tau, smagorinsky_c=smag, les=True, trt=True, u_in=(u_in, 0.0, 0.0),
@@ -115,7 +119,7 @@ def footprint_estimate(req: Request, storage="fp16") -> int:
     nx, ny, nz = req.grid
     cells = nx * ny * nz
     pop = 19 * (2 if storage != "fp32" else 4)
-    tris = 20 * 4 ** req.level
+    tris = 20 * req.freq * req.freq
     return int(cells * (pop + 4 + 32 + 12 + 4) + tris * 96 + (64 << 20))
 
 
@@ -129,7 +133,7 @@ class Server:
     while the batch steps, Cd-convergence retirement."""
 
     def __init__(self, storage="fp16", budget_bytes=170 << 30, slots=64, check_every=1000, tol=1e-4,
-                 max_steps=30000, chunk=100, levels=SERVE_LEVELS):
+                 max_steps=30000, chunk=100):
         if check_every % chunk or chunk % 2:
             raise ValueError("chunk must be even and divide check_every")
         self.storage = storage
@@ -139,8 +143,6 @@ class Server:
         self.tol = float(tol)
         self.max_steps = int(max_steps)
         self.chunk = int(chunk)
-        for lv in levels:   # unit meshes built once, before any request arrives
-            geometry._unit_icosphere_vertices(int(lv))
 
     def _cd(self, a: _Active) -> float:
         F = a.solver.cv_force_box(a.box)
@@ -260,25 +262,34 @@ def summarize(results: list[Result], wall: float, cell_steps: int) -> dict:
             "steps_total": int(sum(r.steps for r in results))}
 
 
-def sequential_plain(requests: list[Request], steps_of: dict, sample_steps: int = 200) -> dict:
-    """One-at-a-time plain FP32 solves of the same requests: each domain alone
-    (single-domain path, FP32 storage) timed over `sample_steps` steps; its
-    solve time is setup + per-step time x the steps the request needed
-    (`steps_of[rid]`, from the served run: the same convergence rule)."""
-    total = 0.0
-    cells_steps = 0
-    for req in requests:
-        t = time.perf_counter()
-        s, _, _, _, _ = domain_for(req, "fp32")
-        setup = time.perf_counter() - t
-        s.step(2)
-        s.step(sample_steps)
-        per = s.last_step_ms() * 1e-3 / sample_steps
+def sequential_plain(requests: list[Request], storage: str = "fp32", check_every: int = 1000, tol: float = 1e-4,
+                     max_steps: int = 30000) -> dict:
+    """The same requests solved one at a time in plain FP32, each to its own
+    end by the serving loop's rule (Cd every check_every steps, retired when
+    it changes by less than tol, or at max_steps): mesh, GPU voxelization,
+    domain creation and stepping of one request, then the next. Measured
+    wall time, no estimate."""
+    t0 = time.perf_counter()
+    cell_steps = 0
+    per = []
+    for req in sorted(requests, key=lambda r: r.arrival):
+        ts = time.perf_counter()
+        s, box, area, _, u = domain_for(req, storage)
+        steps, cd_prev, cd, conv = 0, float("nan"), float("nan"), False
+        while steps < max_steps:
+            s.step(check_every)
+            steps += check_every
+            F = s.cv_force_box(box)
+            cd_prev, cd = cd, float(F[0] / (0.5 * u * u * area)) if area > 0 else float("nan")
+            conv = (math.isfinite(cd) and math.isfinite(cd_prev) and cd != 0.0 and abs(cd - cd_prev) < tol * abs(cd))
+            if conv:
+                break
         s.close()
-        n = steps_of.get(req.rid, 0)
-        total += setup + per * n
-        cells_steps += req.grid[0] * req.grid[1] * req.grid[2] * n
-    return {"wall_s_estimated": round(total, 3),
-            "solves_per_hour": round(3600.0 * len(requests) / total, 1) if total > 0 else 0.0,
-            "mlups": round(cells_steps / total / 1e6, 1) if total > 0 else 0.0,
-            "sample_steps": sample_steps}
+        cell_steps += req.grid[0] * req.grid[1] * req.grid[2] * steps
+        per.append(dict(rid=req.rid, steps=steps, cd=cd, converged=conv, wall_s=time.perf_counter() - ts))
+    wall = time.perf_counter() - t0
+    n_conv = sum(p["converged"] for p in per)
+    return {"wall_s": round(wall, 3), "solves_per_hour": round(3600.0 * len(per) / wall, 1) if wall > 0 else 0.0,
+            "converged_per_hour": round(3600.0 * n_conv / wall, 1) if wall > 0 else 0.0,
+            "converged": int(n_conv), "mlups": round(cell_steps / wall / 1e6, 1) if wall > 0 else 0.0,
+            "storage": storage, "per_request": per}

@@ -40,9 +40,10 @@ BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 12 + 12 + 1, "fp16": 2 * 19 * 2 + 12 + 12
 LAYOUT_BYTES_PER_CELL = {k: v + 8 + 3 for k, v in BYTES_PER_CELL.items()}
 # DRAM bytes per launch of the step kernel (read + write, mean of an odd and
 # an even step) from the ncu capture summarised in
-# profiles/k_lbm_fused_sphere_240x120x115.md
-NCU_TRAFFIC = {"fp16": (232081408 + 149953536 + 218365952 + 189753344) / 2,
-               "fp32": (364544768 + 275870208 + 354004992 + 316344064) / 2}
+# profiles/k_lbm_fused_sphere_240x120x115.md (this build: shell tiles first
+# in the queue for FP16, one shell block per SM for FP32)
+NCU_TRAFFIC = {"fp16": (238587392 + 159954432 + 225948672 + 198446848) / 2,
+               "fp32": (350971136 + 271097344 + 334143232 + 310798080) / 2}
 # the workload both arms run (the reference arm in its own FP32 form)
 WORKLOAD_CONFIG = {"workload": "sphere Re=100, 240x120x115 (3.31 M cells), icosphere L6 (81,920 triangles), "
                                "TRT+Smagorinsky, zero-gradient outlet, free-slip lateral walls",
@@ -324,27 +325,30 @@ def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20, chunk=1
             "diverged_domains": int(diverged)}
 
 
-def serve_session(n_requests=16, rate=2.0, max_steps=30000, seq_sample=200):
+def serve_session(n_requests=16, rate=2.0, max_steps=30000):
     """The request loop: n_requests Poisson arrivals (rate per second) served
     by continuous batching (FP16), once in real time (latency percentiles) and
     once with every request queued at the start (throughput); the same
-    requests solved one at a time in plain FP32 beside it."""
+    requests solved one at a time in plain FP32 beside it, each to its own
+    convergence (measured)."""
     from aeros_gb300 import serve
     reqs = serve.make_requests(n_requests, rate=rate)
     srv = serve.Server(storage="fp16", max_steps=max_steps)
     live = srv.run(reqs, realtime=True)
     sat = srv.run(reqs, realtime=False)
-    steps_of = {r.rid: r.steps for r in sat["results"]}
-    seq = serve.sequential_plain(reqs, steps_of, sample_steps=seq_sample)
-    conv_seq = sum(r.converged for r in sat["results"])
-    seq_conv_per_h = 3600.0 * conv_seq / seq["wall_s_estimated"] if seq["wall_s_estimated"] > 0 else 0.0
+    seq = serve.sequential_plain(reqs, max_steps=max_steps)
+    per_seq = {p["rid"]: p for p in seq.pop("per_request")}
     return {"requests": n_requests, "rate_per_s": rate, "realtime": live["summary"], "saturated": sat["summary"],
-            "sequential_fp32": seq, "sequential_converged_per_hour": round(seq_conv_per_h, 1),
+            "sequential_fp32": seq,
             "speedup_solves_per_hour": round(sat["summary"]["solves_per_hour"] / seq["solves_per_hour"], 3)
             if seq["solves_per_hour"] > 0 else None,
-            "per_request": [dict(rid=r.rid, grid=reqs[r.rid].grid, level=reqs[r.rid].level, re=round(reqs[r.rid].re, 1),
-                                 steps=r.steps, cd=round(r.cd, 5), converged=r.converged,
-                                 latency_s=round(r.latency, 3)) for r in live["results"]]}
+            "speedup_converged_per_hour": round(sat["summary"]["converged_per_hour"] / seq["converged_per_hour"], 3)
+            if seq["converged_per_hour"] > 0 else None,
+            "per_request": [dict(rid=r.rid, grid=reqs[r.rid].grid, triangles=20 * reqs[r.rid].freq ** 2,
+                                 re=round(reqs[r.rid].re, 1), steps=r.steps, cd=round(r.cd, 5), converged=r.converged,
+                                 latency_s=round(r.latency, 3), fp32_steps=per_seq[r.rid]["steps"],
+                                 fp32_cd=round(per_seq[r.rid]["cd"], 5), fp32_converged=per_seq[r.rid]["converged"])
+                            for r in live["results"]]}
 
 
 def sdf_bench(res=256, reps=5, cpu=True):

@@ -9,26 +9,28 @@ def test_requests_are_seeded_poisson():
     from aeros_gb300 import serve
     a = serve.make_requests(400, rate=2.0, seed=7)
     b = serve.make_requests(400, rate=2.0, seed=7)
-    assert [(r.arrival, r.grid, r.level, r.re) for r in a] == [(r.arrival, r.grid, r.level, r.re) for r in b]
+    assert [(r.arrival, r.grid, r.freq, r.re) for r in a] == [(r.arrival, r.grid, r.freq, r.re) for r in b]
     gaps = np.diff([0.0] + [r.arrival for r in a])
     assert (gaps > 0).all()
     assert 0.4 < gaps.mean() < 0.6            # mean gap 1 / rate
     assert 0.7 < gaps.std() / gaps.mean() < 1.3   # exponential: coefficient of variation 1
     assert all(50.0 <= r.re <= 1000.0 for r in a)
     assert {r.grid for r in a} == set(serve.SERVE_GRIDS)
-    assert {r.level for r in a} == set(serve.SERVE_LEVELS)
+    assert all(serve.SERVE_FREQS[0] <= r.freq <= serve.SERVE_FREQS[1] for r in a)
+    tris = [20 * r.freq * r.freq for r in a]
+    assert min(tris) < 40000 and max(tris) > 450000   # 20k .. 500k triangles
 
 
 def test_footprint_estimate_orders_requests():
     from aeros_gb300 import serve
-    small = serve.Request(0, 0.0, (48, 48, 48), 5, 100.0, 1)
-    big = serve.Request(1, 0.0, (256, 128, 128), 7, 100.0, 2)
+    small = serve.Request(0, 0.0, (48, 48, 48), 32, 100.0, 1)
+    big = serve.Request(1, 0.0, (256, 128, 128), 158, 100.0, 2)
     assert serve.footprint_estimate(small) < serve.footprint_estimate(big)
     assert serve.footprint_estimate(big, "fp32") > serve.footprint_estimate(big, "fp16")
 
 
 def _reqs(serve, n):
-    return serve.make_requests(n, rate=50.0, seed=11, grids=SMALL_GRIDS, levels=(2, 3))
+    return serve.make_requests(n, rate=50.0, seed=11, grids=SMALL_GRIDS, freqs=(4, 8))
 
 
 @pytest.mark.gpu
@@ -76,3 +78,32 @@ def test_admission_respects_slots_and_budget():
                          chunk=100).run(reqs, realtime=False)
     assert max_overlap(tight["results"]) == 1 and tight["summary"]["requests"] == 5
     assert all(r.steps == 400 or r.converged for r in tight["results"])
+
+
+def test_geodesic_meshes_are_closed_and_outward():
+    """The serving meshes (class-I geodesic spheres, 20 n^2 triangles): every
+    edge is shared by exactly two triangles in opposite directions (closed,
+    as the voxelizer's parity test needs) and every face points outward."""
+    from aeros_gb300 import geometry
+    for n in (1, 3, 32):
+        v, c = geometry.geodesic_unit(n)
+        assert len(c) == 20 * n * n and len(v) == 10 * n * n + 2
+        e = np.concatenate([c[:, [0, 1]], c[:, [1, 2]], c[:, [2, 0]]])
+        fwd = set((e[:, 0] * len(v) + e[:, 1]).tolist())
+        assert len(fwd) == len(e) and fwd == set((e[:, 1] * len(v) + e[:, 0]).tolist())
+        t = v[c]
+        nrm = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+        assert (np.einsum("ij,ij->i", nrm, t.mean(axis=1)) > 0).all()
+
+
+@pytest.mark.gpu
+def test_sequential_baseline_runs_each_request_to_its_end():
+    """The one-at-a-time baseline steps every request until its own Cd
+    converges or the cap: measured, with the serving loop's rule."""
+    from aeros_gb300 import serve
+    reqs = _reqs(serve, 3)
+    seq = serve.sequential_plain(reqs, check_every=200, tol=1e-3, max_steps=600)
+    assert len(seq["per_request"]) == 3 and seq["wall_s"] > 0
+    for p in seq["per_request"]:
+        assert p["steps"] % 200 == 0 and 0 < p["steps"] <= 600
+        assert p["converged"] or p["steps"] == 600
