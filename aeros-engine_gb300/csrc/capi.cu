@@ -589,6 +589,10 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
         A.fq[q] = static_cast<char*>(h->f) + (size_t)q * (size_t)h->qstride * h->esize;
         A.nbq[q] = cx19(q) + cy19(q) * h->nx + cz19(q) * h->nx * h->ny;
     }
+    for (int q = 0; q < Q19; ++q) {
+        A.goff[q] = ((long long)opp19(q) * h->qstride - A.nbq[q]) * h->esize;
+        A.soff[q] = ((long long)q * h->qstride + A.nbq[q]) * h->esize;
+    }
     A.f = h->f; A.desc = h->desc; A.shell = h->shell; A.shell_kind = h->shell_kind;
     A.shell_gth = h->shell_gth; A.shell_sct = h->shell_sct;
     A.zg_src = h->zg_src;

@@ -78,6 +78,10 @@ struct StepArgs {
     void* f;
     void* fq[Q19];              // start of population plane q (f + q * qstride)
     int nbq[Q19];               // linear offset of c_q: cx + cy * nx + cz * nx * ny
+    long long goff[Q19];        // odd steps, bytes from a cell's slot in plane 0 to the slot population q is
+                                // gathered from: ((opp q) * qstride - nbq[q]) * element size
+    long long soff[Q19];        // ... and to the slot post-collision population j goes to:
+                                // (j * qstride + nbq[j]) * element size
     const uint32_t* desc;
     const int* shell;
     const uint32_t* shell_gth;  // odd steps: element offset (plane * qstride + cell) of the source of
@@ -823,15 +827,17 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
         // issuing both forms costs more registers than the round trip saves)
         if (d & D_WALL) return;
         if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
+        // one address per cell; every gather is a constant byte offset from it
+        const char* pc = static_cast<const char*>(A.f) + (long long)cell * (long long)sizeof(typename S::T);
         if ((d & D_LINKS) == 0) {
 #pragma unroll
-            for (int q = 0; q < Q19; ++q) f[q] = ldp<S>(A, q, fplane<S>(A, opp19(q)) + (cell - nb19(A, q)));
+            for (int q = 0; q < Q19; ++q) f[q] = ldp<S>(A, q, reinterpret_cast<const typename S::T*>(pc + A.goff[q]));
         } else {
 #pragma unroll
             for (int q = 0; q < Q19; ++q) {
                 const bool special = (d >> q) & 1u;
-                const int src = special ? cell : cell - nb19(A, q);
-                f[q] = ldp<S>(A, q, fplane<S>(A, special ? q : opp19(q)) + src);
+                f[q] = ldp<S>(A, q, special ? fplane<S>(A, q) + cell
+                                            : reinterpret_cast<const typename S::T*>(pc + A.goff[q]));
             }
         }
     }
@@ -864,15 +870,18 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
                     stp<S>(A, solid ? opp19(j) : j, fplane<S>(A, opp19(j)) + cell, f[j]);
                 }
             }
-        } else if (plain) {
-#pragma unroll
-            for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
         } else {
+            char* pc = static_cast<char*>(A.f) + (long long)cell * (long long)sizeof(typename S::T);
+            if (plain) {
 #pragma unroll
-            for (int j = 0; j < Q19; ++j) {
-                const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
-                if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
-                else stp<S>(A, j, fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+                for (int j = 0; j < Q19; ++j) stp<S>(A, j, reinterpret_cast<typename S::T*>(pc + A.soff[j]), f[j]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < Q19; ++j) {
+                    const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
+                    if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
+                    else stp<S>(A, j, reinterpret_cast<typename S::T*>(pc + A.soff[j]), f[j]);
+                }
             }
         }
         if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
@@ -1723,15 +1732,18 @@ __device__ __forceinline__ void warp_cell(const StepArgs& A, const StepVar& V, i
             if constexpr (SH) S::raw_store(slot(opp19(j)), st_shift<S>(A, rd, f[j]));
             else *slot(opp19(j)) = f[j];
         }
-    } else if ((d & D_LINKS) == 0) {
-#pragma unroll
-        for (int j = 0; j < Q19; ++j) stp<S>(A, j, fplane<S>(A, j) + (cell + nb19(A, j)), f[j]);
     } else {
+        char* pc = static_cast<char*>(A.f) + (long long)cell * (long long)sizeof(T);
+        if ((d & D_LINKS) == 0) {
 #pragma unroll
-        for (int j = 0; j < Q19; ++j) {
-            const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
-            if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
-            else stp<S>(A, j, fplane<S>(A, j) + cell + nb19(A, j), f[j]);
+            for (int j = 0; j < Q19; ++j) stp<S>(A, j, reinterpret_cast<T*>(pc + A.soff[j]), f[j]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < Q19; ++j) {
+                const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
+                if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
+                else stp<S>(A, j, reinterpret_cast<T*>(pc + A.soff[j]), f[j]);
+            }
         }
     }
     if (V.write_u) V.uc[cell] = make_float4(r.ux, r.uy, r.uz, 0.0f);
