@@ -1366,7 +1366,8 @@ __device__ __forceinline__ void add_slice_sums(WarpSums& W, const Acc& acc, floa
 }
 
 // A warp's sums of the step into the domain's fixed-point accumulators; the
-// last of the step's `nwarps` warps applies the totals (statistics, divergence
+// last of the step's `nwarps` callers (warps, or blocks when one warp per
+// block calls for its block) applies the totals (statistics, divergence
 // guard, Nusselt number) and rewinds the accumulators for the next step.
 template <bool THERMAL>
 __device__ __forceinline__ void finish_warp_sums(const StepArgs& A, const WarpSums& W, float mx, int lane,
@@ -1405,6 +1406,32 @@ __device__ __forceinline__ void finish_warp_sums(const StepArgs& A, const WarpSu
         vc->warps_done = 0;
         apply_totals(A, t, m, c);   // also rewinds tile_next
     }
+}
+
+// The block's warp sums into the step's accumulators, by its first warp: one
+// fence per block instead of one per warp (a fence waits for the fencing
+// thread's own outstanding stores; the finisher reads only the accumulators,
+// which the first warp writes, so the other warps' stores need no ordering).
+// The last block to arrive applies the totals.
+template <bool THERMAL>
+__device__ __forceinline__ void finish_block_sums(const StepArgs& A, const WarpSums* s_sums, float* s_mx, float mx,
+                                                  int lane, int wid) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_mx[wid] = mx;
+    __syncthreads();
+    if (wid != 0) return;
+    WarpSums W = s_sums[0];
+    float m = s_mx[0];
+#pragma unroll
+    for (int w = 1; w < STEP_BLOCK / 32; ++w) {
+        const WarpSums& o = s_sums[w];
+        W.drho += o.drho; W.ke += o.ke; W.tke += o.tke;
+        for (int j = 0; j < 7; ++j) W.cnt[j] += o.cnt[j];
+        W.nu += o.nu; W.tsum += o.tsum; W.nun += o.nun;
+        m = fmaxf(m, s_mx[w]);
+    }
+    finish_warp_sums<THERMAL>(A, W, m, lane, gridDim.x);
 }
 
 // The single-launch step: the first shell_blocks blocks take the boundary
@@ -1517,7 +1544,8 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
             par ^= 1;
         }
     }
-    finish_warp_sums<THERMAL>(A, W, mx, lane, gridDim.x * (STEP_BLOCK / 32));
+    __shared__ float s_mx[STEP_BLOCK / 32];
+    finish_block_sums<THERMAL>(A, s_sums, s_mx, mx, lane, wid);
 }
 
 // ---- warp-tiled interior: 16-byte async copies into per-warp shared memory ------
