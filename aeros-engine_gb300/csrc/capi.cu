@@ -569,6 +569,16 @@ static ShiftT th_shift(const aeros_lbm* h) {
     return ts;
 }
 
+StepOffsets step_offsets(const aeros_lbm* h) {
+    StepOffsets O;
+    for (int q = 0; q < Q19; ++q) {
+        const long long nb = cx19(q) + cy19(q) * (long long)h->nx + cz19(q) * (long long)h->nx * h->ny;
+        O.goff[q] = ((long long)opp19(q) * h->qstride - nb) * h->esize;
+        O.soff[q] = ((long long)q * h->qstride + nb) * h->esize;
+    }
+    return O;
+}
+
 void base_args(const aeros_lbm* h, StepArgs& A) {
     memset(&A, 0, sizeof(A));
     A.nx = h->nx; A.ny = h->ny; A.nz = h->nz; A.nxny = h->nx * h->ny; A.ncell = h->ncell;
@@ -588,10 +598,6 @@ void base_args(const aeros_lbm* h, StepArgs& A) {
     for (int q = 0; q < Q19; ++q) {
         A.fq[q] = static_cast<char*>(h->f) + (size_t)q * (size_t)h->qstride * h->esize;
         A.nbq[q] = cx19(q) + cy19(q) * h->nx + cz19(q) * h->nx * h->ny;
-    }
-    for (int q = 0; q < Q19; ++q) {
-        A.goff[q] = ((long long)opp19(q) * h->qstride - A.nbq[q]) * h->esize;
-        A.soff[q] = ((long long)q * h->qstride + A.nbq[q]) * h->esize;
     }
     A.f = h->f; A.desc = h->desc; A.shell = h->shell; A.shell_kind = h->shell_kind;
     A.shell_gth = h->shell_gth; A.shell_sct = h->shell_sct;
@@ -710,7 +716,7 @@ static int launch_materialize(aeros_lbm* h, float* d_f, float* d_g) {
     A.mat_g = d_g;
     const StepVar V = step_var(h, false);
     const int grid = h->grid[h->next_odd][h->th_on];
-    CUDA_TRY(h->L->step(A, V, h->next_odd, h->th_on, true, grid, h->stream));
+    CUDA_TRY(h->L->step(A, V, step_offsets(h), h->next_odd, h->th_on, true, grid, h->stream));
     return AEROS_OK;
 }
 
@@ -752,7 +758,7 @@ static int enqueue_steps(aeros_lbm* h, int nsteps) {
         const StepVar V = step_var(h, i == nsteps - 1);
         A.th_buoy_mode = h->th_buoy_mode;
         const int grid = h->grid[h->next_odd][h->th_on];
-        CUDA_TRY(h->L->step(A, V, h->next_odd, h->th_on, false, grid, h->stream));
+        CUDA_TRY(h->L->step(A, V, step_offsets(h), h->next_odd, h->th_on, false, grid, h->stream));
         h->last_launches++;
         h->last_kernels += A.split ? 2 : 1;
         h->next_odd = !h->next_odd;

@@ -151,7 +151,8 @@ __global__ void k_thermal_prestream(const StepArgs A) {
 // Launcher table, one instance per storage format (the translation unit of
 // each format is compiled with its own floating-point contraction setting).
 struct Launchers {
-    cudaError_t (*step)(const StepArgs& A, const StepVar& V, bool odd, bool thermal, bool mat, int grid, cudaStream_t s);
+    cudaError_t (*step)(const StepArgs& A, const StepVar& V, const StepOffsets& O, bool odd, bool thermal, bool mat,
+                        int grid, cudaStream_t s);
     int (*occupancy)(bool odd, bool thermal);
     cudaError_t (*fill_uniform)(const FillArgs& a, cudaStream_t s);
     cudaError_t (*set_equilibrium)(void* f, const uint32_t* desc, long long qstride, int ncell, const float* rho,
@@ -177,17 +178,17 @@ const Launchers& launchers_bf16();
 #define AEROS_DEFINE_LAUNCHERS(NAME, STORE)                                                                           \
     namespace NAME##_detail {                                                                                         \
     template <bool O, bool T, bool M>                                                                                 \
-    cudaError_t launch_one(const StepArgs& A, const StepVar& V, int grid, cudaStream_t s) {                          \
+    cudaError_t launch_one(const StepArgs& A, const StepVar& V, const StepOffsets& OF, int grid, cudaStream_t s) {   \
         if (!M && !T && A.warp) {                                                                                     \
             const int g = (O ? A.warp_grid_odd : A.warp_grid) + A.shell_blocks;                                       \
             if (A.Fx != 0.0f || A.Fy != 0.0f || A.Fz != 0.0f)                                                         \
-                k_lbm_warp<STORE, O, true><<<g, STEP_BLOCK, WarpLayout<STORE>::BYTES, s>>>(A, V);                     \
+                k_lbm_warp<STORE, O, true><<<g, STEP_BLOCK, WarpLayout<STORE>::BYTES, s>>>(A, V, OF);                     \
             else                                                                                                      \
-                k_lbm_warp<STORE, O, false><<<g, STEP_BLOCK, WarpLayout<STORE>::BYTES, s>>>(A, V);                    \
+                k_lbm_warp<STORE, O, false><<<g, STEP_BLOCK, WarpLayout<STORE>::BYTES, s>>>(A, V, OF);                    \
         } else if (!M && A.fused) {                                                                                   \
             const int g = (O ? A.fused_grid_odd : A.fused_grid) + A.shell_blocks;                                      \
-            if (A.shell_blocks > 0) k_lbm_fused<STORE, O, T, false><<<g, STEP_BLOCK, 0, s>>>(A, V);                    \
-            else k_lbm_fused<STORE, O, T, true><<<g, STEP_BLOCK, 0, s>>>(A, V);                                        \
+            if (A.shell_blocks > 0) k_lbm_fused<STORE, O, T, false><<<g, STEP_BLOCK, 0, s>>>(A, V, OF);                    \
+            else k_lbm_fused<STORE, O, T, true><<<g, STEP_BLOCK, 0, s>>>(A, V, OF);                                        \
         } else if (!M && A.split) {                                                                                   \
             StepArgs B = A;                                                                                           \
             B.shell_part_base = grid;                                                                                 \
@@ -198,14 +199,14 @@ const Launchers& launchers_bf16();
         }                                                                                                             \
         return cudaGetLastError();                                                                                    \
     }                                                                                                                 \
-    cudaError_t step_(const StepArgs& A, const StepVar& V, bool odd, bool thermal, bool mat, int grid,             \
-                      cudaStream_t s) {                                                                               \
+    cudaError_t step_(const StepArgs& A, const StepVar& V, const StepOffsets& OF, bool odd, bool thermal, bool mat,  \
+                      int grid, cudaStream_t s) {                                                                     \
         if (mat) {                                                                                                    \
-            if (odd) return thermal ? launch_one<true, true, true>(A, V, grid, s) : launch_one<true, false, true>(A, V, grid, s); \
-            return thermal ? launch_one<false, true, true>(A, V, grid, s) : launch_one<false, false, true>(A, V, grid, s);  \
+            if (odd) return thermal ? launch_one<true, true, true>(A, V, OF, grid, s) : launch_one<true, false, true>(A, V, OF, grid, s); \
+            return thermal ? launch_one<false, true, true>(A, V, OF, grid, s) : launch_one<false, false, true>(A, V, OF, grid, s);  \
         }                                                                                                             \
-        if (odd) return thermal ? launch_one<true, true, false>(A, V, grid, s) : launch_one<true, false, false>(A, V, grid, s); \
-        return thermal ? launch_one<false, true, false>(A, V, grid, s) : launch_one<false, false, false>(A, V, grid, s);    \
+        if (odd) return thermal ? launch_one<true, true, false>(A, V, OF, grid, s) : launch_one<true, false, false>(A, V, OF, grid, s); \
+        return thermal ? launch_one<false, true, false>(A, V, OF, grid, s) : launch_one<false, false, false>(A, V, OF, grid, s);    \
     }                                                                                                                 \
     template <bool O, bool T>                                                                                         \
     int occ_one() {                                                                                                   \

@@ -78,10 +78,6 @@ struct StepArgs {
     void* f;
     void* fq[Q19];              // start of population plane q (f + q * qstride)
     int nbq[Q19];               // linear offset of c_q: cx + cy * nx + cz * nx * ny
-    long long goff[Q19];        // odd steps, bytes from a cell's slot in plane 0 to the slot population q is
-                                // gathered from: ((opp q) * qstride - nbq[q]) * element size
-    long long soff[Q19];        // ... and to the slot post-collision population j goes to:
-                                // (j * qstride + nbq[j]) * element size
     const uint32_t* desc;
     const int* shell;
     const uint32_t* shell_gth;  // odd steps: element offset (plane * qstride + cell) of the source of
@@ -805,10 +801,24 @@ __device__ __forceinline__ void thermal_substep(const StepArgs& A, int cell, int
     }
 }
 
+// Odd-step addressing by byte offsets, a kernel parameter of its own beside
+// StepArgs (the many-domain kernel copies StepArgs into shared memory and
+// keeps that copy unchanged): from a cell's slot in plane 0 to the slot
+// population q is gathered from, ((opp q) * qstride - nb_q) * element size,
+// and to the slot post-collision population j goes to, (j * qstride + nb_j)
+// * element size.
+struct StepOffsets {
+    long long goff[Q19];
+    long long soff[Q19];
+};
+
 // ---- interior cell (1 <= x,y,z <= N-2): flat neighbour offsets ---------------
-template <class S, bool ODD, bool THERMAL, bool MAT>
+// OFFS: odd-step gathers and scatters as one cell address plus the byte
+// offsets O; otherwise plane pointer plus neighbour offset.
+template <class S, bool ODD, bool THERMAL, bool MAT, bool OFFS = false>
 __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVar& V, int cell, int x, int y, int z,
-                                                 Acc& acc, const uint32_t* dpre = nullptr) {
+                                                 Acc& acc, const uint32_t* dpre = nullptr,
+                                                 const StepOffsets* O = nullptr) {
     const uint32_t d = dpre ? *dpre : A.desc[cell];
     constexpr bool SH = S::shifted;
     float f[Q19];
@@ -829,15 +839,18 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
         if (!MAT && A.use_les && (d & D_LES)) strainPre = strain_prev(A, V, cell);
         // one address per cell; every gather is a constant byte offset from it
         const char* pc = static_cast<const char*>(A.f) + (long long)cell * (long long)sizeof(typename S::T);
+        auto src = [&](int q) -> const typename S::T* {
+            if constexpr (OFFS) return reinterpret_cast<const typename S::T*>(pc + O->goff[q]);
+            else return fplane<S>(A, opp19(q)) + (cell - nb19(A, q));
+        };
         if ((d & D_LINKS) == 0) {
 #pragma unroll
-            for (int q = 0; q < Q19; ++q) f[q] = ldp<S>(A, q, reinterpret_cast<const typename S::T*>(pc + A.goff[q]));
+            for (int q = 0; q < Q19; ++q) f[q] = ldp<S>(A, q, src(q));
         } else {
 #pragma unroll
             for (int q = 0; q < Q19; ++q) {
                 const bool special = (d >> q) & 1u;
-                f[q] = ldp<S>(A, q, special ? fplane<S>(A, q) + cell
-                                            : reinterpret_cast<const typename S::T*>(pc + A.goff[q]));
+                f[q] = ldp<S>(A, q, special ? fplane<S>(A, q) + cell : src(q));
             }
         }
     }
@@ -872,15 +885,19 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
             }
         } else {
             char* pc = static_cast<char*>(A.f) + (long long)cell * (long long)sizeof(typename S::T);
+            auto dst = [&](int j) -> typename S::T* {
+                if constexpr (OFFS) return reinterpret_cast<typename S::T*>(pc + O->soff[j]);
+                else return fplane<S>(A, j) + (cell + nb19(A, j));
+            };
             if (plain) {
 #pragma unroll
-                for (int j = 0; j < Q19; ++j) stp<S>(A, j, reinterpret_cast<typename S::T*>(pc + A.soff[j]), f[j]);
+                for (int j = 0; j < Q19; ++j) stp<S>(A, j, dst(j), f[j]);
             } else {
 #pragma unroll
                 for (int j = 0; j < Q19; ++j) {
                     const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
                     if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
-                    else stp<S>(A, j, reinterpret_cast<typename S::T*>(pc + A.soff[j]), f[j]);
+                    else stp<S>(A, j, dst(j), f[j]);
                 }
             }
         }
@@ -1187,16 +1204,16 @@ __device__ __forceinline__ void shell_cell(const StepArgs& A, const StepVar& V, 
 
 // Interior cell li: the interior (x, y, z in 1 .. n-2) in x-fastest order.
 // dpre: its descriptor, already loaded (NULL: load it here).
-template <class S, bool ODD, bool THERMAL, bool MAT>
+template <class S, bool ODD, bool THERMAL, bool MAT, bool OFFS = false>
 __device__ __forceinline__ void interior_cell(const StepArgs& A, const StepVar& V, int li, Acc& acc,
-                                              const uint32_t* dpre = nullptr) {
+                                              const uint32_t* dpre = nullptr, const StepOffsets* O = nullptr) {
     if (li < A.n_interior) {
         const uint32_t r = A.div_ix.div((uint32_t)li);
         const int x = li - (int)r * (A.nx - 2) + 1;
         const uint32_t zq = A.div_iy.div(r);
         const int y = (int)(r - zq * (uint32_t)(A.ny - 2)) + 1;
         const int z = (int)zq + 1;
-        process_interior<S, ODD, THERMAL, MAT>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc, dpre);
+        process_interior<S, ODD, THERMAL, MAT, OFFS>(A, V, (z * A.ny + y) * A.nx + x, x, y, z, acc, dpre, O);
     }
 }
 
@@ -1205,9 +1222,10 @@ __device__ __forceinline__ void shell_tile(const StepArgs& A, const StepVar& V, 
     shell_cell<S, ODD, THERMAL, MAT>(A, V, st * STEP_BLOCK + (int)threadIdx.x, acc);
 }
 
-template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __forceinline__ void interior_tile(const StepArgs& A, const StepVar& V, int it, Acc& acc) {
-    interior_cell<S, ODD, THERMAL, MAT>(A, V, it * STEP_BLOCK + (int)threadIdx.x, acc);
+template <class S, bool ODD, bool THERMAL, bool MAT, bool OFFS = false>
+__device__ __forceinline__ void interior_tile(const StepArgs& A, const StepVar& V, int it, Acc& acc,
+                                              const StepOffsets* O = nullptr) {
+    interior_cell<S, ODD, THERMAL, MAT, OFFS>(A, V, it * STEP_BLOCK + (int)threadIdx.x, acc, nullptr, O);
 }
 
 template <class S, bool ODD, bool THERMAL, bool MAT>
@@ -1442,7 +1460,7 @@ __device__ __forceinline__ void finish_block_sums(const StepArgs& A, const WarpS
 template <class S, bool ODD, bool THERMAL, bool QUEUE>
 __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCKS
                                                       : (ODD ? AEROS_FUSED_ODD_MIN_BLOCKS : AEROS_FUSED_MIN_BLOCKS))
-    k_lbm_fused(const StepArgs A, const StepVar V) {
+    k_lbm_fused(const StepArgs A, const StepVar V, const StepOffsets O) {
     if (A.ctl->halt) return;   // uniform: every thread reads the same flag
     __shared__ WarpSums s_sums[STEP_BLOCK / 32];
     __shared__ int s_tile[2];
@@ -1527,7 +1545,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
                 const int x = ccur - (int)r * A.nx;
                 const uint32_t z = A.div_y.div(r);
                 const int y = (int)(r - z * (uint32_t)A.ny);
-                process_interior<S, ODD, THERMAL, false>(A, V, ccur, x, y, (int)z, acc, &dcur);
+                process_interior<S, ODD, THERMAL, false, true>(A, V, ccur, x, y, (int)z, acc, &dcur, &O);
             }
             add_slice(acc);
             it = itn;
@@ -1536,7 +1554,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
         while (it < nall) {
             Acc acc;
             acc.zero();
-            interior_tile<S, ODD, THERMAL, false>(A, V, it - nq, acc);
+            interior_tile<S, ODD, THERMAL, false, true>(A, V, it - nq, acc, &O);
             add_slice(acc);
             if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
             __syncthreads();
@@ -1718,8 +1736,8 @@ __device__ __forceinline__ float strain_rows(const float4* vel, int t) {
 // One interior cell of a warp tile (non-thermal). buf: the tile's buffer;
 // t: the cell's position in the tile; strainPre: its previous-step |S|.
 template <class S, bool ODD, bool FORCE>
-__device__ __forceinline__ void warp_cell(const StepArgs& A, const StepVar& V, int cell, uint32_t d,
-                                          unsigned char* buf, int t, float strainPre, Acc& acc) {
+__device__ __forceinline__ void warp_cell(const StepArgs& A, const StepVar& V, const StepOffsets& O, int cell,
+                                          uint32_t d, unsigned char* buf, int t, float strainPre, Acc& acc) {
     using L = WarpLayout<S>;
     using T = typename S::T;
     constexpr bool SH = S::shifted;
@@ -1764,13 +1782,13 @@ __device__ __forceinline__ void warp_cell(const StepArgs& A, const StepVar& V, i
         char* pc = static_cast<char*>(A.f) + (long long)cell * (long long)sizeof(T);
         if ((d & D_LINKS) == 0) {
 #pragma unroll
-            for (int j = 0; j < Q19; ++j) stp<S>(A, j, reinterpret_cast<T*>(pc + A.soff[j]), f[j]);
+            for (int j = 0; j < Q19; ++j) stp<S>(A, j, reinterpret_cast<T*>(pc + O.soff[j]), f[j]);
         } else {
 #pragma unroll
             for (int j = 0; j < Q19; ++j) {
                 const bool solid = (d >> opp19(j)) & 1u;   // target c + c_j is a wall
                 if (solid) stp<S>(A, opp19(j), fplane<S>(A, opp19(j)) + cell, f[j]);
-                else stp<S>(A, j, reinterpret_cast<T*>(pc + A.soff[j]), f[j]);
+                else stp<S>(A, j, reinterpret_cast<T*>(pc + O.soff[j]), f[j]);
             }
         }
     }
@@ -1813,7 +1831,7 @@ __device__ __forceinline__ void warp_issue_vel(const StepArgs& A, const StepVar&
 // One lattice step (non-thermal) in one launch: shell blocks as in
 // k_lbm_fused, interior warps over warp tiles.
 template <class S, bool ODD, bool FORCE>
-__global__ void __launch_bounds__(STEP_BLOCK, WarpLayout<S>::MIN_BLOCKS) k_lbm_warp(const StepArgs A, const StepVar V) {
+__global__ void __launch_bounds__(STEP_BLOCK, WarpLayout<S>::MIN_BLOCKS) k_lbm_warp(const StepArgs A, const StepVar V, const StepOffsets O) {
     using L = WarpLayout<S>;
     using T = typename S::T;
     if (A.ctl->halt) return;   // uniform: every thread reads the same flag
@@ -1901,7 +1919,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, WarpLayout<S>::MIN_BLOCKS) k_lbm_w
                     if (m == k) s = sp[k];
                 Acc acc;
                 acc.zero();
-                if (cell < A.ncell && !(d & (D_WALL | D_SHELL))) warp_cell<S, ODD, FORCE>(A, V, cell, d, buf, t, s, acc);
+                if (cell < A.ncell && !(d & (D_WALL | D_SHELL))) warp_cell<S, ODD, FORCE>(A, V, O, cell, d, buf, t, s, acc);
                 lane_add(A, sums, lane, acc, mx);
             }
             __syncwarp();
@@ -2070,6 +2088,9 @@ __global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_s
             int* dst = reinterpret_cast<int*>(s_args);
             for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / 4); i += BATCH_BLOCK) dst[i] = src[i];
             __syncthreads();
+            // The arguments are written as ints and read as StepArgs fields:
+            // no load of a field may be kept from before the copy.
+            asm volatile("" ::: "memory");
             cur = dom;
         }
         // a halted domain stays halted for the rest of the call (its flag is
