@@ -2020,6 +2020,8 @@ __global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_s
     // domain or runs out of items.
     __shared__ __align__(16) unsigned char s_args[sizeof(StepArgs)];
     __shared__ WarpSums s_sums[BATCH_BLOCK / 32];
+    __shared__ float s_mx[BATCH_BLOCK / 32];
+    __shared__ int s_ws[BATCH_BLOCK / 32];
     __shared__ int s_item[2];
     const int lane = (int)(threadIdx.x & 31u), wid = (int)(threadIdx.x >> 5);
     StepArgs& A = *reinterpret_cast<StepArgs*>(s_args);   // StepArgs is not trivially constructible
@@ -2033,35 +2035,57 @@ __global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_s
     __syncwarp();
     float mx = 0.0f;
     int w_slices = 0;
+    // The block's sums for `dom` into the domain's accumulators, by its
+    // first warp: one fence per block instead of one per warp (the finisher
+    // reads only the accumulators). Called by the whole block.
     auto flush = [&](int dom) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        __syncwarp();
-        BatchAcc* ac = B.acc + dom;
-        if (lane == 0) atomicAdd(&ac->drho, (unsigned long long)W.drho);
-        else if (lane == 1) atomicAdd(&ac->ke, (unsigned long long)W.ke);
-        else if (lane == 2) atomicAdd(&ac->tke, (unsigned long long)W.tke);
-        else if (lane >= 3 && lane < 10 && W.cnt[lane - 3]) atomicAdd(&ac->cnt[lane - 3], (unsigned long long)W.cnt[lane - 3]);
-        else if (lane == 10 && mx > 0.0f) atomicMax(&ac->maxu2, __float_as_uint(mx));
-        __threadfence();
-        __syncwarp();
-        int last = 0;
-        if (lane == 0)
-            last = atomicAdd(&ac->done, (unsigned int)w_slices) + (unsigned int)w_slices == (unsigned int)B.doms[dom].nslices;
-        if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
-            __threadfence();
-            volatile BatchAcc* va = ac;
-            const double t[5] = {(double)(long long)va->drho / (double)FX_DRHO, (double)(long long)va->ke / (double)FX_KE,
-                                 (double)(long long)va->tke / (double)FX_TKE, 0.0, 0.0};
-            const long long c[8] = {(long long)va->cnt[0], (long long)va->cnt[1], (long long)va->cnt[2],
-                                    (long long)va->cnt[3], (long long)va->cnt[4], (long long)va->cnt[5], 0,
-                                    (long long)va->cnt[6]};
-            apply_totals(A, t, __uint_as_float(va->maxu2), c);
-            va->drho = 0; va->ke = 0; va->tke = 0;
-            for (int j = 0; j < 7; ++j) va->cnt[j] = 0;
-            va->maxu2 = 0;
-            va->done = 0;
+        if (lane == 0) {
+            s_mx[wid] = mx;
+            s_ws[wid] = w_slices;
         }
+        __syncthreads();
+        if (wid == 0) {
+            WarpSums T = s_sums[0];
+            float m = s_mx[0];
+            int ns = s_ws[0];
+            for (int w = 1; w < BATCH_BLOCK / 32; ++w) {
+                T.drho += s_sums[w].drho; T.ke += s_sums[w].ke; T.tke += s_sums[w].tke;
+                for (int j = 0; j < 7; ++j) T.cnt[j] += s_sums[w].cnt[j];
+                m = fmaxf(m, s_mx[w]);
+                ns += s_ws[w];
+            }
+            if (ns > 0) {
+                BatchAcc* ac = B.acc + dom;
+                if (lane == 0) atomicAdd(&ac->drho, (unsigned long long)T.drho);
+                else if (lane == 1) atomicAdd(&ac->ke, (unsigned long long)T.ke);
+                else if (lane == 2) atomicAdd(&ac->tke, (unsigned long long)T.tke);
+                else if (lane >= 3 && lane < 10 && T.cnt[lane - 3]) atomicAdd(&ac->cnt[lane - 3], (unsigned long long)T.cnt[lane - 3]);
+                else if (lane == 10 && m > 0.0f) atomicMax(&ac->maxu2, __float_as_uint(m));
+                __threadfence();
+                __syncwarp();
+                int last = 0;
+                if (lane == 0)
+                    last = atomicAdd(&ac->done, (unsigned int)ns) + (unsigned int)ns == (unsigned int)B.doms[dom].nslices;
+                if (__shfl_sync(0xffffffffu, last, 0) && lane == 0) {
+                    __threadfence();
+                    volatile BatchAcc* va = ac;
+                    const double t[5] = {(double)(long long)va->drho / (double)FX_DRHO,
+                                         (double)(long long)va->ke / (double)FX_KE,
+                                         (double)(long long)va->tke / (double)FX_TKE, 0.0, 0.0};
+                    const long long c[8] = {(long long)va->cnt[0], (long long)va->cnt[1], (long long)va->cnt[2],
+                                            (long long)va->cnt[3], (long long)va->cnt[4], (long long)va->cnt[5], 0,
+                                            (long long)va->cnt[6]};
+                    apply_totals(A, t, __uint_as_float(va->maxu2), c);
+                    va->drho = 0; va->ke = 0; va->tke = 0;
+                    for (int j = 0; j < 7; ++j) va->cnt[j] = 0;
+                    va->maxu2 = 0;
+                    va->done = 0;
+                }
+            }
+        }
+        __syncthreads();
         if (lane == 0) {
             W.drho = W.ke = W.tke = 0;
             for (int j = 0; j < 7; ++j) W.cnt[j] = 0;
@@ -2078,7 +2102,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK, AEROS_BATCH_MIN_BLOCKS) k_batch_s
         par ^= 1;
         const bool end = item >= B.item_end;
         const int dom = end ? -1 : B.work[item].dom;
-        if (cur >= 0 && dom != cur && w_slices > 0) flush(cur);
+        if (cur >= 0 && dom != cur) flush(cur);   // block-uniform
         if (end) break;
         const BatchWork wk = B.work[item];
         const BatchDomain& D = B.doms[dom];
