@@ -129,6 +129,14 @@ struct StepArgs {
     double th_rows_n;           // Nx*Nz*(yhi-ylo+1), thermal_lbm.cpp:76
 };
 
+// The many-domain kernel copies a member's StepArgs into shared memory. With
+// StepArgs grown to 1232 bytes (odd-step byte offsets inside it) that kernel
+// read a mix of two members' arguments and faulted on the 64-domain sweep;
+// at 928 bytes it runs clean. The cause was not found: keep StepArgs at its
+// size, pass additions as kernel parameters of their own (StepOffsets), and
+// run any change to it on the full sweep.
+static_assert(sizeof(StepArgs) <= 928, "StepArgs is copied by the many-domain kernel: see above");
+
 // What changes from one step to the next (AA parity of the double-buffered
 // velocity and outlet side buffers, first-step and last-step flags).
 struct StepVar {
