@@ -10,6 +10,13 @@ reports its drag coefficient from the control-volume momentum balance; it is
 retired when Cd changed by less than `tol` (relative) since the previous
 check, or at `max_steps`. Latency is arrival to retirement.
 
+A request can be cancelled at any time (`Server.cancel`, from any thread or
+from the `on_check` callback): a waiting request is dropped, a running one
+leaves the batch after the chunk in flight. Every finished or cancelled
+request can be written as one JSON line (`Server(log=...)`): its step count,
+Cd and the Cd readings so far, latency, and its lattice updates and
+algorithmic bytes per second over its time in the batch.
+
 A domain's trajectory does not depend on the other members of the batch
 (include/aeros_batch.h), and checks fall on the same own-step counts whatever
 the mix, so a request gives the same Cd, the same step count and the same
@@ -20,6 +27,7 @@ The reference has no request loop; this module has no reference counterpart.
 from __future__ import annotations
 
 import dataclasses
+import json
 import math
 import queue
 import threading
@@ -34,6 +42,9 @@ from .solver import Solver, voxel_grid, voxelize
 SERVE_GRIDS = ((48, 48, 48), (96, 48, 48), (128, 64, 64), (192, 96, 96), (256, 128, 128))
 # geodesic sphere frequencies: 20 n^2 triangles, 20,480 (n = 32) to 499,280 (n = 158)
 SERVE_FREQS = (32, 158)
+# Algorithmic bytes of one cell update: 19 populations read and written, the
+# previous and current velocity (3 floats each) and the one-byte solid mask.
+BYTES_PER_CELL = {"fp16": 101, "bf16": 101, "fp32": 177}
 
 
 @dataclasses.dataclass
@@ -50,7 +61,7 @@ class Request:
 class Result:
     rid: int
     arrival: float
-    admitted: float
+    admitted: float         # memory reserved, preparation queued
     finished: float
     steps: int
     cd: float
@@ -58,10 +69,36 @@ class Result:
     cells: int
     tris: int
     footprint: int
+    started: float = float("nan")   # attached to the batch (nan: never ran)
+    cancelled: bool = False
+    cd_trace: list = dataclasses.field(default_factory=list)   # (own step, Cd) at every reading
+    storage: str = "fp16"
 
     @property
     def latency(self) -> float:
         return self.finished - self.arrival
+
+    @property
+    def mlups(self) -> float:
+        """The request's own cell updates per second of its time in the batch
+        (its share of the GPU while it ran beside the others)."""
+        t = self.finished - self.started
+        return self.cells * self.steps / t / 1e6 if self.steps and t > 0 else 0.0
+
+    @property
+    def gbs(self) -> float:
+        """Algorithmic bytes per second of the request's own updates."""
+        return self.mlups * 1e6 * BYTES_PER_CELL.get(self.storage, 101) / 1e9
+
+    def json_line(self) -> str:
+        """One JSON line describing the solve."""
+        r = lambda v, n=4: round(v, n) if math.isfinite(v) else None   # noqa: E731
+        return json.dumps({
+            "rid": self.rid, "status": "cancelled" if self.cancelled else ("converged" if self.converged else "capped"),
+            "steps": self.steps, "cells": self.cells, "triangles": self.tris, "storage": self.storage,
+            "cd": r(self.cd, 6), "cd_trace": [[k, r(c, 6)] for k, c in self.cd_trace],
+            "latency_s": r(self.latency), "queued_s": r(self.admitted - self.arrival),
+            "mlups": round(self.mlups, 1), "gbs": round(self.gbs, 1), "footprint_bytes": self.footprint})
 
 
 def make_requests(n: int, rate: float = 2.0, seed: int = 0x5E12, grids=SERVE_GRIDS, freqs=SERVE_FREQS,
@@ -124,16 +161,20 @@ def footprint_estimate(req: Request, storage="fp16") -> int:
 
 
 class _Active:
-    __slots__ = ("req", "solver", "box", "area", "u", "tris", "admitted", "steps", "cd_prev", "cd", "bytes")
+    __slots__ = ("req", "solver", "box", "area", "u", "tris", "admitted", "started", "steps", "cd_prev", "cd",
+                 "bytes", "trace")
 
 
 class Server:
     """Continuous batching: admission by slots and HBM footprint, domain
     preparation (mesh, GPU voxelization, domain creation) on a worker thread
-    while the batch steps, Cd-convergence retirement."""
+    while the batch steps, Cd-convergence retirement, cancellation.
+
+    log: a writable text file; one JSON line per finished or cancelled
+    request (`Result.json_line`), flushed as it is written."""
 
     def __init__(self, storage="fp16", budget_bytes=170 << 30, slots=64, check_every=1000, tol=1e-4,
-                 max_steps=30000, chunk=100):
+                 max_steps=30000, chunk=100, log=None):
         if check_every % chunk or chunk % 2:
             raise ValueError("chunk must be even and divide check_every")
         self.storage = storage
@@ -143,6 +184,23 @@ class Server:
         self.tol = float(tol)
         self.max_steps = int(max_steps)
         self.chunk = int(chunk)
+        self.log = log
+        self._lock = threading.Lock()
+        self._cancel: set = set()
+
+    def cancel(self, rid: int) -> None:
+        """Cancels request rid (safe from any thread). It takes effect at the
+        next chunk boundary of the running `run`, or of the next `run` if none
+        is running: a waiting or preparing request never runs, a running one
+        leaves the batch with the steps it has made. Its result is marked
+        cancelled and counts in no throughput or latency figure."""
+        with self._lock:
+            self._cancel.add(int(rid))
+
+    def _take_cancelled(self) -> set:
+        with self._lock:
+            out, self._cancel = self._cancel, set()
+        return out
 
     def _cd(self, a: _Active) -> float:
         F = a.solver.cv_force_box(a.box)
@@ -159,9 +217,11 @@ class Server:
             except Exception as e:   # reported on the serving thread
                 done.put((req, est, t_adm, e))
 
-    def run(self, requests: list[Request], realtime: bool = True, on_retire=None) -> dict:
+    def run(self, requests: list[Request], realtime: bool = True, on_retire=None, on_check=None) -> dict:
         """Serves the requests; returns per-request results and the summary.
-        realtime=False admits each request at once (no waiting for arrivals)."""
+        realtime=False admits each request at once (no waiting for arrivals).
+        on_retire(result, solver): a request converged or reached max_steps.
+        on_check(rid, steps, cd): a Cd reading of a running request."""
         pending = sorted(requests, key=lambda r: r.arrival)
         batch = Batch(self.storage)
         batch.set_tuning(chunk_steps=self.chunk)
@@ -176,6 +236,13 @@ class Server:
         cell_steps = 0
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0   # noqa: E731
+        cancelled: set = set()   # cancellations not yet applied
+
+        def finish(res: Result) -> None:
+            results.append(res)
+            if self.log is not None:
+                self.log.write(res.json_line() + "\n")
+                self.log.flush()
 
         def attach(item):
             nonlocal used, preparing
@@ -184,6 +251,13 @@ class Server:
             if isinstance(built, Exception):
                 used -= est
                 raise built
+            if req.rid in cancelled:   # cancelled while it was being prepared
+                cancelled.discard(req.rid)
+                used -= est
+                built[0].close()
+                finish(Result(req.rid, req.arrival, t_adm, now(), 0, float("nan"), False, req.grid[0] * req.grid[1]
+                              * req.grid[2], built[3], est, cancelled=True, storage=self.storage))
+                return
             a = _Active()
             a.req = req
             a.admitted = t_adm
@@ -192,11 +266,35 @@ class Server:
             used += a.bytes - est
             a.steps = 0
             a.cd_prev = a.cd = float("nan")
+            a.trace = []
             batch.add(a.solver)
+            a.started = now()
             active.append(a)
+
+        def apply_cancellations():
+            nonlocal used
+            cancelled.update(self._take_cancelled())
+            if not cancelled:
+                return
+            for req in [r for r in pending if r.rid in cancelled]:
+                pending.remove(req)
+                cancelled.discard(req.rid)
+                t = now()
+                finish(Result(req.rid, req.arrival, t, t, 0, float("nan"), False, req.grid[0] * req.grid[1]
+                              * req.grid[2], 20 * req.freq * req.freq, 0, cancelled=True, storage=self.storage))
+            for a in [a for a in active if a.req.rid in cancelled]:
+                cancelled.discard(a.req.rid)
+                batch.remove(a.solver)
+                res = Result(a.req.rid, a.req.arrival, a.admitted, now(), a.steps, a.cd, False, a.solver.n, a.tris,
+                             a.bytes, started=a.started, cancelled=True, cd_trace=a.trace, storage=self.storage)
+                a.solver.close()
+                used -= a.bytes
+                active.remove(a)
+                finish(res)
 
         try:
             while pending or active or preparing:
+                apply_cancellations()
                 # admission: arrived requests in order while a slot and memory are free
                 while pending and (not realtime or pending[0].arrival <= now()) \
                         and len(active) + preparing < self.slots:
@@ -222,6 +320,9 @@ class Server:
                     a.steps += self.chunk
                     if a.steps % self.check_every == 0:
                         a.cd_prev, a.cd = a.cd, self._cd(a)
+                        a.trace.append((a.steps, a.cd))
+                        if on_check is not None:
+                            on_check(a.req.rid, a.steps, a.cd)
                         conv = (math.isfinite(a.cd) and math.isfinite(a.cd_prev) and a.cd != 0.0
                                 and abs(a.cd - a.cd_prev) < self.tol * abs(a.cd))
                         if conv or a.steps >= self.max_steps:
@@ -229,13 +330,14 @@ class Server:
                 for a, conv in retired:
                     batch.remove(a.solver)
                     res = Result(a.req.rid, a.req.arrival, a.admitted, now(), a.steps, a.cd, conv,
-                                 a.solver.n, a.tris, a.bytes)
+                                 a.solver.n, a.tris, a.bytes, started=a.started, cd_trace=a.trace,
+                                 storage=self.storage)
                     if on_retire is not None:
                         on_retire(res, a.solver)
                     a.solver.close()
                     used -= a.bytes
                     active.remove(a)
-                    results.append(res)
+                    finish(res)
         finally:
             todo.put(None)
             worker.join()
@@ -252,9 +354,13 @@ class Server:
 
 
 def summarize(results: list[Result], wall: float, cell_steps: int) -> dict:
+    """Throughput and latency over the requests that ran to their end
+    (cancelled ones are counted apart); cell_steps counts every update made."""
+    n_cancel = sum(r.cancelled for r in results)
+    results = [r for r in results if not r.cancelled]
     lat = np.array([r.latency for r in results], np.float64)
     pct = (lambda q: float(np.percentile(lat, q))) if len(lat) else (lambda q: float("nan"))
-    return {"requests": len(results), "converged": int(sum(r.converged for r in results)),
+    return {"requests": len(results), "cancelled": int(n_cancel), "converged": int(sum(r.converged for r in results)),
             "wall_s": round(wall, 3), "solves_per_hour": round(3600.0 * len(results) / wall, 1) if wall > 0 else 0.0,
             "converged_per_hour": round(3600.0 * sum(r.converged for r in results) / wall, 1) if wall > 0 else 0.0,
             "p50_s": round(pct(50), 3), "p95_s": round(pct(95), 3), "p99_s": round(pct(99), 3),

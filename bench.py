@@ -325,16 +325,22 @@ def batch_sweep(n_domains=64, steps=10000, storage="fp16", seq_steps=20, chunk=1
             "diverged_domains": int(diverged)}
 
 
-def serve_session(n_requests=16, rate=2.0, max_steps=30000):
+def serve_session(n_requests=16, rate=2.0, max_steps=30000, log_path=None):
     """The request loop: n_requests Poisson arrivals (rate per second) served
     by continuous batching (FP16), once in real time (latency percentiles) and
     once with every request queued at the start (throughput); the same
     requests solved one at a time in plain FP32 beside it, each to its own
-    convergence (measured)."""
+    convergence (measured). log_path: the real-time session's per-solve JSON
+    lines are written there."""
     from aeros_gb300 import serve
     reqs = serve.make_requests(n_requests, rate=rate)
+    log = open(log_path, "w") if log_path else None
+    try:
+        live = serve.Server(storage="fp16", max_steps=max_steps, log=log).run(reqs, realtime=True)
+    finally:
+        if log is not None:
+            log.close()
     srv = serve.Server(storage="fp16", max_steps=max_steps)
-    live = srv.run(reqs, realtime=True)
     sat = srv.run(reqs, realtime=False)
     seq = serve.sequential_plain(reqs, max_steps=max_steps)
     per_seq = {p["rid"]: p for p in seq.pop("per_request")}
@@ -595,6 +601,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16)
     ap.add_argument("--serve-rate", type=float, default=2.0)
     ap.add_argument("--serve-max-steps", type=int, default=30000)
+    ap.add_argument("--serve-log", default=None, help="file for the real-time session's per-solve JSON lines")
     ap.add_argument("--batch-domains", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=10000)
     ap.add_argument("--batch-chunk", type=int, default=100, help="steps per captured CUDA graph")
@@ -606,7 +613,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "serve":
-        r = serve_session(args.serve_requests, args.serve_rate, args.serve_max_steps)
+        r = serve_session(args.serve_requests, args.serve_rate, args.serve_max_steps, args.serve_log)
         print(json.dumps(r), flush=True)
     elif args.workload == "rb":
         print(json.dumps(rb_bench(args.rb_steps)), flush=True)

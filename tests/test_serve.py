@@ -1,4 +1,7 @@
 """Continuous-batching request loop (aeros_gb300/serve.py)."""
+import io
+import json
+
 import numpy as np
 import pytest
 
@@ -107,3 +110,56 @@ def test_sequential_baseline_runs_each_request_to_its_end():
     for p in seq["per_request"]:
         assert p["steps"] % 200 == 0 and 0 < p["steps"] <= 600
         assert p["converged"] or p["steps"] == 600
+
+
+def test_solve_json_line():
+    """Per-solve line: status, Cd trace, latency and the request's own rate
+    over its time in the batch (cells x steps / (finished - started))."""
+    from aeros_gb300 import serve
+    r = serve.Result(3, 1.0, 1.5, 11.0, 2000, 0.61, True, 1_000_000, 20480, 123, started=2.0,
+                     cd_trace=[(1000, 0.6), (2000, 0.61)], storage="fp16")
+    d = json.loads(r.json_line())
+    assert d["status"] == "converged" and d["steps"] == 2000 and d["cd_trace"] == [[1000, 0.6], [2000, 0.61]]
+    assert d["latency_s"] == 10.0 and d["queued_s"] == 0.5
+    assert d["mlups"] == round(1e6 * 2000 / 9.0 / 1e6, 1)
+    assert d["gbs"] == round(r.mlups * 101 / 1e3, 1)
+    c = serve.Result(4, 0.0, 0.2, 0.2, 0, float("nan"), False, 8, 20, 0, cancelled=True)
+    d = json.loads(c.json_line())
+    assert d["status"] == "cancelled" and d["cd"] is None and d["mlups"] == 0.0 and d["cd_trace"] == []
+    s = serve.summarize([r, c], 10.0, 0)
+    assert s["requests"] == 1 and s["cancelled"] == 1 and s["p50_s"] == 10.0
+
+
+@pytest.mark.gpu
+def test_cancel_mid_solve_and_waiting():
+    """One request cancelled at its first Cd reading, another before it ever
+    runs: both are reported cancelled (the first with the steps it made), the
+    others end exactly as in a run without cancellations, and the log holds
+    one JSON line per request."""
+    from aeros_gb300 import serve
+    reqs = _reqs(serve, 4)
+    kw = dict(check_every=200, max_steps=600, chunk=100, tol=1e-3)
+    base = {r.rid: r for r in serve.Server(**kw).run(reqs, realtime=False)["results"]}
+    log = io.StringIO()
+    srv = serve.Server(slots=3, log=log, **kw)
+    victim, waiting = reqs[1].rid, reqs[3].rid
+    srv.cancel(waiting)
+
+    def check(rid, steps, cd):
+        if rid == victim:
+            srv.cancel(rid)
+
+    out = srv.run(reqs, realtime=False, on_check=check)
+    res = {r.rid: r for r in out["results"]}
+    assert res[victim].cancelled and res[victim].steps == 200 and len(res[victim].cd_trace) == 1
+    assert res[waiting].cancelled and res[waiting].steps == 0
+    for rid in (reqs[0].rid, reqs[2].rid):
+        assert not res[rid].cancelled
+        assert (res[rid].steps, res[rid].cd) == (base[rid].steps, base[rid].cd)
+        assert [c for _, c in res[rid].cd_trace][-1] == base[rid].cd
+    lines = [json.loads(x) for x in log.getvalue().splitlines()]
+    assert sorted(d["rid"] for d in lines) == sorted(r.rid for r in reqs)
+    st = {d["rid"]: d["status"] for d in lines}
+    assert st[victim] == "cancelled" and st[waiting] == "cancelled"
+    assert all(d["mlups"] > 0 for d in lines if d["status"] != "cancelled")
+    assert out["summary"]["requests"] == 2 and out["summary"]["cancelled"] == 2
