@@ -129,13 +129,17 @@ struct StepArgs {
     double th_rows_n;           // Nx*Nz*(yhi-ylo+1), thermal_lbm.cpp:76
 };
 
-// The many-domain kernel copies a member's StepArgs into shared memory. With
-// StepArgs grown to 1232 bytes (odd-step byte offsets inside it) that kernel
-// read a mix of two members' arguments and faulted on the 64-domain sweep;
-// at 928 bytes it runs clean. The cause was not found: keep StepArgs at its
-// size, pass additions as kernel parameters of their own (StepOffsets), and
-// run any change to it on the full sweep.
+// The many-domain kernel copies a member's StepArgs into shared memory, one
+// 32-bit word per thread. Three configurations in which that copy took a
+// second pass (StepArgs of 1080 or 1232 bytes with blocks of 256 threads,
+// 928 bytes with blocks of 128) read a mix of two members' arguments: a hang,
+// and illegal addresses on the 16- and 64-domain sweeps. Every configuration
+// with a single pass (928 bytes, 256 threads) runs clean. The cause was not
+// found: keep StepArgs at its size and the copy in one pass, pass additions
+// as kernel parameters of their own (StepOffsets), and run any change to
+// either on the full sweep.
 static_assert(sizeof(StepArgs) <= 928, "StepArgs is copied by the many-domain kernel: see above");
+static_assert(sizeof(StepArgs) / 4 <= BATCH_BLOCK, "the many-domain kernel copies StepArgs in one pass: see above");
 
 // What changes from one step to the next (AA parity of the double-buffered
 // velocity and outlet side buffers, first-step and last-step flags).
@@ -915,11 +919,10 @@ __device__ __forceinline__ void process_interior(const StepArgs& A, const StepVa
     if (THERMAL) thermal_substep<S, ODD, MAT, true>(A, cell, x, y, z, d, 0ull, r, acc);
 }
 
-// ---- boundary-shell cell: precomputed link kinds (kept out of line so the
-// interior loop stays small in the instruction cache) ------------------------
+// ---- boundary-shell cell: precomputed link kinds -----------------------------
 template <class S, bool ODD, bool THERMAL, bool MAT>
-__device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, int si, int cell, int x, int y, int z,
-                                           unsigned long long skind, Acc& acc) {
+__device__ __forceinline__ void process_shell_body(const StepArgs& A, const StepVar& V, int si, int cell, int x, int y,
+                                                   int z, unsigned long long skind, Acc& acc) {
     // the link kinds give in-domain sources for every shell cell: the
     // populations are loaded before the descriptor arrives
     const uint32_t d = A.desc[cell];
@@ -1047,6 +1050,25 @@ __device__ __noinline__ void process_shell(const StepArgs& A, const StepVar& V, 
         if (V.write_obs) { A.rho[cell] = r.rho; A.strain[cell] = r.strain; A.tke[cell] = r.tke; }
     }
     if (THERMAL) thermal_substep<S, ODD, MAT, false>(A, cell, x, y, z, d, skind, r, acc);
+}
+
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __noinline__ void process_shell_call(const StepArgs& A, const StepVar& V, int si, int cell, int x, int y,
+                                                int z, unsigned long long skind, Acc& acc) {
+    process_shell_body<S, ODD, THERMAL, MAT>(A, V, si, cell, x, y, z, skind, acc);
+}
+
+// 16-bit storage without the thermal lattice: the shell cell inline (measured
+// on the 3.3 M-cell sphere, one box: FP16 step 0.1297 -> 0.1231 ms, 16-domain
+// batch step 0.322 -> 0.308 ms). FP32 storage and the thermal lattice call it
+// out of line (FP32 inline: 0.1521 -> 0.1533 ms).
+template <class S, bool ODD, bool THERMAL, bool MAT>
+__device__ __forceinline__ void process_shell(const StepArgs& A, const StepVar& V, int si, int cell, int x, int y, int z,
+                                              unsigned long long skind, Acc& acc) {
+    if constexpr (sizeof(typename S::T) == 2 && !THERMAL)
+        process_shell_body<S, ODD, THERMAL, MAT>(A, V, si, cell, x, y, z, skind, acc);
+    else
+        process_shell_call<S, ODD, THERMAL, MAT>(A, V, si, cell, x, y, z, skind, acc);
 }
 
 // Block reduction of the per-thread accumulators into one partial (FP64),
@@ -1499,7 +1521,7 @@ __global__ void __launch_bounds__(STEP_BLOCK, THERMAL ? AEROS_FUSED_TH_MIN_BLOCK
     } else if (QUEUE) {
         // The counter only grows: a block that has drawn an interior tile
         // never draws a shell tile again, and the interior loops below hold
-        // no call to the out-of-line shell path.
+        // no shell code.
         for (;;) {
             if (threadIdx.x == 0) s_tile[par] = (int)atomicAdd(&ctl->tile_next, 1u);
             __syncthreads();
