@@ -19,6 +19,7 @@ Under torchrun (N > 1) each rank runs an independent replica on its GPU
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import os
 import subprocess
@@ -90,28 +91,37 @@ def replica_rate(cells: int, steps: int, seconds: float, world: int) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, polled about every 50 ms and
+    stamped at the middle of each query. `window(kind)` marks a stretch in
+    which the GPU runs the stepping workload: "steps" (warm-up and timed
+    steps) or "after" (the same steps, untimed, right after the timed
+    region: a timed region of a few milliseconds falls between two polls).
+    The summary is taken over the samples inside the marked windows."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, period_s: float = 0.05):
         self.idx = gpu_index
-        self.samples = []
+        self.period = period_s
+        self.samples = []    # (time, fields)
+        self.windows = []    # (t0, t1, kind)
         self.stop = threading.Event()
         self.t = None
 
     def _run(self):
         while not self.stop.is_set():
             try:
+                t0 = time.perf_counter()
                 out = subprocess.run(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
                                       "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                t1 = time.perf_counter()
                 if out.returncode == 0 and out.stdout.strip():
-                    self.samples.append([v.strip() for v in out.stdout.strip().split(",")])
+                    self.samples.append((0.5 * (t0 + t1), [v.strip() for v in out.stdout.strip().split(",")]))
             except Exception:
                 pass
-            self.stop.wait(0.2)
+            self.stop.wait(self.period)
 
     def __enter__(self):
         self.t = threading.Thread(target=self._run, daemon=True)
@@ -123,15 +133,36 @@ class ClockSampler:
         if self.t:
             self.t.join(timeout=10)
 
+    @contextlib.contextmanager
+    def window(self, kind: str):
+        t0 = time.perf_counter()
+        try:
+            yield
+        finally:
+            self.windows.append((t0, time.perf_counter(), kind))
+
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        inside = lambda t, kinds: any(a <= t <= b for a, b, k in self.windows if k in kinds)   # noqa: E731
+        load = [f for t, f in self.samples if inside(t, ("steps", "after"))]
+        n_steps = sum(1 for t, _ in self.samples if inside(t, ("steps",)))
+        if not load:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0, "samples_steps": 0}
+        sm = [float(s[0]) for s in load if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in load if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i] == "Active"})
+        reasons = sorted({names[i] for s in load for i in range(4) if len(s) > 3 + i and s[3 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(load), "samples_steps": n_steps,
+                "window": "polled every 50 ms during the warm-up and timed steps and during 0.4 s of the same "
+                          "steps right after the timed region, for each storage form"}
+
+
+def load_after(solver, seconds=0.4, chunk=100):
+    """The same steps, untimed, for `seconds` after a timed region."""
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        solver.step(chunk)
+    solver.synchronize()
 
 
 def measured_peak():
@@ -186,7 +217,10 @@ def run_gb300(args):
         for storage in (("fp32", "fp16") if args.only == "both" else (args.only,)):
             p, _, _ = sphere_case(storage, mask=mask)
             s = solver.Solver(p, mask)
-            ms, launches, st = time_steps(s, args.steps, args.warmup, world)
+            with clk.window("steps"):
+                ms, launches, st = time_steps(s, args.steps, args.warmup, world)
+            with clk.window("after"):
+                load_after(s)
             mlups = cells * args.steps / (ms * 1e-3) / 1e6
             gbs = BYTES_PER_CELL[storage] * cells * args.steps / (ms * 1e-3) / 1e9
             results[storage] = dict(ms_per_step=ms / args.steps, mlups=mlups, achieved_gbs=gbs, launches=launches,

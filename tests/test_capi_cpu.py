@@ -133,3 +133,19 @@ def test_bench_control_block_size_matches_device_struct(tmp_path):
     subprocess.check_call(["nvcc", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-I",
                            os.path.join(ROOT, "aeros-engine_gb300", "csrc"), str(src), "-o", str(exe)])
     assert int(subprocess.check_output([str(exe)]).decode().strip()) == bench.CONTROL_BYTES
+
+
+def test_bench_clock_summary_counts_only_samples_under_load():
+    """bench.py's clock record: the median SM clock and the throttle reasons
+    are taken over the samples inside the marked step windows only."""
+    import bench
+    c = bench.ClockSampler(0)
+    c.windows = [(1.0, 2.0, "steps"), (2.0, 3.0, "after")]
+    idle = ["800", "2070", "100", "Not Active", "Not Active", "Not Active", "Not Active"]
+    busy = ["2070", "2070", "900", "Not Active", "Not Active", "Not Active", "Active"]
+    c.samples = [(0.5, idle), (1.5, busy), (2.5, busy), (2.7, busy), (3.5, ["600"] + idle[1:3] + ["Active"] * 4)]
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["samples"] == 3 and s["samples_steps"] == 1
+    assert s["reasons"] == ["sw_power_cap"]
+    c.samples = [(0.5, idle)]
+    assert c.summary()["reasons"] == ["unsampled"]
